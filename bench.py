@@ -1,0 +1,311 @@
+"""Benchmark: cell-updates/s of the split MUSCL-Hancock + HLLE update.
+
+Workload (one GPU): 3-D perfect gas (gamma 1.4) on a uniform 256^3 FP64 grid,
+periodic, Strang splitting (6 sweeps of dt/2 per step), CFL 0.8, seeded
+piecewise-constant octants with Gaussian density bumps.  One "step" is one
+Strang step: the device-side stable-dt pass, the dt selection and six fused
+sweeps, all captured in CUDA graphs.  A cell-update is one cell advanced by
+one directional sweep (6 * 256^3 per step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--precision fp64_exact] [--n 256]
+
+Under torchrun every rank runs an independent replica of the workload on its
+own GPU (the update has no data-path exchange on a single-level periodic
+grid); `value` is the sum of the replicas' cell-updates over the slowest
+rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-updates/s"
+UNIT = "cell-updates/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64_exact")
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--cpu-sample-n", type=int, default=128,
+                    help="edge of the cube the CPU reference arm times per step")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        d["source"] = "measured"
+        return d
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
+def profile_traffic(name: str):
+    """Per-launch DRAM bytes of the sweep kernel recorded from an ncu capture
+    (profiles/<name>: a line 'traffic_bytes_per_launch: <int>')."""
+    p = ROOT / "profiles" / name
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(float(ln.split(":", 1)[1]))
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_reference_rate(n: int, steps: int, threads: int) -> dict:
+    """The oracle (scalar C++17 restatement of the reference's CPU update)
+    advancing the same workload on an n^3 cube: cell-updates/s."""
+    from oracle import oracle as orc
+    from finitevolumesolver_gb300 import workloads
+    cons = workloads.octants_3d(n)
+    g = orc.Grid(3, [n] * 3, [0, 0, 0], [1.0 / n] * 3)
+    m = orc.method()
+    t0 = time.perf_counter()
+    cons, dts, _ = g.run(m, cons, 0.8, 1e9, max_steps=steps, nthreads=threads)
+    el = time.perf_counter() - t0
+    return {"value": 6 * n ** 3 * steps / el, "seconds": el}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import build as obuild
+    obuild.build()
+    from oracle import oracle as orc
+    threads = orc.max_threads()
+    n = args.cpu_sample_n
+    # warm-up then timed steps, one oracle Strang step per bench step
+    if args.warmup > 0:
+        cpu_reference_rate(n, args.warmup, threads)
+    r = cpu_reference_rate(n, args.steps, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * r["seconds"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"3D perfect gas {n}^3 periodic, Strang MUSCL-Hancock/VanLeer + "
+                               "HLLE, CFL 0.8, seeded octants + Gaussian bumps (CPU sample of "
+                               f"the {args.n}^3 workload)", "n": n,
+                   "parallelism": f"{threads} OpenMP threads"},
+        "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} Strang steps of the {n}^3 cube"},
+        "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import finitevolumesolver_gb300 as fvs
+    from finitevolumesolver_gb300 import build, workloads
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    build.build()
+    n = args.n
+    cells = n ** 3
+    cons = workloads.octants_3d(n)
+    method = fvs.make_method(precision=args.precision)
+    solver = fvs.Solver([n] * 3, [1.0 / n] * 3, "periodic", method=method)
+    stream = torch.cuda.ExternalStream(solver.stream_handle())
+    solver.upload(cons)
+    if args.warmup:
+        solver.run(cfl=0.8, t_end=1e9, max_steps=args.warmup)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    st, _ = solver.run(cfl=0.8, t_end=1e9, max_steps=args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    assert st.steps == args.steps, "run stopped early"
+    updates = 6 * cells * args.steps * world
+    value = updates / (ms / 1e3)
+
+    # dominant kernel: the fused sweep; time single launches per direction
+    sweep_ms = []
+    dt = 0.4 * solver.ComputeStableDt(-1)
+    for rep in range(2):
+        for d in range(3):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            solver.sweep(d, dt)
+            b.record(stream)
+            torch.cuda.synchronize()
+            if rep == 1:
+                sweep_ms.append(a.elapsed_time(b))
+    sweep_s = statistics.mean(sweep_ms) / 1e3
+    algo_bytes = 16 * (3 + 2) * cells  # state read once + written once, FP64
+    peaks = load_peaks()
+    achieved = algo_bytes / sweep_s / 1e9
+    traffic = profile_traffic(f"sweep_{args.precision}_256.md")
+
+    # end to end through the public API with host buffers: upload the state
+    # from pinned host memory, K steps, download the state
+    pinned = torch.from_numpy(cons).pin_memory()
+    out_host = torch.empty_like(pinned).pin_memory()
+    state_bytes = cons.nbytes
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fvs.lib().fvs_solver_upload(solver._h, pinned.data_ptr())
+    st2, _ = solver.run(cfl=0.8, t_end=1e9, max_steps=args.steps)
+    fvs.lib().fvs_solver_download(solver._h, out_host.data_ptr())
+    e2e_s = time.perf_counter() - t0
+    e2e_value = 6 * cells * args.steps * world / e2e_s
+
+    cpu = None
+    if rank == 0:
+        from oracle import build as obuild
+        obuild.build()
+        from oracle import oracle as orc
+        threads = orc.max_threads()
+        r = cpu_reference_rate(n, 1, threads)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"1 Strang step of the {n}^3 workload ({6 * cells} cell-updates)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": f"3D perfect gas {n}^3 periodic, Strang MUSCL-Hancock/VanLeer"
+                                   " + HLLE, CFL 0.8, seeded octants + Gaussian bumps",
+                       "n": n, "precision": args.precision, "sweeps_per_step": 6,
+                       "l2": "inputs larger than L2 (state 671 MB per copy)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                         "traffic": traffic,
+                         "kernel": "SweepMarchKernel (fused flux + update + CFL)",
+                         "algorithmic_bytes_per_launch": algo_bytes,
+                         "launch_ms": sweep_s * 1e3, "peak_source": peaks["source"]},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": state_bytes / args.steps,
+                    "d2h_bytes_per_step": (state_bytes + 136 * (args.steps // 30 + 1)) / args.steps},
+            "gpu_launches": 9 * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,241 @@
+"""finitevolumesolver_gb300 -- GB300 (sm_103a) split finite-volume patch update
+for the perfect-gas Euler equations.
+
+Host-side mirror of maikel/FiniteVolumeSolver's patch-level interface for the
+split update (the names, argument meaning and error behaviour follow the
+reference):
+
+  FluxMethod.ComputeNumericFluxes / ComputeStableDt / GetStencilWidth
+      include/fub/flux_method/FluxMethod.hpp:115-170
+  HyperbolicPatchIntegrator.UpdateConservatively
+      include/fub/HyperbolicPatchIntegrator.hpp:34-54
+  CompleteFromCons
+      src/equations/PerfectGas.cpp:96-124
+  Solver (a uniform single-level grid run by RunSimulation's loop)
+      include/fub/RunSimulation.hpp:86-191,
+      include/fub/solver/DimensionalSplitLevelIntegrator.hpp:204-276
+
+Every call goes through the C ABI of libfvs_gb300.so (include/fvs_gpu.h).
+Data arguments are device pointers: ints or objects with ``data_ptr()``
+(e.g. CUDA tensors).  There is no CPU fallback: without the library or a GPU
+the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from . import _capi
+from ._capi import Box, FvsError, GridDesc, Method, RunStats
+
+__all__ = ["PerfectGas", "FluxMethod", "HyperbolicPatchIntegrator", "CompleteFromCons",
+           "Solver", "FvsError", "make_method", "box", "lib"]
+
+FLUX_METHODS = {"muscl_hlle": 0, "hlle": 1, "godunov": 2, "muscl_godunov": 3}
+LIMITERS = {"van_leer": 0, "minmod": 1, "none": 2}
+PRECISIONS = {"fp64_exact": 0, "fp64_fast": 1, "mixed": 2}
+GUESSES = {"mean": 0, "pvrs_tr": 1, "mlp": 2}
+BCS = {"periodic": 0, "transmissive": 1}
+
+
+def lib() -> C.CDLL:
+    return _capi.load()
+
+
+def _ptr(x) -> int:
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        if hasattr(x, "is_cuda") and not x.is_cuda:
+            raise ValueError("data must live in device memory")
+        return int(x.data_ptr())
+    raise TypeError(f"expected a device pointer, got {type(x)!r}")
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        return 0
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+def box(lo, hi) -> Box:
+    """Half-open index box [lo, hi); missing dimensions become [0, 1)."""
+    lo = list(lo) + [0] * (3 - len(lo))
+    hi = list(hi) + [1] * (3 - len(hi))
+    b = Box()
+    for d in range(3):
+        b.lo[d] = int(lo[d])
+        b.hi[d] = int(hi[d])
+    return b
+
+
+def _as_box(b) -> Box:
+    return b if isinstance(b, Box) else box(*b)
+
+
+def make_method(flux_method="muscl_hlle", limiter="van_leer", precision="fp64_exact",
+                guess="mean", max_iterations=5000, tolerance=1e-7, gamma=1.4) -> Method:
+    m = Method()
+    lib().fvs_method_default(C.byref(m))
+    m.flux_method = FLUX_METHODS[flux_method] if isinstance(flux_method, str) else flux_method
+    m.limiter = LIMITERS[limiter] if isinstance(limiter, str) else limiter
+    m.precision = PRECISIONS[precision] if isinstance(precision, str) else precision
+    m.guess = GUESSES[guess] if isinstance(guess, str) else guess
+    m.max_iterations = max_iterations
+    m.tolerance = tolerance
+    m.gamma = gamma
+    return m
+
+
+class PerfectGas:
+    """fub::PerfectGas<Rank> (include/fub/equations/PerfectGas.hpp:164-211)."""
+
+    def __init__(self, rank: int, gamma: float = 1.4):
+        if rank not in (1, 2, 3):
+            raise ValueError("rank must be 1, 2 or 3")
+        self.rank = rank
+        self.gamma = gamma
+        self.gamma_minus_1_inv = 1.0 / (gamma - 1.0)
+
+    def n_cons(self) -> int:
+        return self.rank + 2
+
+    def n_complete(self) -> int:
+        return self.rank + 4
+
+
+class FluxMethod:
+    """fub::FluxMethod<Base> for Base in MusclHancock<PerfectGas, Hll<Einfeldt>,
+    Limiter> (the default), Hll<PerfectGas, Einfeldt>, Godunov<ExactRiemannSolver>."""
+
+    def __init__(self, equation: PerfectGas, flux_method="muscl_hlle", limiter="van_leer",
+                 precision="fp64_exact", **kw):
+        self.equation = equation
+        self.method = make_method(flux_method, limiter, precision, gamma=equation.gamma, **kw)
+
+    def GetStencilWidth(self) -> int:
+        return 2 if self.method.flux_method in (0, 3) else 1
+
+    def ComputeNumericFluxes(self, fluxes, face_box, states, cell_box, dt, dx, dir,
+                             stream=None) -> None:
+        _capi.check(lib().fvs_compute_numeric_fluxes(
+            C.byref(self.method), self.equation.rank, _ptr(fluxes), _as_box(face_box),
+            _ptr(states), _as_box(cell_box), float(dt), float(dx), int(dir), _stream(stream)))
+
+    def ComputeStableDt(self, states, cell_box, dx, dir, window_rule=1, stream=None) -> float:
+        out = C.c_double(0.0)
+        _capi.check(lib().fvs_compute_stable_dt(
+            C.byref(self.method), self.equation.rank, _ptr(states), _as_box(cell_box),
+            float(dx), int(dir), int(window_rule), C.byref(out), _stream(stream)))
+        return out.value
+
+
+class HyperbolicPatchIntegrator:
+    """fub::HyperbolicPatchIntegrator<Tag> (include/fub/HyperbolicPatchIntegrator.hpp:34-54)."""
+
+    def UpdateConservatively(self, next, next_box, prev, prev_box, fluxes, face_box, ncomp,
+                             dt, dx, dir, stream=None) -> None:
+        _capi.check(lib().fvs_update_conservatively(
+            _ptr(next), _as_box(next_box), _ptr(prev), _as_box(prev_box), _ptr(fluxes),
+            _as_box(face_box), int(ncomp), float(dt), float(dx), int(dir), _stream(stream)))
+
+
+def CompleteFromCons(equation: PerfectGas, complete, complete_box, cons, cons_box, region,
+                     stream=None) -> None:
+    _capi.check(lib().fvs_complete_from_cons(
+        equation.rank, equation.gamma, _ptr(complete), _as_box(complete_box), _ptr(cons),
+        _as_box(cons_box), _as_box(region), _stream(stream)))
+
+
+class Solver:
+    """A uniform single-level grid advanced by the reference's split step
+    sequence, with the time step kept on the device."""
+
+    def __init__(self, n, dx, bc="periodic", method: Method | None = None, dt_rule=0):
+        rank = len(n)
+        g = GridDesc()
+        g.rank = rank
+        bcs = [bc] * rank if isinstance(bc, (str, int)) else list(bc)
+        for d in range(3):
+            g.n[d] = int(n[d]) if d < rank else 1
+            b = bcs[d] if d < rank else 0
+            g.bc[d] = BCS[b] if isinstance(b, str) else int(b)
+            g.dx[d] = float(dx[d] if not isinstance(dx, (int, float)) else dx) if d < rank else 1.0
+        g.dt_rule = dt_rule
+        self.rank = rank
+        self.n = [int(x) for x in n]
+        self.method = method if method is not None else make_method()
+        self._h = C.c_void_p()
+        _capi.check(lib().fvs_solver_create(C.byref(g), C.byref(self.method),
+                                            C.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().fvs_solver_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def shape(self):
+        return (self.rank + 2,) + tuple(reversed(self.n + [1] * (3 - self.rank)))
+
+    def upload(self, cons_host) -> None:
+        import numpy as np
+        a = np.ascontiguousarray(cons_host, dtype=np.float64)
+        assert a.size == int(np.prod(self.shape()))
+        _capi.check(lib().fvs_solver_upload(self._h, a.ctypes.data))
+
+    def download(self):
+        import numpy as np
+        a = np.empty(self.shape(), dtype=np.float64)
+        _capi.check(lib().fvs_solver_download(self._h, a.ctypes.data))
+        return a
+
+    def state_device_ptr(self) -> int:
+        p = C.c_void_p()
+        _capi.check(lib().fvs_solver_state_device(self._h, C.byref(p)))
+        return int(p.value or 0)
+
+    def stream_handle(self) -> int:
+        p = C.c_void_p()
+        _capi.check(lib().fvs_solver_stream(self._h, C.byref(p)))
+        return int(p.value or 0)
+
+    def set_tiling(self, seg_len: int) -> None:
+        _capi.check(lib().fvs_solver_set_tiling(self._h, int(seg_len)))
+
+    def set_cycle(self, cycle: int) -> None:
+        _capi.check(lib().fvs_solver_set_cycle(self._h, int(cycle)))
+
+    def set_time(self, t: float) -> None:
+        _capi.check(lib().fvs_solver_set_time(self._h, float(t)))
+
+    def ComputeStableDt(self, dir: int = -1) -> float:
+        out = C.c_double(0.0)
+        _capi.check(lib().fvs_solver_stable_dt(self._h, int(dir), C.byref(out)))
+        return out.value
+
+    def sweep(self, dir: int, dt: float) -> float:
+        out = C.c_double(0.0)
+        _capi.check(lib().fvs_solver_sweep(self._h, int(dir), float(dt), C.byref(out)))
+        return out.value
+
+    def step(self, dt: float, cycle: int) -> None:
+        _capi.check(lib().fvs_solver_step(self._h, float(dt), int(cycle)))
+
+    def run(self, cfl=0.8, t_end=1.0, max_steps=-1, log_len=0):
+        import numpy as np
+        log = np.zeros(max(log_len, 1))
+        st = RunStats()
+        code = lib().fvs_solver_run(self._h, float(cfl), float(t_end), int(max_steps),
+                                    log.ctypes.data_as(C.POINTER(C.c_double)), int(log_len),
+                                    C.byref(st))
+        _capi.check(code)
+        return st, log[:min(log_len, st.steps)].copy()

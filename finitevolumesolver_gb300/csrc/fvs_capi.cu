@@ -1,0 +1,711 @@
+// fvs_capi.cu -- the C ABI of libfvs_gb300 (include/fvs_gpu.h): argument
+// checking, the patch-level entry points, and the uniform-grid solver
+// context with its device-resident time stepping and CUDA graphs.
+#include "../../include/fvs_gpu.h"
+#include "fvs_internal.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int Fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int CudaFail(cudaError_t e, const char* what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return FVS_ERR_CUDA;
+}
+
+#define FVS_CUDA(call)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return CudaFail(e_, #call);  \
+  } while (0)
+
+int CheckDevice() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return Fail(FVS_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  return FVS_OK;
+}
+
+fvs::BoxDesc ToDesc(const fvs_box& b) {
+  fvs::BoxDesc d;
+  for (int i = 0; i < 3; ++i) {
+    d.lo[i] = b.lo[i];
+    d.n[i] = b.hi[i] - b.lo[i];
+  }
+  return d;
+}
+
+bool ValidBox(const fvs_box& b) {
+  for (int i = 0; i < 3; ++i)
+    if (b.hi[i] < b.lo[i]) return false;
+  return true;
+}
+
+bool Contains(const fvs_box& outer, const int* lo, const int* hi) {
+  for (int i = 0; i < 3; ++i)
+    if (lo[i] < outer.lo[i] || hi[i] > outer.hi[i]) return false;
+  return true;
+}
+
+int64_t Volume(const fvs_box& b) {
+  return int64_t(b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]) * (b.hi[2] - b.lo[2]);
+}
+
+int CheckMethod(const fvs_method* m, int rank) {
+  if (!m) return Fail(FVS_ERR_INVALID, "method is NULL");
+  if (rank < 1 || rank > 3) return Fail(FVS_ERR_INVALID, "rank must be 1, 2 or 3");
+  if (m->flux_method < 0 || m->flux_method > 3)
+    return Fail(FVS_ERR_INVALID, "unknown flux method");
+  if (m->limiter < 0 || m->limiter > 2) return Fail(FVS_ERR_INVALID, "unknown limiter");
+  if (m->precision < 0 || m->precision > 2)
+    return Fail(FVS_ERR_INVALID, "unknown precision");
+  if (!(m->gamma > 1.0)) return Fail(FVS_ERR_INVALID, "gamma must exceed 1");
+  return FVS_OK;
+}
+
+int StencilWidth(int method) {
+  return (method == FVS_MUSCL_HLLE || method == FVS_MUSCL_GODUNOV) ? 2 : 1;
+}
+
+double BitsToDouble(unsigned long long b) {
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Control kernels of the device-resident time loop.
+
+namespace fvs {
+
+__device__ __forceinline__ double BitsToDoubleDev(unsigned long long b) {
+  return __longlong_as_double(static_cast<long long>(b));
+}
+
+struct StepPlan {
+  int nsweeps;
+  int dir[6];
+  double dx[6];
+  double frac;  // split dt = frac * dt
+  int rank;
+  double dxd[3];
+};
+
+// RunSimulation's dt selection (include/fub/RunSimulation.hpp:125-131):
+// dt = min(t_end - t, cfl * stable_dt), or the failed check's dt after a
+// restart; stops when t + 1e-12 >= t_end.
+__global__ void BeginStepKernel(Control* c, StepPlan plan) {
+  if (c->abort || c->done) return;
+  const double eps = 1e-12;
+  if (!(c->t + eps < c->t_end)) {
+    c->done = 1;
+    return;
+  }
+  double stable;
+  if (c->have_failure) {
+    stable = c->fail_dt;
+    c->have_failure = 0;
+  } else {
+    stable = 1.7976931348623157e308;
+    for (int d = 0; d < plan.rank; ++d) {
+      const double s = BitsToDoubleDev(c->smax_stable[d]);
+      const double dtd = plan.dxd[d] / s;
+      stable = dtd < stable ? dtd : stable;
+    }
+  }
+  double dt;
+  if (c->dt_override > 0.0) {
+    dt = c->dt_override;
+  } else {
+    const double a = c->t_end - c->t;
+    const double b = c->cfl * stable;
+    dt = a < b ? a : b;
+  }
+  c->dt = dt;
+  for (int q = 0; q < 6; ++q) c->smax_check[q] = 0ull;
+  c->step_status = 0;
+}
+
+// The per-sweep checks (DimensionalSplitLevelIntegrator.hpp:240-245), in
+// sweep order; commits the step or records the first failure.
+__global__ void EndStepKernel(Control* c, StepPlan plan, int step_in_batch,
+                              double* dt_log, int dt_log_len) {
+  if (c->abort || c->done) return;
+  const double split_dt = plan.frac * c->dt;
+  for (int q = 0; q < plan.nsweeps; ++q) {
+    const double level_dt = plan.dx[q] / BitsToDoubleDev(c->smax_check[q]);
+    if (level_dt < split_dt) {
+      c->abort = 1;
+      c->failed_step = step_in_batch;
+      c->fail_dt = level_dt;
+      c->have_failure = 1;
+      return;
+    }
+  }
+  if (dt_log && c->steps_done < dt_log_len) dt_log[c->steps_done] = c->dt;  // cumulative index
+  c->t = c->t + c->dt;
+  c->steps_done += 1;
+  c->status |= c->step_status;
+  for (int d = 0; d < 3; ++d) c->smax_stable[d] = 0ull;
+}
+
+}  // namespace fvs
+
+// ---------------------------------------------------------------------------
+
+struct fvs_solver {
+  fvs_grid_desc g;
+  fvs_method m;
+  cudaStream_t stream = nullptr;
+  double* buf[3] = {nullptr, nullptr, nullptr};
+  int cur = 0;
+  fvs::Control* ctrl = nullptr;
+  fvs::Control* ctrl_host = nullptr;  // pinned
+  unsigned long long* scratch_words = nullptr;  // [8]
+  double* dt_log_dev = nullptr;
+  int dt_log_cap = 0;
+  int seg_len = 0;
+  int64_t cycle = 0;
+  double t = 0.0;
+  int64_t cells = 0;
+  int ncons = 0;
+  std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
+  ~fvs_solver() {
+    for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+    for (double* b : buf)
+      if (b) cudaFree(b);
+    if (ctrl) cudaFree(ctrl);
+    if (ctrl_host) cudaFreeHost(ctrl_host);
+    if (scratch_words) cudaFree(scratch_words);
+    if (dt_log_dev) cudaFree(dt_log_dev);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+int SegLen(const fvs_solver* s, int dir) {
+  if (s->seg_len > 0) return s->seg_len;
+  const int nd = s->g.n[dir];
+  int64_t ntrans = s->cells / nd;
+  // Aim for at least ~64K threads; never shorter than 16 cells.
+  int seg = nd;
+  while (seg > 16 && ntrans * ((nd + seg - 1) / seg) < 65536) seg = (seg + 1) / 2;
+  return seg;
+}
+
+cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
+                        int dir, const double* dt_ptr, double dt_scale,
+                        double dt_value, unsigned long long* smax_out,
+                        fvs::Control* ctrl, int prev_check, double prev_dx) {
+  fvs::SweepArgs a{};
+  a.in = in;
+  a.out = out;
+  for (int d = 0; d < 3; ++d) a.n[d] = s->g.n[d];
+  a.rank = s->g.rank;
+  a.dir = dir;
+  a.bc = s->g.bc[dir];
+  a.limiter = s->m.limiter;
+  a.seg_len = SegLen(s, dir);
+  a.gamma = s->m.gamma;
+  a.dx = s->g.dx[dir];
+  a.dt_ptr = dt_ptr;
+  a.dt_scale = dt_scale;
+  a.dt_value = dt_value;
+  a.smax_out = smax_out;
+  a.ctrl = ctrl;
+  a.prev_check = prev_check;
+  a.prev_dx = prev_dx;
+  switch (s->m.precision) {
+  case FVS_FP64_EXACT:
+    return fvs::LaunchSweepExact(a, s->stream);
+  default:
+    return cudaErrorNotSupported;
+  }
+}
+
+cudaError_t LaunchStable(const fvs_solver* s, const double* in,
+                         unsigned long long* smax_out, fvs::Control* ctrl) {
+  fvs::StableDtArgs a{};
+  a.in = in;
+  for (int d = 0; d < 3; ++d) {
+    a.n[d] = s->g.n[d];
+    a.bc[d] = s->g.bc[d];
+  }
+  a.rank = s->g.rank;
+  a.rule = s->g.dt_rule;
+  a.gamma = s->m.gamma;
+  a.smax_out = smax_out;
+  a.ctrl = ctrl;
+  return fvs::LaunchStableDtExact(a, s->stream);
+}
+
+fvs::StepPlan MakePlan(const fvs_solver* s, int64_t cycle) {
+  fvs::StepPlan p{};
+  const int D = s->g.rank;
+  // MakeSplitDirections (SplittingMethod.hpp:115-126)
+  int dirs[3];
+  const int odd = static_cast<int>(cycle % 2);
+  for (int i = 0; i < D; ++i) dirs[i] = odd ? D - 1 - i : i;
+  // StrangSplitting::Advance (StrangSplitting.cpp:25-69)
+  if (D == 1) {
+    p.nsweeps = 1;
+    p.dir[0] = dirs[0];
+    p.frac = 1.0;
+  } else if (D == 2) {
+    const int q[4] = {dirs[0], dirs[1], dirs[1], dirs[0]};
+    p.nsweeps = 4;
+    for (int i = 0; i < 4; ++i) p.dir[i] = q[i];
+    p.frac = 0.5;
+  } else {
+    const int q[6] = {dirs[0], dirs[1], dirs[2], dirs[2], dirs[1], dirs[0]};
+    p.nsweeps = 6;
+    for (int i = 0; i < 6; ++i) p.dir[i] = q[i];
+    p.frac = 0.5;
+  }
+  for (int i = 0; i < p.nsweeps; ++i) p.dx[i] = s->g.dx[p.dir[i]];
+  p.rank = D;
+  for (int d = 0; d < 3; ++d) p.dxd[d] = s->g.dx[d];
+  return p;
+}
+
+int NextBuffer(int start, int nsweeps) { return (start + (nsweeps % 2 ? 1 : 2)) % 3; }
+
+// Enqueue one device-driven split step starting in buffer `start`.
+cudaError_t EnqueueStep(fvs_solver* s, int start, int64_t cycle, int step_in_batch) {
+  const fvs::StepPlan plan = MakePlan(s, cycle);
+  cudaError_t e = LaunchStable(s, s->buf[start], s->ctrl->smax_stable, s->ctrl);
+  if (e != cudaSuccess) return e;
+  fvs::BeginStepKernel<<<1, 1, 0, s->stream>>>(s->ctrl, plan);
+  const int X = (start + 1) % 3, Y = (start + 2) % 3;
+  int src = start, dst = X;
+  for (int q = 0; q < plan.nsweeps; ++q) {
+    e = LaunchSweep(s, s->buf[src], s->buf[dst], plan.dir[q], &s->ctrl->dt,
+                    plan.frac, 0.0, &s->ctrl->smax_check[q], s->ctrl,
+                    q > 0 ? q - 1 : -1, q > 0 ? plan.dx[q - 1] : 0.0);
+    if (e != cudaSuccess) return e;
+    src = dst;
+    dst = (dst == X) ? Y : X;
+  }
+  fvs::EndStepKernel<<<1, 1, 0, s->stream>>>(s->ctrl, plan, step_in_batch,
+                                             s->dt_log_dev, s->dt_log_cap);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" {
+
+void fvs_method_default(fvs_method* m) {
+  if (!m) return;
+  std::memset(m, 0, sizeof *m);
+  m->flux_method = FVS_MUSCL_HLLE;
+  m->limiter = FVS_VAN_LEER;
+  m->precision = FVS_FP64_EXACT;
+  m->guess = FVS_GUESS_MEAN;
+  m->max_iterations = 5000;
+  m->tolerance = 1e-7;
+  m->gamma = 1.4;
+}
+
+const char* fvs_last_error(void) { return g_last_error.c_str(); }
+
+int fvs_abi_version(void) { return 1; }
+
+int fvs_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int fvs_compute_numeric_fluxes(const fvs_method* m, int rank,
+                               double* fluxes_dev, fvs_box face_box,
+                               const double* states_dev, fvs_box cell_box,
+                               double dt, double dx, int dir, void* stream) {
+  if (int r = CheckMethod(m, rank)) return r;
+  if (dir < 0 || dir >= rank) return Fail(FVS_ERR_INVALID, "direction out of range");
+  if (!ValidBox(face_box) || !ValidBox(cell_box))
+    return Fail(FVS_ERR_INVALID, "invalid box");
+  if (Volume(face_box) == 0) return FVS_OK;
+  if (!fluxes_dev || !states_dev) return Fail(FVS_ERR_INVALID, "NULL data pointer");
+  // every stencil cell must lie in cell_box
+  const int w = StencilWidth(m->flux_method);
+  int lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = face_box.lo[d];
+    hi[d] = face_box.hi[d];
+  }
+  lo[dir] -= w;
+  hi[dir] += w - 1;
+  if (!Contains(cell_box, lo, hi))
+    return Fail(FVS_ERR_INVALID, "cell box does not cover the faces' stencils");
+  if (m->flux_method == FVS_GODUNOV || m->flux_method == FVS_MUSCL_GODUNOV)
+    return Fail(FVS_ERR_UNSUPPORTED, "Godunov patch fluxes not built");
+  if (m->precision != FVS_FP64_EXACT)
+    return Fail(FVS_ERR_UNSUPPORTED, "patch-level calls run in exact FP64");
+  if (int r = CheckDevice()) return r;
+  FVS_CUDA(fvs::LaunchPatchFluxesExact(m->flux_method, m->limiter, rank, m->gamma,
+                                       fluxes_dev, ToDesc(face_box), states_dev,
+                                       ToDesc(cell_box), dt, dx, dir,
+                                       static_cast<cudaStream_t>(stream)));
+  return FVS_OK;
+}
+
+int fvs_compute_stable_dt(const fvs_method* m, int rank, const double* states_dev,
+                          fvs_box cell_box, double dx, int dir, int window_rule,
+                          double* dt_out, void* stream) {
+  if (int r = CheckMethod(m, rank)) return r;
+  if (dir < 0 || dir >= rank) return Fail(FVS_ERR_INVALID, "direction out of range");
+  if (!ValidBox(cell_box)) return Fail(FVS_ERR_INVALID, "invalid box");
+  if (!dt_out) return Fail(FVS_ERR_INVALID, "dt_out is NULL");
+  if (window_rule != 0 && window_rule != 1)
+    return Fail(FVS_ERR_INVALID, "window_rule must be 0 or 1");
+  if (m->flux_method == FVS_GODUNOV || m->flux_method == FVS_MUSCL_GODUNOV)
+    return Fail(FVS_ERR_UNSUPPORTED, "Godunov stable dt not built");
+  if (int r = CheckDevice()) return r;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned long long* word = nullptr;
+  FVS_CUDA(cudaMallocAsync(&word, sizeof *word, st));
+  FVS_CUDA(cudaMemsetAsync(word, 0, sizeof *word, st));
+  cudaError_t e = fvs::LaunchPatchStableDtExact(m->flux_method, rank, m->gamma,
+                                                states_dev, ToDesc(cell_box),
+                                                window_rule, dir, word, st);
+  unsigned long long bits = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&bits, word, sizeof bits, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(word, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return CudaFail(e, "fvs_compute_stable_dt");
+  const double smax = BitsToDouble(bits);
+  *dt_out = (smax > 0.0) ? dx / smax : INFINITY;
+  return FVS_OK;
+}
+
+int fvs_update_conservatively(double* next_dev, fvs_box next_box,
+                              const double* prev_dev, fvs_box prev_box,
+                              const double* fluxes_dev, fvs_box face_box,
+                              int ncomp, double dt, double dx, int dir,
+                              void* stream) {
+  if (dir < 0 || dir > 2) return Fail(FVS_ERR_INVALID, "direction out of range");
+  if (ncomp < 1) return Fail(FVS_ERR_INVALID, "ncomp must be positive");
+  if (!ValidBox(next_box) || !ValidBox(prev_box) || !ValidBox(face_box))
+    return Fail(FVS_ERR_INVALID, "invalid box");
+  if (Volume(next_box) == 0) return FVS_OK;
+  if (!Contains(prev_box, next_box.lo, next_box.hi))
+    return Fail(FVS_ERR_INVALID, "prev box does not cover next box");
+  int hi[3] = {next_box.hi[0], next_box.hi[1], next_box.hi[2]};
+  hi[dir] += 1;
+  if (!Contains(face_box, next_box.lo, hi))
+    return Fail(FVS_ERR_INVALID, "face box does not cover the faces of next box");
+  if (int r = CheckDevice()) return r;
+  FVS_CUDA(fvs::LaunchPatchUpdate(next_dev, ToDesc(next_box), prev_dev,
+                                  ToDesc(prev_box), fluxes_dev, ToDesc(face_box),
+                                  ncomp, dt, dx, dir,
+                                  static_cast<cudaStream_t>(stream)));
+  return FVS_OK;
+}
+
+int fvs_complete_from_cons(int rank, double gamma, double* complete_dev,
+                           fvs_box complete_box, const double* cons_dev,
+                           fvs_box cons_box, fvs_box region, void* stream) {
+  if (rank < 1 || rank > 3) return Fail(FVS_ERR_INVALID, "rank must be 1, 2 or 3");
+  if (!(gamma > 1.0)) return Fail(FVS_ERR_INVALID, "gamma must exceed 1");
+  if (!ValidBox(complete_box) || !ValidBox(cons_box) || !ValidBox(region))
+    return Fail(FVS_ERR_INVALID, "invalid box");
+  if (Volume(region) == 0) return FVS_OK;
+  if (!Contains(complete_box, region.lo, region.hi) ||
+      !Contains(cons_box, region.lo, region.hi))
+    return Fail(FVS_ERR_INVALID, "region outside the data boxes");
+  if (int r = CheckDevice()) return r;
+  FVS_CUDA(fvs::LaunchPatchCompleteFromCons(rank, gamma, complete_dev,
+                                            ToDesc(complete_box), cons_dev,
+                                            ToDesc(cons_box), ToDesc(region),
+                                            static_cast<cudaStream_t>(stream)));
+  return FVS_OK;
+}
+
+int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
+                      fvs_solver** out) {
+  if (!grid || !out) return Fail(FVS_ERR_INVALID, "NULL argument");
+  if (int r = CheckMethod(m, grid->rank)) return r;
+  if (m->flux_method != FVS_MUSCL_HLLE)
+    return Fail(FVS_ERR_UNSUPPORTED, "solver supports MUSCL-Hancock + HLLE");
+  if (m->precision != FVS_FP64_EXACT)
+    return Fail(FVS_ERR_UNSUPPORTED, "precision not built");
+  for (int d = 0; d < 3; ++d) {
+    const bool used = d < grid->rank;
+    if (used && grid->n[d] < 1) return Fail(FVS_ERR_INVALID, "extent must be >= 1");
+    if (!used && grid->n[d] != 1)
+      return Fail(FVS_ERR_INVALID, "unused directions must have extent 1");
+    if (used && grid->bc[d] != FVS_BC_PERIODIC && grid->bc[d] != FVS_BC_TRANSMISSIVE)
+      return Fail(FVS_ERR_INVALID, "unknown boundary condition");
+    if (used && !(grid->dx[d] > 0.0)) return Fail(FVS_ERR_INVALID, "dx must be positive");
+  }
+  if (grid->dt_rule != 0 && grid->dt_rule != 1)
+    return Fail(FVS_ERR_INVALID, "dt_rule must be 0 or 1");
+  if (int r = CheckDevice()) return r;
+  fvs_solver* s = new fvs_solver();
+  s->g = *grid;
+  s->m = *m;
+  s->cells = int64_t(grid->n[0]) * grid->n[1] * grid->n[2];
+  s->ncons = grid->rank + 2;
+  const size_t bytes = size_t(s->cells) * s->ncons * sizeof(double);
+  cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  for (int b = 0; b < 3 && e == cudaSuccess; ++b) e = cudaMalloc(&s->buf[b], bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&s->ctrl, sizeof(fvs::Control));
+  if (e == cudaSuccess) e = cudaMallocHost(&s->ctrl_host, sizeof(fvs::Control));
+  if (e == cudaSuccess) e = cudaMalloc(&s->scratch_words, 8 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(s->ctrl, 0, sizeof(fvs::Control));
+  if (e != cudaSuccess) {
+    delete s;
+    return CudaFail(e, "fvs_solver_create");
+  }
+  *out = s;
+  return FVS_OK;
+}
+
+int fvs_solver_destroy(fvs_solver* s) {
+  if (!s) return FVS_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  delete s;
+  return FVS_OK;
+}
+
+int fvs_solver_upload(fvs_solver* s, const double* cons_host) {
+  if (!s || !cons_host) return Fail(FVS_ERR_INVALID, "NULL argument");
+  const size_t bytes = size_t(s->cells) * s->ncons * sizeof(double);
+  FVS_CUDA(cudaMemcpyAsync(s->buf[s->cur], cons_host, bytes, cudaMemcpyHostToDevice,
+                           s->stream));
+  FVS_CUDA(cudaStreamSynchronize(s->stream));
+  return FVS_OK;
+}
+
+int fvs_solver_download(fvs_solver* s, double* cons_host) {
+  if (!s || !cons_host) return Fail(FVS_ERR_INVALID, "NULL argument");
+  const size_t bytes = size_t(s->cells) * s->ncons * sizeof(double);
+  FVS_CUDA(cudaMemcpyAsync(cons_host, s->buf[s->cur], bytes, cudaMemcpyDeviceToHost,
+                           s->stream));
+  FVS_CUDA(cudaStreamSynchronize(s->stream));
+  return FVS_OK;
+}
+
+int fvs_solver_state_device(fvs_solver* s, double** cons_dev) {
+  if (!s || !cons_dev) return Fail(FVS_ERR_INVALID, "NULL argument");
+  *cons_dev = s->buf[s->cur];
+  return FVS_OK;
+}
+
+int fvs_solver_set_tiling(fvs_solver* s, int seg_len) {
+  if (!s || seg_len < 0) return Fail(FVS_ERR_INVALID, "bad tiling");
+  s->seg_len = seg_len;
+  return FVS_OK;
+}
+
+int fvs_solver_set_cycle(fvs_solver* s, int64_t cycle) {
+  if (!s || cycle < 0) return Fail(FVS_ERR_INVALID, "bad cycle");
+  s->cycle = cycle;
+  return FVS_OK;
+}
+
+int fvs_solver_set_time(fvs_solver* s, double t) {
+  if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
+  s->t = t;
+  return FVS_OK;
+}
+
+int fvs_solver_stable_dt(fvs_solver* s, int dir, double* dt_out) {
+  if (!s || !dt_out) return Fail(FVS_ERR_INVALID, "NULL argument");
+  if (dir < -1 || dir >= s->g.rank) return Fail(FVS_ERR_INVALID, "direction out of range");
+  FVS_CUDA(cudaMemsetAsync(s->scratch_words, 0, 3 * sizeof(unsigned long long), s->stream));
+  FVS_CUDA(LaunchStable(s, s->buf[s->cur], s->scratch_words, nullptr));
+  unsigned long long bits[3];
+  FVS_CUDA(cudaMemcpyAsync(bits, s->scratch_words, sizeof bits, cudaMemcpyDeviceToHost,
+                           s->stream));
+  FVS_CUDA(cudaStreamSynchronize(s->stream));
+  double best = INFINITY;
+  for (int d = 0; d < s->g.rank; ++d) {
+    if (dir >= 0 && d != dir) continue;
+    const double smax = BitsToDouble(bits[d]);
+    const double dtd = smax > 0.0 ? s->g.dx[d] / smax : INFINITY;
+    best = dtd < best ? dtd : best;
+  }
+  *dt_out = best;
+  return FVS_OK;
+}
+
+int fvs_solver_sweep(fvs_solver* s, int dir, double dt, double* level_dt_out) {
+  if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
+  if (dir < 0 || dir >= s->g.rank) return Fail(FVS_ERR_INVALID, "direction out of range");
+  const int out = (s->cur + 1) % 3;
+  FVS_CUDA(cudaMemsetAsync(s->scratch_words, 0, sizeof(unsigned long long), s->stream));
+  FVS_CUDA(LaunchSweep(s, s->buf[s->cur], s->buf[out], dir, nullptr, 1.0, dt,
+                       s->scratch_words, nullptr, -1, 0.0));
+  unsigned long long bits = 0;
+  FVS_CUDA(cudaMemcpyAsync(&bits, s->scratch_words, sizeof bits, cudaMemcpyDeviceToHost,
+                           s->stream));
+  FVS_CUDA(cudaStreamSynchronize(s->stream));
+  s->cur = out;
+  if (level_dt_out) {
+    const double smax = BitsToDouble(bits);
+    *level_dt_out = smax > 0.0 ? s->g.dx[dir] / smax : INFINITY;
+  }
+  return FVS_OK;
+}
+
+int fvs_solver_step(fvs_solver* s, double dt, int cycle) {
+  if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
+  if (!(dt > 0.0)) return Fail(FVS_ERR_INVALID, "dt must be positive");
+  const fvs::StepPlan plan = MakePlan(s, cycle);
+  const double split_dt = plan.frac * dt;
+  FVS_CUDA(cudaMemsetAsync(s->scratch_words, 0, 8 * sizeof(unsigned long long), s->stream));
+  const int start = s->cur;
+  const int X = (start + 1) % 3, Y = (start + 2) % 3;
+  int src = start, dst = X;
+  for (int q = 0; q < plan.nsweeps; ++q) {
+    FVS_CUDA(LaunchSweep(s, s->buf[src], s->buf[dst], plan.dir[q], nullptr, 1.0,
+                         split_dt, s->scratch_words + q, nullptr, -1, 0.0));
+    src = dst;
+    dst = (dst == X) ? Y : X;
+  }
+  unsigned long long bits[8];
+  FVS_CUDA(cudaMemcpyAsync(bits, s->scratch_words, sizeof bits, cudaMemcpyDeviceToHost,
+                           s->stream));
+  FVS_CUDA(cudaStreamSynchronize(s->stream));
+  for (int q = 0; q < plan.nsweeps; ++q) {
+    const double level_dt = plan.dx[q] / BitsToDouble(bits[q]);
+    if (level_dt < split_dt) {
+      return Fail(FVS_ERR_DT_TOO_LARGE, "per-sweep CFL check failed");
+    }
+  }
+  s->cur = src;
+  return FVS_OK;
+}
+
+int fvs_solver_stream(fvs_solver* s, void** stream) {
+  if (!s || !stream) return Fail(FVS_ERR_INVALID, "NULL argument");
+  *stream = static_cast<void*>(s->stream);
+  return FVS_OK;
+}
+
+int fvs_solver_run(fvs_solver* s, double cfl, double t_end, int max_steps,
+                   double* dt_log, int dt_log_len, fvs_run_stats* stats) {
+  if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
+  if (!(cfl > 0.0)) return Fail(FVS_ERR_INVALID, "cfl must be positive");
+  if (dt_log_len < 0 || (dt_log_len > 0 && !dt_log))
+    return Fail(FVS_ERR_INVALID, "bad dt log");
+  if (dt_log_len > s->dt_log_cap) {
+    FVS_CUDA(cudaStreamSynchronize(s->stream));
+    if (s->dt_log_dev) cudaFree(s->dt_log_dev);
+    s->dt_log_dev = nullptr;
+    FVS_CUDA(cudaMalloc(&s->dt_log_dev, size_t(dt_log_len) * sizeof(double)));
+    s->dt_log_cap = dt_log_len;
+    for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+    s->graphs.clear();
+  }
+  fvs::Control c{};
+  c.t = s->t;
+  c.t_end = t_end;
+  c.cfl = cfl;
+  FVS_CUDA(cudaMemcpyAsync(s->ctrl, &c, sizeof c, cudaMemcpyHostToDevice, s->stream));
+  int committed = 0;
+  int restarts = 0;
+  const int nsweeps = s->g.rank == 1 ? 1 : 2 * s->g.rank;
+  const int kBatch = 3;          // steps per graph (buffer rotation period)
+  const int kChunk = 10 * kBatch;  // steps enqueued between host checks
+  bool done = false;
+  while (!done && (max_steps < 0 || committed < max_steps)) {
+    int chunk = kChunk;
+    if (max_steps >= 0) chunk = std::min(chunk, max_steps - committed);
+    // Enqueue `chunk` steps assuming they all commit; a failed check or the
+    // end time makes the remaining kernels return without touching state.
+    int cur = s->cur;
+    int64_t cycle = s->cycle;
+    int enq = 0;
+    while (enq < chunk) {
+      const int batch = std::min(kBatch, chunk - enq);
+      const auto key = std::make_tuple(cur, static_cast<int>(cycle % 2), batch);
+      auto it = s->graphs.find(key);
+      if (it == s->graphs.end()) {
+        cudaGraph_t graph;
+        FVS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        int b = cur;
+        cudaError_t e = cudaSuccess;
+        for (int q = 0; q < batch && e == cudaSuccess; ++q) {
+          e = EnqueueStep(s, b, cycle + q, q);
+          b = NextBuffer(b, nsweeps);
+        }
+        cudaError_t e2 = cudaStreamEndCapture(s->stream, &graph);
+        if (e != cudaSuccess) return CudaFail(e, "capture split step");
+        if (e2 != cudaSuccess) return CudaFail(e2, "cudaStreamEndCapture");
+        cudaGraphExec_t exec;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return CudaFail(e, "cudaGraphInstantiate");
+        it = s->graphs.emplace(key, exec).first;
+      }
+      FVS_CUDA(cudaGraphLaunch(it->second, s->stream));
+      for (int q = 0; q < batch; ++q) cur = NextBuffer(cur, nsweeps);
+      cycle += batch;
+      enq += batch;
+    }
+    FVS_CUDA(cudaMemcpyAsync(s->ctrl_host, s->ctrl, sizeof(fvs::Control),
+                             cudaMemcpyDeviceToHost, s->stream));
+    FVS_CUDA(cudaStreamSynchronize(s->stream));
+    const fvs::Control& h = *s->ctrl_host;
+    const int new_steps = h.steps_done - committed;
+    for (int q = 0; q < new_steps; ++q) s->cur = NextBuffer(s->cur, nsweeps);
+    s->cycle += new_steps;
+    committed = h.steps_done;
+    s->t = h.t;
+    if (h.abort) {
+      ++restarts;
+      const int zero = 0;
+      FVS_CUDA(cudaMemcpyAsync(&s->ctrl->abort, &zero, sizeof zero,
+                               cudaMemcpyHostToDevice, s->stream));
+      continue;
+    }
+    if (h.done) done = true;
+  }
+  if (dt_log && committed > 0) {
+    const int n = std::min(committed, dt_log_len);
+    FVS_CUDA(cudaMemcpyAsync(dt_log, s->dt_log_dev, n * sizeof(double),
+                             cudaMemcpyDeviceToHost, s->stream));
+  }
+  FVS_CUDA(cudaStreamSynchronize(s->stream));
+  const fvs::Control& h = *s->ctrl_host;
+  if (stats) {
+    stats->time = h.t;
+    stats->steps = committed;
+    stats->restarts = restarts;
+    stats->status = h.status;
+    stats->last_dt = h.dt;
+  }
+  if (h.status) return Fail(FVS_ERR_STATE, "non-positive density encountered");
+  return FVS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,102 @@
+// fvs_internal.h -- declarations shared between the translation units of
+// libfvs_gb300 (not part of the C ABI).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fvs {
+
+// Per-run control block resident in device memory.  The time step lives on
+// the device so that a whole split step (stable dt, sweeps, checks) runs
+// without a host round trip and can be captured in a CUDA graph.
+struct Control {
+  double t;          // current time point
+  double dt;         // time step of the step in flight
+  double t_end;      // final time
+  double cfl;        // CFL number
+  double fail_dt;    // level dt of the first failed per-sweep check
+  double dt_override;  // > 0: use this dt for the next step instead of cfl*stable
+  unsigned long long smax_stable[3];  // bits of max face speed, per direction
+  unsigned long long smax_check[6];   // bits of max face speed, per sweep
+  int abort;         // a per-sweep check failed; later kernels do nothing
+  int done;          // t reached t_end; later kernels do nothing
+  int failed_step;   // index of the failed step within the batch
+  int steps_done;    // committed steps since the counter was reset
+  int status;        // FVS_STATUS_* bits of committed steps
+  int step_status;   // status bits of the step in flight
+  int have_failure;  // next step uses fail_dt instead of the stable dt pass
+  int pad;
+};
+
+enum StatusBits : int {
+  kStatusNonPositiveDensity = 1,
+  kStatusNonFinite = 2,
+  kStatusNewtonNotConverged = 4,
+};
+
+// One directional sweep of a uniform grid: fluxes, conservative update and
+// the CFL reduction of the input state, in one pass.
+struct SweepArgs {
+  const double* in;     // conservative state, component-major [D+2][nz][ny][nx]
+  double* out;          // updated state, same layout (must not alias `in`)
+  int n[3];
+  int rank;
+  int dir;
+  int bc;               // 0 periodic, 1 transmissive (in `dir`)
+  int limiter;
+  int seg_len;          // cells per thread segment along `dir`
+  int block;            // threads per block
+  double gamma;
+  double dx;
+  // split dt = dt_scale * (*dt_ptr) when dt_ptr is set, else dt_value
+  const double* dt_ptr;
+  double dt_scale;
+  double dt_value;
+  unsigned long long* smax_out;  // atomicMax of the input state's face speeds
+  Control* ctrl;        // optional: abort/done gating and status bits
+  // previous sweep's check (skip this sweep when it failed); -1 for none
+  int prev_check;
+  double prev_dx;
+};
+
+// Stable-dt pass over all directions (max face speed per direction).
+struct StableDtArgs {
+  const double* in;
+  int n[3];
+  int rank;
+  int bc[3];
+  int rule;             // 0 all faces, 1 reference MFIter tiles of 8 in y/z
+  double gamma;
+  unsigned long long* smax_out;  // [rank]
+  Control* ctrl;
+};
+
+// Exact FP64 kernels (fvs_kernels_exact.cu, compiled with -fmad=false).
+cudaError_t LaunchSweepExact(const SweepArgs& a, cudaStream_t s);
+cudaError_t LaunchStableDtExact(const StableDtArgs& a, cudaStream_t s);
+
+// Patch-level kernels over FArrayBox-layout views (fvs_kernels_exact.cu).
+struct BoxDesc {
+  int lo[3];
+  int n[3];
+};
+cudaError_t LaunchPatchFluxesExact(int method, int limiter, int rank, double gamma,
+                                   double* fluxes, BoxDesc fbox,
+                                   const double* states, BoxDesc cbox,
+                                   double dt, double dx, int dir,
+                                   cudaStream_t s);
+cudaError_t LaunchPatchStableDtExact(int method, int rank, double gamma,
+                                     const double* states, BoxDesc cbox,
+                                     int window_rule, int dir,
+                                     unsigned long long* smax, cudaStream_t s);
+cudaError_t LaunchPatchUpdate(double* next, BoxDesc nbox, const double* prev,
+                              BoxDesc pbox, const double* fluxes, BoxDesc fbox,
+                              int ncomp, double dt, double dx, int dir,
+                              cudaStream_t s);
+cudaError_t LaunchPatchCompleteFromCons(int rank, double gamma, double* complete,
+                                        BoxDesc qbox, const double* cons,
+                                        BoxDesc ubox, BoxDesc region,
+                                        cudaStream_t s);
+
+}  // namespace fvs

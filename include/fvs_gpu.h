@@ -1,0 +1,203 @@
+/* fvs_gpu.h -- C ABI of libfvs_gb300: the GB300 (sm_103a) split
+ * finite-volume patch update for the perfect-gas Euler equations.
+ *
+ * This library is a drop-in for the patch-level calls of
+ * maikel/FiniteVolumeSolver's FluxMethod / HyperbolicPatchIntegrator API:
+ * ComputeNumericFluxes, ComputeStableDt and UpdateConservatively on a ghosted
+ * patch, one direction at a time, plus CompleteFromCons.  A solver context
+ * runs whole split steps on a device-resident uniform grid.
+ *
+ * Conventions
+ *  - Patch data uses the reference's FArrayBox layout: component-major,
+ *    x fastest; element (c, i, j, k) of a box [lo, hi) is at
+ *    ((c*n2 + k-lo2)*n1 + j-lo1)*n0 + i-lo0 with n = hi - lo
+ *    (include/fub/AMReX/ViewFArrayBox.hpp:73-82).  Unused dimensions have
+ *    lo = 0, hi = 1.
+ *  - Complete states have rank+4 components (rho, m[rank], E, p, c);
+ *    conservative states rank+2 (rho, m[rank], E)
+ *    (include/fub/equations/PerfectGas.hpp:132-161).
+ *  - Face boxes follow AMReX: face i in direction d lies between cells i-1
+ *    and i.
+ *  - Pointers named *_dev are device pointers; `stream` is a cudaStream_t
+ *    (NULL = legacy default stream).
+ *  - Every call returns an fvs_status.  The library never falls back to a
+ *    CPU path: without a usable GPU the calls return FVS_ERR_NO_DEVICE.
+ */
+#ifndef FVS_GPU_H
+#define FVS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum fvs_status {
+  FVS_OK = 0,
+  FVS_ERR_INVALID = 1,        /* bad argument (box, rank, direction, ...) */
+  FVS_ERR_CUDA = 2,           /* a CUDA call failed; see fvs_last_error() */
+  FVS_ERR_DT_TOO_LARGE = 3,   /* a per-sweep CFL check failed */
+  FVS_ERR_UNSUPPORTED = 4,    /* method / precision not available here */
+  FVS_ERR_NO_DEVICE = 5,      /* no CUDA device */
+  FVS_ERR_STATE = 6           /* non-positive density / non-finite state */
+} fvs_status;
+
+typedef enum fvs_flux_method {
+  FVS_MUSCL_HLLE = 0,   /* MusclHancock<PerfectGas, Hll<Einfeldt>, Limiter> */
+  FVS_HLLE = 1,         /* Hll<PerfectGas, EinfeldtSignalVelocities> */
+  FVS_GODUNOV = 2,      /* Godunov<PerfectGas, ExactRiemannSolver> */
+  FVS_MUSCL_GODUNOV = 3 /* MusclHancock<PerfectGas, Godunov<Exact>, Limiter> */
+} fvs_flux_method;
+
+typedef enum fvs_limiter {
+  FVS_VAN_LEER = 0,
+  FVS_MINMOD = 1,
+  FVS_NO_LIMITER = 2
+} fvs_limiter;
+
+typedef enum fvs_precision {
+  FVS_FP64_EXACT = 0, /* reference operation order, no FMA: bit-identical */
+  FVS_FP64_FAST = 1,  /* FP64 with FMA and shared reciprocals (<= 1e-12 rel) */
+  FVS_MIXED = 2       /* FP32 reconstruction/flux, FP64 state and update */
+} fvs_precision;
+
+typedef enum fvs_guess {
+  FVS_GUESS_MEAN = 0,    /* reference: 0.5 (pL + pR) */
+  FVS_GUESS_PVRS_TR = 1, /* PVRS, two-rarefaction below min(pL, pR) */
+  FVS_GUESS_MLP = 2      /* learned guess, PVRS/TR fallback */
+} fvs_guess;
+
+typedef enum fvs_bc {
+  FVS_BC_PERIODIC = 0,
+  FVS_BC_TRANSMISSIVE = 1
+} fvs_bc;
+
+typedef struct fvs_box {
+  int32_t lo[3];
+  int32_t hi[3]; /* half-open */
+} fvs_box;
+
+typedef struct fvs_method {
+  int32_t flux_method;   /* fvs_flux_method */
+  int32_t limiter;       /* fvs_limiter */
+  int32_t precision;     /* fvs_precision */
+  int32_t guess;         /* fvs_guess (exact Riemann solver only) */
+  int32_t max_iterations;/* Newton iteration bound (exact solver) */
+  int32_t reserved;
+  double tolerance;      /* Newton tolerance on |f(p)| (reference: 1e-7) */
+  double gamma;          /* ratio of specific heats (reference: 1.4) */
+} fvs_method;
+
+/* Fills `m` with the reference's defaults: MUSCL-Hancock + HLLE, van Leer,
+ * exact FP64, mean guess, 5000 iterations, tolerance 1e-7, gamma 1.4. */
+void fvs_method_default(fvs_method* m);
+
+const char* fvs_last_error(void);
+int fvs_abi_version(void);
+/* Number of CUDA devices visible (0 without a GPU); never fails. */
+int fvs_device_count(void);
+
+/* ---- Patch level: drop-in for the reference's per-patch calls ---------- */
+
+/* FluxMethod<Base>::ComputeNumericFluxes(View<Conservative> fluxes,
+ *   View<const Complete> states, Duration dt, double dx, Direction dir)
+ * include/fub/flux_method/FluxMethod.hpp:115-134, 200-293.
+ * `states_dev` holds rank+4 components over `cell_box`, which must contain
+ * every stencil cell of every face of `face_box` (w = 2 for MUSCL, 1 for
+ * HLLE/Godunov); `fluxes_dev` receives rank+2 components over `face_box`. */
+int fvs_compute_numeric_fluxes(const fvs_method* m, int rank,
+                               double* fluxes_dev, fvs_box face_box,
+                               const double* states_dev, fvs_box cell_box,
+                               double dt, double dx, int dir, void* stream);
+
+/* FluxMethod<Base>::ComputeStableDt(View<const Complete> states, double dx,
+ * Direction dir)  include/fub/flux_method/FluxMethod.hpp:154-170, 295-382.
+ * window_rule 0 = sequential tag windows, 1 = simd tag windows (the
+ * reference's default OpenMpSimdTag).  Synchronises `stream`; writes the
+ * minimum stable dt of the patch to *dt_out (host). */
+int fvs_compute_stable_dt(const fvs_method* m, int rank,
+                          const double* states_dev, fvs_box cell_box,
+                          double dx, int dir, int window_rule, double* dt_out,
+                          void* stream);
+
+/* HyperbolicPatchIntegrator<Tag>::UpdateConservatively(next, prev, fluxes,
+ * dt, dx, dir)  include/fub/HyperbolicPatchIntegrator.hpp:34-54,
+ * src/HyperbolicPatchIntegrator.cpp:35-105:
+ *   next = prev + dt/dx (F[face i] - F[face i+1]), `ncomp` components.
+ * next_box is the updated region; prev_box / face_box are the boxes the
+ * prev / fluxes arrays are laid out over. */
+int fvs_update_conservatively(double* next_dev, fvs_box next_box,
+                              const double* prev_dev, fvs_box prev_box,
+                              const double* fluxes_dev, fvs_box face_box,
+                              int ncomp, double dt, double dx, int dir,
+                              void* stream);
+
+/* PerfectGas<D>::CompleteFromCons over `region` (src/equations/
+ * PerfectGas.cpp:96-124; the scratch update of include/fub/AMReX/
+ * Reconstruction.hpp:44-60).  cons: rank+2 components over cons_box,
+ * complete: rank+4 components over complete_box. */
+int fvs_complete_from_cons(int rank, double gamma, double* complete_dev,
+                           fvs_box complete_box, const double* cons_dev,
+                           fvs_box cons_box, fvs_box region, void* stream);
+
+/* ---- Solver context: a uniform single-level grid ----------------------- */
+
+typedef struct fvs_grid_desc {
+  int32_t rank;
+  int32_t n[3];   /* cells per direction (1 for unused directions) */
+  int32_t bc[3];  /* fvs_bc per direction */
+  int32_t dt_rule;/* 0: every face; 1: the reference's MFIter tile rule */
+  double dx[3];
+} fvs_grid_desc;
+
+typedef struct fvs_solver fvs_solver;
+
+typedef struct fvs_run_stats {
+  double time;          /* time point reached */
+  int32_t steps;        /* committed steps */
+  int32_t restarts;     /* steps redone after a failed CFL check */
+  int32_t status;       /* state status bits of committed steps */
+  int32_t reserved;
+  double last_dt;
+} fvs_run_stats;
+
+int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
+                      fvs_solver** out);
+int fvs_solver_destroy(fvs_solver* s);
+/* Conservative state, rank+2 components, [c][nz][ny][nx], host memory. */
+int fvs_solver_upload(fvs_solver* s, const double* cons_host);
+int fvs_solver_download(fvs_solver* s, double* cons_host);
+/* Device pointer of the current state (valid until the next call). */
+int fvs_solver_state_device(fvs_solver* s, double** cons_dev);
+/* Threads per block / cells per thread segment of the sweep kernels
+ * (0 = automatic). */
+int fvs_solver_set_tiling(fvs_solver* s, int seg_len);
+/* Stable dt of the current state: dir = -1 for the minimum over all
+ * directions (DimensionalSplitLevelIntegrator::ComputeStableDt). */
+int fvs_solver_stable_dt(fvs_solver* s, int dir, double* dt_out);
+/* One fused sweep in `dir` with time step `dt`: fluxes + update + the CFL
+ * reduction of the input state; *level_dt_out (may be NULL) receives the
+ * input state's stable dt in `dir`. */
+int fvs_solver_sweep(fvs_solver* s, int dir, double dt, double* level_dt_out);
+/* One split step of size dt (Strang for rank >= 2; direction order reversed
+ * on odd cycles).  Returns FVS_ERR_DT_TOO_LARGE (state unchanged) when a
+ * per-sweep check fails. */
+int fvs_solver_step(fvs_solver* s, double dt, int cycle);
+/* RunSimulation without outputs: steps with dt = min(t_end - t,
+ * cfl * stable_dt) until t_end or max_steps (< 0: unbounded), redoing a
+ * step with the failed check's dt like the reference's backup/restart.
+ * The time step stays on the device; steps run as CUDA graphs.
+ * dt_log (host, may be NULL) receives up to `dt_log_len` committed dts. */
+int fvs_solver_run(fvs_solver* s, double cfl, double t_end, int max_steps,
+                   double* dt_log, int dt_log_len, fvs_run_stats* stats);
+/* The solver's CUDA stream (cudaStream_t): every solver call runs on it. */
+int fvs_solver_stream(fvs_solver* s, void** stream);
+/* Cycle counter used for the direction order of the next step. */
+int fvs_solver_set_cycle(fvs_solver* s, int64_t cycle);
+int fvs_solver_set_time(fvs_solver* s, double t);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FVS_GPU_H */

@@ -1,0 +1,311 @@
+// fvs_oracle.hpp -- CPU oracle for the split finite-volume patch update.
+//
+// TEST INFRASTRUCTURE ONLY.  This is a scalar C++17 restatement of the
+// reference's (maikel/FiniteVolumeSolver) perfect-gas Euler patch update,
+// written to reproduce its arithmetic operation by operation so that the GPU
+// kernels can be checked against it.  Only tests/, __graft_entry__.smoke()
+// and the CPU-baseline leg of bench.py may load it; the product path never
+// does.
+//
+// Build flags: -O2 -ffp-contract=off -fno-fast-math (no FMA contraction), the
+// same IEEE behaviour as the reference's x86-64 SSE2 build (CMakeLists.txt
+// sets no -march and no fast-math).
+//
+// Every function names the reference file:line it follows.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <limits>
+
+namespace fvs_oracle {
+
+// PerfectGas<D> parameters: include/fub/equations/PerfectGas.hpp:207-211.
+struct Gas {
+  double gamma = 1.4;
+  double gamma_minus_1_inv = 1.0 / (1.4 - 1.0);
+};
+
+template <int D> struct Cons {
+  double rho;
+  double m[D];
+  double E;
+};
+
+// Complete state component order (rho, m[D], E, p, c):
+// include/fub/equations/PerfectGas.hpp:132-161.
+template <int D> struct Complete {
+  double rho;
+  double m[D];
+  double E;
+  double p;
+  double c;
+};
+
+// sum_d m_d^2 in the evaluation order of the reference's array (production)
+// path: Eigen's colwise().squaredNorm() over the row-major Dim x 8 momentum
+// block uses the default (non-vectorised, fully unrolled) traversal, which
+// splits the sum recursively into halves: m0^2 + (m1^2 + m2^2) for D = 3.
+// src/equations/PerfectGas.cpp:32-37.
+template <int D> inline double SquaredNorm(const double* m) {
+  if constexpr (D == 1) {
+    return m[0] * m[0];
+  } else if constexpr (D == 2) {
+    return m[0] * m[0] + m[1] * m[1];
+  } else {
+    return m[0] * m[0] + (m[1] * m[1] + m[2] * m[2]);
+  }
+}
+
+// KineticEnergy: 0.5 * |m|^2 / rho.  src/equations/PerfectGas.cpp:25-37.
+template <int D> inline double KineticEnergy(double rho, const double* m) {
+  return 0.5 * SquaredNorm<D>(m) / rho;
+}
+
+// PerfectGas<D>::CompleteFromCons  src/equations/PerfectGas.cpp:96-124.
+// Note the pressure is e_int DIVIDED by gamma_minus_1_inv (not multiplied by
+// gamma - 1).
+template <int D>
+inline void CompleteFromCons(const Gas& eq, Complete<D>& q, const double* u) {
+  q.rho = u[0];
+  for (int d = 0; d < D; ++d) q.m[d] = u[1 + d];
+  q.E = u[1 + D];
+  const double e_kin = KineticEnergy<D>(q.rho, q.m);
+  const double e_int = q.E - e_kin;
+  q.p = e_int / eq.gamma_minus_1_inv;
+  q.c = std::sqrt(eq.gamma * q.p / q.rho);
+}
+
+// Masked CompleteFromCons: zero where the mask is false or rho <= 0.
+// src/equations/PerfectGas.cpp:126-144.
+template <int D>
+inline void CompleteFromConsMasked(const Gas& eq, Complete<D>& q,
+                                   const double* u, bool mask) {
+  mask = mask && (u[0] > 0.0);
+  if (!mask) {
+    q.rho = 0.0;
+    for (int d = 0; d < D; ++d) q.m[d] = 0.0;
+    q.E = 0.0;
+    q.p = 0.0;
+    q.c = 0.0;
+    return;
+  }
+  CompleteFromCons<D>(eq, q, u);
+}
+
+template <int D> inline void AsCons(double* u, const Complete<D>& q) {
+  u[0] = q.rho;
+  for (int d = 0; d < D; ++d) u[1 + d] = q.m[d];
+  u[1 + D] = q.E;
+}
+
+// PerfectGas<D>::Flux  src/equations/PerfectGas.cpp:52-77.
+template <int D>
+inline void Flux(double* f, const Complete<D>& q, int dir) {
+  const double velocity = q.m[dir] / q.rho;
+  f[0] = q.m[dir];
+  for (int d = 0; d < D; ++d) f[1 + d] = velocity * q.m[d];
+  f[1 + dir] += q.p;
+  f[1 + D] = velocity * (q.E + q.p);
+}
+
+// Masked flux: rho replaced by 1 where the mask is false or rho <= 0.
+// src/equations/PerfectGas.cpp:79-93.
+template <int D>
+inline void FluxMasked(double* f, const Complete<D>& q, bool mask, int dir) {
+  mask = mask && (q.rho > 0.0);
+  const double rho = mask ? q.rho : 1.0;
+  const double velocity = q.m[dir] / rho;
+  f[0] = q.m[dir];
+  for (int d = 0; d < D; ++d) f[1 + d] = velocity * q.m[d];
+  f[1 + dir] += q.p;
+  f[1 + D] = velocity * (q.E + q.p);
+}
+
+// Eigen's SSE2 packet min / max (_mm_min_pd / _mm_max_pd semantics), used by
+// the reference's array path.
+inline double PMin(double a, double b) { return a < b ? a : b; }
+inline double PMax(double a, double b) { return a > b ? a : b; }
+
+// EinfeldtSignalVelocities<PerfectGas<D>>
+// src/equations/perfect_gas/EinfeldtSignalVelocities.hpp:25-97.
+template <int D>
+inline void Einfeldt(const Gas& eq, const Complete<D>& L, const Complete<D>& R,
+                     int dir, double& sL, double& sR) {
+  const double rhoL = L.rho;
+  const double rhoR = R.rho;
+  const double rhoUL = L.m[dir];
+  const double rhoUR = R.m[dir];
+  const double aL = L.c;
+  const double aR = R.c;
+  const double sqRhoL = std::sqrt(rhoL);
+  const double sqRhoR = std::sqrt(rhoR);
+  const double oosqRhoSum = 1.0 / (sqRhoL + sqRhoR);
+  const double uL = rhoUL / rhoL;
+  const double uR = rhoUR / rhoR;
+  const double roeU = (uL * sqRhoL + uR * sqRhoR) * oosqRhoSum;
+  const double hL = (L.E + L.p) / rhoL;
+  const double hR = (R.E + R.p) / rhoR;
+  const double roeH = (hL * sqRhoL + hR * sqRhoR) * oosqRhoSum;
+  const double roeA2 = (eq.gamma - 1.0) * (roeH - 0.5 * roeU * roeU);
+  const double roeA = std::sqrt(roeA2);
+  const double sL1 = uL - aL;
+  const double sL2 = roeU - roeA;
+  const double sR1 = roeU + roeA;
+  const double sR2 = uR + aR;
+  sL = PMin(sL1, sL2);
+  sR = PMax(sR1, sR2);
+}
+
+// Masked Einfeldt: uses sqrt(rho)/sum weights (a different operation order).
+// src/equations/perfect_gas/EinfeldtSignalVelocities.hpp:99-142.
+template <int D>
+inline void EinfeldtMasked(const Gas& eq, const Complete<D>& L,
+                           const Complete<D>& R, bool mask, int dir,
+                           double& sL, double& sR) {
+  const double rhoL = L.rho;
+  const double rhoR = R.rho;
+  const double rhoUL = mask ? L.m[dir] : 0.0;
+  const double rhoUR = mask ? R.m[dir] : 0.0;
+  const double aL = mask ? L.c : 0.0;
+  const double aR = mask ? R.c : 0.0;
+  const double rhoLs = mask ? rhoL : 1.0;
+  const double rhoRs = mask ? rhoR : 1.0;
+  const double sqRhoL = std::sqrt(rhoLs);
+  const double sqRhoR = std::sqrt(rhoRs);
+  const double sqRho = sqRhoL + sqRhoR;
+  const double uL = rhoUL / rhoLs;
+  const double uR = rhoUR / rhoRs;
+  const double wL = sqRhoL / sqRho;
+  const double wR = sqRhoR / sqRho;
+  const double roeU = uL * wL + uR * wR;
+  const double rhoEL = mask ? L.E : 0.0;
+  const double rhoER = mask ? R.E : 0.0;
+  const double pL = mask ? L.p : 0.0;
+  const double pR = mask ? R.p : 0.0;
+  // the reference divides by the unmasked densities here
+  const double hL = (rhoEL + pL) / rhoL;
+  const double hR = (rhoER + pR) / rhoR;
+  const double roeH = hL * wL + hR * wR;
+  const double roeA2 = (eq.gamma - 1.0) * (roeH - 0.5 * roeU * roeU);
+  const double roeA = std::sqrt(roeA2);
+  sL = PMin(uL - aL, roeU - roeA);
+  sR = PMax(roeU + roeA, uR + aR);
+}
+
+// Hll<Eq, Einfeldt>::ComputeNumericFlux (array path)
+// include/fub/flux_method/HllMethod.hpp:260-293.
+template <int D>
+inline void HllFlux(const Gas& eq, double* nf, const Complete<D>& L,
+                    const Complete<D>& R, int dir) {
+  double s0, s1;
+  Einfeldt<D>(eq, L, R, dir, s0, s1);
+  double fL[D + 2], fR[D + 2], qL[D + 2], qR[D + 2];
+  Flux<D>(fL, L, dir);
+  Flux<D>(fR, R, dir);
+  AsCons<D>(qL, L);
+  AsCons<D>(qR, R);
+  const double sL = PMin(s0, 0.0);
+  const double sR = PMax(s1, 0.0);
+  const double sLsR = sL * sR;
+  double ds = sR - sL;
+  ds = (ds > 0.0) ? ds : 1.0;
+  for (int k = 0; k < D + 2; ++k) {
+    nf[k] = (sR * fL[k] - sL * fR[k] + sLsR * (qR[k] - qL[k])) / ds;
+  }
+}
+
+// Hll<Eq, Einfeldt>::ComputeStableDt  include/fub/flux_method/HllMethod.hpp:337-347.
+template <int D>
+inline double HllStableDt(const Gas& eq, const Complete<D>& L,
+                          const Complete<D>& R, double dx, int dir) {
+  double s0, s1;
+  Einfeldt<D>(eq, L, R, dir, s0, s1);
+  const double mx = PMax(PMax(0.0, std::abs(s0)), std::abs(s1));
+  return dx / mx;
+}
+
+// Hll<Eq, Einfeldt>::SolveRiemannProblem (scalar path, completes the
+// middle state)  include/fub/flux_method/HllMethod.hpp:161-184.
+template <int D>
+inline void HllRiemannState(const Gas& eq, Complete<D>& sol,
+                            const Complete<D>& L, const Complete<D>& R,
+                            int dir) {
+  double sL, sR;
+  Einfeldt<D>(eq, L, R, dir, sL, sR);
+  double fL[D + 2], fR[D + 2], qL[D + 2], qR[D + 2];
+  Flux<D>(fL, L, dir);
+  Flux<D>(fR, R, dir);
+  AsCons<D>(qL, L);
+  AsCons<D>(qR, R);
+  const double ds = sL != sR ? sR - sL : 1.0;
+  if (0.0 < sL) {
+    sol = L;
+  } else if (sR < 0.0) {
+    sol = R;
+  } else {
+    double u[D + 2];
+    for (int k = 0; k < D + 2; ++k) {
+      u[k] = (sR * qR[k] - sL * qL[k] + fL[k] - fR[k]) / ds;
+    }
+    CompleteFromCons<D>(eq, sol, u);
+  }
+}
+
+// Slope limiters  include/fub/flux_method/MusclHancockMethod.hpp:92-187.
+enum Limiter : int { kVanLeer = 0, kMinMod = 1, kNoLimiter = 2 };
+
+inline double VanLeer(double sL, double sR) {
+  const double c = 2.0 * sL * sR;
+  return (c > 0.0) ? c / (sL + sR) : 0.0;
+}
+
+inline double MinMod(double sL, double sR) {
+  // array path: (sR > 0).select(zero.max(sL.min(sR)), zero.min(sL.max(sR)))
+  return (sR > 0) ? PMax(0.0, PMin(sL, sR)) : PMin(0.0, PMax(sL, sR));
+}
+
+inline double LimitedSlope(int limiter, double qL, double qM, double qR) {
+  const double sL = qM - qL;
+  const double sR = qR - qM;
+  switch (limiter) {
+  case kMinMod:
+    return MinMod(sL, sR);
+  case kNoLimiter:
+    return 0.0;
+  default:
+    return VanLeer(sL, sR);
+  }
+}
+
+// One half of MusclHancock::ComputeNumericFlux: the predicted (Hancock) state
+// of a cell at its right face (side = +1, "rec_[0]") or its left face
+// (side = -1, "rec_[1]").  q0, q1, q2 are the cell's left neighbour, the cell
+// and its right neighbour.  include/fub/flux_method/MusclHancockMethod.hpp:419-485.
+template <int D>
+inline void MusclPredict(const Gas& eq, Complete<D>& rec, const double* q0,
+                         const double* q1, const double* q2, int limiter,
+                         double lambda_half, int dir, int side) {
+  constexpr int K = D + 2;
+  double slope[K], uL[K], uR[K];
+  for (int k = 0; k < K; ++k) slope[k] = LimitedSlope(limiter, q0[k], q1[k], q2[k]);
+  for (int k = 0; k < K; ++k) {
+    uL[k] = q1[k] - 0.5 * slope[k];
+    uR[k] = q1[k] + 0.5 * slope[k];
+  }
+  Complete<D> qL, qR;
+  CompleteFromCons<D>(eq, qL, uL);
+  CompleteFromCons<D>(eq, qR, uR);
+  double fL[K], fR[K];
+  Flux<D>(fL, qL, dir);
+  Flux<D>(fR, qR, dir);
+  double u[K];
+  const double* base = side > 0 ? uR : uL;
+  for (int k = 0; k < K; ++k) u[k] = base[k] + lambda_half * (fL[k] - fR[k]);
+  CompleteFromCons<D>(eq, rec, u);
+}
+
+enum Method : int { kMusclHlle = 0, kHlle = 1, kGodunov = 2, kMusclGodunov = 3 };
+
+}  // namespace fvs_oracle

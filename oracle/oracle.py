@@ -1,0 +1,196 @@
+"""ctypes bindings of the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product package.  The oracle is a
+scalar C++17 restatement of maikel/FiniteVolumeSolver's perfect-gas patch
+update (see fvs_oracle.hpp for the file:line citations).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+MUSCL_HLLE, HLLE, GODUNOV, MUSCL_GODUNOV = 0, 1, 2, 3
+VAN_LEER, MINMOD, NO_LIMITER = 0, 1, 2
+GUESS_MEAN, GUESS_PVRS_TR, GUESS_GIVEN = 0, 1, 2
+
+
+class OrcMethod(C.Structure):
+    _fields_ = [("method", C.c_int32), ("limiter", C.c_int32), ("guess", C.c_int32),
+                ("max_iterations", C.c_int32), ("tol", C.c_double)]
+
+
+def method(kind=MUSCL_HLLE, limiter=VAN_LEER, guess=GUESS_MEAN, max_iterations=5000,
+           tol=1e-7) -> OrcMethod:
+    return OrcMethod(kind, limiter, guess, max_iterations, tol)
+
+
+_lib = None
+_P = C.POINTER(C.c_double)
+_I32 = C.POINTER(C.c_int32)
+_I64 = C.POINTER(C.c_int64)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        M = C.POINTER(OrcMethod)
+        L.orc_complete_from_cons.argtypes = [C.c_int, C.c_int64, _P, _P]
+        L.orc_compute_numeric_fluxes.argtypes = [M, C.c_int, _P, _I32, _I32, _P, _I32, _I32,
+                                                 C.c_double, C.c_double, C.c_int, _I64, _I64]
+        L.orc_compute_numeric_fluxes.restype = C.c_int
+        L.orc_compute_stable_dt.argtypes = [M, C.c_int, _P, _I32, _I32, C.c_double, C.c_int,
+                                            C.c_int]
+        L.orc_compute_stable_dt.restype = C.c_double
+        L.orc_update_conservatively.argtypes = [_P, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32,
+                                                C.c_int, C.c_double, C.c_double, C.c_int]
+        L.orc_grid_sweep.argtypes = [M, C.c_int, _I32, _I32, _P, _P, _P, C.c_double, C.c_int,
+                                     C.c_int, _I64, _I64]
+        L.orc_grid_stable_dt.argtypes = [M, C.c_int, _I32, _I32, _P, _P, C.c_int, C.c_int,
+                                         C.c_int]
+        L.orc_grid_stable_dt.restype = C.c_double
+        L.orc_grid_step.argtypes = [M, C.c_int, _I32, _I32, _P, _P, C.c_double, C.c_int,
+                                    C.c_int]
+        L.orc_grid_step.restype = C.c_int
+        L.orc_run.argtypes = [M, C.c_int, _I32, _I32, _P, _P, C.c_double, C.c_double, C.c_int,
+                              C.c_int, _P, C.c_int, _P, C.POINTER(C.c_int), C.c_int, _I64, _I64]
+        L.orc_run.restype = C.c_int
+        L.orc_exact_star.argtypes = [C.c_int64, _P, _P, _P, _P, _P, _P, C.c_int, _P, C.c_double,
+                                     C.c_int, _P, _P, _I32, _I32]
+        L.orc_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _d(a: np.ndarray):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_P)
+
+
+def _i3(v):
+    a = (C.c_int32 * 3)(*[int(x) for x in v])
+    return a
+
+
+def _pad3(v, fill):
+    v = list(v)
+    return v + [fill] * (3 - len(v))
+
+
+def max_threads() -> int:
+    return int(lib().orc_max_threads())
+
+
+def complete_from_cons(rank: int, cons: np.ndarray) -> np.ndarray:
+    """cons: (rank+2, n) -> complete (rank+4, n)."""
+    cons = np.ascontiguousarray(cons, dtype=np.float64)
+    n = cons.shape[1]
+    out = np.zeros((rank + 4, n))
+    lib().orc_complete_from_cons(rank, n, _d(cons), _d(out))
+    return out
+
+
+def compute_numeric_fluxes(m: OrcMethod, rank, states, cell_box, face_box, dt, dx, dir):
+    """states: (rank+4, nz, ny, nx) over cell_box; returns fluxes over face_box."""
+    states = np.ascontiguousarray(states, dtype=np.float64)
+    flo, fhi = _pad3(face_box[0], 0), _pad3(face_box[1], 1)
+    clo, chi = _pad3(cell_box[0], 0), _pad3(cell_box[1], 1)
+    shape = (rank + 2, fhi[2] - flo[2], fhi[1] - flo[1], fhi[0] - flo[0])
+    fluxes = np.zeros(shape)
+    it = C.c_int64(0)
+    fl = C.c_int64(0)
+    lib().orc_compute_numeric_fluxes(C.byref(m), rank, _d(fluxes), _i3(flo), _i3(fhi),
+                                     _d(states), _i3(clo), _i3(chi), dt, dx, dir,
+                                     C.byref(it), C.byref(fl))
+    return fluxes
+
+
+def compute_stable_dt(m: OrcMethod, rank, states, cell_box, dx, dir, window_rule=1):
+    states = np.ascontiguousarray(states, dtype=np.float64)
+    clo, chi = _pad3(cell_box[0], 0), _pad3(cell_box[1], 1)
+    return lib().orc_compute_stable_dt(C.byref(m), rank, _d(states), _i3(clo), _i3(chi), dx,
+                                       dir, window_rule)
+
+
+def update_conservatively(next_box, prev, prev_box, fluxes, face_box, dt, dx, dir):
+    prev = np.ascontiguousarray(prev, dtype=np.float64)
+    fluxes = np.ascontiguousarray(fluxes, dtype=np.float64)
+    nlo, nhi = _pad3(next_box[0], 0), _pad3(next_box[1], 1)
+    ncomp = prev.shape[0]
+    out = np.full((ncomp, nhi[2] - nlo[2], nhi[1] - nlo[1], nhi[0] - nlo[0]), np.nan)
+    lib().orc_update_conservatively(
+        _d(out), _i3(nlo), _i3(nhi), _d(prev), _i3(_pad3(prev_box[0], 0)),
+        _i3(_pad3(prev_box[1], 1)), _d(fluxes), _i3(_pad3(face_box[0], 0)),
+        _i3(_pad3(face_box[1], 1)), ncomp, dt, dx, dir)
+    return out
+
+
+class Grid:
+    """A uniform single-patch grid; cons arrays are (rank+2, nz, ny, nx)."""
+
+    def __init__(self, rank, n, bc, dx):
+        self.rank = rank
+        self.n = _pad3(n, 1)
+        self.bc = _pad3(bc, 0)
+        self.dx = np.array(_pad3(dx, 1.0), dtype=np.float64)
+
+    def _args(self):
+        return _i3(self.n), _i3(self.bc), _d(self.dx)
+
+    def sweep(self, m, cons, dt, dir, nthreads=0):
+        cons = np.ascontiguousarray(cons, dtype=np.float64)
+        out = np.empty_like(cons)
+        n, bc, dx = self._args()
+        lib().orc_grid_sweep(C.byref(m), self.rank, n, bc, dx, _d(cons), _d(out), dt, dir,
+                             nthreads, None, None)
+        return out
+
+    def stable_dt(self, m, cons, dir=-1, rule=0, nthreads=0):
+        cons = np.ascontiguousarray(cons, dtype=np.float64)
+        n, bc, dx = self._args()
+        return lib().orc_grid_stable_dt(C.byref(m), self.rank, n, bc, dx, _d(cons), dir, rule,
+                                        nthreads)
+
+    def step(self, m, cons, dt, cycle, nthreads=0):
+        cons = np.array(cons, dtype=np.float64, copy=True, order="C")
+        n, bc, dx = self._args()
+        lib().orc_grid_step(C.byref(m), self.rank, n, bc, dx, _d(cons), dt, cycle, nthreads)
+        return cons
+
+    def run(self, m, cons, cfl, t_end, max_steps=-1, dt_rule=0, dt_override=None,
+            nthreads=0):
+        cons = np.array(cons, dtype=np.float64, copy=True, order="C")
+        n, bc, dx = self._args()
+        cap = max_steps if max_steps >= 0 else 100000
+        log = np.zeros(max(cap, 1))
+        restarts = C.c_int(0)
+        if dt_override is not None:
+            dto = np.ascontiguousarray(dt_override, dtype=np.float64)
+            dptr, nov = _d(dto), len(dto)
+        else:
+            dptr, nov = None, 0
+        steps = lib().orc_run(C.byref(m), self.rank, n, bc, dx, _d(cons), cfl, t_end,
+                              max_steps, dt_rule, dptr, nov, _d(log), C.byref(restarts),
+                              nthreads, None, None)
+        return cons, log[:steps].copy(), restarts.value
+
+
+def exact_star(rhoL, uL, pL, rhoR, uR, pR, guess=GUESS_MEAN, given=None, tol=1e-7,
+               max_iterations=5000):
+    arrs = [np.ascontiguousarray(np.atleast_1d(x), dtype=np.float64)
+            for x in (rhoL, uL, pL, rhoR, uR, pR)]
+    n = len(arrs[0])
+    ps, us = np.zeros(n), np.zeros(n)
+    it = np.zeros(n, dtype=np.int32)
+    cv = np.zeros(n, dtype=np.int32)
+    g = None if given is None else np.ascontiguousarray(given, dtype=np.float64)
+    lib().orc_exact_star(n, *[_d(a) for a in arrs], guess, None if g is None else _d(g), tol,
+                         max_iterations, _d(ps), _d(us), it.ctypes.data_as(_I32),
+                         cv.ctypes.data_as(_I32))
+    return ps, us, it, cv

@@ -1,0 +1,222 @@
+"""CPU tests of the oracle: pinned against the reference's own test vectors,
+the independent golden vectors of tests/golden/make_golden.py and published
+exact Riemann solutions."""
+import math
+
+import numpy as np
+import pytest
+
+X, Y, Z = 0, 1, 2
+
+
+def fromhex(a):
+    return np.array([float.fromhex(x) for x in a])
+
+
+def test_update_hand_vectors(orc, golden):
+    # tests/test.HyperbolicSplitPatchIntegrator.cpp:37-71
+    g = golden["update_1cell"]
+    prev = np.array(g["prev"]).reshape(1, 1, 1, 1)
+    flux = np.array(g["flux"]).reshape(1, 1, 1, 2)
+    out = orc.update_conservatively(((0,), (1,)), prev, ((0,), (1,)), flux, ((0,), (2,)),
+                                    1.0, 1.0, 0)
+    assert out[0, 0, 0, 0] == pytest.approx(0.9)
+    assert out.ravel()[0] == fromhex(g["next"])[0]
+    g = golden["update_8cell"]
+    prev = np.array(g["prev"]).reshape(1, 1, 1, 8)
+    flux = np.array(g["flux"]).reshape(1, 1, 1, 9)
+    out = orc.update_conservatively(((0,), (8,)), prev, ((0,), (8,)), flux, ((0,), (9,)),
+                                    1.0, 1.0, 0)
+    np.testing.assert_array_equal(out.ravel(), fromhex(g["next"]))
+
+
+def test_single_muscl_stencil_minmod(orc, golden):
+    # tests/test.simd_FluxMethod.cpp:54-105
+    g = golden["muscl_minmod_single"]
+    cons = np.array(g["stencil"]).T  # (4 comps, 4 cells)
+    comp = orc.complete_from_cons(2, cons)  # (6, 4)
+    states = comp.reshape(6, 1, 1, 4)
+    m = orc.method(orc.MUSCL_HLLE, orc.MINMOD)
+    f = orc.compute_numeric_fluxes(m, 2, states, ((-2, 0), (2, 1)), ((0, 0), (1, 1)),
+                                   g["dt"], g["dx"], X)
+    np.testing.assert_array_equal(f.ravel(), fromhex(g["flux"]))
+
+
+def _sin_states(orc, g):
+    lo, hi = g["cell_lo"], g["cell_hi"]
+    dx = g["dx"]
+    ny, nx = hi[1] - lo[1], hi[0] - lo[0]
+    cons = np.zeros((4, 1, ny, nx))
+    for j in range(lo[1], hi[1]):
+        for i in range(lo[0], hi[0]):
+            x, y = float(i) * dx, float(j) * dx
+            cons[:, 0, j - lo[1], i - lo[0]] = [1.0, 0.0, 0.0, 1.0 + 0.5 * math.sin(x * x + y * y)]
+    comp = orc.complete_from_cons(2, cons.reshape(4, -1)).reshape(6, 1, ny, nx)
+    return comp
+
+
+@pytest.mark.parametrize("name,d", [("hlle_sin16_X", X), ("hlle_sin16_Y", Y)])
+def test_hlle_sin_patch(orc, golden, name, d):
+    # tests/test.simd_FluxMethod.cpp:107-186
+    g = golden[name]
+    states = _sin_states(orc, g)
+    m = orc.method(orc.HLLE)
+    cell_box = (g["cell_lo"], g["cell_hi"])
+    dt = orc.compute_stable_dt(m, 2, states, cell_box, g["dx"], d, window_rule=0)
+    assert dt == float.fromhex(g["dt"])
+    f = orc.compute_numeric_fluxes(m, 2, states, cell_box, (g["face_lo"], g["face_hi"]), dt,
+                                   g["dx"], d)
+    ref = np.stack([fromhex(c) for c in g["fluxes"]])
+    np.testing.assert_array_equal(f.reshape(4, -1), ref)
+
+
+def test_muscl_vanleer_3d_random(orc, golden):
+    g = golden["muscl_vanleer_3d_random"]
+    m = orc.method(orc.MUSCL_HLLE, orc.VAN_LEER)
+    k = 0
+    for st in g["stencils"]:
+        cons = np.array(st).T  # (5, 4)
+        comp = orc.complete_from_cons(3, cons)
+        for d in range(3):
+            shape = [1, 1, 1]
+            shape[2 - d] = 4
+            states = comp.reshape(7, *shape)
+            lo = [0, 0, 0]
+            hi = [1, 1, 1]
+            lo[d], hi[d] = -2, 2
+            flo = [0, 0, 0]
+            fhi = [1, 1, 1]
+            f = orc.compute_numeric_fluxes(m, 3, states, (lo, hi), (flo, fhi), g["dt"], g["dx"], d)
+            np.testing.assert_array_equal(f.ravel(), fromhex(g["fluxes"][k]))
+            k += 1
+
+
+# Exact Riemann problem states of tests/test.PerfectGas.ExactRiemannProblem.cpp:57-181
+REF_STATES = [
+    (1.0, 0.0, 1.0, 0.125, 0.0, 0.1),            # (i) Sod
+    (1.0, -2.0, 0.4, 1.0, 2.0, 0.4),             # (ii) 123
+    (1.0, 0.0, 1000.0, 1.0, 0.0, 0.01),          # (iii) severe Sod
+    (1.0, 0.0, 0.1, 1.0, 0.0, 100.0),            # (iv)
+    (2.52667, 1204.31 / 2.52667, 312160.0, 2.28972, 1150.82 / 2.28972, 278308.0),
+    (2.28972, 1150.82 / 2.28972, 278308.0, 2.06243, 1084.96 / 2.06243, 248331.0),
+]
+
+# Published exact star states (Toro, Riemann Solvers and Numerical Methods for
+# Fluid Dynamics, 3rd ed., Table 4.2, tests 1-3)
+TORO = {0: (0.30313, 0.92745), 1: (0.00189, 0.0), 2: (460.894, 19.5975)}
+
+
+def _f_star(p, rho, u, pk, g=1.4):
+    a = math.sqrt(g * pk / rho)
+    if p > pk:
+        A = 2.0 / ((g + 1) * rho)
+        B = (g - 1) / (g + 1) * pk
+        return (p - pk) * math.sqrt(A / (p + B))
+    return 2 * a / (g - 1) * ((p / pk) ** ((g - 1) / (2 * g)) - 1)
+
+
+def _bisect(rhoL, uL, pL, rhoR, uR, pR):
+    f = lambda p: _f_star(p, rhoL, uL, pL) + _f_star(p, rhoR, uR, pR) + (uR - uL)
+    lo, hi = 0.0, max(pL, pR)
+    while f(hi) < 0:
+        hi *= 2
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if f(mid) < 0:
+            lo = mid
+        else:
+            hi = mid
+    p = 0.5 * (lo + hi)
+    u = 0.5 * (uL + uR) + 0.5 * (_f_star(p, rhoR, uR, pR) - _f_star(p, rhoL, uL, pL))
+    return p, u
+
+
+@pytest.mark.parametrize("guess", [0, 1])
+def test_exact_star_states(orc, guess):
+    arr = np.array(REF_STATES).T
+    ps, us, it, cv = orc.exact_star(*arr, guess=guess)
+    assert cv.all()
+    for k, st in enumerate(REF_STATES):
+        pb, ub = _bisect(*st)
+        assert ps[k] == pytest.approx(pb, rel=1e-6, abs=1e-9)
+        assert us[k] == pytest.approx(ub, rel=1e-5, abs=1e-6)
+        if k in TORO:
+            pt, ut = TORO[k]
+            assert ps[k] == pytest.approx(pt, rel=5e-4, abs=1e-5)
+            assert us[k] == pytest.approx(ut, rel=5e-4, abs=1e-5)
+
+
+def test_exact_star_tight_tolerance(orc):
+    arr = np.array(REF_STATES).T
+    ps, us, it, cv = orc.exact_star(*arr, tol=1e-12)
+    for k, st in enumerate(REF_STATES):
+        pb, _ = _bisect(*st)
+        assert ps[k] == pytest.approx(pb, rel=1e-10)
+
+
+def test_newton_reports_vacuum(orc):
+    # u_R - u_L >= 2 (aL + aR)/(gamma - 1): no positive star pressure
+    ps, us, it, cv = orc.exact_star([1.0], [-10.0], [1.0], [1.0], [10.0], [1.0], max_iterations=50)
+    assert cv[0] == 0 and it[0] == 50
+
+
+def sod_initial(n):
+    x = (np.arange(n) + 0.5) / n
+    rho = np.where(x < 0.5, 1.0, 0.125)
+    p = np.where(x < 0.5, 1.0, 0.1)
+    cons = np.zeros((3, 1, 1, n))
+    cons[0, 0, 0] = rho
+    cons[2, 0, 0] = p / 0.4
+    return cons
+
+
+def test_sod_1d_run_converges(orc):
+    n = 256
+    g = orc.Grid(1, [n], [1], [1.0 / n])
+    m = orc.method(orc.MUSCL_HLLE, orc.VAN_LEER)
+    cons, dts, restarts = g.run(m, sod_initial(n), 0.8, 0.2)
+    assert restarts == 0
+    assert abs(dts.sum() - 0.2) < 1e-12
+    # conservation with transmissive ends: mass changes only by boundary flux (zero here)
+    assert cons[0].sum() / n == pytest.approx(sod_initial(n)[0].sum() / n, rel=1e-12)
+    # plateau density of the exact solution between contact and shock
+    x = (np.arange(n) + 0.5) / n
+    plateau = cons[0, 0, 0][(x > 0.72) & (x < 0.8)]
+    assert np.allclose(plateau, 0.26557, rtol=0.02)
+
+
+def test_periodic_3d_sweep_conserves(orc):
+    rng = np.random.default_rng(3)
+    n = [8, 6, 5]
+    cons = np.zeros((5, n[2], n[1], n[0]))
+    rho = rng.uniform(0.5, 1.5, (n[2], n[1], n[0]))
+    v = rng.uniform(-0.3, 0.3, (3, n[2], n[1], n[0]))
+    p = rng.uniform(0.5, 1.5, (n[2], n[1], n[0]))
+    cons[0] = rho
+    cons[1:4] = rho * v
+    cons[4] = p / 0.4 + 0.5 * rho * (v ** 2).sum(0)
+    g = orc.Grid(3, n, [0, 0, 0], [0.1, 0.1, 0.1])
+    m = orc.method()
+    dt = 0.5 * g.stable_dt(m, cons)
+    for d in range(3):
+        out = g.sweep(m, cons, dt, d)
+        np.testing.assert_allclose(out.reshape(5, -1).sum(1), cons.reshape(5, -1).sum(1),
+                                   rtol=1e-13, atol=1e-13)
+
+
+def test_reference_tile_rule_is_subset(orc):
+    rng = np.random.default_rng(5)
+    n = [12, 20, 17]
+    cons = np.zeros((5, n[2], n[1], n[0]))
+    rho = rng.uniform(0.5, 1.5, (n[2], n[1], n[0]))
+    p = rng.uniform(0.5, 1.5, (n[2], n[1], n[0]))
+    cons[0] = rho
+    cons[4] = p / 0.4
+    g = orc.Grid(3, n, [0, 0, 0], [0.1, 0.1, 0.1])
+    m = orc.method()
+    for d in range(3):
+        all_faces = g.stable_dt(m, cons, d, rule=0)
+        tiles = g.stable_dt(m, cons, d, rule=1)
+        assert tiles >= all_faces
+        if d == 0:
+            assert tiles == all_faces
