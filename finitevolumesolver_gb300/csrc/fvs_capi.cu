@@ -96,6 +96,8 @@ double BitsToDouble(unsigned long long b) {
 
 namespace fvs {
 
+void SetLastError(const std::string& msg) { g_last_error = msg; }
+
 __device__ __forceinline__ double BitsToDoubleDev(unsigned long long b) {
   return __longlong_as_double(static_cast<long long>(b));
 }

@@ -3,6 +3,8 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
+
 #include <cuda_runtime.h>
 
 namespace fvs {
@@ -71,6 +73,9 @@ struct StableDtArgs {
   unsigned long long* smax_out;  // [rank]
   Control* ctrl;
 };
+
+// Sets the message returned by fvs_last_error() (fvs_capi.cu).
+void SetLastError(const std::string& msg);
 
 // Exact FP64 kernels (fvs_kernels_exact.cu, compiled with -fmad=false).
 cudaError_t LaunchSweepExact(const SweepArgs& a, cudaStream_t s);

@@ -120,6 +120,35 @@ int fvs_compute_stable_dt(const fvs_method* m, int rank,
                           double dx, int dir, int window_rule, double* dt_out,
                           void* stream);
 
+/* Allocation-free variant of fvs_compute_stable_dt, for callers that cannot
+ * let a library allocate device memory -- for example an integrator that
+ * hands out every byte of device memory through its own arena, where a
+ * cudaMalloc/cudaFree behind its back would synchronise the device, escape
+ * the arena's budget, and can fail once the arena holds the memory.  This
+ * entry point has no counterpart in the reference (whose CPU code allocates
+ * nothing on a device); it returns the same dt as fvs_compute_stable_dt, bit
+ * for bit, for the HLLE methods (FVS_MUSCL_HLLE, FVS_HLLE).
+ *  - Scratch: a fixed 65,544-byte array inside the library (8192 partial
+ *    maxima + 1 result), held by every GPU that loads the library until the
+ *    process exits.  It calls no cudaMalloc, cudaFree or other allocating
+ *    routine.
+ *  - Limit: at most 2,097,152 stencil windows per call (8192 blocks x 256
+ *    threads); larger patches return FVS_ERR_INVALID with a message naming
+ *    the limit -- split the patch or use fvs_compute_stable_dt.
+ *  - The first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress, with that device current); make that first call
+ *    before any stream capture.
+ *  - All calls share the one array, and each call overwrites what the
+ *    previous one left there (every slot it reads it has written first, so
+ *    nothing needs clearing).  Calls that overlap on the GPU -- from several
+ *    streams or host threads at once -- race on the array and may return a
+ *    wrong dt; serialise them.
+ *  - Synchronises `stream`; writes the patch's minimum stable dt to *dt_out. */
+int fvs_compute_stable_dt_noalloc(const fvs_method* m, int rank,
+                                  const double* states_dev, fvs_box cell_box,
+                                  double dx, int dir, int window_rule,
+                                  double* dt_out, void* stream);
+
 /* HyperbolicPatchIntegrator<Tag>::UpdateConservatively(next, prev, fluxes,
  * dt, dx, dir)  include/fub/HyperbolicPatchIntegrator.hpp:34-54,
  * src/HyperbolicPatchIntegrator.cpp:35-105:
