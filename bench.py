@@ -123,16 +123,17 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
-def profile_traffic(name: str):
-    """Per-launch DRAM bytes of the sweep kernel recorded from an ncu capture
-    (profiles/<name>: a line 'traffic_bytes_per_launch: <int>')."""
+def profile_traffic(name: str, cells: int):
+    """DRAM bytes per sweep launch from an ncu capture of a smaller case:
+    profiles/<name> records 'traffic_bytes_per_cell_update: <B>' (mean of the
+    x, y, z launches), scaled here to `cells` cells per launch."""
     p = ROOT / "profiles" / name
     if not p.exists():
         return None
     for ln in p.read_text().splitlines():
-        if ln.strip().startswith("traffic_bytes_per_launch:"):
+        if ln.strip().startswith("traffic_bytes_per_cell_update:"):
             try:
-                return int(float(ln.split(":", 1)[1]))
+                return float(ln.split(":", 1)[1]) * cells
             except ValueError:
                 return None
     return None
@@ -245,7 +246,7 @@ def run_ours(args):
     algo_bytes = 16 * (3 + 2) * cells  # state read once + written once, FP64
     peaks = load_peaks()
     achieved = algo_bytes / sweep_s / 1e9
-    traffic = profile_traffic(f"sweep_{args.precision}_256.md")
+    traffic = profile_traffic(f"sweep_{args.precision}_160.md", cells)
 
     # end to end through the public API with host buffers: upload the state
     # from pinned host memory, K steps, download the state
