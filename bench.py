@@ -42,7 +42,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64_exact")
+    ap.add_argument("--precision", default="fp64_exact",
+                    choices=["fp64_exact", "fp64_fast", "mixed"])
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip timing the other precision flavours")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--cpu-sample-n", type=int, default=128,
                     help="edge of the cube the CPU reference arm times per step")
@@ -197,56 +200,62 @@ def run_ours(args):
     n = args.n
     cells = n ** 3
     cons = workloads.octants_3d(n)
-    method = fvs.make_method(precision=args.precision)
-    solver = fvs.Solver([n] * 3, [1.0 / n] * 3, "periodic", method=method)
-    stream = torch.cuda.ExternalStream(solver.stream_handle())
-    solver.upload(cons)
-    if args.warmup:
-        solver.run(cfl=0.8, t_end=1e9, max_steps=args.warmup)
+    peaks = load_peaks()
+    algo_bytes = 16 * (3 + 2) * cells  # state read once + written once, FP64
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    clocks = ClockSampler(torch.cuda.current_device())
-    clocks.start()
-    barrier()
-    torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
-    st, _ = solver.run(cfl=0.8, t_end=1e9, max_steps=args.steps)
-    ev1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    assert st.steps == args.steps, "run stopped early"
-    updates = 6 * cells * args.steps * world
-    value = updates / (ms / 1e3)
+    def measure(precision: str, with_clocks: bool):
+        method = fvs.make_method(precision=precision)
+        solver = fvs.Solver([n] * 3, [1.0 / n] * 3, "periodic", method=method)
+        stream = torch.cuda.ExternalStream(solver.stream_handle())
+        solver.upload(cons)
+        if args.warmup:
+            solver.run(cfl=0.8, t_end=1e9, max_steps=args.warmup)
+        clocks = ClockSampler(torch.cuda.current_device()) if with_clocks else None
+        if clocks:
+            clocks.start()
+        barrier()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        st, _ = solver.run(cfl=0.8, t_end=1e9, max_steps=args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        clk = clocks.stop() if clocks else None
+        ms = ev0.elapsed_time(ev1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        assert st.steps == args.steps, "run stopped early"
+        final = solver.download()
+        # dominant kernel: the fused sweep; time single launches per direction
+        sweep_ms = []
+        dt = 0.4 * solver.ComputeStableDt(-1)
+        for rep in range(2):
+            for d in range(3):
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                solver.sweep(d, dt)
+                b.record(stream)
+                torch.cuda.synchronize()
+                if rep == 1:
+                    sweep_ms.append(a.elapsed_time(b))
+        sweep_s = statistics.mean(sweep_ms) / 1e3
+        achieved = algo_bytes / sweep_s / 1e9
+        res = {"ms": ms, "value": 6 * cells * args.steps * world / (ms / 1e3),
+               "final": final, "clocks": clk, "sweep_s": sweep_s, "achieved": achieved,
+               "solver": solver}
+        return res
 
-    # dominant kernel: the fused sweep; time single launches per direction
-    sweep_ms = []
-    dt = 0.4 * solver.ComputeStableDt(-1)
-    for rep in range(2):
-        for d in range(3):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            solver.sweep(d, dt)
-            b.record(stream)
-            torch.cuda.synchronize()
-            if rep == 1:
-                sweep_ms.append(a.elapsed_time(b))
-    sweep_s = statistics.mean(sweep_ms) / 1e3
-    algo_bytes = 16 * (3 + 2) * cells  # state read once + written once, FP64
-    peaks = load_peaks()
-    achieved = algo_bytes / sweep_s / 1e9
-    traffic = profile_traffic(f"sweep_{args.precision}_160.md", cells)
+    main = measure(args.precision, with_clocks=True)
+    solver = main["solver"]
 
     # end to end through the public API with host buffers: upload the state
     # from pinned host memory, K steps, download the state
@@ -256,10 +265,37 @@ def run_ours(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     fvs.lib().fvs_solver_upload(solver._h, pinned.data_ptr())
-    st2, _ = solver.run(cfl=0.8, t_end=1e9, max_steps=args.steps)
+    solver.run(cfl=0.8, t_end=1e9, max_steps=args.steps)
     fvs.lib().fvs_solver_download(solver._h, out_host.data_ptr())
     e2e_s = time.perf_counter() - t0
     e2e_value = 6 * cells * args.steps * world / e2e_s
+    solver.close()
+    main.pop("solver")
+
+    variants = {}
+    if not args.no_variants:
+        for prec in ("fp64_exact", "fp64_fast", "mixed"):
+            if prec == args.precision:
+                continue
+            r = measure(prec, with_clocks=False)
+            r["solver"].close()
+            r.pop("solver")
+            variants[prec] = r
+    ref_final = None
+    if args.precision == "fp64_exact":
+        ref_final = main["final"]
+    elif "fp64_exact" in variants:
+        ref_final = variants["fp64_exact"]["final"]
+
+    def accuracy(final):
+        if ref_final is None:
+            return None
+        l1 = float(np.abs(final[0] - ref_final[0]).mean())
+        tot0 = cons.reshape(5, -1).sum(1)
+        tot = final.reshape(5, -1).sum(1)
+        scale = np.abs(cons).reshape(5, -1).sum(1)
+        return {"l1_density_vs_fp64_exact": l1,
+                "max_conservation_drift_rel": float(np.max(np.abs(tot - tot0) / scale))}
 
     cpu = None
     if rank == 0:
@@ -272,9 +308,10 @@ def run_ours(args):
                "sample": f"1 Strang step of the {n}^3 workload ({6 * cells} cell-updates)"}
 
     if rank == 0:
+        traffic = profile_traffic(f"sweep_{args.precision}_160.md", cells)
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "metric": METRIC, "value": main["value"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic",
             "config": {"workload": f"3D perfect gas {n}^3 periodic, Strang MUSCL-Hancock/VanLeer"
@@ -282,18 +319,24 @@ def run_ours(args):
                        "n": n, "precision": args.precision, "sweeps_per_step": 6,
                        "l2": "inputs larger than L2 (state 671 MB per copy)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
-                         "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+            "roofline": {"bound": "hbm", "achieved": main["achieved"], "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": main["achieved"] / peaks["hbm_gbs"],
                          "traffic": traffic,
                          "kernel": "SweepMarchKernel (fused flux + update + CFL)",
                          "algorithmic_bytes_per_launch": algo_bytes,
-                         "launch_ms": sweep_s * 1e3, "peak_source": peaks["source"]},
+                         "launch_ms": main["sweep_s"] * 1e3, "peak_source": peaks["source"]},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": state_bytes / args.steps,
                     "d2h_bytes_per_step": (state_bytes + 136 * (args.steps // 30 + 1)) / args.steps},
             "gpu_launches": 9 * args.steps,
-            "clocks": clk,
+            "clocks": main["clocks"],
+            "accuracy": accuracy(main["final"]),
+            "variants": {k: {"value": v["value"], "ms_per_step": v["ms"] / args.steps,
+                             "sweep_launch_ms": v["sweep_s"] * 1e3,
+                             "hbm_frac": v["achieved"] / peaks["hbm_gbs"],
+                             "accuracy": accuracy(v["final"])}
+                         for k, v in variants.items()},
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -26,6 +26,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 # (source, extra flags)
 UNITS = [
     ("fvs_kernels_exact.cu", ["-fmad=false"]),
+    ("fvs_kernels_fast.cu", []),
     ("fvs_capi.cu", []),
     ("fvs_noalloc.cu", ["-fmad=false"]),
 ]

@@ -239,8 +239,10 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
   switch (s->m.precision) {
   case FVS_FP64_EXACT:
     return fvs::LaunchSweepExact(a, s->stream);
+  case FVS_FP64_FAST:
+    return fvs::LaunchSweepFast(a, s->stream);
   default:
-    return cudaErrorNotSupported;
+    return fvs::LaunchSweepMixed(a, s->stream);
   }
 }
 
@@ -257,7 +259,14 @@ cudaError_t LaunchStable(const fvs_solver* s, const double* in,
   a.gamma = s->m.gamma;
   a.smax_out = smax_out;
   a.ctrl = ctrl;
-  return fvs::LaunchStableDtExact(a, s->stream);
+  switch (s->m.precision) {
+  case FVS_FP64_EXACT:
+    return fvs::LaunchStableDtExact(a, s->stream);
+  case FVS_FP64_FAST:
+    return fvs::LaunchStableDtFast(a, s->stream);
+  default:
+    return fvs::LaunchStableDtMixed(a, s->stream);
+  }
 }
 
 fvs::StepPlan MakePlan(const fvs_solver* s, int64_t cycle) {
@@ -456,8 +465,6 @@ int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
   if (int r = CheckMethod(m, grid->rank)) return r;
   if (m->flux_method != FVS_MUSCL_HLLE)
     return Fail(FVS_ERR_UNSUPPORTED, "solver supports MUSCL-Hancock + HLLE");
-  if (m->precision != FVS_FP64_EXACT)
-    return Fail(FVS_ERR_UNSUPPORTED, "precision not built");
   for (int d = 0; d < 3; ++d) {
     const bool used = d < grid->rank;
     if (used && grid->n[d] < 1) return Fail(FVS_ERR_INVALID, "extent must be >= 1");

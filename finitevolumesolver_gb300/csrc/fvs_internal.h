@@ -81,6 +81,12 @@ void SetLastError(const std::string& msg);
 cudaError_t LaunchSweepExact(const SweepArgs& a, cudaStream_t s);
 cudaError_t LaunchStableDtExact(const StableDtArgs& a, cudaStream_t s);
 
+// Fast FP64 and mixed FP32/FP64 kernels (fvs_kernels_fast.cu).
+cudaError_t LaunchSweepFast(const SweepArgs& a, cudaStream_t s);
+cudaError_t LaunchSweepMixed(const SweepArgs& a, cudaStream_t s);
+cudaError_t LaunchStableDtFast(const StableDtArgs& a, cudaStream_t s);
+cudaError_t LaunchStableDtMixed(const StableDtArgs& a, cudaStream_t s);
+
 // Patch-level kernels over FArrayBox-layout views (fvs_kernels_exact.cu).
 struct BoxDesc {
   int lo[3];

@@ -11,6 +11,7 @@ namespace fvs {
 
 // Exact policy for the marching sweep.
 template <int D> struct ExactPolicy {
+  using Real = double;
   using Gas = exact::Gas;
   using Wave = exact::CellWave;
   using Rec = exact::Complete<D>;
@@ -19,6 +20,10 @@ template <int D> struct ExactPolicy {
     g.gamma = gamma;
     g.gamma_minus_1_inv = 1.0 / (gamma - 1.0);
     return g;
+  }
+  static __device__ __forceinline__ void ToCell(double* c, const double* u) {
+#pragma unroll
+    for (int k = 0; k < D + 2; ++k) c[k] = u[k];
   }
   static __device__ __forceinline__ void Predict(const Gas& eq, Rec& recL,
                                                  Rec& recR, const double* q0,

@@ -66,9 +66,9 @@ __device__ __forceinline__ bool SweepGate(const SweepArgs& a, double split_dt) {
   return true;
 }
 
-// Policy P provides: Gas, Rec (face state), Wave (cell wave data),
-// Predict(), HllFlux() (fluxes as double), MakeWave(), FaceMaxSpeed(),
-// MakeGas().
+// Policy P = PT<D> provides: Real (compute precision), Gas, Rec (face
+// state), Wave (cell wave data), MakeGas(), ToCell() (double -> Real),
+// Predict(), HllFlux() (fluxes as double), MakeWave(), FaceMaxSpeed().
 template <int D, int DIR, template <int> class PT>
 __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
   using P = PT<D>;
@@ -108,6 +108,7 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
   double smax = 0.0;
   int status = 0;
   if (active) {
+    using R = typename P::Real;
     const double* __restrict__ in = a.in;
     double* __restrict__ out = a.out;
     auto load = [&](double* u, int j) {
@@ -115,18 +116,22 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * cs + off);
     };
-    double um[K], uc[K], up[K];
-    load(um, j0 - 2);
-    load(uc, j0 - 1);
+    // double window for the update, compute-precision window for the rest
+    double dm[K], dc[K], dp[K];
+    R cm[K], cc[K], cp[K];
+    load(dm, j0 - 2);
+    load(dc, j0 - 1);
+    P::ToCell(cm, dm);
+    P::ToCell(cc, dc);
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
     double F_prev[K];
     for (int j = j0 - 1; j <= j1; ++j) {
-      load(up, j + 1);
+      load(dp, j + 1);
+      P::ToCell(cp, dp);
       typename P::Rec recL, recR;
-      P::Predict(eq, recL, recR, um, uc, up, a.limiter,
-                             lambda_half, DIR);
-      const typename P::Wave w = P::MakeWave(eq, uc, DIR);
+      P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
+      const typename P::Wave w = P::MakeWave(eq, cc, DIR);
       if (j >= j0) {
         double F[K];
         P::HllFlux(eq, F, recR_prev, recL, DIR);
@@ -137,7 +142,7 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
           const int64_t off = base + int64_t(j - 1) * stride;
 #pragma unroll
           for (int c = 0; c < K; ++c) {
-            const double v = um[c] + dt_dx * (F_prev[c] - F[c]);
+            const double v = dm[c] + dt_dx * (F_prev[c] - F[c]);
             out[c * cs + off] = v;
             if (c == 0 && !(v > 0.0)) status |= kStatusNonPositiveDensity;
           }
@@ -149,8 +154,10 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
       w_prev = w;
 #pragma unroll
       for (int c = 0; c < K; ++c) {
-        um[c] = uc[c];
-        uc[c] = up[c];
+        dm[c] = dc[c];
+        dc[c] = dp[c];
+        cm[c] = cc[c];
+        cc[c] = cp[c];
       }
     }
   }

@@ -1,0 +1,114 @@
+"""GPU tests of the fast FP64 and the mixed-precision flavours.
+
+fast FP64 ("fp64_fast"): per call within 1e-12 relative per cell of the
+oracle (the tolerance stated for the plain FP64 path: FMA contraction and
+reordered divisions), with an absolute floor of 1e-12 x the component's
+max |value| for components that cross zero (momenta).
+
+mixed ("mixed"): FP32 reconstruction and flux, FP64 state and update.  The
+state after a step differs from the FP64 oracle by FP32 round-off in the
+fluxes (L1 density error per step bounded below), while mass, momentum and
+energy of a periodic box are conserved to FP64 round-off.
+"""
+import numpy as np
+import pytest
+
+from finitevolumesolver_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+RTOL_FP64 = 1e-12
+
+
+def assert_close_rel(a, b, rtol):
+    """|a - b| <= rtol * (|b| + max|b_c|) per cell and component c."""
+    b = np.asarray(b)
+    scale = np.abs(b).reshape(b.shape[0], -1).max(axis=1)
+    scale = scale.reshape((-1,) + (1,) * (b.ndim - 1))
+    err = np.abs(a - b)
+    bad = err > rtol * (np.abs(b) + scale)
+    assert not bad.any(), f"max rel err {np.max(err / (np.abs(b) + scale)):.3e}"
+
+
+GRIDS = [
+    (1, [64], [1]),
+    (2, [40, 24], [0, 1]),
+    (3, [24, 20, 16], [0, 0, 0]),
+]
+
+
+@pytest.mark.parametrize("rank,n,bc", GRIDS)
+def test_fast_fp64_sweeps_and_steps(fvs, orc, rank, n, bc):
+    cons = workloads.random_state(tuple(reversed(n)), rank, seed=7 + rank, v=0.6)
+    cons = cons.reshape([rank + 2] + [1] * (3 - rank) + list(reversed(n)))
+    dx = [0.1, 0.07, 0.05][:rank]
+    g = orc.Grid(rank, n, bc, dx)
+    m = orc.method()
+    s = fvs.Solver(n, dx, bc, method=fvs.make_method(precision="fp64_fast"))
+    s.upload(cons)
+    dt_ref = g.stable_dt(m, cons)
+    assert s.ComputeStableDt(-1) == pytest.approx(dt_ref, rel=RTOL_FP64)
+    dt = 0.4 * dt_ref
+    for d in range(rank):
+        s.upload(cons)
+        level = s.sweep(d, dt)
+        assert level == pytest.approx(g.stable_dt(m, cons, d, 0), rel=RTOL_FP64)
+        assert_close_rel(s.download(), g.sweep(m, cons, dt, d), RTOL_FP64)
+    for cycle in (0, 1):
+        s.upload(cons)
+        s.step(dt, cycle)
+        assert_close_rel(s.download(), g.step(m, cons, dt, cycle), RTOL_FP64)
+    s.close()
+
+
+def test_fast_fp64_octants_run(fvs, orc):
+    n = 32
+    cons = workloads.octants_3d(n, seed=5)
+    dx = [1.0 / n] * 3
+    g = orc.Grid(3, [n] * 3, [0, 0, 0], dx)
+    ref, ref_dts, _ = g.run(orc.method(), cons, 0.8, 10.0, max_steps=4)
+    s = fvs.Solver([n] * 3, dx, "periodic", method=fvs.make_method(precision="fp64_fast"))
+    s.upload(cons)
+    st, dts = s.run(cfl=0.8, t_end=10.0, max_steps=4, log_len=8)
+    assert st.steps == 4
+    np.testing.assert_allclose(dts, ref_dts, rtol=1e-12)
+    assert_close_rel(s.download(), ref, 1e-11)
+
+
+def test_mixed_precision_step_accuracy_and_conservation(fvs, orc):
+    n = 48
+    cons = workloads.octants_3d(n, seed=9)
+    dx = [1.0 / n] * 3
+    g = orc.Grid(3, [n] * 3, [0, 0, 0], dx)
+    m = orc.method()
+    s = fvs.Solver([n] * 3, dx, "periodic", method=fvs.make_method(precision="mixed"))
+    s.upload(cons)
+    dt = 0.8 * g.stable_dt(m, cons)
+    s.step(dt, 0)
+    out = s.download()
+    ref = g.step(m, cons, dt, 0)
+    # L1 density error of one Strang step, relative to the mean density
+    l1 = np.abs(out[0] - ref[0]).mean() / np.abs(ref[0]).mean()
+    assert l1 < 2e-7, l1
+    # conservation to FP64 round-off over several steps
+    tot0 = cons.reshape(5, -1).sum(1)
+    scale = np.abs(cons).reshape(5, -1).sum(1)
+    s.upload(cons)
+    st, _ = s.run(cfl=0.8, t_end=10.0, max_steps=10)
+    tot = s.download().reshape(5, -1).sum(1)
+    assert np.all(np.abs(tot - tot0) <= 1e-13 * scale), (tot - tot0) / scale
+
+
+def test_mixed_sod_1d(fvs, orc):
+    n = 1024
+    cons = workloads.sod_1d(n)
+    g = orc.Grid(1, [n], [1], [1.0 / n])
+    ref, ref_dts, _ = g.run(orc.method(), cons, 0.8, 0.2)
+    s = fvs.Solver([n], [1.0 / n], "transmissive", method=fvs.make_method(precision="mixed"))
+    s.set_tiling(32)
+    s.upload(cons)
+    st, dts = s.run(cfl=0.8, t_end=0.2, log_len=4096)
+    assert st.time == pytest.approx(0.2, abs=1e-12)
+    out = s.download()
+    l1 = np.abs(out[0] - ref[0]).mean()
+    assert l1 < 1e-5, l1
