@@ -77,7 +77,8 @@ def _as_box(b) -> Box:
 
 
 def make_method(flux_method="muscl_hlle", limiter="van_leer", precision="fp64_exact",
-                guess="mean", max_iterations=5000, tolerance=1e-7, gamma=1.4) -> Method:
+                guess="mean", max_iterations=5000, tolerance=1e-7, gamma=1.4,
+                mlp_params=None) -> Method:
     m = Method()
     lib().fvs_method_default(C.byref(m))
     m.flux_method = FLUX_METHODS[flux_method] if isinstance(flux_method, str) else flux_method
@@ -87,7 +88,18 @@ def make_method(flux_method="muscl_hlle", limiter="van_leer", precision="fp64_ex
     m.max_iterations = max_iterations
     m.tolerance = tolerance
     m.gamma = gamma
+    m.mlp_params = _ptr(mlp_params) or None
     return m
+
+
+def exact_riemann_star(method: Method, rhoL, uL, pL, rhoR, uR, pR, pstar, ustar=None,
+                       iterations=None, status=None, stream=None) -> None:
+    """ExactRiemannSolver<PerfectGas<1>>::ComputeMiddleState for arrays of
+    problems (device arrays, float64; iterations/status int32)."""
+    n = int(rhoL.numel()) if hasattr(rhoL, "numel") else int(len(rhoL))
+    _capi.check(lib().fvs_exact_riemann_star(
+        C.byref(method), n, _ptr(rhoL), _ptr(uL), _ptr(pL), _ptr(rhoR), _ptr(uR), _ptr(pR),
+        _ptr(pstar), _ptr(ustar), _ptr(iterations), _ptr(status), _stream(stream)))
 
 
 class PerfectGas:
@@ -221,6 +233,12 @@ class Solver:
         out = C.c_double(0.0)
         _capi.check(lib().fvs_solver_stable_dt(self._h, int(dir), C.byref(out)))
         return out.value
+
+    def newton_stats(self, reset: bool = False):
+        it = C.c_uint64(0)
+        fl = C.c_uint64(0)
+        _capi.check(lib().fvs_solver_newton_stats(self._h, C.byref(it), C.byref(fl), int(reset)))
+        return it.value, fl.value
 
     def sweep(self, dir: int, dt: float) -> float:
         out = C.c_double(0.0)

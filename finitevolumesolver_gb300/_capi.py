@@ -32,7 +32,7 @@ class Box(C.Structure):
 class Method(C.Structure):
     _fields_ = [("flux_method", C.c_int32), ("limiter", C.c_int32), ("precision", C.c_int32),
                 ("guess", C.c_int32), ("max_iterations", C.c_int32), ("reserved", C.c_int32),
-                ("tolerance", C.c_double), ("gamma", C.c_double)]
+                ("tolerance", C.c_double), ("gamma", C.c_double), ("mlp_params", C.c_void_p)]
 
 
 class GridDesc(C.Structure):
@@ -99,6 +99,9 @@ def load() -> C.CDLL:
     L.fvs_solver_run.argtypes = [_VP, C.c_double, C.c_double, C.c_int, _DP, C.c_int,
                                  P(RunStats)]
     L.fvs_solver_stream.argtypes = [_VP, P(_VP)]
+    L.fvs_solver_newton_stats.argtypes = [_VP, P(C.c_uint64), P(C.c_uint64), C.c_int]
+    L.fvs_exact_riemann_star.argtypes = [P(Method), C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
+                                         _VP, _VP, _VP, _VP]
     L.fvs_solver_set_cycle.argtypes = [_VP, C.c_int64]
     L.fvs_solver_set_time.argtypes = [_VP, C.c_double]
     _lib = L

@@ -182,6 +182,7 @@ struct fvs_solver {
   fvs::Control* ctrl = nullptr;
   fvs::Control* ctrl_host = nullptr;  // pinned
   unsigned long long* scratch_words = nullptr;  // [8]
+  unsigned long long* newton_words = nullptr;   // [2] host-driven sweeps
   double* dt_log_dev = nullptr;
   int dt_log_cap = 0;
   int seg_len = 0;
@@ -197,6 +198,7 @@ struct fvs_solver {
     if (ctrl) cudaFree(ctrl);
     if (ctrl_host) cudaFreeHost(ctrl_host);
     if (scratch_words) cudaFree(scratch_words);
+    if (newton_words) cudaFree(newton_words);
     if (dt_log_dev) cudaFree(dt_log_dev);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -236,6 +238,13 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
   a.ctrl = ctrl;
   a.prev_check = prev_check;
   a.prev_dx = prev_dx;
+  a.guess = s->m.guess;
+  a.max_iterations = s->m.max_iterations;
+  a.tolerance = s->m.tolerance;
+  a.mlp = s->m.mlp_params;
+  a.stats_out = ctrl ? ctrl->newton : s->newton_words;
+  if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
+    return fvs::LaunchSweepGodunov(a, s->m.flux_method == FVS_MUSCL_GODUNOV, s->stream);
   switch (s->m.precision) {
   case FVS_FP64_EXACT:
     return fvs::LaunchSweepExact(a, s->stream);
@@ -259,6 +268,9 @@ cudaError_t LaunchStable(const fvs_solver* s, const double* in,
   a.gamma = s->m.gamma;
   a.smax_out = smax_out;
   a.ctrl = ctrl;
+  if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
+    return fvs::LaunchStableDtGodunov(a, s->m.guess, s->m.max_iterations, s->m.tolerance,
+                                      s->m.mlp_params, s->stream);
   switch (s->m.precision) {
   case FVS_FP64_EXACT:
     return fvs::LaunchStableDtExact(a, s->stream);
@@ -374,11 +386,18 @@ int fvs_compute_numeric_fluxes(const fvs_method* m, int rank,
   hi[dir] += w - 1;
   if (!Contains(cell_box, lo, hi))
     return Fail(FVS_ERR_INVALID, "cell box does not cover the faces' stencils");
-  if (m->flux_method == FVS_GODUNOV || m->flux_method == FVS_MUSCL_GODUNOV)
-    return Fail(FVS_ERR_UNSUPPORTED, "Godunov patch fluxes not built");
   if (m->precision != FVS_FP64_EXACT)
     return Fail(FVS_ERR_UNSUPPORTED, "patch-level calls run in exact FP64");
+  if (m->flux_method >= FVS_GODUNOV && m->guess == FVS_GUESS_MLP && !m->mlp_params)
+    return Fail(FVS_ERR_INVALID, "FVS_GUESS_MLP needs mlp_params");
   if (int r = CheckDevice()) return r;
+  if (m->flux_method == FVS_GODUNOV || m->flux_method == FVS_MUSCL_GODUNOV) {
+    FVS_CUDA(fvs::LaunchPatchGodunovFluxes(
+        m->flux_method == FVS_MUSCL_GODUNOV, m->limiter, rank, m->gamma, m->guess,
+        m->max_iterations, m->tolerance, m->mlp_params, fluxes_dev, ToDesc(face_box),
+        states_dev, ToDesc(cell_box), dt, dx, dir, nullptr, static_cast<cudaStream_t>(stream)));
+    return FVS_OK;
+  }
   FVS_CUDA(fvs::LaunchPatchFluxesExact(m->flux_method, m->limiter, rank, m->gamma,
                                        fluxes_dev, ToDesc(face_box), states_dev,
                                        ToDesc(cell_box), dt, dx, dir,
@@ -395,16 +414,23 @@ int fvs_compute_stable_dt(const fvs_method* m, int rank, const double* states_de
   if (!dt_out) return Fail(FVS_ERR_INVALID, "dt_out is NULL");
   if (window_rule != 0 && window_rule != 1)
     return Fail(FVS_ERR_INVALID, "window_rule must be 0 or 1");
-  if (m->flux_method == FVS_GODUNOV || m->flux_method == FVS_MUSCL_GODUNOV)
-    return Fail(FVS_ERR_UNSUPPORTED, "Godunov stable dt not built");
+  if (m->flux_method >= FVS_GODUNOV && m->guess == FVS_GUESS_MLP && !m->mlp_params)
+    return Fail(FVS_ERR_INVALID, "FVS_GUESS_MLP needs mlp_params");
   if (int r = CheckDevice()) return r;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   unsigned long long* word = nullptr;
   FVS_CUDA(cudaMallocAsync(&word, sizeof *word, st));
   FVS_CUDA(cudaMemsetAsync(word, 0, sizeof *word, st));
-  cudaError_t e = fvs::LaunchPatchStableDtExact(m->flux_method, rank, m->gamma,
-                                                states_dev, ToDesc(cell_box),
-                                                window_rule, dir, word, st);
+  cudaError_t e;
+  if (m->flux_method == FVS_GODUNOV || m->flux_method == FVS_MUSCL_GODUNOV) {
+    e = fvs::LaunchPatchGodunovStableDt(m->flux_method == FVS_MUSCL_GODUNOV, rank, m->gamma,
+                                        m->guess, m->max_iterations, m->tolerance,
+                                        m->mlp_params, states_dev, ToDesc(cell_box),
+                                        window_rule, dir, word, st);
+  } else {
+    e = fvs::LaunchPatchStableDtExact(m->flux_method, rank, m->gamma, states_dev,
+                                      ToDesc(cell_box), window_rule, dir, word, st);
+  }
   unsigned long long bits = 0;
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&bits, word, sizeof bits, cudaMemcpyDeviceToHost, st);
@@ -463,8 +489,12 @@ int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
                       fvs_solver** out) {
   if (!grid || !out) return Fail(FVS_ERR_INVALID, "NULL argument");
   if (int r = CheckMethod(m, grid->rank)) return r;
-  if (m->flux_method != FVS_MUSCL_HLLE)
-    return Fail(FVS_ERR_UNSUPPORTED, "solver supports MUSCL-Hancock + HLLE");
+  if ((m->flux_method == FVS_HLLE))
+    return Fail(FVS_ERR_UNSUPPORTED, "the solver runs MUSCL-Hancock or Godunov fluxes");
+  if (m->flux_method >= FVS_GODUNOV && m->precision == FVS_MIXED)
+    return Fail(FVS_ERR_UNSUPPORTED, "the exact Riemann solver runs in FP64");
+  if (m->flux_method >= FVS_GODUNOV && m->guess == FVS_GUESS_MLP && !m->mlp_params)
+    return Fail(FVS_ERR_INVALID, "FVS_GUESS_MLP needs mlp_params");
   for (int d = 0; d < 3; ++d) {
     const bool used = d < grid->rank;
     if (used && grid->n[d] < 1) return Fail(FVS_ERR_INVALID, "extent must be >= 1");
@@ -488,6 +518,8 @@ int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
   if (e == cudaSuccess) e = cudaMalloc(&s->ctrl, sizeof(fvs::Control));
   if (e == cudaSuccess) e = cudaMallocHost(&s->ctrl_host, sizeof(fvs::Control));
   if (e == cudaSuccess) e = cudaMalloc(&s->scratch_words, 8 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&s->newton_words, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(s->newton_words, 0, 2 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(s->ctrl, 0, sizeof(fvs::Control));
   if (e != cudaSuccess) {
     delete s;
@@ -611,6 +643,43 @@ int fvs_solver_step(fvs_solver* s, double dt, int cycle) {
     }
   }
   s->cur = src;
+  return FVS_OK;
+}
+
+int fvs_solver_newton_stats(fvs_solver* s, uint64_t* iterations, uint64_t* failures,
+                            int reset) {
+  if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
+  unsigned long long a[2], b[2];
+  FVS_CUDA(cudaMemcpyAsync(a, s->newton_words, sizeof a, cudaMemcpyDeviceToHost, s->stream));
+  FVS_CUDA(cudaMemcpyAsync(b, s->ctrl->newton, sizeof b, cudaMemcpyDeviceToHost, s->stream));
+  FVS_CUDA(cudaStreamSynchronize(s->stream));
+  if (iterations) *iterations = a[0] + b[0];
+  if (failures) *failures = a[1] + b[1];
+  if (reset) {
+    FVS_CUDA(cudaMemsetAsync(s->newton_words, 0, sizeof a, s->stream));
+    FVS_CUDA(cudaMemsetAsync(s->ctrl->newton, 0, sizeof b, s->stream));
+    FVS_CUDA(cudaStreamSynchronize(s->stream));
+  }
+  return FVS_OK;
+}
+
+int fvs_exact_riemann_star(const fvs_method* m, int64_t n, const double* rhoL_dev,
+                           const double* uL_dev, const double* pL_dev,
+                           const double* rhoR_dev, const double* uR_dev,
+                           const double* pR_dev, double* pstar_dev, double* ustar_dev,
+                           int32_t* iterations_dev, int32_t* status_dev, void* stream) {
+  if (int r = CheckMethod(m, 1)) return r;
+  if (n < 0) return Fail(FVS_ERR_INVALID, "n must be non-negative");
+  if (n > 0 && (!rhoL_dev || !uL_dev || !pL_dev || !rhoR_dev || !uR_dev || !pR_dev))
+    return Fail(FVS_ERR_INVALID, "NULL input array");
+  if (m->max_iterations < 0) return Fail(FVS_ERR_INVALID, "max_iterations must be >= 0");
+  if (m->guess == FVS_GUESS_MLP && !m->mlp_params)
+    return Fail(FVS_ERR_INVALID, "FVS_GUESS_MLP needs mlp_params");
+  if (int r = CheckDevice()) return r;
+  FVS_CUDA(fvs::LaunchExactStar(n, m->gamma, m->guess, m->max_iterations, m->tolerance,
+                                m->mlp_params, rhoL_dev, uL_dev, pL_dev, rhoR_dev, uR_dev, pR_dev,
+                                pstar_dev, ustar_dev, iterations_dev, status_dev,
+                                static_cast<cudaStream_t>(stream)));
   return FVS_OK;
 }
 

@@ -9,6 +9,12 @@
 
 namespace fvs {
 
+// A box of an FArrayBox-layout array: lower corner and extents.
+struct BoxDesc {
+  int lo[3];
+  int n[3];
+};
+
 // Per-run control block resident in device memory.  The time step lives on
 // the device so that a whole split step (stable dt, sweeps, checks) runs
 // without a host round trip and can be captured in a CUDA graph.
@@ -21,6 +27,7 @@ struct Control {
   double dt_override;  // > 0: use this dt for the next step instead of cfl*stable
   unsigned long long smax_stable[3];  // bits of max face speed, per direction
   unsigned long long smax_check[6];   // bits of max face speed, per sweep
+  unsigned long long newton[2];       // Newton iterations, non-converged faces
   int abort;         // a per-sweep check failed; later kernels do nothing
   int done;          // t reached t_end; later kernels do nothing
   int failed_step;   // index of the failed step within the batch
@@ -60,6 +67,12 @@ struct SweepArgs {
   // previous sweep's check (skip this sweep when it failed); -1 for none
   int prev_check;
   double prev_dx;
+  // exact Riemann solver (Godunov policies)
+  int guess;            // fvs_guess
+  int max_iterations;
+  double tolerance;
+  const float* mlp;     // learned-guess weights (guess == FVS_GUESS_MLP)
+  unsigned long long* stats_out;  // [2]: Newton iterations, non-converged faces
 };
 
 // Stable-dt pass over all directions (max face speed per direction).
@@ -87,11 +100,26 @@ cudaError_t LaunchSweepMixed(const SweepArgs& a, cudaStream_t s);
 cudaError_t LaunchStableDtFast(const StableDtArgs& a, cudaStream_t s);
 cudaError_t LaunchStableDtMixed(const StableDtArgs& a, cudaStream_t s);
 
+// Godunov / exact Riemann solver kernels (fvs_kernels_godunov.cu).
+cudaError_t LaunchSweepGodunov(const SweepArgs& a, bool muscl, cudaStream_t s);
+cudaError_t LaunchStableDtGodunov(const StableDtArgs& a, int guess, int max_it, double tol,
+                                  const float* mlp, cudaStream_t s);
+cudaError_t LaunchPatchGodunovFluxes(bool muscl, int limiter, int rank, double gamma, int guess,
+                                     int max_it, double tol, const float* mlp, double* fluxes,
+                                     BoxDesc fbox, const double* states, BoxDesc cbox, double dt,
+                                     double dx, int dir, unsigned long long* stats,
+                                     cudaStream_t s);
+cudaError_t LaunchPatchGodunovStableDt(bool muscl, int rank, double gamma, int guess, int max_it,
+                                       double tol, const float* mlp, const double* states,
+                                       BoxDesc cbox, int window_rule, int dir,
+                                       unsigned long long* smax, cudaStream_t s);
+cudaError_t LaunchExactStar(int64_t n, double gamma, int guess, int max_it, double tol,
+                            const float* mlp, const double* rhoL, const double* uL,
+                            const double* pL, const double* rhoR, const double* uR,
+                            const double* pR, double* pstar, double* ustar, int* iters,
+                            int* converged, cudaStream_t s);
+
 // Patch-level kernels over FArrayBox-layout views (fvs_kernels_exact.cu).
-struct BoxDesc {
-  int lo[3];
-  int n[3];
-};
 cudaError_t LaunchPatchFluxesExact(int method, int limiter, int rank, double gamma,
                                    double* fluxes, BoxDesc fbox,
                                    const double* states, BoxDesc cbox,

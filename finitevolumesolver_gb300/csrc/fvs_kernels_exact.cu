@@ -21,6 +21,9 @@ template <int D> struct ExactPolicy {
     g.gamma_minus_1_inv = 1.0 / (gamma - 1.0);
     return g;
   }
+  static __device__ __forceinline__ Gas MakeGasFor(const SweepArgs& a) {
+    return MakeGas(a.gamma);
+  }
   static __device__ __forceinline__ void ToCell(double* c, const double* u) {
 #pragma unroll
     for (int k = 0; k < D + 2; ++k) c[k] = u[k];
@@ -33,19 +36,16 @@ template <int D> struct ExactPolicy {
     exact::MusclPredictBoth<D>(eq, recL, recR, q0, q1, q2, limiter,
                                lambda_half, dir);
   }
-  static __device__ __forceinline__ void HllFlux(const Gas& eq, double* F,
-                                                 const Rec& L, const Rec& R,
-                                                 int dir) {
+  using Stats = NoStats;
+  static __device__ __forceinline__ double Face(const Gas& eq, double* F, const Rec& L,
+                                                const Rec& R, const Wave& wL,
+                                                const Wave& wR, int dir, Stats&) {
     exact::HllFlux<D>(eq, F, L, R, dir);
+    return exact::FaceMaxSpeed(eq, wL, wR);
   }
   static __device__ __forceinline__ Wave MakeWave(const Gas& eq, const double* u,
                                                   int dir) {
     return exact::MakeCellWave<D>(eq, u, dir);
-  }
-  static __device__ __forceinline__ double FaceMaxSpeed(const Gas& eq,
-                                                        const Wave& L,
-                                                        const Wave& R) {
-    return exact::FaceMaxSpeed(eq, L, R);
   }
 };
 

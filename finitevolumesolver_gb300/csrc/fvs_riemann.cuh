@@ -1,0 +1,350 @@
+// fvs_riemann.cuh -- exact Riemann solver for the perfect gas on the device
+// (FP64) and the Godunov flux built on it.
+//
+// Restates maikel/FiniteVolumeSolver's
+//   ExactRiemannSolver<PerfectGas<D>>::ComputeMiddleState
+//       src/equations/perfect_gas/ExactRiemannSolver.hpp:34-97
+//   NewtonIteration                 include/fub/NewtonIteration.hpp:28-52
+//   ExactRiemannSolver::ComputeSignals   ExactRiemannSolver.hpp:105-148
+//   ExactRiemannSolver::SolveRiemannProblem (x/t = 0)  ExactRiemannSolver.hpp:204-353
+//   Godunov::ComputeNumericFlux / ComputeStableDt
+//       include/fub/flux_method/GodunovMethod.hpp:129-183
+// with the reference's operation order (the including translation unit is
+// compiled with -fmad=false).  pow() is CUDA's, so results agree with the
+// CPU oracle to a few ulps rather than bit for bit.
+//
+// Differences by design:
+//  - Newton is bounded by `max_iterations` and never throws: a face that has
+//    not met the tolerance keeps its last iterate and is counted as a
+//    failure (the reference throws std::runtime_error after 5000 steps).
+//  - The start value is selectable: the reference's arithmetic mean, the
+//    PVRS/two-rarefaction estimate, or a learned (MLP) estimate that falls
+//    back to PVRS/two-rarefaction when non-positive or not finite, or when
+//    Newton from it fails to converge.
+#pragma once
+
+#include "fvs_mlp.cuh"
+#include "fvs_physics_exact.cuh"
+
+namespace fvs {
+namespace riemann {
+
+enum Guess : int { kGuessMean = 0, kGuessPvrsTr = 1, kGuessMlp = 2 };
+
+struct Options {
+  int guess;
+  int max_iterations;
+  double tol;
+  const float* mlp;  // learned-guess parameters (kGuessMlp)
+};
+
+struct Star {
+  double p;
+  double u;
+  int iterations;
+  int converged;
+  int fallback;  // the learned start value was rejected
+};
+
+// Scalar-path |m|^2 of the reference's exact solver: (m0^2 + m1^2) + m2^2.
+template <int D> __device__ __forceinline__ double SquaredNormScalar(const double* m) {
+  if constexpr (D == 1) {
+    return m[0] * m[0];
+  } else if constexpr (D == 2) {
+    return m[0] * m[0] + m[1] * m[1];
+  } else {
+    return (m[0] * m[0] + m[1] * m[1]) + m[2] * m[2];
+  }
+}
+
+// PVRS estimate, replaced by the two-rarefaction estimate below min(pL, pR)
+// (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics, 3rd ed.,
+// section 9.5); floored at 1e-8 min(pL, pR).
+__device__ __forceinline__ double PvrsTrGuess(double g, double rhoL, double uL, double pL,
+                                              double aL, double rhoR, double uR, double pR,
+                                              double aR) {
+  const double pmin = pL < pR ? pL : pR;
+  const double ppv = 0.5 * (pL + pR) - 0.125 * (uR - uL) * (rhoL + rhoR) * (aL + aR);
+  double p0;
+  if (ppv >= pmin) {
+    p0 = ppv;
+  } else {
+    const double z = (g - 1.0) / (2.0 * g);
+    const double num = aL + aR - 0.5 * (g - 1.0) * (uR - uL);
+    const double den = aL / pow(pL, z) + aR / pow(pR, z);
+    p0 = (num > 0.0) ? pow(num / den, 1.0 / z) : 0.0;
+  }
+  const double floor = 1e-8 * pmin;
+  return p0 > floor ? p0 : floor;
+}
+
+struct SideFn {
+  double rho, p, a, A, B;
+};
+
+__device__ __forceinline__ double FSide(const SideFn& s, double gm1, double exponent,
+                                        double q) {
+  if (q > s.p) {
+    return (q - s.p) * sqrt(s.A / (q + s.B));
+  }
+  return 2.0 * s.a / gm1 * (pow(q / s.p, exponent) - 1.0);
+}
+
+__device__ __forceinline__ double DfSide(const SideFn& s, double d_exponent, double q) {
+  if (q > s.p) {
+    return sqrt(s.A / (s.B + q)) * (1.0 - 0.5 * (q - s.p) / (s.B + q));
+  }
+  return pow(q / s.p, d_exponent) / (s.rho * s.a);
+}
+
+// NewtonIteration from x0 (NewtonIteration.hpp:28-52), bounded.
+__device__ __forceinline__ void Newton(const SideFn& L, const SideFn& R, double du, double gm1,
+                                       double exponent, double d_exponent, double x0,
+                                       double tol, int max_iterations, double& x_out,
+                                       int& iterations, int& converged) {
+  // f(h) = f_right(h) + f_left(h) + du (ExactRiemannSolver.hpp:89)
+  double x = x0;
+  double fx = FSide(R, gm1, exponent, x) + FSide(L, gm1, exponent, x) + du;
+  int counter = 0;
+  double err = fabs(fx);
+  while (err > tol && counter < max_iterations) {
+    const double dfx = DfSide(R, d_exponent, x) + DfSide(L, d_exponent, x);
+    const double offset = fx / dfx;
+    const double next = x - offset;
+    x = ((next - next) != (next - next) || next < 0.0) ? 0.5 * x : next;
+    fx = FSide(R, gm1, exponent, x) + FSide(L, gm1, exponent, x) + du;
+    err = fabs(fx);
+    counter += 1;
+  }
+  x_out = x;
+  iterations = counter;
+  converged = !(err > tol);
+}
+
+template <int D>
+__device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
+                                                   const exact::Complete<D>& left,
+                                                   const exact::Complete<D>& right, int dir,
+                                                   const Options& opt) {
+  const double g = eq.gamma;
+  const double gp1 = g + 1.0;
+  const double gm1 = g - 1.0;
+  SideFn L, R;
+  L.rho = left.rho;
+  L.p = left.p;
+  L.a = left.c;
+  L.A = 2.0 / (gp1 * L.rho);
+  L.B = gm1 / gp1 * L.p;
+  R.rho = right.rho;
+  R.p = right.p;
+  R.a = right.c;
+  R.A = 2.0 / (gp1 * R.rho);
+  R.B = gm1 / gp1 * R.p;
+  const double exponent = 0.5 * gm1 / g;
+  const double d_exponent = -0.5 * gp1 / g;
+  const double uL = left.m[dir] / left.rho;
+  const double uR = right.m[dir] / right.rho;
+  const double du = uR - uL;
+  Star st;
+  st.fallback = 0;
+  double x0;
+  if (opt.guess == kGuessMean) {
+    x0 = 0.5 * (L.p + R.p);
+  } else {
+    const double pv = PvrsTrGuess(g, L.rho, uL, L.p, L.a, R.rho, uR, R.p, R.a);
+    x0 = pv;
+    if (opt.guess == kGuessMlp && opt.mlp) {
+      const double learned = mlp::GuessStarPressure(opt.mlp, L.rho, uL, L.p, L.a, R.rho, uR,
+                                                    R.p, R.a);
+      if (learned > 0.0 && learned < 1.7976931348623157e308) {
+        x0 = learned;
+      } else {
+        st.fallback = 1;
+      }
+    }
+    if (opt.guess == kGuessMlp && !st.fallback) {
+      double x;
+      int it, ok;
+      Newton(L, R, du, gm1, exponent, d_exponent, x0, opt.tol, opt.max_iterations, x, it, ok);
+      if (!ok) {
+        // the learned start did not converge within the bound: fall back
+        st.fallback = 1;
+        double x2;
+        int it2, ok2;
+        Newton(L, R, du, gm1, exponent, d_exponent, pv, opt.tol, opt.max_iterations, x2, it2,
+               ok2);
+        x = x2;
+        it += it2;
+        ok = ok2;
+      }
+      st.p = x;
+      st.iterations = it;
+      st.converged = ok;
+      const double fL = FSide(L, gm1, exponent, st.p);
+      const double fR = FSide(R, gm1, exponent, st.p);
+      st.u = 0.5 * (uL + uR) + 0.5 * (fR - fL);
+      return st;
+    }
+  }
+  Newton(L, R, du, gm1, exponent, d_exponent, x0, opt.tol, opt.max_iterations, st.p,
+         st.iterations, st.converged);
+  const double fL = FSide(L, gm1, exponent, st.p);
+  const double fR = FSide(R, gm1, exponent, st.p);
+  st.u = 0.5 * (uL + uR) + 0.5 * (fR - fL);
+  return st;
+}
+
+// max(0, |s0|, |s1|) with the exact solver's signal speeds
+// (ExactRiemannSolver.hpp:105-148, GodunovMethod.hpp:173-183).
+template <int D>
+__device__ __forceinline__ double SignalMaxSpeed(const exact::Gas& eq,
+                                                 const exact::Complete<D>& left,
+                                                 const exact::Complete<D>& right, int dir,
+                                                 double pM) {
+  const double g = eq.gamma;
+  const double gp1 = g + 1.0;
+  const double gm1 = g - 1.0;
+  const double uL = left.m[dir] / left.rho;
+  const double aL = left.c;
+  const double pL = left.p;
+  const double pL_ratio = pM / pL;
+  double s0, s1;
+  if (pM > pL) {
+    s0 = uL - aL * sqrt((gp1 * pL_ratio + gm1) / (2.0 * g));
+  } else {
+    s0 = uL - aL;
+  }
+  const double uR = right.m[dir] / right.rho;
+  const double aR = right.c;
+  const double pR = right.p;
+  const double pR_ratio = pM / pR;
+  if (pM > pR) {
+    s1 = uR + aR * sqrt((gp1 * pR_ratio + gm1) / (2.0 * g));
+  } else {
+    s1 = uR + aR;
+  }
+  double s = 0.0;
+  const double a0 = fabs(s0), a1 = fabs(s1);
+  s = (s < a0) ? a0 : s;  // std::max(x, |y|)
+  s = (s < a1) ? a1 : s;
+  return s;
+}
+
+// SolveRiemannProblem sampled at x/t = 0 (ExactRiemannSolver.hpp:204-353).
+template <int D>
+__device__ __forceinline__ void Sample(const exact::Gas& eq, exact::Complete<D>& state,
+                                       const exact::Complete<D>& left,
+                                       const exact::Complete<D>& right, int dir, double pM,
+                                       double uM) {
+  const double g = eq.gamma;
+  const double gp1 = g + 1.0;
+  const double gm1 = g - 1.0;
+  auto set_momentum = [dir](exact::Complete<D>& s, double momentum,
+                            const exact::Complete<D>& side) {
+    if constexpr (D == 1) {
+      s.m[0] = momentum;
+    } else {
+#pragma unroll
+      for (int d = 0; d < D; ++d) s.m[d] = s.rho * (side.m[d] / side.rho);
+      s.m[dir] = momentum;
+    }
+  };
+  auto from_prim = [&eq](exact::Complete<D>& s) {
+    const double rhoE_kin = 0.5 * SquaredNormScalar<D>(s.m) / s.rho;
+    const double rhoE_internal = s.p * eq.gamma_minus_1_inv;
+    s.E = rhoE_internal + rhoE_kin;
+    s.c = sqrt(eq.gamma * s.p / s.rho);
+  };
+  if (0.0 <= uM) {
+    const double uL = left.m[dir] / left.rho;
+    const double aL = left.c;
+    const double pL = left.p;
+    const double p_ratio = pM / pL;
+    const double g_ratio = gm1 / gp1;
+    if (pM > pL) {
+      const double shock_speed = uL - aL * sqrt((gp1 * p_ratio + gm1) / (2.0 * g));
+      if (shock_speed < 0.0) {
+        state.rho = left.rho * (p_ratio + g_ratio) / (g_ratio * p_ratio + 1.0);
+        set_momentum(state, state.rho * uM, left);
+        state.p = pM;
+        from_prim(state);
+      } else {
+        state = left;
+      }
+    } else {
+      const double aM = aL * pow(p_ratio, gm1 / (2.0 * g));
+      const double shock_speed_TL = uM - aM;
+      const double shock_speed_HL = uL - aL;
+      if (0.0 < shock_speed_HL) {
+        state = left;
+      } else if (shock_speed_TL < 0.0) {
+        state.rho = left.rho * pow(p_ratio, 1 / g);
+        set_momentum(state, state.rho * uM, left);
+        state.p = pM;
+        from_prim(state);
+      } else {
+        state.rho = left.rho * pow(2.0 / gp1 + g_ratio * uL / aL, 2.0 / gm1);
+        const double u = 2.0 / gp1 * (aL + 0.5 * gm1 * uL);
+        set_momentum(state, state.rho * u, left);
+        state.p = pL * pow(2.0 / gp1 + g_ratio * uL / aL, 2.0 * g / gm1);
+        from_prim(state);
+      }
+    }
+  } else {
+    const double uR = right.m[dir] / right.rho;
+    const double aR = right.c;
+    const double pR = right.p;
+    const double p_ratio = pM / pR;
+    const double g_ratio = gm1 / gp1;
+    if (pM > pR) {
+      const double shock_speed = uR + aR * sqrt((gp1 * p_ratio + gm1) / (2.0 * g));
+      if (0.0 < shock_speed) {
+        state.rho = right.rho * (p_ratio + g_ratio) / (g_ratio * p_ratio + 1.0);
+        set_momentum(state, state.rho * uM, right);
+        state.p = pM;
+        from_prim(state);
+      } else {
+        state = right;
+      }
+    } else {
+      const double aM = aR * pow(p_ratio, gm1 / (2.0 * g));
+      const double shock_speed_TR = uM + aM;
+      const double shock_speed_HR = uR + aR;
+      if (shock_speed_HR <= 0.0) {
+        state = right;
+      } else if (shock_speed_TR >= 0.0) {
+        state.rho = right.rho * pow(p_ratio, 1 / g);
+        set_momentum(state, state.rho * uM, right);
+        state.p = pM;
+        from_prim(state);
+      } else {
+        state.rho = right.rho * pow(2.0 / gp1 - g_ratio * uR / aR, 2.0 / gm1);
+        const double u = 2.0 / gp1 * (-aR + 0.5 * gm1 * uR);
+        set_momentum(state, state.rho * u, right);
+        state.p = pR * pow(2.0 / gp1 - g_ratio * uR / aR, 2.0 * g / gm1);
+        from_prim(state);
+      }
+    }
+  }
+}
+
+// Godunov flux: the physical flux of the exact solution at x/t = 0
+// (GodunovMethod.hpp:129-135).  Faces with a non-positive density keep the
+// left state (the reference leaves the solution untouched there).
+template <int D>
+__device__ __forceinline__ Star GodunovFlux(const exact::Gas& eq, double* nf,
+                                            const exact::Complete<D>& L,
+                                            const exact::Complete<D>& R, int dir,
+                                            const Options& opt) {
+  exact::Complete<D> sol = L;
+  Star st{0.0, 0.0, 0, 1, 0};
+  if (0.0 < L.rho && 0.0 < R.rho) {
+    st = ComputeMiddleState<D>(eq, L, R, dir, opt);
+    Sample<D>(eq, sol, L, R, dir, st.p, st.u);
+  }
+  exact::Flux<D>(nf, sol, dir);
+  return st;
+}
+
+}  // namespace riemann
+}  // namespace fvs

@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(256) StableDtKernelT(StableDtArgs a) {
         for (int c = 0; c < K; ++c) vd[c] = __ldg(a.in + c * cs + ocell);
         P::ToCell(v, vd);
         const typename P::Wave wo = P::MakeWave(eq, v, d);
-        const double s = (fi == 0) ? P::FaceMaxSpeed(eq, wo, w) : P::FaceMaxSpeed(eq, w, wo);
+        const double s = static_cast<double>((fi == 0) ? P::FaceMaxSpeed(eq, wo, w)
+                                                       : P::FaceMaxSpeed(eq, w, wo));
         smax[d] = s > smax[d] ? s : smax[d];
       }
     }

@@ -66,9 +66,34 @@ __device__ __forceinline__ bool SweepGate(const SweepArgs& a, double split_dt) {
   return true;
 }
 
+// Counters of the exact Riemann solver (Newton iterations, faces whose
+// Newton iteration did not converge); empty for the HLLE policies.
+struct NoStats {
+  __device__ __forceinline__ void Flush(unsigned long long*) const {}
+};
+
+struct NewtonStats {
+  unsigned long long iterations = 0;
+  unsigned long long failures = 0;
+  __device__ __forceinline__ void Flush(unsigned long long* out) const {
+    unsigned long long it = iterations, fl = failures;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      it += __shfl_xor_sync(0xffffffffu, it, o);
+      fl += __shfl_xor_sync(0xffffffffu, fl, o);
+    }
+    if (out && (threadIdx.x & 31) == 0) {
+      if (it) atomicAdd(out, it);
+      if (fl) atomicAdd(out + 1, fl);
+    }
+  }
+};
+
 // Policy P = PT<D> provides: Real (compute precision), Gas, Rec (face
-// state), Wave (cell wave data), MakeGas(), ToCell() (double -> Real),
-// Predict(), HllFlux() (fluxes as double), MakeWave(), FaceMaxSpeed().
+// state), Wave (cell wave data), Stats, MakeGas(), ToCell() (double ->
+// Real), Predict(), MakeWave(), and Face(): the numeric flux of the face
+// between recR of the left cell and recL of the right cell (as double) and
+// the face's max signal speed of the input state (the CFL check).
 template <int D, int DIR, template <int> class PT>
 __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
   using P = PT<D>;
@@ -101,14 +126,15 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
     stride = int64_t(nx) * ny;
   }
 
-  const typename P::Gas eq = P::MakeGas(a.gamma);
+  const typename P::Gas eq = P::MakeGasFor(a);
   const double lambda_half = 0.5 * split_dt / a.dx;
   const double dt_dx = split_dt / a.dx;
 
-  double smax = 0.0;
+  using R = typename P::Real;
+  R smax = R(0);
   int status = 0;
+  typename P::Stats stats;
   if (active) {
-    using R = typename P::Real;
     const double* __restrict__ in = a.in;
     double* __restrict__ out = a.out;
     auto load = [&](double* u, int j) {
@@ -134,8 +160,7 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
       const typename P::Wave w = P::MakeWave(eq, cc, DIR);
       if (j >= j0) {
         double F[K];
-        P::HllFlux(eq, F, recR_prev, recL, DIR);
-        const double s = P::FaceMaxSpeed(eq, w_prev, w);
+        const R s = P::Face(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
         smax = s > smax ? s : smax;
         if (j > j0) {
           // cell j-1: U' = U + dt/dx (F_{j-1} - F_j)
@@ -144,7 +169,8 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
           for (int c = 0; c < K; ++c) {
             const double v = dm[c] + dt_dx * (F_prev[c] - F[c]);
             out[c * cs + off] = v;
-            if (c == 0 && !(v > 0.0)) status |= kStatusNonPositiveDensity;
+            // non-positive density: sign bit set or zero (integer test)
+            if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
           }
         }
 #pragma unroll
@@ -161,9 +187,10 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
       }
     }
   }
-  smax = WarpMax(smax);
+  stats.Flush(a.stats_out);
+  const double smax_w = WarpMax(static_cast<double>(smax));
   if ((threadIdx.x & 31) == 0) {
-    if (a.smax_out && smax > 0.0) AtomicMaxPositive(a.smax_out, smax);
+    if (a.smax_out && smax_w > 0.0) AtomicMaxPositive(a.smax_out, smax_w);
   }
   if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
 }

@@ -67,3 +67,54 @@ def random_state(shape, rank, seed=0, rho=(0.5, 1.5), p=(0.5, 1.5), v=0.4):
     pp = rng.uniform(*p, shape)
     vel = [rng.uniform(-v, v, shape) for _ in range(rank)]
     return cons_from_prim(r, vel, pp)
+
+
+def riemann_samples(n, seed=0, gamma=GAMMA, exclude_vacuum=True):
+    """Random 1-D Riemann problems: rho_L, rho_R, p_L, p_R log-uniform on
+    [1e-3, 1e1]; u_L, u_R uniform on [-3c, 3c] with c the larger sound
+    speed.  Problems whose states generate vacuum (u_R - u_L >=
+    2 (a_L + a_R) / (gamma - 1)) are redrawn.  Returns six float64 arrays."""
+    rng = np.random.default_rng(seed)
+    out = [np.empty(0) for _ in range(6)]
+    need = n
+    while need > 0:
+        m = int(need * 1.3) + 16
+        lo, hi = np.log(1e-3), np.log(1e1)
+        rL, rR, pL, pR = (np.exp(rng.uniform(lo, hi, m)) for _ in range(4))
+        aL = np.sqrt(gamma * pL / rL)
+        aR = np.sqrt(gamma * pR / rR)
+        c = np.maximum(aL, aR)
+        uL = rng.uniform(-3, 3, m) * c
+        uR = rng.uniform(-3, 3, m) * c
+        ok = (uR - uL) < 2 * (aL + aR) / (gamma - 1) if exclude_vacuum else np.ones(m, bool)
+        for k, arr in enumerate((rL, uL, pL, rR, uR, pR)):
+            out[k] = np.concatenate([out[k], arr[ok]])
+        need = n - len(out[0])
+    return tuple(a[:n] for a in out)
+
+
+def quadrants_2d(n=2048, seed=3, gamma=GAMMA, margin=0.8):
+    """2-D four-quadrant Riemann problem on the unit square, n^2 cells; the
+    four states are drawn from the distribution of riemann_samples, redrawn
+    until no interface (in x or y, including the periodic wrap) comes within
+    `margin` of generating vacuum."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(1e-3), np.log(1e1)
+    while True:
+        rho = np.exp(rng.uniform(lo, hi, 4))
+        p = np.exp(rng.uniform(lo, hi, 4))
+        a = np.sqrt(gamma * p / rho)
+        c = a.max()
+        u = rng.uniform(-3, 3, 4) * c
+        v = rng.uniform(-3, 3, 4) * c
+        # quadrants: 0 = (x<.5,y<.5), 1 = (x>=.5,y<.5), 2 = (x<.5,y>=.5), 3 = (x>=.5,y>=.5)
+        ok = True
+        for l, r in ((0, 1), (2, 3), (1, 0), (3, 2)):
+            ok &= (u[r] - u[l]) < margin * 2 * (a[l] + a[r]) / (gamma - 1)
+        for l, r in ((0, 2), (1, 3), (2, 0), (3, 1)):
+            ok &= (v[r] - v[l]) < margin * 2 * (a[l] + a[r]) / (gamma - 1)
+        if ok:
+            break
+    x = (np.arange(n) + 0.5) / n
+    q = (x[None, :] >= 0.5).astype(np.int64) + 2 * (x[:, None] >= 0.5)
+    return cons_from_prim(rho[q], [u[q], v[q]], p[q], gamma).reshape(4, 1, n, n)

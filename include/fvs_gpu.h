@@ -86,6 +86,8 @@ typedef struct fvs_method {
   int32_t reserved;
   double tolerance;      /* Newton tolerance on |f(p)| (reference: 1e-7) */
   double gamma;          /* ratio of specific heats (reference: 1.4) */
+  const float* mlp_params; /* device pointer to the learned-guess parameters
+                              (FVS_GUESS_MLP); see fvs_mlp_param_count() */
 } fvs_method;
 
 /* Fills `m` with the reference's defaults: MUSCL-Hancock + HLLE, van Leer,
@@ -169,6 +171,20 @@ int fvs_complete_from_cons(int rank, double gamma, double* complete_dev,
                            fvs_box complete_box, const double* cons_dev,
                            fvs_box cons_box, fvs_box region, void* stream);
 
+/* ExactRiemannSolver<PerfectGas<1>>::ComputeMiddleState for n independent
+ * problems given by primitive states (device arrays of length n)
+ * (src/equations/perfect_gas/ExactRiemannSolver.hpp:34-97,
+ * include/fub/NewtonIteration.hpp:28-52), with the start value of
+ * m->guess, tolerance m->tolerance and at most m->max_iterations Newton
+ * steps.  Outputs (device, may be NULL): p*, u*, iteration counts and a
+ * status per problem (1 converged, 2 converged after the learned start was
+ * rejected, 0 not converged). */
+int fvs_exact_riemann_star(const fvs_method* m, int64_t n, const double* rhoL_dev,
+                           const double* uL_dev, const double* pL_dev,
+                           const double* rhoR_dev, const double* uR_dev,
+                           const double* pR_dev, double* pstar_dev, double* ustar_dev,
+                           int32_t* iterations_dev, int32_t* status_dev, void* stream);
+
 /* ---- Solver context: a uniform single-level grid ----------------------- */
 
 typedef struct fvs_grid_desc {
@@ -219,6 +235,11 @@ int fvs_solver_step(fvs_solver* s, double dt, int cycle);
  * dt_log (host, may be NULL) receives up to `dt_log_len` committed dts. */
 int fvs_solver_run(fvs_solver* s, double cfl, double t_end, int max_steps,
                    double* dt_log, int dt_log_len, fvs_run_stats* stats);
+/* Newton iterations and non-converged faces of the exact Riemann solver,
+ * accumulated by the solver's Godunov sweeps (fvs_solver_sweep/step since
+ * the last reset, plus the last fvs_solver_run, which restarts its count). */
+int fvs_solver_newton_stats(fvs_solver* s, uint64_t* iterations, uint64_t* failures,
+                            int reset);
 /* The solver's CUDA stream (cudaStream_t): every solver call runs on it. */
 int fvs_solver_stream(fvs_solver* s, void** stream);
 /* Cycle counter used for the direction order of the next step. */
