@@ -212,6 +212,7 @@ def run_ours(args):
         solver = fvs.Solver([n] * 3, [1.0 / n] * 3, "periodic", method=method)
         stream = torch.cuda.ExternalStream(solver.stream_handle())
         solver.upload(cons)
+        segs = solver.autotune()
         if args.warmup:
             solver.run(cfl=0.8, t_end=1e9, max_steps=args.warmup)
         clocks = ClockSampler(torch.cuda.current_device()) if with_clocks else None
@@ -249,7 +250,7 @@ def run_ours(args):
                     sweep_ms.append(a.elapsed_time(b))
         sweep_s = statistics.mean(sweep_ms) / 1e3
         achieved = algo_bytes / sweep_s / 1e9
-        res = {"ms": ms, "value": 6 * cells * args.steps * world / (ms / 1e3),
+        res = {"ms": ms, "value": 6 * cells * args.steps * world / (ms / 1e3), "segs": segs,
                "final": final, "clocks": clk, "sweep_s": sweep_s, "achieved": achieved,
                "solver": solver}
         return res
@@ -317,6 +318,7 @@ def run_ours(args):
             "config": {"workload": f"3D perfect gas {n}^3 periodic, Strang MUSCL-Hancock/VanLeer"
                                    " + HLLE, CFL 0.8, seeded octants + Gaussian bumps",
                        "n": n, "precision": args.precision, "sweeps_per_step": 6,
+                       "autotuned_segment_cells": main["segs"],
                        "l2": "inputs larger than L2 (state 671 MB per copy)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": main["achieved"], "peak": peaks["hbm_gbs"],
@@ -334,6 +336,7 @@ def run_ours(args):
             "accuracy": accuracy(main["final"]),
             "variants": {k: {"value": v["value"], "ms_per_step": v["ms"] / args.steps,
                              "sweep_launch_ms": v["sweep_s"] * 1e3,
+                             "autotuned_segment_cells": v["segs"],
                              "hbm_frac": v["achieved"] / peaks["hbm_gbs"],
                              "accuracy": accuracy(v["final"])}
                          for k, v in variants.items()},

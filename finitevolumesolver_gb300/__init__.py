@@ -223,6 +223,11 @@ class Solver:
     def set_tiling(self, seg_len: int) -> None:
         _capi.check(lib().fvs_solver_set_tiling(self._h, int(seg_len)))
 
+    def autotune(self):
+        segs = (C.c_int * 3)()
+        _capi.check(lib().fvs_solver_autotune(self._h, segs))
+        return list(segs)[: self.rank]
+
     def set_cycle(self, cycle: int) -> None:
         _capi.check(lib().fvs_solver_set_cycle(self._h, int(cycle)))
 

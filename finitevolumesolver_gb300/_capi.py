@@ -93,6 +93,7 @@ def load() -> C.CDLL:
     L.fvs_solver_download.argtypes = [_VP, _VP]
     L.fvs_solver_state_device.argtypes = [_VP, P(_VP)]
     L.fvs_solver_set_tiling.argtypes = [_VP, C.c_int]
+    L.fvs_solver_autotune.argtypes = [_VP, P(C.c_int)]
     L.fvs_solver_stable_dt.argtypes = [_VP, C.c_int, _DP]
     L.fvs_solver_sweep.argtypes = [_VP, C.c_int, C.c_double, _DP]
     L.fvs_solver_step.argtypes = [_VP, C.c_double, C.c_int]

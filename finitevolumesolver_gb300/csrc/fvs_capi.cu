@@ -186,6 +186,7 @@ struct fvs_solver {
   double* dt_log_dev = nullptr;
   int dt_log_cap = 0;
   int seg_len = 0;
+  int seg_tuned[3] = {0, 0, 0};  // autotuned cells per thread segment, per direction
   int64_t cycle = 0;
   double t = 0.0;
   int64_t cells = 0;
@@ -208,11 +209,15 @@ namespace {
 
 int SegLen(const fvs_solver* s, int dir) {
   if (s->seg_len > 0) return s->seg_len;
+  if (s->seg_tuned[dir] > 0) return s->seg_tuned[dir];
   const int nd = s->g.n[dir];
   int64_t ntrans = s->cells / nd;
-  // Aim for at least ~64K threads; never shorter than 16 cells.
+  // Enough threads for several waves of resident blocks on 152 SMs
+  // (~60K threads per wave at 150 registers per thread); never shorter than
+  // 16 cells (the 2-cell halo of a segment is recomputed).
+  const int64_t target = 262144;
   int seg = nd;
-  while (seg > 16 && ntrans * ((nd + seg - 1) / seg) < 65536) seg = (seg + 1) / 2;
+  while (seg > 16 && ntrans * ((nd + seg - 1) / seg) < target) seg = (seg + 1) / 2;
   return seg;
 }
 
@@ -563,6 +568,56 @@ int fvs_solver_state_device(fvs_solver* s, double** cons_dev) {
 int fvs_solver_set_tiling(fvs_solver* s, int seg_len) {
   if (!s || seg_len < 0) return Fail(FVS_ERR_INVALID, "bad tiling");
   s->seg_len = seg_len;
+  return FVS_OK;
+}
+
+int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
+  if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
+  // Candidate segment lengths per direction, timed on the current state with
+  // a small dt (output goes to a spare buffer; the state is not changed).
+  const int cands[] = {16, 32, 64, 128, 256, 512};
+  const int saved = s->seg_len;
+  cudaEvent_t e0, e1;
+  FVS_CUDA(cudaEventCreate(&e0));
+  FVS_CUDA(cudaEventCreate(&e1));
+  double dt = 0.0;
+  {
+    const int r = fvs_solver_stable_dt(s, -1, &dt);
+    if (r) return r;
+  }
+  dt = std::isfinite(dt) ? 0.1 * dt : 1e-6;
+  const int out = (s->cur + 1) % 3;
+  for (int d = 0; d < s->g.rank; ++d) {
+    const int nd = s->g.n[d];
+    float best = 1e30f;
+    int best_seg = 0;
+    for (int c : cands) {
+      if (c > 2 * nd && c != cands[0]) break;
+      s->seg_len = c;
+      float ms_sum = 0.f;
+      for (int rep = 0; rep < 3; ++rep) {
+        FVS_CUDA(cudaEventRecord(e0, s->stream));
+        FVS_CUDA(LaunchSweep(s, s->buf[s->cur], s->buf[out], d, nullptr, 1.0, dt,
+                             s->scratch_words, nullptr, -1, 0.0));
+        FVS_CUDA(cudaEventRecord(e1, s->stream));
+        FVS_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        FVS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) ms_sum += ms;
+      }
+      if (ms_sum < best) {
+        best = ms_sum;
+        best_seg = c;
+      }
+    }
+    s->seg_tuned[d] = best_seg;
+    if (seg_out) seg_out[d] = best_seg;
+  }
+  s->seg_len = saved;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
   return FVS_OK;
 }
 

@@ -12,6 +12,7 @@ namespace fvs {
 // Exact policy for the marching sweep.
 template <int D> struct ExactPolicy {
   using Real = double;
+  static constexpr bool kWarpX = false;
   using Gas = exact::Gas;
   using Wave = exact::CellWave;
   using Rec = exact::Complete<D>;

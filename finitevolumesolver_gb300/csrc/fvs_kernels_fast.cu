@@ -50,6 +50,8 @@ __device__ __forceinline__ double FloatToDoubleBits(float x) {
 
 template <int D, typename T> struct FastBase {
   using Real = T;
+  // the mixed flavour is memory-bound: its x sweep uses lanes along x
+  static constexpr bool kWarpX = sizeof(T) == 4;
   using Gas = fast::Gas<T>;
   using Rec = fast::State<D, T>;
   using Wave = fast::Wave<T>;

@@ -36,6 +36,7 @@ __device__ __forceinline__ GodunovGas MakeGodunovGas(double gamma, int guess, in
 // for the CFL check, as the reference does.
 template <int D, bool kMuscl> struct GodunovPolicyT {
   using Real = double;
+  static constexpr bool kWarpX = false;
   using Gas = GodunovGas;
   using Rec = exact::Complete<D>;
   using Wave = exact::Complete<D>;

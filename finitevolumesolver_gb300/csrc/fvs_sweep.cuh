@@ -22,6 +22,8 @@
 
 #include "fvs_internal.h"
 
+#include <cstring>
+
 namespace fvs {
 
 __device__ __forceinline__ int BcIndex(int j, int n, int bc) {
@@ -142,18 +144,22 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * cs + off);
     };
-    // double window for the update, compute-precision window for the rest
-    double dm[K], dc[K], dp[K];
+    // double window for the update, compute-precision window for the rest;
+    // the loads run one cell ahead of the arithmetic (dn is the next "up")
+    double dm[K], dc[K], dp[K], dn[K];
     R cm[K], cc[K], cp[K];
     load(dm, j0 - 2);
     load(dc, j0 - 1);
+    load(dn, j0);
     P::ToCell(cm, dm);
     P::ToCell(cc, dc);
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
     double F_prev[K];
     for (int j = j0 - 1; j <= j1; ++j) {
-      load(dp, j + 1);
+#pragma unroll
+      for (int c = 0; c < K; ++c) dp[c] = dn[c];
+      if (j + 2 <= j1 + 1) load(dn, j + 2);
       P::ToCell(cp, dp);
       typename P::Rec recL, recR;
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
@@ -195,6 +201,206 @@ __global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
   if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
 }
 
+// Warp shuffles of whole structs (32-bit words).
+template <class T> __device__ __forceinline__ T ShflUp(const T& v, unsigned delta) {
+  static_assert(sizeof(T) % 4 == 0, "shuffle of 32-bit words");
+  constexpr int N = sizeof(T) / 4;
+  unsigned w[N];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int i = 0; i < N; ++i) w[i] = __shfl_up_sync(0xffffffffu, w[i], delta);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+template <class T> __device__ __forceinline__ T ShflDown(const T& v, unsigned delta) {
+  constexpr int N = sizeof(T) / 4;
+  unsigned w[N];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int i = 0; i < N; ++i) w[i] = __shfl_down_sync(0xffffffffu, w[i], delta);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+template <class T> __device__ __forceinline__ T ShflIdx(const T& v, int src) {
+  constexpr int N = sizeof(T) / 4;
+  unsigned w[N];
+  memcpy(w, &v, sizeof(T));
+#pragma unroll
+  for (int i = 0; i < N; ++i) w[i] = __shfl_sync(0xffffffffu, w[i], src);
+  T r;
+  memcpy(&r, w, sizeof(T));
+  return r;
+}
+
+template <class R, int K> struct CellArr {
+  R v[K];
+};
+
+// x sweep with the lanes of a warp along x: every load and store of a warp
+// touches 32 consecutive doubles of one row, and the neighbours a cell needs
+// come from the adjacent lanes by shuffles.  One warp owns one row and walks
+// it in chunks of 32 cells; lane l of a chunk reconstructs cell x, computes
+// the flux of face x (between x-1 and x) and updates cell x-1.  A warm-up
+// step reconstructs cells -2 and -1; on a periodic row lane 0 of the first
+// chunk then updates cell -1 = nx-1, which closes the ring without a partial
+// last step.  A transmissive row finishes with a one-lane step for cell
+// nx-1.  The arithmetic per face and cell is the policy's, exactly as in
+// SweepMarchKernel.
+template <int D, template <int> class PT>
+__global__ void __launch_bounds__(128) SweepXWarpKernel(SweepArgs a) {
+  using P = PT<D>;
+  using R = typename P::Real;
+  constexpr int K = D + 2;
+  using Cell = CellArr<R, K>;
+  using Dbl = CellArr<double, K>;
+  const int nx = a.n[0];
+  const int64_t cs = int64_t(nx) * a.n[1] * a.n[2];
+  const int64_t rows = int64_t(a.n[1]) * a.n[2];
+  const int lane = threadIdx.x & 31;
+  const int64_t row = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
+  if (!SweepGate(a, split_dt)) return;
+  if (row >= rows) return;  // warp-uniform
+  const int64_t base = row * nx;
+  const bool periodic = (a.bc == 0);
+  const typename P::Gas eq = P::MakeGasFor(a);
+  const double lambda_half = 0.5 * split_dt / a.dx;
+  const double dt_dx = split_dt / a.dx;
+  const double* __restrict__ in = a.in;
+  double* __restrict__ out = a.out;
+  auto load = [&](Dbl& u, int x) {
+    const int64_t off = base + BcIndex(x, nx, a.bc);
+#pragma unroll
+    for (int c = 0; c < K; ++c) u.v[c] = __ldg(in + c * cs + off);
+  };
+  auto to_cell = [&](const Dbl& u) {
+    Cell c;
+    P::ToCell(c.v, u.v);
+    return c;
+  };
+  R smax = R(0);
+  int status = 0;
+  typename P::Stats stats;
+
+  // ---- warm-up: cells -3..-1 in lanes 29..31, cell 0 from the first chunk
+  Dbl U0;
+  load(U0, lane);                      // chunk 0
+  Dbl Uw;
+  load(Uw, lane >= 29 ? lane - 32 : -3);  // lanes 0..28 hold a copy of cell -3
+  Cell Cw = to_cell(Uw);
+  const Cell C0 = to_cell(U0);
+  Cell Cwm = ShflUp(Cw, 1);
+  Cell Cwp = ShflDown(Cw, 1);
+  const Cell C0first = ShflIdx(C0, 0);
+  if (lane == 31) Cwp = C0first;
+  if (lane == 0) Cwm = Cw;
+  typename P::Rec wrecL, wrecR;
+  P::Predict(eq, wrecL, wrecR, Cwm.v, Cw.v, Cwp.v, a.limiter, lambda_half, 0);
+  typename P::Wave wW = P::MakeWave(eq, Cw.v, 0);
+  // face -1 (between cells -2 and -1), used to update cell -1 on a periodic row
+  const typename P::Rec wrecRm = ShflUp(wrecR, 1);
+  const typename P::Wave wWm = ShflUp(wW, 1);
+  double Fw[K];
+  typename P::Stats wstats;
+  P::Face(eq, Fw, wrecRm, wrecL, wWm, wW, 0, wstats);
+  // carries into chunk 0 (from lane 31 = cell -1)
+  typename P::Rec carry_rec = ShflIdx(wrecR, 31);
+  typename P::Wave carry_w = ShflIdx(wW, 31);
+  Cell carry_c = ShflIdx(Cw, 31);
+  Dbl carry_u = ShflIdx(Uw, 31);
+  Dbl carry_f;
+#pragma unroll
+  for (int c = 0; c < K; ++c) carry_f.v[c] = Fw[c];
+  carry_f = ShflIdx(carry_f, 31);
+
+  Dbl U = U0;
+  Cell C = C0;
+  const int nchunks = (nx + 31) / 32;
+  Dbl Unext;  // the chunk after the next one is loaded one iteration early
+  load(Unext, lane + 32);
+  for (int ch = 0; ch < nchunks; ++ch) {
+    const int x0 = ch * 32;
+    const int x = x0 + lane;
+    const bool valid = x < nx;
+    const Dbl Un = Unext;
+    if (ch + 1 < nchunks) load(Unext, x + 64);
+    const Cell Cn = to_cell(Un);
+    Cell Cp = ShflDown(C, 1);
+    const Cell Cn0 = ShflIdx(Cn, 0);
+    if (lane == 31) Cp = Cn0;
+    if (x + 1 >= nx && !periodic) Cp = C;  // transmissive: cells >= nx copy nx-1
+    Cell Cm = ShflUp(C, 1);
+    if (lane == 0) Cm = carry_c;
+    typename P::Rec recL, recR;
+    P::Predict(eq, recL, recR, Cm.v, C.v, Cp.v, a.limiter, lambda_half, 0);
+    const typename P::Wave W = P::MakeWave(eq, C.v, 0);
+    typename P::Rec recRm = ShflUp(recR, 1);
+    typename P::Wave Wm = ShflUp(W, 1);
+    if (lane == 0) {
+      recRm = carry_rec;
+      Wm = carry_w;
+    }
+    double F[K];
+    const R sp = P::Face(eq, F, recRm, recL, Wm, W, 0, stats);
+    if (valid) smax = sp > smax ? sp : smax;
+    Dbl Fd;
+#pragma unroll
+    for (int c = 0; c < K; ++c) Fd.v[c] = F[c];
+    Dbl Fm = ShflUp(Fd, 1);
+    Dbl Um = ShflUp(U, 1);
+    if (lane == 0) {
+      Fm = carry_f;
+      Um = carry_u;
+    }
+    // update cell x-1 (lane 0 of chunk 0: cell -1, i.e. nx-1 on a periodic row)
+    const bool upd = valid && (x >= 1 || periodic);
+    if (upd) {
+      const int64_t off = base + BcIndex(x - 1, nx, a.bc);
+#pragma unroll
+      for (int c = 0; c < K; ++c) {
+        const double v = Um.v[c] + dt_dx * (Fm.v[c] - Fd.v[c]);
+        out[c * cs + off] = v;
+        if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
+      }
+    }
+    // carries: the chunk's last cell
+    const int last = min(31, nx - 1 - x0);
+    carry_rec = ShflIdx(recR, last);
+    carry_w = ShflIdx(W, last);
+    carry_c = ShflIdx(C, last);
+    carry_u = ShflIdx(U, last);
+    carry_f = ShflIdx(Fd, last);
+    U = Un;
+    C = Cn;
+  }
+  if (!periodic) {
+    // face nx and cell nx-1 of a transmissive row (cells >= nx copy nx-1)
+    typename P::Rec recL, recR;
+    P::Predict(eq, recL, recR, carry_c.v, carry_c.v, carry_c.v, a.limiter, lambda_half, 0);
+    const typename P::Wave W = P::MakeWave(eq, carry_c.v, 0);
+    double F[K];
+    const R sp = P::Face(eq, F, carry_rec, recL, carry_w, W, 0, stats);
+    if (lane == 0) {
+      smax = sp > smax ? sp : smax;
+      const int64_t off = base + (nx - 1);
+#pragma unroll
+      for (int c = 0; c < K; ++c) {
+        const double v = carry_u.v[c] + dt_dx * (carry_f.v[c] - F[c]);
+        out[c * cs + off] = v;
+        if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
+      }
+    }
+  }
+  stats.Flush(a.stats_out);
+  const double smax_w = WarpMax(static_cast<double>(smax));
+  if (lane == 0 && a.smax_out && smax_w > 0.0) AtomicMaxPositive(a.smax_out, smax_w);
+  if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
+}
+
 template <int D, template <int> class P>
 cudaError_t LaunchSweepT(const SweepArgs& a, cudaStream_t s) {
   const int nd = a.n[a.dir];
@@ -209,7 +415,13 @@ cudaError_t LaunchSweepT(const SweepArgs& a, cudaStream_t s) {
             static_cast<unsigned>((nd + seg - 1) / seg));
   switch (a.dir) {
   case 0:
-    SweepMarchKernel<D, 0, P><<<grid, block, 0, s>>>(b);
+    if constexpr (P<D>::kWarpX) {
+      const int64_t rows = int64_t(a.n[1]) * a.n[2];
+      const unsigned xgrid = static_cast<unsigned>((rows * 32 + block - 1) / block);
+      SweepXWarpKernel<D, P><<<xgrid, block, 0, s>>>(b);
+    } else {
+      SweepMarchKernel<D, 0, P><<<grid, block, 0, s>>>(b);
+    }
     break;
   case 1:
     if constexpr (D >= 2) SweepMarchKernel<D, 1, P><<<grid, block, 0, s>>>(b);

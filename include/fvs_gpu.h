@@ -217,6 +217,11 @@ int fvs_solver_state_device(fvs_solver* s, double** cons_dev);
 /* Threads per block / cells per thread segment of the sweep kernels
  * (0 = automatic). */
 int fvs_solver_set_tiling(fvs_solver* s, int seg_len);
+/* Autotuner: times the sweep kernel on the current state for candidate
+ * segment lengths (cells per thread along the sweep direction) and keeps
+ * the fastest per direction (used unless fvs_solver_set_tiling forces one).
+ * seg_out (may be NULL) receives rank values.  Does not change the state. */
+int fvs_solver_autotune(fvs_solver* s, int* seg_out);
 /* Stable dt of the current state: dir = -1 for the minimum over all
  * directions (DimensionalSplitLevelIntegrator::ComputeStableDt). */
 int fvs_solver_stable_dt(fvs_solver* s, int dir, double* dt_out);

@@ -191,6 +191,14 @@ def test_solver_sweeps_and_dt(fvs, orc, rank, n, bc):
         s.upload(cons)
         s.step(dt, cycle)
         np.testing.assert_array_equal(s.download(), g.step(m, cons, dt, cycle))
+    # the autotuner only picks segment lengths: results stay bit-identical
+    s.set_tiling(0)
+    s.upload(cons)
+    segs = s.autotune()
+    assert len(segs) == rank and all(v > 0 for v in segs)
+    np.testing.assert_array_equal(s.download(), cons)
+    s.step(dt, 0)
+    np.testing.assert_array_equal(s.download(), g.step(m, cons, dt, 0))
     s.close()
 
 
