@@ -223,6 +223,29 @@ class Solver:
     def set_tiling(self, seg_len: int) -> None:
         _capi.check(lib().fvs_solver_set_tiling(self._h, int(seg_len)))
 
+    def set_embedded_circles(self, circles, x0=0.0, y0=0.0) -> None:
+        """Union of circles (rows cx, cy, r; the body is their inside) as an
+        embedded boundary: the solver switches to the KBN cut-cell update."""
+        import numpy as np
+        c = np.ascontiguousarray(circles, dtype=np.float64).reshape(-1, 3)
+        self._circles = c
+        _capi.check(lib().fvs_solver_set_embedded_circles(self._h, c.ctypes.data, len(c),
+                                                          float(x0), float(y0)))
+
+    def cutcell_geometry(self):
+        import numpy as np
+        G = lib().fvs_cutcell_ghost_layers()
+        nx, ny = self.n[0], self.n[1]
+        NX, NY = nx + 2 * G, ny + 2 * G
+        out = {"alpha": np.zeros((NY, NX)), "betax": np.zeros((NY, NX + 1)),
+               "betay": np.zeros((NY + 1, NX)), "normal": np.zeros((2, NY, NX)),
+               "center": np.zeros((2, NY, NX)), "cut": np.zeros((NY, NX), dtype=np.int8)}
+        _capi.check(lib().fvs_solver_cutcell_geometry(
+            self._h, *[out[k].ctypes.data for k in ("alpha", "betax", "betay", "normal", "center",
+                                                   "cut")]))
+        out["ghost"] = G
+        return out
+
     def autotune(self):
         segs = (C.c_int * 3)()
         _capi.check(lib().fvs_solver_autotune(self._h, segs))

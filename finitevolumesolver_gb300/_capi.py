@@ -103,6 +103,9 @@ def load() -> C.CDLL:
     L.fvs_solver_newton_stats.argtypes = [_VP, P(C.c_uint64), P(C.c_uint64), C.c_int]
     L.fvs_exact_riemann_star.argtypes = [P(Method), C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                                          _VP, _VP, _VP, _VP]
+    L.fvs_cutcell_ghost_layers.restype = C.c_int
+    L.fvs_solver_set_embedded_circles.argtypes = [_VP, _VP, C.c_int, C.c_double, C.c_double]
+    L.fvs_solver_cutcell_geometry.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
     L.fvs_solver_set_cycle.argtypes = [_VP, C.c_int64]
     L.fvs_solver_set_time.argtypes = [_VP, C.c_double]
     _lib = L

@@ -28,6 +28,7 @@ UNITS = [
     ("fvs_kernels_exact.cu", ["-fmad=false"]),
     ("fvs_kernels_fast.cu", []),
     ("fvs_kernels_godunov.cu", ["-fmad=false"]),
+    ("fvs_kernels_cutcell.cu", ["-fmad=false"]),
     ("fvs_capi.cu", []),
     ("fvs_noalloc.cu", ["-fmad=false"]),
 ]

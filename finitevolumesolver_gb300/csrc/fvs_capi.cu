@@ -2,6 +2,7 @@
 // checking, the patch-level entry points, and the uniform-grid solver
 // context with its device-resident time stepping and CUDA graphs.
 #include "../../include/fvs_gpu.h"
+#include "fvs_cutcell.h"
 #include "fvs_internal.h"
 
 #include <cmath>
@@ -192,7 +193,13 @@ struct fvs_solver {
   int64_t cells = 0;
   int ncons = 0;
   std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
+  // embedded boundary (KBN cut cells, rank 2)
+  bool cc = false;
+  fvs::CcGeom ccg{};
+  double* cc_refs = nullptr;
+  std::vector<void*> cc_allocs;
   ~fvs_solver() {
+    for (void* p : cc_allocs) cudaFree(p);
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     for (double* b : buf)
       if (b) cudaFree(b);
@@ -221,10 +228,38 @@ int SegLen(const fvs_solver* s, int dir) {
   return seg;
 }
 
+fvs::CcStateArgs MakeCcState(const fvs_solver* s, const double* in) {
+  fvs::CcStateArgs a{};
+  a.g = s->ccg;
+  a.in = in;
+  a.bc[0] = s->g.bc[0];
+  a.bc[1] = s->g.bc[1];
+  a.gamma = s->m.gamma;
+  a.refs = s->cc_refs;
+  return a;
+}
+
 cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
                         int dir, const double* dt_ptr, double dt_scale,
                         double dt_value, unsigned long long* smax_out,
                         fvs::Control* ctrl, int prev_check, double prev_dx) {
+  if (s->cc) {
+    fvs::CcSweepArgs c{};
+    c.s = MakeCcState(s, in);
+    c.out = out;
+    c.dir = dir;
+    c.limiter = s->m.limiter;
+    c.seg_len = SegLen(s, dir);
+    c.dx = s->g.dx[dir];
+    c.dt_ptr = dt_ptr;
+    c.dt_scale = dt_scale;
+    c.dt_value = dt_value;
+    c.smax_out = smax_out;
+    c.ctrl = ctrl;
+    c.prev_check = prev_check;
+    c.prev_dx = prev_dx;
+    return fvs::LaunchCutCellSweep(c, s->stream);
+  }
   fvs::SweepArgs a{};
   a.in = in;
   a.out = out;
@@ -262,6 +297,7 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
 
 cudaError_t LaunchStable(const fvs_solver* s, const double* in,
                          unsigned long long* smax_out, fvs::Control* ctrl) {
+  if (s->cc) return fvs::LaunchCutCellStableDt(MakeCcState(s, in), smax_out, ctrl, s->stream);
   fvs::StableDtArgs a{};
   a.in = in;
   for (int d = 0; d < 3; ++d) {
@@ -320,7 +356,13 @@ int NextBuffer(int start, int nsweeps) { return (start + (nsweeps % 2 ? 1 : 2)) 
 // Enqueue one device-driven split step starting in buffer `start`.
 cudaError_t EnqueueStep(fvs_solver* s, int start, int64_t cycle, int step_in_batch) {
   const fvs::StepPlan plan = MakePlan(s, cycle);
-  cudaError_t e = LaunchStable(s, s->buf[start], s->ctrl->smax_stable, s->ctrl);
+  cudaError_t e = cudaSuccess;
+  if (s->cc) {
+    // KbnCutCellMethod::PreAdvanceHierarchy: reference states of the step
+    e = fvs::LaunchCutCellReferenceStates(MakeCcState(s, s->buf[start]), s->stream);
+    if (e != cudaSuccess) return e;
+  }
+  e = LaunchStable(s, s->buf[start], s->ctrl->smax_stable, s->ctrl);
   if (e != cudaSuccess) return e;
   fvs::BeginStepKernel<<<1, 1, 0, s->stream>>>(s->ctrl, plan);
   const int X = (start + 1) % 3, Y = (start + 2) % 3;
@@ -621,6 +663,90 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   return FVS_OK;
 }
 
+int fvs_cutcell_ghost_layers(void) { return fvs::kCcGhost; }
+
+int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int ncircles,
+                                    double x0, double y0) {
+  if (!s || !circles) return Fail(FVS_ERR_INVALID, "NULL argument");
+  if (s->g.rank != 2) return Fail(FVS_ERR_UNSUPPORTED, "cut cells need a rank-2 grid");
+  if (s->m.flux_method != FVS_MUSCL_HLLE || s->m.precision != FVS_FP64_EXACT)
+    return Fail(FVS_ERR_UNSUPPORTED, "cut cells run MUSCL-Hancock + HLLE in exact FP64");
+  if (ncircles < 1 || ncircles > 16) return Fail(FVS_ERR_INVALID, "1 to 16 circles");
+  for (int k = 0; k < ncircles; ++k)
+    if (!(circles[3 * k + 2] > 0.0)) return Fail(FVS_ERR_INVALID, "circle radius must be > 0");
+  if (s->cc) return Fail(FVS_ERR_INVALID, "embedded boundary already set");
+  fvs::CcGeom& g = s->ccg;
+  g.nx = s->g.n[0];
+  g.ny = s->g.n[1];
+  const size_t cells = size_t(g.NX()) * g.NY();
+  const size_t fx = size_t(g.NX() + 1) * g.NY(), fy = size_t(g.NX()) * (g.NY() + 1);
+  auto alloc = [&](double** p, size_t n) -> cudaError_t {
+    cudaError_t e = cudaMalloc(p, n * sizeof(double));
+    if (e == cudaSuccess) {
+      s->cc_allocs.push_back(*p);
+      e = cudaMemset(*p, 0, n * sizeof(double));
+    }
+    return e;
+  };
+  FVS_CUDA(alloc(&g.alpha, cells));
+  FVS_CUDA(alloc(&g.beta[0], fx));
+  FVS_CUDA(alloc(&g.beta[1], fy));
+  FVS_CUDA(alloc(&g.normal, 2 * cells));
+  FVS_CUDA(alloc(&g.center, 2 * cells));
+  for (int d = 0; d < 2; ++d) {
+    const size_t nf = d == 0 ? fx : fy;
+    FVS_CUDA(alloc(&g.us[d], nf));
+    FVS_CUDA(alloc(&g.sL[d], nf));
+    FVS_CUDA(alloc(&g.sR[d], nf));
+    FVS_CUDA(alloc(&g.us_rel[d], nf));
+    FVS_CUDA(alloc(&g.sL_rel[d], nf));
+    FVS_CUDA(alloc(&g.sR_rel[d], nf));
+  }
+  FVS_CUDA(alloc(&s->cc_refs, 6 * cells));
+  void* cut = nullptr;
+  FVS_CUDA(cudaMalloc(&cut, cells));
+  s->cc_allocs.push_back(cut);
+  g.cut = static_cast<signed char*>(cut);
+  double* dcirc = nullptr;
+  FVS_CUDA(alloc(&dcirc, size_t(3) * ncircles));
+  FVS_CUDA(cudaMemcpy(dcirc, circles, sizeof(double) * 3 * ncircles, cudaMemcpyHostToDevice));
+  fvs::CcGeomArgs ga{};
+  ga.nx = g.nx;
+  ga.ny = g.ny;
+  ga.x0 = x0;
+  ga.y0 = y0;
+  ga.dx = s->g.dx[0];
+  ga.dy = s->g.dx[1];
+  ga.ncirc = ncircles;
+  ga.circles = dcirc;
+  ga.alpha = g.alpha;
+  ga.betax = g.beta[0];
+  ga.betay = g.beta[1];
+  ga.normal = g.normal;
+  ga.center = g.center;
+  FVS_CUDA(fvs::LaunchCutCellGeometry(ga, g, s->stream));
+  FVS_CUDA(cudaStreamSynchronize(s->stream));
+  s->cc = true;
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+  return FVS_OK;
+}
+
+int fvs_solver_cutcell_geometry(fvs_solver* s, double* alpha, double* betax, double* betay,
+                                double* normal, double* center, int8_t* cut_flags) {
+  if (!s || !s->cc) return Fail(FVS_ERR_INVALID, "no embedded boundary");
+  const fvs::CcGeom& g = s->ccg;
+  const size_t cells = size_t(g.NX()) * g.NY();
+  const size_t fx = size_t(g.NX() + 1) * g.NY(), fy = size_t(g.NX()) * (g.NY() + 1);
+  if (alpha) FVS_CUDA(cudaMemcpy(alpha, g.alpha, cells * 8, cudaMemcpyDeviceToHost));
+  if (betax) FVS_CUDA(cudaMemcpy(betax, g.beta[0], fx * 8, cudaMemcpyDeviceToHost));
+  if (betay) FVS_CUDA(cudaMemcpy(betay, g.beta[1], fy * 8, cudaMemcpyDeviceToHost));
+  if (normal) FVS_CUDA(cudaMemcpy(normal, g.normal, 2 * cells * 8, cudaMemcpyDeviceToHost));
+  if (center) FVS_CUDA(cudaMemcpy(center, g.center, 2 * cells * 8, cudaMemcpyDeviceToHost));
+  if (cut_flags) FVS_CUDA(cudaMemcpy(cut_flags, g.cut, cells, cudaMemcpyDeviceToHost));
+  return FVS_OK;
+}
+
 int fvs_solver_set_cycle(fvs_solver* s, int64_t cycle) {
   if (!s || cycle < 0) return Fail(FVS_ERR_INVALID, "bad cycle");
   s->cycle = cycle;
@@ -657,6 +783,8 @@ int fvs_solver_sweep(fvs_solver* s, int dir, double dt, double* level_dt_out) {
   if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
   if (dir < 0 || dir >= s->g.rank) return Fail(FVS_ERR_INVALID, "direction out of range");
   const int out = (s->cur + 1) % 3;
+  if (s->cc)
+    FVS_CUDA(fvs::LaunchCutCellReferenceStates(MakeCcState(s, s->buf[s->cur]), s->stream));
   FVS_CUDA(cudaMemsetAsync(s->scratch_words, 0, sizeof(unsigned long long), s->stream));
   FVS_CUDA(LaunchSweep(s, s->buf[s->cur], s->buf[out], dir, nullptr, 1.0, dt,
                        s->scratch_words, nullptr, -1, 0.0));
@@ -679,6 +807,8 @@ int fvs_solver_step(fvs_solver* s, double dt, int cycle) {
   const double split_dt = plan.frac * dt;
   FVS_CUDA(cudaMemsetAsync(s->scratch_words, 0, 8 * sizeof(unsigned long long), s->stream));
   const int start = s->cur;
+  if (s->cc)
+    FVS_CUDA(fvs::LaunchCutCellReferenceStates(MakeCcState(s, s->buf[start]), s->stream));
   const int X = (start + 1) % 3, Y = (start + 2) % 3;
   int src = start, dst = X;
   for (int q = 0; q < plan.nsweeps; ++q) {

@@ -118,3 +118,29 @@ def quadrants_2d(n=2048, seed=3, gamma=GAMMA, margin=0.8):
     x = (np.arange(n) + 0.5) / n
     q = (x[None, :] >= 0.5).astype(np.int64) + 2 * (x[:, None] >= 0.5)
     return cons_from_prim(rho[q], [u[q], v[q]], p[q], gamma).reshape(4, 1, n, n)
+
+
+def shock_circles_2d(n=1024, seed=5, mach=2.0, gamma=GAMMA, x_shock=0.1, ncirc=8):
+    """2-D Mach `mach` planar shock moving in +x into still gas (rho 1, p 1)
+    over a union of `ncirc` circles (radii U[0.05, 0.15], centres
+    U[0.3, 0.9]^2) on the unit square, n^2 cells.  The post-shock state
+    follows from the Rankine-Hugoniot conditions.  Returns (circles [ncirc][3],
+    cons (4, 1, n, n)); cells covered by the circles are left to the caller
+    (the solver zeroes them)."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(0.05, 0.15, ncirc)
+    c = rng.uniform(0.3, 0.9, (ncirc, 2))
+    circles = np.column_stack([c, r])
+    rho1, p1 = 1.0, 1.0
+    a1 = np.sqrt(gamma * p1 / rho1)
+    m2 = mach * mach
+    rho2 = rho1 * (gamma + 1) * m2 / ((gamma - 1) * m2 + 2)
+    p2 = p1 * (1 + 2 * gamma / (gamma + 1) * (m2 - 1))
+    u2 = mach * a1 * (1 - rho1 / rho2)
+    x = (np.arange(n) + 0.5) / n
+    post = np.broadcast_to(x[None, :] < x_shock, (n, n))
+    rho = np.where(post, rho2, rho1)
+    u = np.where(post, u2, 0.0)
+    p = np.where(post, p2, p1)
+    cons = cons_from_prim(rho, [u, np.zeros((n, n))], p, gamma).reshape(4, 1, n, n)
+    return circles, cons

@@ -247,6 +247,27 @@ int fvs_solver_newton_stats(fvs_solver* s, uint64_t* iterations, uint64_t* failu
                             int reset);
 /* The solver's CUDA stream (cudaStream_t): every solver call runs on it. */
 int fvs_solver_stream(fvs_solver* s, void** stream);
+/* ---- Embedded boundary: KBN h-box cut cells (rank 2) ------------------ */
+
+/* Ghost layers of the cut-cell geometry arrays. */
+int fvs_cutcell_ghost_layers(void);
+/* Embeds the union of `ncircles` (1..16) circles, host array of (cx, cy, r)
+ * triples, the body being their inside, into a rank-2 MUSCL-HLLE exact-FP64
+ * solver whose cell (0, 0) has its lower-left corner at (x0, y0).  The FP64
+ * geometry (volume / face fractions, normals, centroids, shielded fractions)
+ * is computed on the device; from then on every sweep is the
+ * KbnCutCellMethod update (include/fub/cutcell_method/KbnStabilisation.hpp:
+ * 188-450, src/AMReX/cutcell/TimeIntegrator.cpp:65-221) with HLL boundary
+ * states, and each step starts by computing the cut cells' reference
+ * states (PreAdvanceHierarchy). */
+int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int ncircles,
+                                    double x0, double y0);
+/* Copies the geometry to host arrays over the grid grown by
+ * fvs_cutcell_ghost_layers() = G layers (NX = nx + 2G, NY = ny + 2G):
+ * alpha [NY][NX], betax [NY][NX+1], betay [NY+1][NX], normal and center
+ * [2][NY][NX], cut flags [NY][NX].  Any pointer may be NULL. */
+int fvs_solver_cutcell_geometry(fvs_solver* s, double* alpha, double* betax, double* betay,
+                                double* normal, double* center, int8_t* cut_flags);
 /* Cycle counter used for the direction order of the next step. */
 int fvs_solver_set_cycle(fvs_solver* s, int64_t cycle);
 int fvs_solver_set_time(fvs_solver* s, double t);

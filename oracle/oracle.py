@@ -194,3 +194,104 @@ def exact_star(rhoL, uL, pL, rhoR, uR, pR, guess=GUESS_MEAN, given=None, tol=1e-
                          max_iterations, _d(ps), _d(us), it.ctypes.data_as(_I32),
                          cv.ctypes.data_as(_I32))
     return ps, us, it, cv
+
+
+# ---------------------------------------------------------------------------
+# KBN cut-cell (2-D)
+
+def _cc_lib():
+    L = lib()
+    if not getattr(L, "_cc_ready", False):
+        I = C.c_int
+        L.orc_cc_ghost_layers.restype = C.c_int
+        L.orc_cc_geometry.argtypes = [I, I, C.c_double, C.c_double, C.c_double, C.c_double, I, I,
+                                      _P, _P, _P, _P, _P, _P]
+        L.orc_cc_shielded.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, _P, _P]
+        L.orc_cc_cutcells.argtypes = [_I32, _P, _P, _P, _I32]
+        L.orc_cc_reference_states.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P]
+        L.orc_cc_sweep.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P, _P, C.c_double,
+                                   I, I, I]
+        L.orc_cc_stable_dt.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, I]
+        L.orc_cc_stable_dt.restype = C.c_double
+        L.orc_cc_run.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, _P, _P, C.c_double, C.c_double,
+                                 I, I, _P, C.POINTER(C.c_int), I]
+        L.orc_cc_run.restype = C.c_int
+        L._cc_ready = True
+    return L
+
+
+class CutCellGeometry:
+    """FP64 geometry of a union of circles (solid inside) on an nx x ny grid
+    grown by `ghost` layers: alpha [NY][NX], betax [NY][NX+1],
+    betay [NY+1][NX], normal/center [2][NY][NX]."""
+
+    def __init__(self, nx, ny, circles, x0=0.0, y0=0.0, dx=None, dy=None):
+        L = _cc_lib()
+        self.G = int(L.orc_cc_ghost_layers())
+        self.nx, self.ny = nx, ny
+        self.dx = 1.0 / nx if dx is None else dx
+        self.dy = 1.0 / ny if dy is None else dy
+        NX, NY = nx + 2 * self.G, ny + 2 * self.G
+        self.alpha = np.zeros((NY, NX))
+        self.betax = np.zeros((NY, NX + 1))
+        self.betay = np.zeros((NY + 1, NX))
+        self.normal = np.zeros((2, NY, NX))
+        self.center = np.zeros((2, NY, NX))
+        circ = np.ascontiguousarray(circles, dtype=np.float64).reshape(-1, 3)
+        self.circles = circ
+        L.orc_cc_geometry(nx, ny, x0, y0, self.dx, self.dy, self.G, len(circ), _d(circ.ravel()),
+                          _d(self.alpha), _d(self.betax), _d(self.betay), _d(self.normal),
+                          _d(self.center))
+
+    def shielded(self, dir):
+        L = _cc_lib()
+        shape = self.betax.shape if dir == 0 else self.betay.shape
+        outs = [np.zeros(shape) for _ in range(6)]
+        L.orc_cc_shielded(self.nx, self.ny, dir, _d(self.betax), _d(self.betay),
+                          *[_d(o) for o in outs])
+        return outs
+
+    def cut_cells(self):
+        L = _cc_lib()
+        flags = np.zeros((self.ny, self.nx), dtype=np.int32)
+        L.orc_cc_cutcells(_i3([self.nx, self.ny, 1]), _d(self.alpha), _d(self.betax),
+                          _d(self.betay), flags.ctypes.data_as(_I32))
+        return flags
+
+    def _args(self, bc):
+        dx = np.array([self.dx, self.dy])
+        self._dxarr = dx
+        return (_i3([self.nx, self.ny, 1]), _i3(list(bc) + [0]), _d(dx), _d(self.alpha),
+                _d(self.betax), _d(self.betay))
+
+    def reference_states(self, cons, bc=(1, 1)):
+        L = _cc_lib()
+        cons = np.ascontiguousarray(cons, dtype=np.float64)
+        refs = np.zeros((6,) + self.alpha.shape)
+        L.orc_cc_reference_states(*self._args(bc), _d(self.normal), _d(self.center), _d(cons),
+                                  _d(refs))
+        return refs
+
+    def sweep(self, cons_ref_src, cons, dt, dir, bc=(1, 1), limiter=VAN_LEER, nthreads=0):
+        L = _cc_lib()
+        src = np.ascontiguousarray(cons_ref_src, dtype=np.float64)
+        cons = np.ascontiguousarray(cons, dtype=np.float64)
+        out = np.empty_like(cons)
+        L.orc_cc_sweep(*self._args(bc), _d(self.normal), _d(self.center), _d(src), _d(cons),
+                       _d(out), dt, dir, limiter, nthreads)
+        return out
+
+    def stable_dt(self, cons, dir=-1, bc=(1, 1)):
+        L = _cc_lib()
+        cons = np.ascontiguousarray(cons, dtype=np.float64)
+        return L.orc_cc_stable_dt(*self._args(bc), _d(cons), dir)
+
+    def run(self, cons, cfl, t_end, max_steps=-1, bc=(1, 1), limiter=VAN_LEER, nthreads=0):
+        L = _cc_lib()
+        cons = np.array(cons, dtype=np.float64, copy=True, order="C")
+        cap = max_steps if max_steps >= 0 else 100000
+        log = np.zeros(max(cap, 1))
+        rs = C.c_int(0)
+        steps = L.orc_cc_run(*self._args(bc), _d(self.normal), _d(self.center), _d(cons), cfl,
+                             t_end, max_steps, limiter, _d(log), C.byref(rs), nthreads)
+        return cons, log[:steps].copy(), rs.value

@@ -220,3 +220,53 @@ def test_reference_tile_rule_is_subset(orc):
         assert tiles >= all_faces
         if d == 0:
             assert tiles == all_faces
+
+
+def test_cutcell_geometry_circle(orc):
+    # area of a resolved circle converges at second order; normals point
+    # away from the centre (into the fluid)
+    errs = []
+    for n in (32, 64, 128):
+        g = orc.CutCellGeometry(n, n, [[0.5, 0.5, 0.2]])
+        G = g.G
+        solid = 1.0 - g.alpha[G:-G, G:-G].sum() / n / n
+        errs.append(abs(solid - np.pi * 0.04))
+    assert errs[1] < errs[0] / 3 and errs[2] < errs[1] / 3
+    g = orc.CutCellGeometry(64, 64, [[0.5, 0.5, 0.2]])
+    G = g.G
+    cut = g.cut_cells().astype(bool)
+    j, i = np.nonzero(cut)
+    xc = (i + 0.5) / 64 - 0.5
+    yc = (j + 0.5) / 64 - 0.5
+    nx = g.normal[0, G:-G, G:-G][cut]
+    ny = g.normal[1, G:-G, G:-G][cut]
+    assert np.all(nx * xc + ny * yc > 0)
+    assert np.allclose(nx * nx + ny * ny, 1.0)
+    # symmetric circle: alpha symmetric under x -> -x
+    a = g.alpha[G:-G, G:-G]
+    np.testing.assert_allclose(a, a[:, ::-1], atol=1e-14)
+
+
+def test_cutcell_shielded_fractions(orc):
+    g = orc.CutCellGeometry(40, 40, [[0.5, 0.5, 0.23]])
+    us, sL, sR, usr, sLr, sRr = g.shielded(0)
+    b = g.betax
+    # FillCutCellData: us + sL + sR + ds == beta; relative values sum to 1
+    inner = (slice(None), slice(1, -1))
+    tot = (us + sL + sR)[inner]
+    assert np.all(tot <= b[inner] + 1e-15)
+    pos = b[inner] > 0
+    assert np.all(np.abs((usr + sLr + sRr)[inner][pos] - 1.0) < 1e-12 + (1 - tot[pos] / b[inner][pos]))
+
+
+def test_cutcell_run_oracle_stable(orc):
+    from finitevolumesolver_gb300 import workloads
+    n = 64
+    circles, cons = workloads.shock_circles_2d(n, seed=5)
+    g = orc.CutCellGeometry(n, n, circles)
+    out, dts, rs = g.run(cons, 0.5, 10.0, max_steps=10)
+    assert np.isfinite(out).all() and rs == 0
+    G = g.G
+    covered = g.alpha[G:-G, G:-G] == 0
+    assert np.all(out[:, 0][:, covered] == 0.0)
+    assert out[0, 0][~covered].min() > 0.5
