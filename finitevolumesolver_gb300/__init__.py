@@ -28,7 +28,8 @@ from . import _capi
 from ._capi import Box, FvsError, GridDesc, Method, RunStats
 
 __all__ = ["PerfectGas", "FluxMethod", "HyperbolicPatchIntegrator", "CompleteFromCons",
-           "Solver", "FvsError", "make_method", "box", "lib"]
+           "Solver", "FvsError", "make_method", "box", "lib", "LearnedGuess",
+           "riemann_features", "tc_gemm_bf16"]
 
 FLUX_METHODS = {"muscl_hlle": 0, "hlle": 1, "godunov": 2, "muscl_godunov": 3}
 LIMITERS = {"van_leer": 0, "minmod": 1, "none": 2}
@@ -285,3 +286,87 @@ class Solver:
                                     C.byref(st))
         _capi.check(code)
         return st, log[:min(log_len, st.steps)].copy()
+
+
+def riemann_features(gamma, rhoL, uL, pL, rhoR, uR, pR, features, pstar=None, labels=None,
+                     stream=None) -> None:
+    """Features (float32 [n, 5]) and, given p*, the labels log(p*/max(pL, pR))
+    of the learned start value for n Riemann problems (device arrays)."""
+    n = int(rhoL.numel()) if hasattr(rhoL, "numel") else int(len(rhoL))
+    _capi.check(lib().fvs_riemann_features(
+        n, float(gamma), _ptr(rhoL), _ptr(uL), _ptr(pL), _ptr(rhoR), _ptr(uR), _ptr(pR),
+        _ptr(pstar), _ptr(features), _ptr(labels), _stream(stream)))
+
+
+def tc_gemm_bf16(A, B, C_out, M, N, K, lda=None, ldb=None, ldc=None, splits=1,
+                 accumulate=False, stream=None) -> None:
+    """C[M, N] (+)= A[M, K] . B[N, K]^T on the tcgen05 tensor cores (bf16
+    operands, fp32 result; device arrays)."""
+    _capi.check(lib().fvs_tc_gemm_bf16(
+        _ptr(A), int(lda or K), _ptr(B), int(ldb or K), _ptr(C_out), int(ldc or N), int(M),
+        int(N), int(K), int(splits), int(bool(accumulate)), _stream(stream)))
+
+
+class LearnedGuess:
+    """The learned Newton start value of the exact Riemann solver (no
+    counterpart in the reference): a 5-64-64-1 GELU perceptron trained and
+    evaluated with BF16 operands on the tcgen05 tensor cores."""
+
+    def __init__(self, seed: int = 0):
+        self._h = C.c_void_p()
+        _capi.check(lib().fvs_mlp_create(int(seed), C.byref(self._h)))
+
+    @staticmethod
+    def param_count() -> int:
+        return int(lib().fvs_mlp_param_count())
+
+    def close(self):
+        if self._h:
+            lib().fvs_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_normalization(self, features) -> None:
+        n = int(features.numel()) // 5 if hasattr(features, "numel") else len(features)
+        _capi.check(lib().fvs_mlp_set_normalization(self._h, _ptr(features), n))
+
+    def train(self, features, labels, steps, batch=8192, lr=1e-3, seed=1) -> float:
+        n = int(labels.numel()) if hasattr(labels, "numel") else len(labels)
+        loss = C.c_float(0.0)
+        _capi.check(lib().fvs_mlp_train(self._h, _ptr(features), _ptr(labels), n, int(steps),
+                                        int(batch), float(lr), int(seed), C.byref(loss)))
+        return loss.value
+
+    def gradients(self, features, labels, batch):
+        import numpy as np
+        g = np.zeros(self.param_count(), dtype=np.float32)
+        loss = C.c_float(0.0)
+        _capi.check(lib().fvs_mlp_gradients(self._h, _ptr(features), _ptr(labels), int(batch),
+                                            g.ctypes.data, C.byref(loss)))
+        return g, loss.value
+
+    def predict(self, features, out) -> None:
+        n = int(out.numel()) if hasattr(out, "numel") else len(out)
+        _capi.check(lib().fvs_mlp_predict(self._h, _ptr(features), n, _ptr(out)))
+
+    def params_device_ptr(self) -> int:
+        p = C.c_void_p()
+        _capi.check(lib().fvs_mlp_params(self._h, C.byref(p)))
+        return int(p.value or 0)
+
+    def master(self):
+        import numpy as np
+        h = np.zeros(self.param_count(), dtype=np.float32)
+        _capi.check(lib().fvs_mlp_get_master(self._h, h.ctypes.data))
+        return h
+
+    def set_master(self, params) -> None:
+        import numpy as np
+        h = np.ascontiguousarray(params, dtype=np.float32)
+        assert h.size == self.param_count()
+        _capi.check(lib().fvs_mlp_set_master(self._h, h.ctypes.data))

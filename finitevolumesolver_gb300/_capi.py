@@ -108,6 +108,20 @@ def load() -> C.CDLL:
     L.fvs_solver_cutcell_geometry.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
     L.fvs_solver_set_cycle.argtypes = [_VP, C.c_int64]
     L.fvs_solver_set_time.argtypes = [_VP, C.c_double]
+    L.fvs_mlp_param_count.restype = C.c_int
+    L.fvs_mlp_create.argtypes = [C.c_uint64, P(_VP)]
+    L.fvs_mlp_destroy.argtypes = [_VP]
+    L.fvs_riemann_features.argtypes = [C.c_int64, C.c_double] + [_VP] * 10
+    L.fvs_mlp_set_normalization.argtypes = [_VP, _VP, C.c_int64]
+    L.fvs_mlp_train.argtypes = [_VP, _VP, _VP, C.c_int64, C.c_int, C.c_int, C.c_float,
+                                C.c_uint64, P(C.c_float)]
+    L.fvs_mlp_gradients.argtypes = [_VP, _VP, _VP, C.c_int, _VP, P(C.c_float)]
+    L.fvs_mlp_predict.argtypes = [_VP, _VP, C.c_int64, _VP]
+    L.fvs_mlp_params.argtypes = [_VP, P(_VP)]
+    L.fvs_mlp_get_master.argtypes = [_VP, _VP]
+    L.fvs_mlp_set_master.argtypes = [_VP, _VP]
+    L.fvs_tc_gemm_bf16.argtypes = [_VP, C.c_int, _VP, C.c_int, _VP, C.c_int, C.c_int, C.c_int,
+                                   C.c_int, C.c_int, C.c_int, _VP]
     _lib = L
     return L
 

@@ -31,6 +31,7 @@ UNITS = [
     ("fvs_kernels_cutcell.cu", ["-fmad=false"]),
     ("fvs_capi.cu", []),
     ("fvs_noalloc.cu", ["-fmad=false"]),
+    ("fvs_mlp_train.cu", []),
 ]
 
 

@@ -272,6 +272,54 @@ int fvs_solver_cutcell_geometry(fvs_solver* s, double* alpha, double* betax, dou
 int fvs_solver_set_cycle(fvs_solver* s, int64_t cycle);
 int fvs_solver_set_time(fvs_solver* s, double t);
 
+/* ---- Learned start value of the exact Riemann solver ------------------- */
+/* No counterpart in the reference: its ExactRiemannSolver starts Newton's
+ * iteration from the mean pressure (src/equations/perfect_gas/
+ * ExactRiemannSolver.hpp:34-97).  A 5 -> 64 -> 64 -> 1 GELU perceptron
+ * predicts y = log(p* / max(pL, pR)); it is trained and evaluated with BF16
+ * operands on the tcgen05 tensor cores (FP32 accumulation), and
+ * fvs_mlp_params() gives the blob that fvs_method.mlp_params points to. */
+typedef struct fvs_mlp fvs_mlp;
+
+/* Number of floats in the parameter blob: mean[5], inv_std[5], W1[64][5],
+ * b1[64], W2[64][64], b2[64], w3[64], b3. */
+int fvs_mlp_param_count(void);
+/* Deterministic uniform (He) initialisation from `seed`. */
+int fvs_mlp_create(uint64_t seed, fvs_mlp** out);
+int fvs_mlp_destroy(fvs_mlp* m);
+/* Features (float [n][5]) of n Riemann problems given by primitive states
+ * and, when pstar_dev and labels_dev are given, the labels
+ * log(p* / max(pL, pR)) (float [n]).  Device arrays. */
+int fvs_riemann_features(int64_t n, double gamma, const double* rhoL_dev, const double* uL_dev,
+                         const double* pL_dev, const double* rhoR_dev, const double* uR_dev,
+                         const double* pR_dev, const double* pstar_dev, float* features_dev,
+                         float* labels_dev, void* stream);
+/* Sets the standardisation (mean, 1/std) from n feature rows. */
+int fvs_mlp_set_normalization(fvs_mlp* m, const float* features_dev, int64_t n);
+/* `steps` Adam steps (beta 0.9 / 0.999, eps 1e-8, learning rate lr) on
+ * batches of `batch` rows (a multiple of 256) drawn from the n training rows
+ * by a hash of (seed, step, row); *mean_loss receives the mean squared
+ * error over all rows of all steps. */
+int fvs_mlp_train(fvs_mlp* m, const float* features_dev, const float* labels_dev, int64_t n,
+                  int steps, int batch, float lr, uint64_t seed, float* mean_loss);
+/* Gradients (host, fvs_mlp_param_count() floats in the blob layout; the
+ * normalisation entries are 0) and loss of the mean squared error over the
+ * first `batch` rows, without an update. */
+int fvs_mlp_gradients(fvs_mlp* m, const float* features_dev, const float* labels_dev, int batch,
+                      float* grads_host, float* loss_host);
+/* y (device float [n]) for n feature rows, through the tensor-core path. */
+int fvs_mlp_predict(fvs_mlp* m, const float* features_dev, int64_t n, float* y_dev);
+/* Device pointer to the inference blob (BF16-rounded weights as floats). */
+int fvs_mlp_params(fvs_mlp* m, const float** params_dev);
+/* FP32 master parameters in the blob layout (host copies). */
+int fvs_mlp_get_master(fvs_mlp* m, float* host);
+int fvs_mlp_set_master(fvs_mlp* m, const float* host);
+/* C[M x N] (+)= A[M x K] . B[N x K]^T with A, B bf16 (K contiguous, 16-byte
+ * aligned rows) and C fp32, on the tcgen05 tensor cores; N in {16, 32, 64},
+ * K a multiple of 16; splits > 1 splits K and needs accumulate = 1. */
+int fvs_tc_gemm_bf16(const void* A_dev, int lda, const void* B_dev, int ldb, float* C_dev, int ldc,
+                     int M, int N, int K, int splits, int accumulate, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
