@@ -42,13 +42,24 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64_exact",
+    ap.add_argument("--precision", default="fp64_fast",
                     choices=["fp64_exact", "fp64_fast", "mixed"])
     ap.add_argument("--no-variants", action="store_true",
                     help="skip timing the other precision flavours")
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--cpu-sample-n", type=int, default=128,
                     help="edge of the cube the CPU reference arm times per step")
+    ap.add_argument("--no-reports", action="store_true",
+                    help="skip the secondary workloads (learned start value, 2-D Godunov, "
+                         "2-D cut cells)")
+    ap.add_argument("--mlp-samples", type=int, default=10_000_000)
+    ap.add_argument("--mlp-epochs", type=int, default=24)
+    ap.add_argument("--godunov-n", type=int, default=2048)
+    ap.add_argument("--godunov-steps", type=int, default=200)
+    ap.add_argument("--amr-n0", type=int, default=1024)
+    ap.add_argument("--amr-steps", type=int, default=50)
+    ap.add_argument("--cutcell-n", type=int, default=1024)
+    ap.add_argument("--cutcell-steps", type=int, default=400)
     return ap.parse_args()
 
 
@@ -154,6 +165,212 @@ def cpu_reference_rate(n: int, steps: int, threads: int) -> dict:
     cons, dts, _ = g.run(m, cons, 0.8, 1e9, max_steps=steps, nthreads=threads)
     el = time.perf_counter() - t0
     return {"value": 6 * n ** 3 * steps / el, "seconds": el}
+
+
+def report_mlp(args, torch, fvs, workloads):
+    """Learned Newton start value: 10^7 Riemann problems (rho, p log-uniform
+    on [1e-3, 1e1], u uniform on [-3c, 3c], vacuum-generating pairs redrawn),
+    labels from the exact solver at tolerance 1e-12, Adam (lr 1e-3, batch
+    8192) on the tensor cores; Newton iterations per problem on 10^6
+    held-out problems for the mean, PVRS/TR and learned start values."""
+    n = args.mlp_samples
+    arr = workloads.riemann_samples(n, seed=2025)
+    dev = [torch.from_numpy(a).cuda() for a in arr]
+    del arr
+    ps = torch.empty(n, dtype=torch.float64, device="cuda")
+    st = torch.empty(n, dtype=torch.int32, device="cuda")
+    m = fvs.make_method("godunov", guess="pvrs_tr", tolerance=1e-12, max_iterations=200)
+    fvs.exact_riemann_star(m, *dev, ps, None, None, st)
+    feat = torch.empty(n, 5, dtype=torch.float32, device="cuda")
+    lab = torch.empty(n, dtype=torch.float32, device="cuda")
+    fvs.riemann_features(1.4, *dev, feat, pstar=ps, labels=lab)
+    torch.cuda.synchronize()
+    ok = st == 1
+    feat, lab = feat[ok].contiguous(), lab[ok].contiguous()
+    del dev, ps, st
+    ntrain = int(lab.numel())
+    net = fvs.LearnedGuess(seed=11)
+    net.set_normalization(feat)
+    batch = 8192
+    steps_per_epoch = (ntrain + batch - 1) // batch
+    net.train(feat, lab, steps=20, batch=batch, lr=1e-3, seed=1)  # warm-up, graph capture
+    losses = []
+    t0 = time.perf_counter()
+    for e in range(args.mlp_epochs):
+        losses.append(net.train(feat, lab, steps=steps_per_epoch, batch=batch, lr=1e-3,
+                                seed=100 + e))
+    train_s = time.perf_counter() - t0
+    steps = steps_per_epoch * args.mlp_epochs
+    flop_per_step = 2 * batch * (5 * 64 + 3 * 64 * 64 + 64 * 5)
+    # held-out problems
+    nt = 1_000_000
+    test = [torch.from_numpy(a).cuda() for a in workloads.riemann_samples(nt, seed=77)]
+    tf = torch.empty(nt, 5, dtype=torch.float32, device="cuda")
+    fvs.riemann_features(1.4, *test, tf)
+    y = torch.empty(nt, dtype=torch.float32, device="cuda")
+    net.predict(tf, y)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(5):
+        net.predict(tf, y)
+    torch.cuda.synchronize()
+    infer_s = (time.perf_counter() - t1) / 5
+    iters = {}
+    for guess in ("mean", "pvrs_tr", "mlp"):
+        mm = fvs.make_method("godunov", guess=guess, tolerance=1e-12, max_iterations=200,
+                             mlp_params=net.params_device_ptr() if guess == "mlp" else None)
+        p2 = torch.empty(nt, dtype=torch.float64, device="cuda")
+        it = torch.empty(nt, dtype=torch.int32, device="cuda")
+        s2 = torch.empty_like(it)
+        fvs.exact_riemann_star(mm, *test, p2, None, it, s2)
+        torch.cuda.synchronize()
+        iters[guess] = {"newton_iterations_per_problem": float(it.double().mean()),
+                        "fallback_rate": float((s2 == 2).double().mean()),
+                        "not_converged_rate": float((s2 == 0).double().mean())}
+    return {
+        "workload": f"{n} sampled Riemann problems ({ntrain} with a converged label), "
+                    "5-64-64-1 GELU network, BF16 tcgen05 GEMMs, FP32 accumulation",
+        "training": {"epochs": args.mlp_epochs, "steps": steps, "batch": batch,
+                     "seconds": train_s, "samples_per_s": steps * batch / train_s,
+                     "ms_per_step": 1e3 * train_s / steps,
+                     "loss_first_epoch": losses[0], "loss_last_epoch": losses[-1],
+                     "tensor_tflops": flop_per_step * steps / train_s / 1e12,
+                     "note": "tiny GEMMs (K = 16 / 64, N = 64): latency-bound, "
+                             "not tensor-throughput-bound"},
+        "inference": {"problems": nt, "problems_per_s": nt / infer_s},
+        "newton_tol_1e-12_heldout": iters,
+    }, net
+
+
+def report_godunov(args, torch, fvs, workloads, net):
+    """2-D first-order Godunov with the exact Riemann solver on an n^2
+    four-quadrant problem drawn from the sampled distribution, Strang
+    splitting, for the three Newton start values."""
+    n = args.godunov_n
+    cons = workloads.quadrants_2d(n, seed=3)
+    out = {}
+    finals = {}
+    for guess in ("mean", "pvrs_tr", "mlp"):
+        if guess == "mlp" and net is None:
+            continue
+        m = fvs.make_method("godunov", guess=guess,
+                            mlp_params=net.params_device_ptr() if guess == "mlp" else None)
+        s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive", method=m)
+        stream = torch.cuda.ExternalStream(s.stream_handle())
+        s.upload(cons)
+        s.run(cfl=0.8, t_end=1e9, max_steps=3)
+        s.newton_stats(reset=True)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        st, _ = s.run(cfl=0.8, t_end=1e9, max_steps=args.godunov_steps)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        it, fail, fb = s.newton_stats(fallbacks=True)
+        faces = st.steps * 4 * (n + 1) * n
+        out[guess] = {"steps": st.steps, "ms_per_step": ms / max(st.steps, 1),
+                      "cell_updates_per_s": 4 * n * n * st.steps / (ms / 1e3),
+                      "newton_iterations_per_interface": it / faces,
+                      "fallback_rate": fb / faces, "not_converged": fail}
+        finals[guess] = s.download()
+        s.close()
+    if "mean" in finals:
+        for g in finals:
+            out[g]["max_abs_diff_vs_mean_start"] = float(np.abs(finals[g] - finals["mean"]).max())
+    return {"workload": f"2D perfect gas {n}^2 four quadrants, Godunov + exact Riemann solver "
+                        "(tolerance 1e-7, reference default), Strang, CFL 0.8, transmissive",
+            "by_start_value": out}
+
+
+def report_amr(args, torch, fvs, workloads, peaks):
+    """Batched AMR patch set: 2-D blast (p 10 inside r < 0.1 about a seeded
+    centre), 3 levels, ratio 2, 4096 patches with extents from {8, 16, 32,
+    64}, level 0 covering n0^2, MUSCL-Hancock/VanLeer + HLLE, subcycled
+    coarse steps (one CUDA graph each), for the three precision flavours."""
+    h, cons = workloads.amr_blast_2d(args.amr_n0, 3, seed=7, target=4096)
+    cells = h.cells()
+    upd_per_step = int(4 * sum(int(cells[l]) << l for l in range(h.nlevels)))
+    out = {"workload": f"2D blast on {h.npatches} patches, 3 levels (level 0 {args.amr_n0}^2), "
+                       "ratio 2, extents from {8,16,32,64}, MUSCL-Hancock/VanLeer + HLLE, "
+                       "subcycled Strang coarse steps, CFL 0.8, transmissive",
+           "patches_per_level": np.bincount(h.levels, minlength=3).tolist(),
+           "cells_per_level": cells.tolist(), "cell_updates_per_coarse_step": upd_per_step,
+           "coarse_steps": args.amr_steps, "flavours": {}}
+    finals = {}
+    for prec in ("fp64_exact", "fp64_fast", "mixed"):
+        a = fvs.AmrSolver(h, fvs.make_method(precision=prec))
+        stream = torch.cuda.ExternalStream(a.stream_handle())
+        a.upload(cons)
+        cfg = a.autotune()
+        a.run(cfl=0.8, t_end=1e9, max_steps=2)
+        a.upload(cons)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st, _ = a.run(cfl=0.8, t_end=1e9, max_steps=args.amr_steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        finals[prec] = a.download()
+        rate = upd_per_step * st.steps / (ms / 1e3)
+        out["flavours"][prec] = {
+            "ms_per_coarse_step": ms / max(st.steps, 1), "cell_updates_per_s": rate,
+            "restarts": st.restarts,
+            "hbm_frac_algorithmic": rate * 64 / 1e9 / peaks["hbm_gbs"],
+            "launch_shapes_block_grid": cfg.tolist()}
+        a.close()
+    ref = finals["fp64_exact"]
+    parts_ref = h.split(ref)
+    for prec, f in finals.items():
+        parts = h.split(f)
+        l1 = float(np.mean(np.concatenate([np.abs(p[0] - q[0]).ravel()
+                                           for p, q in zip(parts, parts_ref)])))
+        out["flavours"][prec]["l1_density_vs_fp64_exact"] = l1
+    base = out["flavours"]["fp64_exact"]["cell_updates_per_s"]
+    for prec in out["flavours"]:
+        out["flavours"][prec]["speedup_vs_fp64_exact"] = \
+            out["flavours"][prec]["cell_updates_per_s"] / base
+    # CPU: the oracle's restatement, one coarse step of the same hierarchy
+    from oracle import oracle as orc
+    threads = orc.max_threads()
+    t0 = time.perf_counter()
+    orc.amr_run(h, cons, 0.8, 1e9, max_steps=1, nthreads=threads)
+    cpu_s = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": upd_per_step / cpu_s, "unit": "cell-updates/s",
+                           "cores": threads, "kind": "port",
+                           "sample": "1 coarse step of the same hierarchy"}
+    return out
+
+
+def report_cutcell(args, torch, fvs, workloads):
+    """2-D KBN h-box cut cells: Mach 2 shock over 8 seeded circles on
+    n^2, Strang MUSCL-Hancock/VanLeer + HLLE, exact FP64."""
+    n = args.cutcell_n
+    circles, cons = workloads.shock_circles_2d(n, seed=5)
+    s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive")
+    s.set_embedded_circles(circles)
+    stream = torch.cuda.ExternalStream(s.stream_handle())
+    s.upload(cons)
+    s.run(cfl=0.5, t_end=1e9, max_steps=3)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    st, _ = s.run(cfl=0.5, t_end=1e9, max_steps=args.cutcell_steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    geo = s.cutcell_geometry()
+    G = geo["ghost"]
+    cut = int(geo["cut"][G:-G, G:-G].sum())
+    s.close()
+    return {"workload": f"2D {n}^2 Mach 2 shock over 8 circles, KBN h-box MUSCL/VanLeer + HLLE "
+                        "exact FP64, Strang, CFL 0.5, transmissive",
+            "steps": st.steps, "restarts": st.restarts, "ms_per_step": ms / max(st.steps, 1),
+            "cell_updates_per_s": 4 * n * n * st.steps / (ms / 1e3), "cut_cells": cut}
 
 
 def run_reference(args):
@@ -308,6 +525,22 @@ def run_ours(args):
         cpu = {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"1 Strang step of the {n}^3 workload ({6 * cells} cell-updates)"}
 
+    reports = None
+    if rank == 0 and not args.no_reports:
+        reports = {}
+        try:
+            reports["learned_start_value"], net = report_mlp(args, torch, fvs, workloads)
+        except Exception as e:  # report the failure, keep the headline
+            reports["learned_start_value"] = {"error": repr(e)}
+            net = None
+        for key, fn in (("godunov_2d", lambda: report_godunov(args, torch, fvs, workloads, net)),
+                        ("amr_2d", lambda: report_amr(args, torch, fvs, workloads, peaks)),
+                        ("cutcell_2d", lambda: report_cutcell(args, torch, fvs, workloads))):
+            try:
+                reports[key] = fn()
+            except Exception as e:
+                reports[key] = {"error": repr(e)}
+
     if rank == 0:
         traffic = profile_traffic(f"sweep_{args.precision}_160.md", cells)
         line = {
@@ -340,6 +573,7 @@ def run_ours(args):
                              "hbm_frac": v["achieved"] / peaks["hbm_gbs"],
                              "accuracy": accuracy(v["final"])}
                          for k, v in variants.items()},
+            "reports": reports,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

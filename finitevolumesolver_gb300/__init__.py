@@ -25,11 +25,11 @@ from __future__ import annotations
 import ctypes as C
 
 from . import _capi
-from ._capi import Box, FvsError, GridDesc, Method, RunStats
+from ._capi import AmrDesc, Box, FvsError, GridDesc, Method, RunStats
 
 __all__ = ["PerfectGas", "FluxMethod", "HyperbolicPatchIntegrator", "CompleteFromCons",
            "Solver", "FvsError", "make_method", "box", "lib", "LearnedGuess",
-           "riemann_features", "tc_gemm_bf16"]
+           "riemann_features", "tc_gemm_bf16", "AmrSolver"]
 
 FLUX_METHODS = {"muscl_hlle": 0, "hlle": 1, "godunov": 2, "muscl_godunov": 3}
 LIMITERS = {"van_leer": 0, "minmod": 1, "none": 2}
@@ -263,11 +263,15 @@ class Solver:
         _capi.check(lib().fvs_solver_stable_dt(self._h, int(dir), C.byref(out)))
         return out.value
 
-    def newton_stats(self, reset: bool = False):
+    def newton_stats(self, reset: bool = False, fallbacks: bool = False):
+        """(Newton iterations, non-converged faces[, rejected learned starts])
+        of the Godunov sweeps since the last reset."""
         it = C.c_uint64(0)
         fl = C.c_uint64(0)
-        _capi.check(lib().fvs_solver_newton_stats(self._h, C.byref(it), C.byref(fl), int(reset)))
-        return it.value, fl.value
+        fb = C.c_uint64(0)
+        _capi.check(lib().fvs_solver_newton_stats(self._h, C.byref(it), C.byref(fl),
+                                                  C.byref(fb), int(reset)))
+        return (it.value, fl.value, fb.value) if fallbacks else (it.value, fl.value)
 
     def sweep(self, dir: int, dt: float) -> float:
         out = C.c_double(0.0)
@@ -370,3 +374,98 @@ class LearnedGuess:
         h = np.ascontiguousarray(params, dtype=np.float32)
         assert h.size == self.param_count()
         _capi.check(lib().fvs_mlp_set_master(self._h, h.ctypes.data))
+
+
+class AmrSolver:
+    """A static 2-D AMR patch set (refinement ratio 2) advanced by
+    SubcycleFineFirstSolver's coarse steps: one persistent launch per level
+    and sweep over a device patch-row table, each coarse step one CUDA graph.
+    `hier` has nlevels, n0, bc, dx0, levels [npatch] and boxes [npatch, 4]
+    (lo_x, lo_y, hi_x, hi_y), e.g. workloads.AmrHierarchy."""
+
+    def __init__(self, hier, method: Method | None = None):
+        import numpy as np
+        d = AmrDesc()
+        d.rank = 2
+        d.nlevels = int(hier.nlevels)
+        for k in range(3):
+            d.n0[k] = int(hier.n0[k]) if k < 2 else 1
+            d.bc[k] = int(hier.bc[k]) if k < 2 else 0
+        d.dx0 = float(hier.dx0)
+        npatch = len(hier.levels)
+        d.npatches = npatch
+        self._levels = np.ascontiguousarray(hier.levels, dtype=np.int32)
+        self._boxes = (Box * npatch)()
+        for p, (x0, y0, x1, y1) in enumerate(np.asarray(hier.boxes).reshape(-1, 4)):
+            self._boxes[p].lo[:] = [int(x0), int(y0), 0]
+            self._boxes[p].hi[:] = [int(x1), int(y1), 1]
+        d.patch_level = self._levels.ctypes.data_as(C.POINTER(C.c_int32))
+        d.patch_box = self._boxes
+        self.hier = hier
+        self.method = method if method is not None else make_method()
+        self._h = C.c_void_p()
+        _capi.check(lib().fvs_amr_create(C.byref(d), C.byref(self.method), C.byref(self._h)))
+        self.size = int(sum(4 * (int(b[2]) - int(b[0])) * (int(b[3]) - int(b[1]))
+                            for b in np.asarray(hier.boxes).reshape(-1, 4)))
+
+    def close(self):
+        if self._h:
+            lib().fvs_amr_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, cons) -> None:
+        import numpy as np
+        a = np.ascontiguousarray(cons, dtype=np.float64)
+        assert a.size == self.size
+        _capi.check(lib().fvs_amr_upload(self._h, a.ctypes.data))
+
+    def download(self):
+        import numpy as np
+        a = np.empty(self.size, dtype=np.float64)
+        _capi.check(lib().fvs_amr_download(self._h, a.ctypes.data))
+        return a
+
+    def info(self):
+        import numpy as np
+        nl = int(self.hier.nlevels)
+        cells = np.zeros(nl, dtype=np.int64)
+        storage = np.zeros(nl, dtype=np.int64)
+        ns = C.c_int32(0)
+        _capi.check(lib().fvs_amr_info(self._h, cells.ctypes.data, storage.ctypes.data,
+                                       C.byref(ns)))
+        return {"cells": cells, "storage": storage, "slots": ns.value}
+
+    def stream_handle(self) -> int:
+        p = C.c_void_p()
+        _capi.check(lib().fvs_amr_stream(self._h, C.byref(p)))
+        return int(p.value or 0)
+
+    def stable_dt(self) -> float:
+        out = C.c_double(0.0)
+        _capi.check(lib().fvs_amr_stable_dt(self._h, C.byref(out)))
+        return out.value
+
+    def run(self, cfl=0.8, t_end=1.0, max_steps=-1, log_len=0):
+        import numpy as np
+        log = np.zeros(max(log_len, 1))
+        st = RunStats()
+        _capi.check(lib().fvs_amr_run(self._h, float(cfl), float(t_end), int(max_steps),
+                                      log.ctypes.data_as(C.POINTER(C.c_double)), int(log_len),
+                                      C.byref(st)))
+        return st, log[:min(log_len, st.steps)].copy()
+
+    def set_launch(self, level, dir, block, grid) -> None:
+        _capi.check(lib().fvs_amr_set_launch(self._h, int(level), int(dir), int(block),
+                                             int(grid)))
+
+    def autotune(self):
+        import numpy as np
+        cfg = np.zeros((int(self.hier.nlevels), 2, 2), dtype=np.int32)
+        _capi.check(lib().fvs_amr_autotune(self._h, cfg.ctypes.data))
+        return cfg

@@ -45,6 +45,13 @@ class RunStats(C.Structure):
                 ("status", C.c_int32), ("reserved", C.c_int32), ("last_dt", C.c_double)]
 
 
+class AmrDesc(C.Structure):
+    _fields_ = [("rank", C.c_int32), ("nlevels", C.c_int32), ("n0", C.c_int32 * 3),
+                ("bc", C.c_int32 * 3), ("dx0", C.c_double), ("npatches", C.c_int32),
+                ("reserved", C.c_int32), ("patch_level", C.POINTER(C.c_int32)),
+                ("patch_box", C.POINTER(Box))]
+
+
 class FvsError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"fvs error {STATUS_NAMES.get(code, code)}: {msg}")
@@ -100,7 +107,8 @@ def load() -> C.CDLL:
     L.fvs_solver_run.argtypes = [_VP, C.c_double, C.c_double, C.c_int, _DP, C.c_int,
                                  P(RunStats)]
     L.fvs_solver_stream.argtypes = [_VP, P(_VP)]
-    L.fvs_solver_newton_stats.argtypes = [_VP, P(C.c_uint64), P(C.c_uint64), C.c_int]
+    L.fvs_solver_newton_stats.argtypes = [_VP, P(C.c_uint64), P(C.c_uint64), P(C.c_uint64),
+                                          C.c_int]
     L.fvs_exact_riemann_star.argtypes = [P(Method), C.c_int64, _VP, _VP, _VP, _VP, _VP, _VP, _VP,
                                          _VP, _VP, _VP, _VP]
     L.fvs_cutcell_ghost_layers.restype = C.c_int
@@ -108,6 +116,16 @@ def load() -> C.CDLL:
     L.fvs_solver_cutcell_geometry.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
     L.fvs_solver_set_cycle.argtypes = [_VP, C.c_int64]
     L.fvs_solver_set_time.argtypes = [_VP, C.c_double]
+    L.fvs_amr_create.argtypes = [P(AmrDesc), P(Method), P(_VP)]
+    L.fvs_amr_destroy.argtypes = [_VP]
+    L.fvs_amr_upload.argtypes = [_VP, _VP]
+    L.fvs_amr_download.argtypes = [_VP, _VP]
+    L.fvs_amr_info.argtypes = [_VP, _VP, _VP, _VP]
+    L.fvs_amr_stream.argtypes = [_VP, P(_VP)]
+    L.fvs_amr_stable_dt.argtypes = [_VP, _DP]
+    L.fvs_amr_run.argtypes = [_VP, C.c_double, C.c_double, C.c_int, _DP, C.c_int, P(RunStats)]
+    L.fvs_amr_set_launch.argtypes = [_VP, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.fvs_amr_autotune.argtypes = [_VP, _VP]
     L.fvs_mlp_param_count.restype = C.c_int
     L.fvs_mlp_create.argtypes = [C.c_uint64, P(_VP)]
     L.fvs_mlp_destroy.argtypes = [_VP]

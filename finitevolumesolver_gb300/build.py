@@ -32,6 +32,9 @@ UNITS = [
     ("fvs_capi.cu", []),
     ("fvs_noalloc.cu", ["-fmad=false"]),
     ("fvs_mlp_train.cu", []),
+    ("fvs_amr.cu", []),
+    ("fvs_amr_exact.cu", ["-fmad=false"]),
+    ("fvs_amr_fast.cu", []),
 ]
 
 

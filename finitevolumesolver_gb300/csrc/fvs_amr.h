@@ -1,0 +1,142 @@
+// fvs_amr.h -- device tables and kernel arguments of the batched AMR patch
+// update (2-D, refinement ratio 2, 2 ghost layers).
+//
+// Storage: every level keeps its patches' ghosted blocks back to back in one
+// array per component (structure of arrays over the level):
+//   value(c, cell) = level_buffer[c * ncells + cell],
+// and a patch block is (nx + 4) x (ny + 4) cells, x fastest.  A sweep reads
+// and writes whole rows (x sweeps) or columns (y sweeps) of patches; the work
+// of a sweep is the level's list of rows, processed by one persistent launch.
+#pragma once
+
+#include <cstdint>
+
+#include "fvs_internal.h"
+
+namespace fvs {
+namespace amr {
+
+constexpr int kGhost = 2;
+constexpr int kMaxLevels = 4;
+constexpr int kComp = 4;  // rho, m_x, m_y, E
+// per coarse step at most 4 sweeps on each of 1 + 2 + 4 + 8 level subcycles
+constexpr int kMaxSweeps = 4 * 15;
+
+// One row (x sweep) or column (y sweep) of one patch.
+struct Row {
+  int32_t base;     // storage index of the row's first ghost cell (interior -2)
+  int32_t stride;   // 1 for x rows, the patch pitch for y columns
+  int32_t n;        // interior cells
+  int32_t cap_end;  // captures of this row: [previous row's cap_end, cap_end)
+};
+
+// A flux-register capture: face `face` (0..n, between cells face-1 and face)
+// of a row adds dt_split * F to register entry `dst` (K doubles).
+struct Cap {
+  int32_t face;
+  int32_t dst;
+};
+
+// Ghost cell `dst` of a level takes the value of cell `src` of the same
+// level (src >= 0) or of cell -src-1 of the next coarser level.
+struct Ghost {
+  int32_t dst;
+  int32_t src;
+};
+
+// Reflux of one coarse cell from `count` register slots starting at
+// `first`; the slot's sign is +1 for the cell's low face, -1 for its high face.
+struct RefluxCell {
+  int32_t cell;
+  int32_t first;
+  int32_t count;
+  int32_t pad;
+};
+
+// Average-down of the fine 2 x 2 block whose lower-left cell is `fine`.
+struct AvgDown {
+  int32_t coarse;
+  int32_t fine;
+  int32_t pitch;  // fine patch pitch (cells to the next fine row)
+  int32_t pad;
+};
+
+// Per-run control block (device).
+struct AmrControl {
+  double t;
+  double dt;
+  double t_end;
+  double cfl;
+  double failure_dt;   // > 0: next step uses this instead of the stable dt
+  double dt_override;  // > 0: this step uses dt_override, no checks
+  unsigned long long smax_stable[kMaxLevels][2];
+  unsigned long long smax_sweep[kMaxSweeps];
+  int failed;          // this step failed a per-sweep check
+  int status;          // StatusBits of the committed steps
+  int step_status;
+  int nsweeps;
+};
+
+// Description of one sweep within the coarse step (device, constant).
+struct SweepInfo {
+  int level;
+  double scale;  // split dt = scale * coarse dt
+};
+
+struct PatchSweepArgs {
+  const double* in;
+  double* out;
+  int32_t ncells;  // component stride of the level
+  const Row* rows;
+  int32_t nrows;
+  const Cap* caps;
+  double* reg;     // register entries of the captures
+  double gamma;
+  double dx;
+  int limiter;
+  const double* dt_ptr;  // coarse dt (device)
+  double dt_scale;       // split dt = dt_scale * (*dt_ptr)
+  unsigned long long* smax_out;  // this sweep's max signal speed (bits)
+  AmrControl* ctrl;
+};
+
+struct MaxSpeedArgs {
+  const double* in;
+  int32_t ncells;
+  const Row* rows;
+  int32_t nrows;
+  double gamma;
+  unsigned long long* smax_out;
+};
+
+// Launchers (fvs_amr_exact.cu: exact FP64 and the table kernels, compiled
+// with -fmad=false; fvs_amr_fast.cu: fast FP64 and mixed).  `grid` is the
+// number of persistent blocks.
+cudaError_t LaunchPatchSweepExact(int dir, const PatchSweepArgs& a, int grid, int block,
+                                  cudaStream_t s);
+cudaError_t LaunchPatchSweepFast(int dir, const PatchSweepArgs& a, int grid, int block,
+                                 cudaStream_t s);
+cudaError_t LaunchPatchSweepMixed(int dir, const PatchSweepArgs& a, int grid, int block,
+                                  cudaStream_t s);
+cudaError_t LaunchPatchMaxSpeedExact(int dir, const MaxSpeedArgs& a, int grid, int block,
+                                     cudaStream_t s);
+cudaError_t LaunchPatchMaxSpeedFast(int dir, const MaxSpeedArgs& a, int grid, int block,
+                                    cudaStream_t s);
+cudaError_t LaunchPatchMaxSpeedMixed(int dir, const MaxSpeedArgs& a, int grid, int block,
+                                     cudaStream_t s);
+cudaError_t LaunchGhostFill(double* dst, int32_t n_dst, const double* coarse, int32_t n_coarse,
+                            const Ghost* g, int32_t count, cudaStream_t s);
+cudaError_t LaunchReflux(double* coarse, int32_t n_coarse, const double* reg,
+                         const RefluxCell* cells, int32_t ncells, const float* signs, double dx,
+                         cudaStream_t s);
+cudaError_t LaunchAverageDown(double* coarse, int32_t n_coarse, const double* fine,
+                              int32_t n_fine, const AvgDown* e, int32_t count, cudaStream_t s);
+struct LevelDx {
+  double dx[kMaxLevels];
+};
+cudaError_t LaunchAmrDt(AmrControl* ctrl, int nlevels, LevelDx dx, cudaStream_t s);
+cudaError_t LaunchAmrEndStep(AmrControl* ctrl, const SweepInfo* sweeps, int nsweeps,
+                             LevelDx dx, cudaStream_t s);
+
+}  // namespace amr
+}  // namespace fvs

@@ -1,0 +1,164 @@
+// fvs_amr_kernels.cuh -- kernels of the batched AMR patch update (2-D).
+//
+// PatchSweepKernel: one persistent launch per level and sweep.  Each thread
+// takes rows of the level's row list (grid-stride) and marches along a row
+// with the same three-cell window, policy arithmetic and update as the
+// uniform grid's SweepMarchKernel (fvs_sweep.cuh): for a row of n interior
+// cells it reads the ghosted cells -2..n+1 of the input buffer, computes the
+// n+1 faces, writes the n updated interior cells to the output buffer,
+// accumulates dt_split * F into the flux-register entries of the row's
+// captured faces (each entry belongs to exactly one face, so no atomics and
+// a deterministic sum) and reduces the row's max signal speed for the
+// per-sweep CFL check.  Ghost cells are refilled from the level's gather
+// table before every sweep (GhostFillKernel).
+#pragma once
+
+#include <climits>
+
+#include "fvs_amr.h"
+#include "fvs_sweep.cuh"
+
+namespace fvs {
+namespace amr {
+
+template <int DIR, template <int> class PT>
+__global__ void __launch_bounds__(128) PatchSweepKernel(PatchSweepArgs a) {
+  using P = PT<2>;
+  using R = typename P::Real;
+  constexpr int K = kComp;
+  const double split_dt = a.dt_scale * (*a.dt_ptr);
+  const typename P::Gas eq = P::MakeGas(a.gamma);
+  const double lambda_half = 0.5 * split_dt / a.dx;
+  const double dt_dx = split_dt / a.dx;
+  const int64_t N = a.ncells;
+  const double* __restrict__ in = a.in;
+  double* __restrict__ out = a.out;
+  R smax = R(0);
+  int status = 0;
+  typename P::Stats stats;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.nrows;
+       r += gridDim.x * blockDim.x) {
+    const Row w = a.rows[r];
+    int cap = r > 0 ? a.rows[r - 1].cap_end : 0;
+    int next_face = cap < w.cap_end ? a.caps[cap].face : INT_MAX;
+    const int n = w.n;
+    auto load = [&](double* u, int j) {
+      const int64_t off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
+#pragma unroll
+      for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * N + off);
+    };
+    double dm[K], dc[K], dp[K], dn[K];
+    R cm[K], cc[K], cp[K];
+    load(dm, -2);
+    load(dc, -1);
+    load(dn, 0);
+    P::ToCell(cm, dm);
+    P::ToCell(cc, dc);
+    typename P::Rec recR_prev;
+    typename P::Wave w_prev;
+    double F_prev[K];
+    for (int j = -1; j <= n; ++j) {
+#pragma unroll
+      for (int c = 0; c < K; ++c) dp[c] = dn[c];
+      if (j + 2 <= n + 1) load(dn, j + 2);
+      P::ToCell(cp, dp);
+      typename P::Rec recL, recR;
+      P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
+      const typename P::Wave wv = P::MakeWave(eq, cc, DIR);
+      if (j >= 0) {
+        double F[K];
+        const R s = P::Face(eq, F, recR_prev, recL, w_prev, wv, DIR, stats);
+        smax = s > smax ? s : smax;
+        if (j == next_face) {
+          double* dst = a.reg + int64_t(a.caps[cap].dst) * K;
+#pragma unroll
+          for (int c = 0; c < K; ++c) dst[c] = dst[c] + split_dt * F[c];
+          ++cap;
+          next_face = cap < w.cap_end ? a.caps[cap].face : INT_MAX;
+        }
+        if (j > 0) {
+          const int64_t off = int64_t(w.base) + int64_t(j - 1 + kGhost) * w.stride;
+#pragma unroll
+          for (int c = 0; c < K; ++c) {
+            const double v = dm[c] + dt_dx * (F_prev[c] - F[c]);
+            out[c * N + off] = v;
+            if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < K; ++c) F_prev[c] = F[c];
+      }
+      recR_prev = recR;
+      w_prev = wv;
+#pragma unroll
+      for (int c = 0; c < K; ++c) {
+        dm[c] = dc[c];
+        dc[c] = dp[c];
+        cm[c] = cc[c];
+        cc[c] = cp[c];
+      }
+    }
+  }
+  const double smax_w = WarpMax(static_cast<double>(smax));
+  if ((threadIdx.x & 31) == 0 && smax_w > 0.0) AtomicMaxPositive(a.smax_out, smax_w);
+  if (status) atomicOr(&a.ctrl->step_status, status);
+}
+
+// Max signal speed over the faces 0..n of every row (the stable dt of the
+// level in that direction is dx / max).
+template <int DIR, template <int> class PT>
+__global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
+  using P = PT<2>;
+  using R = typename P::Real;
+  constexpr int K = kComp;
+  const typename P::Gas eq = P::MakeGas(a.gamma);
+  const int64_t N = a.ncells;
+  R smax = R(0);
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.nrows;
+       r += gridDim.x * blockDim.x) {
+    const Row w = a.rows[r];
+    auto wave = [&](int j) {
+      const int64_t off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
+      double u[K];
+      R v[K];
+#pragma unroll
+      for (int c = 0; c < K; ++c) u[c] = __ldg(a.in + c * N + off);
+      P::ToCell(v, u);
+      return P::MakeWave(eq, v, DIR);
+    };
+    typename P::Wave wl = wave(-1);
+    for (int f = 0; f <= w.n; ++f) {
+      const typename P::Wave wr = wave(f);
+      const R s = P::FaceMaxSpeed(eq, wl, wr);
+      smax = s > smax ? s : smax;
+      wl = wr;
+    }
+  }
+  const double smax_w = WarpMax(static_cast<double>(smax));
+  if ((threadIdx.x & 31) == 0 && smax_w > 0.0) AtomicMaxPositive(a.smax_out, smax_w);
+}
+
+template <template <int> class PT>
+cudaError_t LaunchPatchSweepT(int dir, const PatchSweepArgs& a, int grid, int block,
+                              cudaStream_t s) {
+  if (a.nrows == 0) return cudaSuccess;
+  if (dir == 0)
+    PatchSweepKernel<0, PT><<<grid, block, 0, s>>>(a);
+  else
+    PatchSweepKernel<1, PT><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <template <int> class PT>
+cudaError_t LaunchPatchMaxSpeedT(int dir, const MaxSpeedArgs& a, int grid, int block,
+                                 cudaStream_t s) {
+  if (a.nrows == 0) return cudaSuccess;
+  if (dir == 0)
+    PatchMaxSpeedKernel<0, PT><<<grid, block, 0, s>>>(a);
+  else
+    PatchMaxSpeedKernel<1, PT><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace amr
+}  // namespace fvs

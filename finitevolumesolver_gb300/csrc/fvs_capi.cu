@@ -183,7 +183,7 @@ struct fvs_solver {
   fvs::Control* ctrl = nullptr;
   fvs::Control* ctrl_host = nullptr;  // pinned
   unsigned long long* scratch_words = nullptr;  // [8]
-  unsigned long long* newton_words = nullptr;   // [2] host-driven sweeps
+  unsigned long long* newton_words = nullptr;   // [3] host-driven sweeps
   double* dt_log_dev = nullptr;
   int dt_log_cap = 0;
   int seg_len = 0;
@@ -565,8 +565,8 @@ int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
   if (e == cudaSuccess) e = cudaMalloc(&s->ctrl, sizeof(fvs::Control));
   if (e == cudaSuccess) e = cudaMallocHost(&s->ctrl_host, sizeof(fvs::Control));
   if (e == cudaSuccess) e = cudaMalloc(&s->scratch_words, 8 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&s->newton_words, 2 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMemset(s->newton_words, 0, 2 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&s->newton_words, 3 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(s->newton_words, 0, 3 * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemset(s->ctrl, 0, sizeof(fvs::Control));
   if (e != cudaSuccess) {
     delete s;
@@ -832,14 +832,15 @@ int fvs_solver_step(fvs_solver* s, double dt, int cycle) {
 }
 
 int fvs_solver_newton_stats(fvs_solver* s, uint64_t* iterations, uint64_t* failures,
-                            int reset) {
+                            uint64_t* fallbacks, int reset) {
   if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
-  unsigned long long a[2], b[2];
+  unsigned long long a[3], b[3];
   FVS_CUDA(cudaMemcpyAsync(a, s->newton_words, sizeof a, cudaMemcpyDeviceToHost, s->stream));
   FVS_CUDA(cudaMemcpyAsync(b, s->ctrl->newton, sizeof b, cudaMemcpyDeviceToHost, s->stream));
   FVS_CUDA(cudaStreamSynchronize(s->stream));
   if (iterations) *iterations = a[0] + b[0];
   if (failures) *failures = a[1] + b[1];
+  if (fallbacks) *fallbacks = a[2] + b[2];
   if (reset) {
     FVS_CUDA(cudaMemsetAsync(s->newton_words, 0, sizeof a, s->stream));
     FVS_CUDA(cudaMemsetAsync(s->ctrl->newton, 0, sizeof b, s->stream));

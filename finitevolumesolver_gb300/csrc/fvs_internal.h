@@ -27,7 +27,8 @@ struct Control {
   double dt_override;  // > 0: use this dt for the next step instead of cfl*stable
   unsigned long long smax_stable[3];  // bits of max face speed, per direction
   unsigned long long smax_check[6];   // bits of max face speed, per sweep
-  unsigned long long newton[2];       // Newton iterations, non-converged faces
+  unsigned long long newton[3];       // Newton iterations, non-converged faces,
+                                      // faces whose learned start was rejected
   int abort;         // a per-sweep check failed; later kernels do nothing
   int done;          // t reached t_end; later kernels do nothing
   int failed_step;   // index of the failed step within the batch

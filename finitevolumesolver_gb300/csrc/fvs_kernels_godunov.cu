@@ -70,10 +70,12 @@ template <int D, bool kMuscl> struct GodunovPolicyT {
     const riemann::Star s = riemann::GodunovFlux<D>(g.eq, F, L, R, dir, g.opt);
     st.iterations += s.iterations;
     st.failures += s.converged ? 0 : 1;
+    st.fallbacks += s.fallback;
     if constexpr (kMuscl) {
       const riemann::Star c = riemann::ComputeMiddleState<D>(g.eq, wL, wR, dir, g.opt);
       st.iterations += c.iterations;
       st.failures += c.converged ? 0 : 1;
+      st.fallbacks += c.fallback;
       return riemann::SignalMaxSpeed<D>(g.eq, wL, wR, dir, c.p);
     } else {
       return riemann::SignalMaxSpeed<D>(g.eq, L, R, dir, s.p);
@@ -232,6 +234,7 @@ __global__ void PatchGodunovFluxKernel(bool muscl, int limiter, GodunovGas g, do
     }
     ns.iterations = s.iterations;
     ns.failures = s.converged ? 0 : 1;
+    ns.fallbacks = s.fallback;
     GView fv{fluxes, fbox};
 #pragma unroll
     for (int k = 0; k < K; ++k) fluxes[fv.Index(k, f[0], f[1], f[2])] = nf[k];

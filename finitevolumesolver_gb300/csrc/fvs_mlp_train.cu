@@ -11,7 +11,7 @@
 // Backward: dZ2 = (dy w3) * GELU'(Z2); dH1 = dZ2 W2 (tcgen05);
 // dW2 = dZ2^T H1 (tcgen05, split over the batch); dZ1 = dH1 * GELU'(Z1);
 // dW1 = dZ1^T X (tcgen05).  The M = 64 weight-gradient products run as
-// M = 128 tiles whose upper 64 rows are zero.
+// M = 128 tiles whose upper 64 rows are loaded as zeros and not stored.
 #include "../../include/fvs_gpu.h"
 #include "fvs_internal.h"
 #include "fvs_mlp.cuh"
@@ -248,11 +248,11 @@ struct StepBuffers {
   __nv_bfloat16* H1t;  // [64][B]
   float* Z2;           // [B][64]
   __nv_bfloat16* D2;   // dZ2 [B][64]
-  __nv_bfloat16* D2t;  // dZ2^T [128][B] (rows 64..127 zero)
+  __nv_bfloat16* D2t;  // dZ2^T [64][B]
   float* dH1;          // [B][64]
-  __nv_bfloat16* D1t;  // dZ1^T [128][B] (rows 64..127 zero)
-  float* dW2;          // [128][64]
-  float* dW1;          // [128][16]
+  __nv_bfloat16* D1t;  // dZ1^T [64][B]
+  float* dW2;          // [64][64]
+  float* dW1;          // [64][16]
   float* loss;         // accumulated loss (sum of squared errors)
   int use_given_rows;  // 1: rows are 0..B-1 of feat (gradient check)
 };
@@ -287,70 +287,98 @@ __global__ void GatherKernel(StepBuffers b, const float* stats) {
   b.target[r] = b.label[row];
 }
 
+// Tiles of 32 rows x 64 hidden units per 256-thread block: row-major
+// reads and writes are coalesced, the transposed copy goes through shared
+// memory so that its writes are coalesced too.
+constexpr int kTileRows = 32;
+
 // Z1 += b1, H1 = GELU(Z1) in both layouts.
-__global__ void Act1Kernel(StepBuffers b, const float* blob) {
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= int64_t(b.batch) * kH) return;
-  const int r = static_cast<int>(i / kH), o = static_cast<int>(i % kH);
-  const float z = b.Z1[i] + blob[mlp::kOffB1 + o];
-  b.Z1[i] = z;
-  const __nv_bfloat16 h = __float2bfloat16_rn(Gelu(z));
-  b.H1[i] = h;
-  b.H1t[int64_t(o) * b.batch + r] = h;
+__global__ void __launch_bounds__(256) Act1Kernel(StepBuffers b, const float* blob) {
+  __shared__ __nv_bfloat16 tile[kH][kTileRows + 2];
+  const int r0 = blockIdx.x * kTileRows;
+  for (int e = threadIdx.x; e < kTileRows * kH; e += blockDim.x) {
+    const int r = e / kH, o = e % kH;
+    const int64_t i = int64_t(r0 + r) * kH + o;
+    const float z = b.Z1[i] + blob[mlp::kOffB1 + o];
+    b.Z1[i] = z;
+    const __nv_bfloat16 h = __float2bfloat16_rn(Gelu(z));
+    b.H1[i] = h;
+    tile[o][r] = h;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < kTileRows * kH; e += blockDim.x) {
+    const int o = e / kTileRows, r = e % kTileRows;
+    b.H1t[int64_t(o) * b.batch + r0 + r] = tile[o][r];
+  }
 }
 
-// Output layer, loss, and the backward pass down to dZ2 (one thread per row).
+// Output layer, loss, and the backward pass down to dZ2 (one thread per row;
+// dw3, db2, db3 and the loss are reduced over the warp's 32 rows first).
 __global__ void OutKernel(StepBuffers b, const float* blob, float* grad) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  float gw3[kH];
-  float y = 0.0f, dy = 0.0f;
   const bool active = r < b.batch;
+  const int64_t row = int64_t(active ? r : 0) * kH;
+  float y = blob[mlp::kOffB3];
   if (active) {
-    y = blob[mlp::kOffB3];
-    float h2[kH];
 #pragma unroll 8
     for (int o = 0; o < kH; ++o) {
-      const float z = b.Z2[int64_t(r) * kH + o] + blob[mlp::kOffB2 + o];
-      b.Z2[int64_t(r) * kH + o] = z;
-      h2[o] = Gelu(z);
-      y = fmaf(blob[mlp::kOffW3 + o], h2[o], y);
+      const float z = b.Z2[row + o] + blob[mlp::kOffB2 + o];
+      b.Z2[row + o] = z;
+      y = fmaf(blob[mlp::kOffW3 + o], Gelu(z), y);
     }
-    const float e = y - b.target[r];
-    atomicAdd(b.loss, e * e);
-    dy = 2.0f * e / float(b.batch);
-#pragma unroll 8
-    for (int o = 0; o < kH; ++o) {
-      gw3[o] = dy * h2[o];
-      const float d2 = dy * blob[mlp::kOffW3 + o] * GeluGrad(b.Z2[int64_t(r) * kH + o]);
+  }
+  const float e = active ? y - b.target[r] : 0.0f;
+  const float dy = 2.0f * e / float(b.batch);
+  float e2 = e * e, g3 = dy;
+  for (int s = 16; s > 0; s >>= 1) {
+    e2 += __shfl_xor_sync(0xffffffffu, e2, s);
+    g3 += __shfl_xor_sync(0xffffffffu, g3, s);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(b.loss, e2);
+    atomicAdd(grad + mlp::kOffB3, g3);
+  }
+#pragma unroll 4
+  for (int o = 0; o < kH; ++o) {
+    float gw = 0.0f, d2 = 0.0f;
+    if (active) {
+      const float z = b.Z2[row + o];
+      gw = dy * Gelu(z);
+      d2 = dy * blob[mlp::kOffW3 + o] * GeluGrad(z);
       const __nv_bfloat16 h = __float2bfloat16_rn(d2);
-      b.D2[int64_t(r) * kH + o] = h;
+      b.D2[row + o] = h;
       b.D2t[int64_t(o) * b.batch + r] = h;
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+      gw += __shfl_xor_sync(0xffffffffu, gw, s);
+      d2 += __shfl_xor_sync(0xffffffffu, d2, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(grad + mlp::kOffW3 + o, gw);
       atomicAdd(grad + mlp::kOffB2 + o, d2);
     }
-  } else {
-#pragma unroll
-    for (int o = 0; o < kH; ++o) gw3[o] = 0.0f;
   }
-  // dw3 and db3: warp reduction, one atomic per warp
-#pragma unroll 8
-  for (int o = 0; o < kH; ++o) {
-    float v = gw3[o];
-    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-    if ((threadIdx.x & 31) == 0) atomicAdd(grad + mlp::kOffW3 + o, v);
-  }
-  float v = dy;
-  for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-  if ((threadIdx.x & 31) == 0) atomicAdd(grad + mlp::kOffB3, v);
 }
 
-// dZ1 = dH1 * GELU'(Z1) (transposed, bf16) and db1.
-__global__ void Back1Kernel(StepBuffers b, float* grad) {
-  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= int64_t(b.batch) * kH) return;
-  const int r = static_cast<int>(i / kH), o = static_cast<int>(i % kH);
-  const float d1 = b.dH1[i] * GeluGrad(b.Z1[i]);
-  b.D1t[int64_t(o) * b.batch + r] = __float2bfloat16_rn(d1);
-  atomicAdd(grad + mlp::kOffB1 + o, d1);
+// dZ1 = dH1 * GELU'(Z1) (transposed, bf16) and db1, per 32-row tile.
+__global__ void __launch_bounds__(256) Back1Kernel(StepBuffers b, float* grad) {
+  __shared__ float tile[kH][kTileRows + 1];
+  const int r0 = blockIdx.x * kTileRows;
+  for (int e = threadIdx.x; e < kTileRows * kH; e += blockDim.x) {
+    const int r = e / kH, o = e % kH;
+    const int64_t i = int64_t(r0 + r) * kH + o;
+    tile[o][r] = b.dH1[i] * GeluGrad(b.Z1[i]);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < kTileRows * kH; e += blockDim.x) {
+    const int o = e / kTileRows, r = e % kTileRows;
+    const float d1 = tile[o][r];
+    b.D1t[int64_t(o) * b.batch + r0 + r] = __float2bfloat16_rn(d1);
+    // the 32 lanes of a warp hold the 32 rows of one hidden unit
+    float v = d1;
+    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+    if ((threadIdx.x & 31) == 0) atomicAdd(grad + mlp::kOffB1 + o, v);
+  }
 }
 
 // Gather the weight gradients from the GEMM outputs into the blob layout.
@@ -495,9 +523,9 @@ int EnsureBatch(fvs_mlp* m, int batch) {
   MLP_CUDA(Alloc(m, (void**)&b.H1t, B * kH * 2));
   MLP_CUDA(Alloc(m, (void**)&b.Z2, B * kH * 4));
   MLP_CUDA(Alloc(m, (void**)&b.D2, B * kH * 2));
-  MLP_CUDA(Alloc(m, (void**)&b.D2t, B * 128 * 2));
+  MLP_CUDA(Alloc(m, (void**)&b.D2t, B * kH * 2));
   MLP_CUDA(Alloc(m, (void**)&b.dH1, B * kH * 4));
-  MLP_CUDA(Alloc(m, (void**)&b.D1t, B * 128 * 2));
+  MLP_CUDA(Alloc(m, (void**)&b.D1t, B * kH * 2));
   MLP_CUDA(Alloc(m, (void**)&b.dW2, 128 * kH * 4));
   MLP_CUDA(Alloc(m, (void**)&b.dW1, 128 * kXin * 4));
   MLP_CUDA(Alloc(m, (void**)&b.loss, 4));
@@ -523,7 +551,7 @@ cudaError_t EnqueueStep(fvs_mlp* m, bool update, float lr) {
   g.A = b.X; g.lda = kXin; g.B = net.W1; g.ldb = kXin; g.C = b.Z1; g.ldc = kH;
   g.M = B; g.K = kXin; g.k_per_cta = kXin; g.atomic = 0;
   if ((e = LaunchGemm<64>(g, 1, s)) != cudaSuccess) return e;
-  Act1Kernel<<<unsigned((int64_t(B) * kH + 255) / 256), 256, 0, s>>>(b, net.blob);
+  Act1Kernel<<<B / kTileRows, 256, 0, s>>>(b, net.blob);
   // Z2 = H1 W2^T
   g.A = b.H1; g.lda = kH; g.B = net.W2; g.ldb = kH; g.C = b.Z2; g.ldc = kH;
   g.M = B; g.K = kH; g.k_per_cta = kH; g.atomic = 0;
@@ -536,12 +564,12 @@ cudaError_t EnqueueStep(fvs_mlp* m, bool update, float lr) {
   // dW2 = dZ2^T H1 over the batch (split K)
   const int kper = 256;
   g.A = b.D2t; g.lda = B; g.B = b.H1t; g.ldb = B; g.C = b.dW2; g.ldc = kH;
-  g.M = 128; g.K = B; g.k_per_cta = kper; g.atomic = 1;
+  g.M = kH; g.K = B; g.k_per_cta = kper; g.atomic = 1;
   if ((e = LaunchGemm<64>(g, (B + kper - 1) / kper, s)) != cudaSuccess) return e;
-  Back1Kernel<<<unsigned((int64_t(B) * kH + 255) / 256), 256, 0, s>>>(b, net.grad);
+  Back1Kernel<<<B / kTileRows, 256, 0, s>>>(b, net.grad);
   // dW1 = dZ1^T X
   g.A = b.D1t; g.lda = B; g.B = b.Xt; g.ldb = B; g.C = b.dW1; g.ldc = kXin;
-  g.M = 128; g.K = B; g.k_per_cta = kper; g.atomic = 1;
+  g.M = kH; g.K = B; g.k_per_cta = kper; g.atomic = 1;
   if ((e = LaunchGemm<16>(g, (B + kper - 1) / kper, s)) != cudaSuccess) return e;
   CollectKernel<<<(kH * kH + 255) / 256, 256, 0, s>>>(b, net.grad);
   if (update) {

@@ -18,9 +18,10 @@
 //    not met the tolerance keeps its last iterate and is counted as a
 //    failure (the reference throws std::runtime_error after 5000 steps).
 //  - The start value is selectable: the reference's arithmetic mean, the
-//    PVRS/two-rarefaction estimate, or a learned (MLP) estimate that falls
-//    back to PVRS/two-rarefaction when non-positive or not finite, or when
-//    Newton from it fails to converge.
+//    PVRS/two-rarefaction estimate, or a learned (MLP) estimate, used only
+//    where the PVRS/TR start is poor (large residual), that falls back to
+//    PVRS/two-rarefaction when non-positive or not finite, or when Newton
+//    from it has not converged within 64 steps.
 #pragma once
 
 #include "fvs_mlp.cuh"
@@ -153,7 +154,18 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
   } else {
     const double pv = PvrsTrGuess(g, L.rho, uL, L.p, L.a, R.rho, uR, R.p, R.a);
     x0 = pv;
-    if (opt.guess == kGuessMlp && opt.mlp) {
+    // The learned start is used only where the PVRS/TR start is poor: its
+    // residual |f(p_pvrs)| exceeds kLearnedGate (aL + aR), i.e. roughly a
+    // relative error of more than a few per cent in p*.  Weak waves (most
+    // faces of a real flow), where PVRS/TR is accurate to second order in
+    // the wave strength and Newton needs zero or one step from it, keep
+    // their start and never pay for the network.
+    constexpr double kLearnedGate = 0.05;
+    const bool screened =
+        opt.guess == kGuessMlp &&
+        !(fabs(FSide(R, gm1, exponent, pv) + FSide(L, gm1, exponent, pv) + du) >
+          kLearnedGate * (L.a + R.a));
+    if (opt.guess == kGuessMlp && opt.mlp && !screened) {
       const double learned = mlp::GuessStarPressure(opt.mlp, L.rho, uL, L.p, L.a, R.rho, uR,
                                                     R.p, R.a);
       if (learned > 0.0 && learned < 1.7976931348623157e308) {
@@ -165,7 +177,9 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
     if (opt.guess == kGuessMlp && !st.fallback) {
       double x;
       int it, ok;
-      Newton(L, R, du, gm1, exponent, d_exponent, x0, opt.tol, opt.max_iterations, x, it, ok);
+      // a learned start gets at most 64 steps before the PVRS/TR restart
+      const int learned_max = opt.max_iterations < 64 ? opt.max_iterations : 64;
+      Newton(L, R, du, gm1, exponent, d_exponent, x0, opt.tol, learned_max, x, it, ok);
       if (!ok) {
         // the learned start did not converge within the bound: fall back
         st.fallback = 1;

@@ -77,16 +77,19 @@ struct NoStats {
 struct NewtonStats {
   unsigned long long iterations = 0;
   unsigned long long failures = 0;
+  unsigned long long fallbacks = 0;
   __device__ __forceinline__ void Flush(unsigned long long* out) const {
-    unsigned long long it = iterations, fl = failures;
+    unsigned long long it = iterations, fl = failures, fb = fallbacks;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       it += __shfl_xor_sync(0xffffffffu, it, o);
       fl += __shfl_xor_sync(0xffffffffu, fl, o);
+      fb += __shfl_xor_sync(0xffffffffu, fb, o);
     }
     if (out && (threadIdx.x & 31) == 0) {
       if (it) atomicAdd(out, it);
       if (fl) atomicAdd(out + 1, fl);
+      if (fb) atomicAdd(out + 2, fb);
     }
   }
 };

@@ -144,3 +144,153 @@ def shock_circles_2d(n=1024, seed=5, mach=2.0, gamma=GAMMA, x_shock=0.1, ncirc=8
     p = np.where(post, p2, p1)
     cons = cons_from_prim(rho, [u, np.zeros((n, n))], p, gamma).reshape(4, 1, n, n)
     return circles, cons
+
+
+class AmrHierarchy:
+    """A static 2-D block-structured AMR hierarchy with refinement ratio 2:
+    `levels[p]` and `boxes[p] = (lo_x, lo_y, hi_x, hi_y)` (half-open, in
+    level levels[p]'s index space) for every patch p; level l has
+    (n0[0] << l) x (n0[1] << l) cells of size dx0 / 2^l."""
+
+    def __init__(self, nlevels, n0, bc, dx0, levels, boxes):
+        self.nlevels = int(nlevels)
+        self.n0 = [int(v) for v in n0]
+        self.bc = [int(v) for v in bc]
+        self.dx0 = float(dx0)
+        self.levels = np.ascontiguousarray(levels, dtype=np.int32)
+        self.boxes = np.ascontiguousarray(boxes, dtype=np.int32).reshape(-1, 4)
+
+    @property
+    def npatches(self):
+        return len(self.levels)
+
+    def cells(self):
+        ext = (self.boxes[:, 2] - self.boxes[:, 0]).astype(np.int64) * \
+            (self.boxes[:, 3] - self.boxes[:, 1])
+        return np.bincount(self.levels, weights=ext, minlength=self.nlevels).astype(np.int64)
+
+    def cell_centres(self, p):
+        l = int(self.levels[p])
+        dx = self.dx0 / (1 << l)
+        x0, y0, x1, y1 = (int(v) for v in self.boxes[p])
+        x = (np.arange(x0, x1) + 0.5) * dx
+        y = (np.arange(y0, y1) + 0.5) * dx
+        return np.meshgrid(x, y)  # [ny][nx]
+
+    def cons_from(self, fn):
+        """Concatenated patch interiors [4][ny][nx] of cons = fn(X, Y)."""
+        return np.concatenate([np.asarray(fn(*self.cell_centres(p))).reshape(-1)
+                               for p in range(self.npatches)])
+
+    def split(self, flat):
+        """Per-patch views [4][ny][nx] of a concatenated array."""
+        out, off = [], 0
+        for p in range(self.npatches):
+            x0, y0, x1, y1 = (int(v) for v in self.boxes[p])
+            n = 4 * (x1 - x0) * (y1 - y0)
+            out.append(flat[off:off + n].reshape(4, y1 - y0, x1 - x0))
+            off += n
+        return out
+
+
+def _tile_axis(n, rng, sizes=(8, 16, 32, 64)):
+    """Extents drawn from `sizes` that add up to n (a multiple of 8)."""
+    out, left = [], n
+    while left > 0:
+        s = int(rng.choice(sizes))
+        while s > left:
+            s //= 2
+        out.append(s)
+        left -= s
+    return out
+
+
+def _tiling(n, rng, sizes=(8, 16, 32, 64)):
+    w = _tile_axis(n, rng, sizes)
+    h = _tile_axis(n, rng, sizes)
+    xs = np.concatenate([[0], np.cumsum(w)])
+    ys = np.concatenate([[0], np.cumsum(h)])
+    return [(int(xs[i]), int(ys[j]), int(xs[i + 1]), int(ys[j + 1]))
+            for j in range(len(h)) for i in range(len(w))]
+
+
+def amr_hierarchy(n0=1024, nlevels=3, seed=7, centre=None, radius=0.1, bands=None,
+                  bc=(1, 1), target=4096, sizes=(8, 16, 32, 64)):
+    """Patches placed by refinement of the ring |r - radius| < band around a
+    blast centre: level 0 tiles the n0^2 domain, level l >= 1 keeps the tiles
+    of a random tiling of its index space (extents from {8, 16, 32, 64} per
+    axis) that meet the ring of width bands[l-1] and whose footprint grown by
+    the 2 ghost cells lies inside level l-1 (proper nesting).  Without
+    `bands` the widths are scaled until the patch count is close to `target`.
+    Returns (hierarchy, centre)."""
+    rng = np.random.default_rng(seed)
+    if centre is None:
+        centre = rng.uniform(0.3, 0.7, 2)
+    dx0 = 1.0 / n0
+    base_state = rng.bit_generator.state
+
+    def build(bands):
+        rng.bit_generator.state = base_state
+        levels, boxes = [], []
+        tiles0 = _tiling(n0, rng, sizes)
+        levels += [0] * len(tiles0)
+        boxes += tiles0
+        covered_prev = np.ones((n0, n0), dtype=bool)
+        for l in range(1, nlevels):
+            n = n0 << l
+            dx = dx0 / (1 << l)
+            band = bands[l - 1]
+            cov = np.zeros((n, n), dtype=bool)
+            for (x0, y0, x1, y1) in _tiling(n, rng, sizes):
+                # does the tile meet the ring?
+                xs = (np.array([x0, x1]) * dx) - centre[0]
+                ys = (np.array([y0, y1]) * dx) - centre[1]
+                nx_ = np.clip(0.0, xs[0], xs[1])
+                ny_ = np.clip(0.0, ys[0], ys[1])
+                dmin = np.hypot(nx_, ny_)
+                dmax = np.hypot(np.abs(xs).max(), np.abs(ys).max())
+                if dmax < radius - band or dmin > radius + band:
+                    continue
+                # nesting: the grown footprint must lie in level l-1
+                gx0, gy0 = max(x0 - 2, 0), max(y0 - 2, 0)
+                gx1, gy1 = min(x1 + 2, n), min(y1 + 2, n)
+                if not covered_prev[gy0 // 2:(gy1 + 1) // 2, gx0 // 2:(gx1 + 1) // 2].all():
+                    continue
+                levels.append(l)
+                boxes.append((x0, y0, x1, y1))
+                cov[y0:y1, x0:x1] = True
+            covered_prev = cov
+        return levels, boxes
+
+    if bands is None:
+        lo, hi = 0.002, 0.2
+        best = None
+        for _ in range(16):
+            mid = 0.5 * (lo + hi)
+            bs = [mid / (1.5 ** (l - 1)) for l in range(1, nlevels)]
+            lv, bx = build(bs)
+            if best is None or abs(len(lv) - target) < abs(len(best[0]) - target):
+                best = (lv, bx)
+            if len(lv) < target:
+                lo = mid
+            else:
+                hi = mid
+        levels, boxes = best
+    else:
+        levels, boxes = build(bands)
+    return AmrHierarchy(nlevels, (n0, n0), bc, dx0, levels, boxes), centre
+
+
+def amr_blast_2d(n0=1024, nlevels=3, seed=7, target=4096, bc=(1, 1), gamma=GAMMA,
+                 sizes=(8, 16, 32, 64)):
+    """Blast wave on an AMR patch set: rho 1, p 1, p 10 inside radius 0.1
+    about a seeded centre, at rest.  Returns (hierarchy, cons)."""
+    h, centre = amr_hierarchy(n0, nlevels, seed, target=target, bc=bc, sizes=sizes)
+
+    def fn(X, Y):
+        r = np.hypot(X - centre[0], Y - centre[1])
+        rho = np.ones_like(X)
+        p = np.where(r < 0.1, 10.0, 1.0)
+        return cons_from_prim(rho, [np.zeros_like(X), np.zeros_like(X)], p, gamma)
+
+    return h, h.cons_from(fn)

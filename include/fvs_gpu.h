@@ -240,11 +240,13 @@ int fvs_solver_step(fvs_solver* s, double dt, int cycle);
  * dt_log (host, may be NULL) receives up to `dt_log_len` committed dts. */
 int fvs_solver_run(fvs_solver* s, double cfl, double t_end, int max_steps,
                    double* dt_log, int dt_log_len, fvs_run_stats* stats);
-/* Newton iterations and non-converged faces of the exact Riemann solver,
- * accumulated by the solver's Godunov sweeps (fvs_solver_sweep/step since
- * the last reset, plus the last fvs_solver_run, which restarts its count). */
+/* Newton iterations, non-converged faces and faces whose learned start
+ * value was rejected (FVS_GUESS_MLP falls back to the PVRS start) of the
+ * exact Riemann solver, accumulated by the solver's Godunov sweeps
+ * (fvs_solver_sweep/step since the last reset, plus the last
+ * fvs_solver_run, which restarts its count).  Any pointer may be NULL. */
 int fvs_solver_newton_stats(fvs_solver* s, uint64_t* iterations, uint64_t* failures,
-                            int reset);
+                            uint64_t* fallbacks, int reset);
 /* The solver's CUDA stream (cudaStream_t): every solver call runs on it. */
 int fvs_solver_stream(fvs_solver* s, void** stream);
 /* ---- Embedded boundary: KBN h-box cut cells (rank 2) ------------------ */
@@ -271,6 +273,71 @@ int fvs_solver_cutcell_geometry(fvs_solver* s, double* alpha, double* betax, dou
 /* Cycle counter used for the direction order of the next step. */
 int fvs_solver_set_cycle(fvs_solver* s, int64_t cycle);
 int fvs_solver_set_time(fvs_solver* s, double t);
+
+/* ---- Batched AMR patch set (rank 2, refinement ratio 2) ---------------- */
+/* The subcycled, refluxed block-structured update that the reference runs
+ * with SubcycleFineFirstSolver over DimensionalSplitLevelIntegrator
+ * (include/fub/solver/SubcycleFineFirstSolver.hpp:100-191,
+ * include/fub/solver/DimensionalSplitLevelIntegrator.hpp:204-276) on an
+ * AMReX patch hierarchy with FluxRegister refluxing and average_down
+ * (src/AMReX/IntegratorContext.cpp:380-533), for a static hierarchy:
+ *  - level l has (n0 << l) cells per direction of size dx0 / 2^l; level-0
+ *    patches tile the domain, finer patches have even corners, do not
+ *    overlap within a level, and are nested (their footprint grown by the 2
+ *    ghost cells lies inside the next coarser level);
+ *  - every patch of a level is advanced by one persistent kernel launch per
+ *    sweep over a device-resident table of patch rows; a whole coarse step
+ *    (ghost fills, stable dt, dt selection, fine-first subcycles with Strang
+ *    sweeps, refluxing, average-down, per-sweep CFL checks) is one CUDA
+ *    graph;
+ *  - ghost cells are refilled before every sweep: same-level copies, the
+ *    boundary condition (periodic wrap / transmissive clamp), and otherwise
+ *    piecewise-constant injection from the coarser level's state at the
+ *    start of the coarse step.
+ * Methods: MUSCL-Hancock + HLLE (any limiter) in exact FP64, fast FP64 or
+ * mixed precision. */
+typedef struct fvs_amr fvs_amr;
+
+typedef struct fvs_amr_desc {
+  int32_t rank;           /* 2 */
+  int32_t nlevels;        /* 1..4 */
+  int32_t n0[3];          /* level-0 cells per direction */
+  int32_t bc[3];          /* fvs_bc per direction */
+  double dx0;             /* level-0 cell size */
+  int32_t npatches;
+  int32_t reserved;
+  const int32_t* patch_level; /* [npatches] */
+  const fvs_box* patch_box;   /* [npatches], in the patch level's index space */
+} fvs_amr_desc;
+
+int fvs_amr_create(const fvs_amr_desc* d, const fvs_method* m, fvs_amr** out);
+int fvs_amr_destroy(fvs_amr* a);
+/* Host data: the patches' interiors concatenated in patch order, each
+ * [4][ny][nx] (FArrayBox layout of the patch box). */
+int fvs_amr_upload(fvs_amr* a, const double* host);
+int fvs_amr_download(fvs_amr* a, double* host);
+/* Interior cells and storage cells (with ghosts) per level, and the number
+ * of coarse-fine register faces.  Any pointer may be NULL. */
+int fvs_amr_info(fvs_amr* a, int64_t* cells_per_level, int64_t* storage_per_level,
+                 int32_t* nslots);
+int fvs_amr_stream(fvs_amr* a, void** stream);
+/* Coarse-step stable dt: min over levels of 2^l times the level's stable dt
+ * (SubcycleFineFirstSolver.hpp:100-112), without the CFL factor. */
+int fvs_amr_stable_dt(fvs_amr* a, double* dt);
+/* RunSimulation's loop over coarse steps: dt = min(t_end - t,
+ * cfl * stable dt); a failed per-sweep check restarts the coarse step from
+ * its start with cfl times 2^l times the failing level's dt. */
+int fvs_amr_run(fvs_amr* a, double cfl, double t_end, int max_steps, double* dt_log,
+                int log_len, fvs_run_stats* stats);
+/* Persistent launch shape (threads per block, blocks) of a level's sweeps
+ * in direction dir. */
+int fvs_amr_set_launch(fvs_amr* a, int level, int dir, int block, int grid);
+/* Times the sweeps of every level and direction for a set of launch shapes
+ * and keeps the fastest; results are cached per process under the key
+ * (precision, direction, the level's patch-size histogram), so hierarchies
+ * with the same histogram reuse them.  configs (may be NULL) receives
+ * [nlevels][2 directions][block, grid]. */
+int fvs_amr_autotune(fvs_amr* a, int32_t* configs);
 
 /* ---- Learned start value of the exact Riemann solver ------------------- */
 /* No counterpart in the reference: its ExactRiemannSolver starts Newton's

@@ -14,7 +14,7 @@ from pathlib import Path
 
 ORACLE_DIR = Path(__file__).resolve().parent
 LIB_PATH = ORACLE_DIR / "liboracle.so"
-SOURCES = ["fvs_oracle.cpp", "fvs_oracle_cutcell.cpp"]
+SOURCES = ["fvs_oracle.cpp", "fvs_oracle_cutcell.cpp", "fvs_oracle_amr.cpp"]
 HEADERS = ["fvs_oracle.hpp", "fvs_oracle_riemann.hpp"]
 FLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp",
          "-fPIC", "-shared", "-Wall"]

@@ -295,3 +295,37 @@ class CutCellGeometry:
         steps = L.orc_cc_run(*self._args(bc), _d(self.normal), _d(self.center), _d(cons), cfl,
                              t_end, max_steps, limiter, _d(log), C.byref(rs), nthreads)
         return cons, log[:steps].copy(), rs.value
+
+
+# ---------------------------------------------------------------------------
+# Batched AMR patch set (2-D, ratio 2, MUSCL-Hancock/VanLeer + HLLE, FP64)
+
+def amr_run(hier, cons, cfl, t_end, max_steps=-1, dt_override=None, nthreads=0):
+    """Advance an AMR hierarchy (see finitevolumesolver_gb300.workloads
+    .AmrHierarchy: nlevels, n0, bc, dx0, levels [npatch], boxes [npatch, 4]).
+    cons: the patch interiors concatenated, each [4][ny][nx].  Returns
+    (cons, dt_log, restarts)."""
+    L = lib()
+    if not getattr(L, "_amr_ready", False):
+        I = C.c_int
+        L.orc_amr_run.argtypes = [I, _I32, _I32, C.c_double, I, _I32, _I32, _P, C.c_double,
+                                  C.c_double, I, _P, I, _P, C.POINTER(C.c_int), I]
+        L.orc_amr_run.restype = C.c_int
+        L._amr_ready = True
+    cons = np.array(cons, dtype=np.float64, copy=True, order="C")
+    n0 = np.asarray(hier.n0, dtype=np.int32)
+    bc = np.asarray(hier.bc, dtype=np.int32)
+    lv = np.ascontiguousarray(hier.levels, dtype=np.int32)
+    bx = np.ascontiguousarray(hier.boxes, dtype=np.int32)
+    ov = None if dt_override is None else np.ascontiguousarray(dt_override, dtype=np.float64)
+    cap = max_steps if max_steps >= 0 else 100000
+    log = np.zeros(max(cap, 1))
+    rs = C.c_int(0)
+    steps = L.orc_amr_run(int(hier.nlevels), n0.ctypes.data_as(_I32), bc.ctypes.data_as(_I32),
+                          float(hier.dx0), len(lv), lv.ctypes.data_as(_I32),
+                          bx.ctypes.data_as(_I32), _d(cons), float(cfl), float(t_end),
+                          int(max_steps), None if ov is None else _d(ov),
+                          0 if ov is None else len(ov), _d(log), C.byref(rs), int(nthreads))
+    if steps < 0:
+        raise ValueError("invalid AMR hierarchy")
+    return cons, log[:steps].copy(), rs.value
