@@ -29,6 +29,7 @@ UNITS = [
     ("fvs_kernels_fast.cu", []),
     ("fvs_kernels_godunov.cu", ["-fmad=false"]),
     ("fvs_kernels_cutcell.cu", ["-fmad=false"]),
+    ("fvs_kernels_cutcell_mixed.cu", []),
     ("fvs_capi.cu", []),
     ("fvs_noalloc.cu", ["-fmad=false"]),
     ("fvs_mlp_train.cu", []),

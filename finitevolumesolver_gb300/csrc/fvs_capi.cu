@@ -239,6 +239,13 @@ fvs::CcStateArgs MakeCcState(const fvs_solver* s, const double* in) {
   return a;
 }
 
+cudaError_t CcReferenceStates(const fvs_solver* s, const double* in) {
+  const fvs::CcStateArgs a = MakeCcState(s, in);
+  return s->m.precision == FVS_FP64_EXACT
+             ? fvs::LaunchCutCellReferenceStates(a, s->stream)
+             : fvs::LaunchCutCellReferenceStatesT(s->m.precision, a, s->stream);
+}
+
 cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
                         int dir, const double* dt_ptr, double dt_scale,
                         double dt_value, unsigned long long* smax_out,
@@ -258,7 +265,9 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
     c.ctrl = ctrl;
     c.prev_check = prev_check;
     c.prev_dx = prev_dx;
-    return fvs::LaunchCutCellSweep(c, s->stream);
+    return s->m.precision == FVS_FP64_EXACT
+               ? fvs::LaunchCutCellSweep(c, s->stream)
+               : fvs::LaunchCutCellSweepT(s->m.precision, c, s->stream);
   }
   fvs::SweepArgs a{};
   a.in = in;
@@ -297,7 +306,11 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
 
 cudaError_t LaunchStable(const fvs_solver* s, const double* in,
                          unsigned long long* smax_out, fvs::Control* ctrl) {
-  if (s->cc) return fvs::LaunchCutCellStableDt(MakeCcState(s, in), smax_out, ctrl, s->stream);
+  if (s->cc)
+    return s->m.precision == FVS_FP64_EXACT
+               ? fvs::LaunchCutCellStableDt(MakeCcState(s, in), smax_out, ctrl, s->stream)
+               : fvs::LaunchCutCellStableDtT(s->m.precision, MakeCcState(s, in), smax_out, ctrl,
+                                             s->stream);
   fvs::StableDtArgs a{};
   a.in = in;
   for (int d = 0; d < 3; ++d) {
@@ -359,7 +372,7 @@ cudaError_t EnqueueStep(fvs_solver* s, int start, int64_t cycle, int step_in_bat
   cudaError_t e = cudaSuccess;
   if (s->cc) {
     // KbnCutCellMethod::PreAdvanceHierarchy: reference states of the step
-    e = fvs::LaunchCutCellReferenceStates(MakeCcState(s, s->buf[start]), s->stream);
+    e = CcReferenceStates(s, s->buf[start]);
     if (e != cudaSuccess) return e;
   }
   e = LaunchStable(s, s->buf[start], s->ctrl->smax_stable, s->ctrl);
@@ -669,8 +682,8 @@ int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int nc
                                     double x0, double y0) {
   if (!s || !circles) return Fail(FVS_ERR_INVALID, "NULL argument");
   if (s->g.rank != 2) return Fail(FVS_ERR_UNSUPPORTED, "cut cells need a rank-2 grid");
-  if (s->m.flux_method != FVS_MUSCL_HLLE || s->m.precision != FVS_FP64_EXACT)
-    return Fail(FVS_ERR_UNSUPPORTED, "cut cells run MUSCL-Hancock + HLLE in exact FP64");
+  if (s->m.flux_method != FVS_MUSCL_HLLE)
+    return Fail(FVS_ERR_UNSUPPORTED, "cut cells run MUSCL-Hancock + HLLE");
   if (ncircles < 1 || ncircles > 16) return Fail(FVS_ERR_INVALID, "1 to 16 circles");
   for (int k = 0; k < ncircles; ++k)
     if (!(circles[3 * k + 2] > 0.0)) return Fail(FVS_ERR_INVALID, "circle radius must be > 0");
@@ -784,7 +797,7 @@ int fvs_solver_sweep(fvs_solver* s, int dir, double dt, double* level_dt_out) {
   if (dir < 0 || dir >= s->g.rank) return Fail(FVS_ERR_INVALID, "direction out of range");
   const int out = (s->cur + 1) % 3;
   if (s->cc)
-    FVS_CUDA(fvs::LaunchCutCellReferenceStates(MakeCcState(s, s->buf[s->cur]), s->stream));
+    FVS_CUDA(CcReferenceStates(s, s->buf[s->cur]));
   FVS_CUDA(cudaMemsetAsync(s->scratch_words, 0, sizeof(unsigned long long), s->stream));
   FVS_CUDA(LaunchSweep(s, s->buf[s->cur], s->buf[out], dir, nullptr, 1.0, dt,
                        s->scratch_words, nullptr, -1, 0.0));
@@ -808,7 +821,7 @@ int fvs_solver_step(fvs_solver* s, double dt, int cycle) {
   FVS_CUDA(cudaMemsetAsync(s->scratch_words, 0, 8 * sizeof(unsigned long long), s->stream));
   const int start = s->cur;
   if (s->cc)
-    FVS_CUDA(fvs::LaunchCutCellReferenceStates(MakeCcState(s, s->buf[start]), s->stream));
+    FVS_CUDA(CcReferenceStates(s, s->buf[start]));
   const int X = (start + 1) % 3, Y = (start + 2) % 3;
   int src = start, dst = X;
   for (int q = 0; q < plan.nsweeps; ++q) {

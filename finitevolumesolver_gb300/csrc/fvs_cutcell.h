@@ -78,6 +78,11 @@ struct CcSweepArgs {
 
 cudaError_t LaunchCutCellGeometry(const CcGeomArgs& a, const CcGeom& g, cudaStream_t s);
 cudaError_t LaunchCutCellReferenceStates(const CcStateArgs& a, cudaStream_t s);
+// Fast FP64 (precision 1) and mixed (precision 2) flavours of the KBN kernels.
+cudaError_t LaunchCutCellReferenceStatesT(int precision, const CcStateArgs& a, cudaStream_t s);
+cudaError_t LaunchCutCellSweepT(int precision, const CcSweepArgs& a, cudaStream_t s);
+cudaError_t LaunchCutCellStableDtT(int precision, const CcStateArgs& a,
+                                   unsigned long long* smax_out, Control* ctrl, cudaStream_t s);
 cudaError_t LaunchCutCellSweep(const CcSweepArgs& a, cudaStream_t s);
 cudaError_t LaunchCutCellStableDt(const CcStateArgs& a, unsigned long long* smax_out,
                                   Control* ctrl, cudaStream_t s);

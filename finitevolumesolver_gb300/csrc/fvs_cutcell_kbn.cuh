@@ -1,0 +1,592 @@
+// fvs_cutcell_kbn.cuh -- the KBN h-box cut-cell physics and kernels (2-D),
+// generic over the arithmetic type T of the reconstruction, fluxes and wave
+// speeds:
+//   T = double in a -fmad=false translation unit: the exact flavour, bit for
+//     bit the CPU oracle's restatement of the reference;
+//   T = double with FMA contraction: the fast FP64 flavour;
+//   T = float: the mixed flavour -- masked MUSCL-Hancock, HLL/Einfeldt,
+//     boundary (wall) states and CFL speeds in FP32; the state, the face
+//     fractions, the h-box flux combination and the cut-cell update in FP64.
+//
+// Reference (maikel/FiniteVolumeSolver):
+//   KbnCutCellMethod           include/fub/cutcell_method/KbnStabilisation.hpp:188-450
+//   ComputeStableFluxes_Row    src/cutcell_method/KbnStabilisation.cpp:55-105
+//   UpdateConservatively_Row   src/AMReX/cutcell/TimeIntegrator.cpp:65-221
+//   masked MusclHancock / Hll / Einfeldt / Flux / CompleteFromCons
+//       include/fub/flux_method/MusclHancockMethod.hpp:487-571,
+//       include/fub/flux_method/HllMethod.hpp:295-365,
+//       src/equations/perfect_gas/EinfeldtSignalVelocities.hpp:99-142,
+//       src/equations/PerfectGas.cpp:79-93, 126-144
+//   HllBase::SolveRiemannProblem (boundary solver)  include/fub/flux_method/HllMethod.hpp:161-184
+//   MakeRotation, Reflect      include/fub/ext/Eigen.hpp:104-115, src/equations/PerfectGas.cpp:240-252
+#pragma once
+
+#include "fvs_cutcell.h"
+#include "fvs_internal.h"
+#include "fvs_physics_exact.cuh"
+#include "fvs_sweep.cuh"
+
+namespace fvs {
+namespace cc {
+
+template <class T> struct GasT {
+  T gamma;
+  T gamma_minus_1_inv;
+};
+
+template <class T> struct C2T {
+  T rho;
+  T m[2];
+  T E;
+  T p;
+  T c;
+};
+
+template <class T> __device__ __forceinline__ T PMinT(T a, T b) { return a < b ? a : b; }
+template <class T> __device__ __forceinline__ T PMaxT(T a, T b) { return a > b ? a : b; }
+
+template <class T> __device__ __forceinline__ GasT<T> MakeGasT(double gamma) {
+  GasT<T> g;
+  g.gamma = T(gamma);
+  g.gamma_minus_1_inv = T(1.0 / (gamma - 1.0));
+  return g;
+}
+
+// PerfectGas<2>::CompleteFromCons (PerfectGas.cpp:96-110): e_kin = 0.5 |m|^2
+// / rho, p = (E - e_kin) / gamma_minus_1_inv, c = sqrt(gamma p / rho).
+template <class T>
+__device__ __forceinline__ void CompleteT(const GasT<T>& eq, C2T<T>& q, const T* u) {
+  q.rho = u[0];
+  q.m[0] = u[1];
+  q.m[1] = u[2];
+  q.E = u[3];
+  const T e_kin = T(0.5) * (q.m[0] * q.m[0] + q.m[1] * q.m[1]) / q.rho;
+  const T e_int = q.E - e_kin;
+  q.p = e_int / eq.gamma_minus_1_inv;
+  q.c = sqrt(eq.gamma * q.p / q.rho);
+}
+
+// PerfectGas<2>::Flux (PerfectGas.cpp:52-64).
+template <class T> __device__ __forceinline__ void FluxT(T* f, const C2T<T>& q, int dir) {
+  const T velocity = q.m[dir] / q.rho;
+  f[0] = q.m[dir];
+  f[1] = velocity * q.m[0];
+  f[2] = velocity * q.m[1];
+  f[1 + dir] += q.p;
+  f[3] = velocity * (q.E + q.p);
+}
+
+// EinfeldtSignalVelocities (scalar, EinfeldtSignalVelocities.hpp:25-62).
+template <class T>
+__device__ __forceinline__ void EinfeldtT(const GasT<T>& eq, const C2T<T>& L, const C2T<T>& R,
+                                          int dir, T& sL, T& sR) {
+  const T rhoL = L.rho;
+  const T rhoR = R.rho;
+  const T sqRhoL = sqrt(rhoL);
+  const T sqRhoR = sqrt(rhoR);
+  const T oosqRhoSum = T(1) / (sqRhoL + sqRhoR);
+  const T uL = L.m[dir] / rhoL;
+  const T uR = R.m[dir] / rhoR;
+  const T roeU = (uL * sqRhoL + uR * sqRhoR) * oosqRhoSum;
+  const T hL = (L.E + L.p) / rhoL;
+  const T hR = (R.E + R.p) / rhoR;
+  const T roeH = (hL * sqRhoL + hR * sqRhoR) * oosqRhoSum;
+  const T roeA2 = (eq.gamma - T(1)) * (roeH - T(0.5) * roeU * roeU);
+  const T roeA = sqrt(roeA2);
+  sL = PMinT(uL - L.c, roeU - roeA);
+  sR = PMaxT(roeU + roeA, uR + R.c);
+}
+
+// CompleteFromCons masked by `mask && rho > 0` (PerfectGas.cpp:126-144).
+template <class T>
+__device__ __forceinline__ void CompleteMasked(const GasT<T>& eq, C2T<T>& q, const T* u,
+                                               bool mask) {
+  if (!(mask && u[0] > T(0))) {
+    q.rho = T(0);
+    q.m[0] = T(0);
+    q.m[1] = T(0);
+    q.E = T(0);
+    q.p = T(0);
+    q.c = T(0);
+    return;
+  }
+  CompleteT(eq, q, u);
+}
+
+// Flux masked by `rho > 0` (PerfectGas.cpp:79-93, mask true).
+template <class T> __device__ __forceinline__ void FluxMasked(T* f, const C2T<T>& q, int dir) {
+  const T rho = (q.rho > T(0)) ? q.rho : T(1);
+  const T velocity = q.m[dir] / rho;
+  f[0] = q.m[dir];
+  f[1] = velocity * q.m[0];
+  f[2] = velocity * q.m[1];
+  f[1 + dir] += q.p;
+  f[3] = velocity * (q.E + q.p);
+}
+
+// Masked Einfeldt speeds with mask true (EinfeldtSignalVelocities.hpp:99-142).
+template <class T>
+__device__ __forceinline__ void EinfeldtMasked(const GasT<T>& eq, const C2T<T>& L,
+                                               const C2T<T>& R, int dir, T& sL, T& sR) {
+  const T rhoL = L.rho, rhoR = R.rho;
+  const T sqRhoL = sqrt(rhoL);
+  const T sqRhoR = sqrt(rhoR);
+  const T sqRho = sqRhoL + sqRhoR;
+  const T uL = L.m[dir] / rhoL;
+  const T uR = R.m[dir] / rhoR;
+  const T wL = sqRhoL / sqRho;
+  const T wR = sqRhoR / sqRho;
+  const T roeU = uL * wL + uR * wR;
+  const T hL = (L.E + L.p) / rhoL;
+  const T hR = (R.E + R.p) / rhoR;
+  const T roeH = hL * wL + hR * wR;
+  const T roeA2 = (eq.gamma - T(1)) * (roeH - T(0.5) * roeU * roeU);
+  const T roeA = sqrt(roeA2);
+  sL = PMinT(uL - L.c, roeU - roeA);
+  sR = PMaxT(roeU + roeA, uR + R.c);
+}
+
+// Masked MUSCL-Hancock predictor of one cell (both face states); the slope
+// is zeroed unless the three cells of its window have volume.
+template <class T>
+__device__ __forceinline__ void PredictMasked(const GasT<T>& eq, C2T<T>& recL, C2T<T>& recR,
+                                              const T* q0, const T* q1, const T* q2, bool smask,
+                                              int limiter, T lambda_half, int dir) {
+  T uL[4], uR[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const T sL = smask ? q1[k] - q0[k] : T(0);
+    const T sR = smask ? q2[k] - q1[k] : T(0);
+    T slope;
+    if (limiter == exact::kVanLeer) {
+      const T c = T(2) * sL * sR;
+      slope = (c > T(0)) ? c / (sL + sR) : T(0);
+    } else if (limiter == exact::kMinMod) {
+      slope = (sR > 0) ? PMaxT(T(0), PMinT(sL, sR)) : PMinT(T(0), PMaxT(sL, sR));
+    } else {
+      slope = T(0);
+    }
+    uL[k] = q1[k] - T(0.5) * slope;
+    uR[k] = q1[k] + T(0.5) * slope;
+  }
+  C2T<T> qL, qR;
+  CompleteMasked(eq, qL, uL, true);
+  CompleteMasked(eq, qR, uR, true);
+  T fL[4], fR[4];
+  FluxMasked(fL, qL, dir);
+  FluxMasked(fR, qR, dir);
+  T a[4], b[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const T df = fL[k] - fR[k];
+    b[k] = uR[k] + lambda_half * df;
+    a[k] = uL[k] + lambda_half * df;
+  }
+  CompleteMasked(eq, recR, b, true);
+  CompleteMasked(eq, recL, a, true);
+}
+
+// Masked HLL flux of a face with beta > 0 (HllMethod.hpp:295-335).
+template <class T>
+__device__ __forceinline__ void HllMasked(const GasT<T>& eq, T* nf, const C2T<T>& L,
+                                          const C2T<T>& R, int dir) {
+  T s0, s1;
+  EinfeldtMasked(eq, L, R, dir, s0, s1);
+  T fL[4], fR[4];
+  FluxMasked(fL, L, dir);
+  FluxMasked(fR, R, dir);
+  const T qL[4] = {L.rho, L.m[0], L.m[1], L.E};
+  const T qR[4] = {R.rho, R.m[0], R.m[1], R.E};
+  const T sL = PMinT(s0, T(0));
+  const T sR = PMaxT(s1, T(0));
+  const T sLsR = sL * sR;
+  const T ds = sR - sL;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) nf[k] = (sR * fL[k] - sL * fR[k] + sLsR * (qR[k] - qL[k])) / ds;
+}
+
+// HllBase::SolveRiemannProblem (scalar, HllMethod.hpp:161-184), direction x.
+template <class T>
+__device__ __forceinline__ void HllRiemannState(const GasT<T>& eq, C2T<T>& sol,
+                                                const C2T<T>& L, const C2T<T>& R) {
+  T sL, sR;
+  EinfeldtT(eq, L, R, 0, sL, sR);
+  T fL[4], fR[4];
+  FluxT(fL, L, 0);
+  FluxT(fR, R, 0);
+  const T qL[4] = {L.rho, L.m[0], L.m[1], L.E};
+  const T qR[4] = {R.rho, R.m[0], R.m[1], R.E};
+  const T ds = sL != sR ? sR - sL : T(1);
+  if (T(0) < sL) {
+    sol = L;
+  } else if (sR < T(0)) {
+    sol = R;
+  } else {
+    T u[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) u[k] = (sR * qR[k] - sL * qL[k] + fL[k] - fR[k]) / ds;
+    CompleteT(eq, sol, u);
+  }
+}
+
+// Rotation taking unit vector a to b applied to the momentum (MakeRotation).
+template <class T>
+__device__ __forceinline__ void RotateMomentum(C2T<T>& q, T a0, T a1, T b0, T b1) {
+  if (a0 == -b0 && a1 == -b1) {
+    q.m[0] = -q.m[0];
+    q.m[1] = -q.m[1];
+    return;
+  }
+  const T s = a0 * b1 - a1 * b0;
+  const T c = a0 * b0 + a1 * b1;
+  const T m0 = q.m[0], m1 = q.m[1];
+  q.m[0] = c * m0 + (-s) * m1;
+  q.m[1] = s * m0 + c * m1;
+}
+
+// Wall state: HLL solution of (reflected | state) in the frame of the
+// boundary normal, rotated back (KbnStabilisation.hpp:188-210, 229-238).
+template <class T>
+__device__ __forceinline__ C2T<T> WallSolution(const GasT<T>& eq, const C2T<T>& state, T n0,
+                                               T n1) {
+  C2T<T> rot = state;
+  RotateMomentum(rot, n0, n1, T(1), T(0));
+  C2T<T> refl = rot;
+  const T dot = rot.m[0] * T(1) + rot.m[1] * T(0);
+  const T p0 = dot * T(1), p1 = dot * T(0);
+  refl.m[0] = rot.m[0] - 2 * p0;
+  refl.m[1] = rot.m[1] - 2 * p1;
+  C2T<T> sol;
+  HllRiemannState(eq, sol, refl, rot);
+  RotateMomentum(sol, T(1), T(0), n0, n1);
+  return sol;
+}
+
+__device__ __forceinline__ double Clamp01(double x) {
+  x = x < 0.0 ? 0.0 : x;
+  return 1.0 < x ? 1.0 : x;
+}
+
+__device__ __forceinline__ void LoadCons(const CcStateArgs& a, int i, int j, double* u) {
+  const int si = BcIndex(i, a.g.nx, a.bc[0]);
+  const int sj = BcIndex(j, a.g.ny, a.bc[1]);
+  const int64_t cs = int64_t(a.g.nx) * a.g.ny;
+  const int64_t off = int64_t(sj) * a.g.nx + si;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) u[k] = __ldg(a.in + k * cs + off);
+}
+
+template <class T> __device__ __forceinline__ void Narrow(T* t, const double* u) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) t[k] = T(u[k]);
+}
+
+// KbnCutCellMethod::PreAdvanceHierarchy for the cut cells of [-1, n+1)^2.
+template <class T> __global__ void ReferenceStatesKernel(CcStateArgs a) {
+  const int w = a.g.nx + 2, h = a.g.ny + 2;
+  const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (id >= int64_t(w) * h) return;
+  const int i = static_cast<int>(id % w) - 1, j = static_cast<int>(id / w) - 1;
+  const int64_t c = a.g.CellIndex(i, j);
+  if (!a.g.cut[c]) return;
+  const GasT<T> eq = MakeGasT<T>(a.gamma);
+  double ud[4];
+  LoadCons(a, i, j, ud);
+  T u[4];
+  Narrow(u, ud);
+  C2T<T> q;
+  CompleteMasked(eq, q, u, a.g.alpha[c] > 0.0);
+  const int64_t plane = int64_t(a.g.NX()) * a.g.NY();
+  C2T<T> r;
+  if (q.rho > T(0)) {
+    r = WallSolution(eq, q, T(a.g.normal[c]), T(a.g.normal[plane + c]));
+  } else {
+    r = C2T<T>{T(0), {T(0), T(0)}, T(0), T(0), T(0)};
+  }
+  a.refs[c] = r.rho;
+  a.refs[plane + c] = r.m[0];
+  a.refs[2 * plane + c] = r.m[1];
+  a.refs[3 * plane + c] = r.E;
+  a.refs[4 * plane + c] = r.p;
+  a.refs[5 * plane + c] = r.c;
+}
+
+// The fused KBN sweep: one thread marches one grid line (segment) along
+// `dir`, evaluating per cell the masked predictor and the boundary flux, per
+// face the masked HLLE flux, the h-box stabilised fluxes and the CFL speed,
+// and per cell the cut-cell update.
+struct FaceData {
+  double f[4], fs[4], fsL[4], fsR[4];
+  double beta, us, sL, sR;
+};
+
+template <class T> __global__ void __launch_bounds__(128) KbnSweepKernel(CcSweepArgs a) {
+  const CcGeom& g = a.s.g;
+  const int dir = a.dir;
+  const int nd = dir == 0 ? g.nx : g.ny;
+  const int nt = dir == 0 ? g.ny : g.nx;
+  const int64_t t64 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int j0 = blockIdx.y * a.seg_len;
+  const int j1 = min(nd, j0 + a.seg_len);
+  const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
+  if (a.ctrl) {
+    if (a.ctrl->abort || a.ctrl->done) return;
+    if (a.prev_check >= 0) {
+      const double smax = BitsToDouble(a.ctrl->smax_check[a.prev_check]);
+      if (a.prev_dx / smax < split_dt) return;
+    }
+  }
+  T smax = T(0);
+  int status = 0;
+  if (t64 < nt) {
+    const int t = static_cast<int>(t64);
+    const GasT<T> eq = MakeGasT<T>(a.s.gamma);
+    const double dx = a.dx;
+    const T lambda_half = T(0.5 * split_dt / dx);
+    const double dt_dx = split_dt / dx;
+    const int64_t plane = int64_t(g.NX()) * g.NY();
+    const int64_t cs = int64_t(g.nx) * g.ny;
+    auto cell_ij = [&](int c, int& i, int& j) {
+      if (dir == 0) {
+        i = c;
+        j = t;
+      } else {
+        i = t;
+        j = c;
+      }
+    };
+    // masked complete state (alpha > 0 and rho > 0) of cell c
+    auto load_cell = [&](int c, T* u, double& alpha) {
+      int i, j;
+      cell_ij(c, i, j);
+      double vd[4];
+      LoadCons(a.s, i, j, vd);
+      T v[4];
+      Narrow(v, vd);
+      alpha = g.alpha[g.CellIndex(i, j)];
+      C2T<T> q;
+      CompleteMasked(eq, q, v, alpha > 0.0);
+      u[0] = q.rho;
+      u[1] = q.m[0];
+      u[2] = q.m[1];
+      u[3] = q.E;
+    };
+    // boundary flux of cell c (0 unless it is a cut cell)
+    auto boundary_flux = [&](int c, const T* u, double* fb) {
+      int i, j;
+      cell_ij(c, i, j);
+      const int64_t ci = g.CellIndex(i, j);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) fb[k] = 0.0;
+      if (!g.cut[ci]) return;
+      C2T<T> ref;
+      ref.rho = T(a.s.refs[ci]);
+      ref.m[0] = T(a.s.refs[plane + ci]);
+      ref.m[1] = T(a.s.refs[2 * plane + ci]);
+      ref.E = T(a.s.refs[3 * plane + ci]);
+      ref.p = T(a.s.refs[4 * plane + ci]);
+      ref.c = T(a.s.refs[5 * plane + ci]);
+      C2T<T> q;
+      CompleteMasked(eq, q, u, g.alpha[ci] > 0.0);
+      T f[4];
+      FluxT(f, ref, dir);
+      const C2T<T> sol = WallSolution(eq, q, T(g.normal[ci]), T(g.normal[plane + ci]));
+      f[1 + dir] += sol.p - ref.p;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) fb[k] = double(f[k]);
+    };
+    auto center_of = [&](int c) {
+      int i, j;
+      cell_ij(c, i, j);
+      return g.center[int64_t(dir) * plane + g.CellIndex(i, j)];
+    };
+    T um[4], uc[4], up[4];
+    double am, ac, ap;
+    load_cell(j0 - 2, um, am);
+    load_cell(j0 - 1, uc, ac);
+    C2T<T> recR_prev;
+    double fb_prev[4];
+    double xb_prev = 0.0;
+    C2T<T> q_prev;
+    FaceData F_prev;
+    for (int j = j0 - 1; j <= j1; ++j) {
+      load_cell(j + 1, up, ap);
+      const bool smask = am > 0.0 && ac > 0.0 && ap > 0.0;
+      C2T<T> recL, recR;
+      PredictMasked(eq, recL, recR, um, uc, up, smask, a.limiter, lambda_half, dir);
+      double fb[4];
+      boundary_flux(j, uc, fb);
+      const double xb = center_of(j);
+      C2T<T> q;
+      CompleteMasked(eq, q, uc, true);  // uc is already masked by alpha
+      if (j >= j0) {
+        FaceData F;
+        const int64_t fi = g.FaceIndex(dir, j, t);
+        F.beta = g.beta[dir][fi];
+        F.us = g.us[dir][fi];
+        F.sL = g.sL[dir][fi];
+        F.sR = g.sR[dir][fi];
+        const double us_rel = g.us_rel[dir][fi];
+        const double sL_rel = g.sL_rel[dir][fi];
+        const double sR_rel = g.sR_rel[dir][fi];
+        if (F.beta > 0.0) {
+          T f[4];
+          HllMasked(eq, f, recR_prev, recL, dir);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) F.f[k] = double(f[k]);
+          T s0, s1;
+          EinfeldtMasked(eq, q_prev, q, dir, s0, s1);
+          const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
+          smax = mx > smax ? mx : smax;
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) F.f[k] = 0.0;
+        }
+        const double dL = Clamp01(0.5 - xb_prev);
+        const double dR = Clamp01(0.5 + xb);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const double fk = F.f[k];
+          const double sLk = dL * fk + (1.0 - dL) * fb_prev[k];
+          const double sRk = dR * fk + (1.0 - dR) * fb[k];
+          F.fsL[k] = sLk;
+          F.fsR[k] = sRk;
+          F.fs[k] = us_rel * fk + sL_rel * sLk + sR_rel * sRk;
+        }
+        if (j > j0) {
+          // cut-cell update of cell j-1 (faces j-1 and j)
+          const int c = j - 1;
+          int i, jj;
+          cell_ij(c, i, jj);
+          const int64_t out = int64_t(jj) * g.nx + i;
+          const double alpha = am;  // alpha of cell j-1
+          const double betaL = F_prev.beta, betaR = F.beta;
+          const double center = xb_prev;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            double next;
+            if (alpha == 0.0) {
+              next = 0.0;
+            } else {
+              const double prev = __ldg(a.s.in + k * cs + out);
+              const double fLs = F_prev.fs[k], fRs = F.fs[k];
+              const double fLu = F_prev.f[k], fRu = F.f[k];
+              if (betaL == betaR) {
+                next = prev + dt_dx * (fLs - fRs);
+              } else if (betaL > betaR) {
+                const double bus = F_prev.us / alpha;
+                const double bsL = F_prev.sL / alpha;
+                const double dist = 0.5 + center;
+                const double dBeta = Clamp01((F_prev.sR * dist) / alpha);
+                const double dF_us = fLu - fRs;
+                const double dF_sL = F_prev.fsL[k] - fRs;
+                const double dB = fLu - fb_prev[k];
+                next = prev + dt_dx * bus * dF_us + dt_dx * bsL * dF_sL + dt_dx * dBeta * dB;
+              } else {
+                const double bus = F.us / alpha;
+                const double bsR = F.sR / alpha;
+                const double dist = 0.5 - center;
+                const double dBeta = Clamp01((F.sL * dist) / alpha);
+                const double dF_us = fLs - fRu;
+                const double dF_sR = fLs - F.fsR[k];
+                const double dB = fb_prev[k] - fRu;
+                next = prev + dt_dx * bus * dF_us + dt_dx * bsR * dF_sR + dt_dx * dBeta * dB;
+              }
+            }
+            a.out[k * cs + out] = next;
+          }
+          if (alpha > 0.0 && __double_as_longlong(a.out[out]) <= 0)
+            status |= kStatusNonPositiveDensity;
+        }
+        F_prev = F;
+      }
+      recR_prev = recR;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) fb_prev[k] = fb[k];
+      xb_prev = xb;
+      q_prev = q;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        um[k] = uc[k];
+        uc[k] = up[k];
+      }
+      am = ac;
+      ac = ap;
+    }
+  }
+  const double m = WarpMax(static_cast<double>(smax));
+  if ((threadIdx.x & 31) == 0 && a.smax_out && m > 0.0) AtomicMaxPositive(a.smax_out, m);
+  if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
+}
+
+// Masked stable dt over both directions: faces 0..n with beta > 0
+// (KbnStabilisation.hpp:275-345).
+template <class T>
+__global__ void KbnStableDtKernel(CcStateArgs a, unsigned long long* smax_out, Control* ctrl) {
+  if (ctrl && (ctrl->abort || ctrl->done)) return;
+  const CcGeom& g = a.g;
+  const int w = g.nx + 1, h = g.ny + 1;
+  const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  T sm[2] = {T(0), T(0)};
+  if (id < int64_t(w) * h) {
+    const int i = static_cast<int>(id % w), j = static_cast<int>(id / w);
+    const GasT<T> eq = MakeGasT<T>(a.gamma);
+    for (int d = 0; d < 2; ++d) {
+      const int f = d == 0 ? i : j;
+      const int t = d == 0 ? j : i;
+      const int nt = d == 0 ? g.ny : g.nx;
+      if (t >= nt) continue;
+      if (!(g.beta[d][g.FaceIndex(d, f, t)] > 0.0)) continue;
+      const int il = d == 0 ? f - 1 : t, jl = d == 0 ? t : f - 1;
+      const int ir = d == 0 ? f : t, jr = d == 0 ? t : f;
+      double uld[4], urd[4];
+      LoadCons(a, il, jl, uld);
+      LoadCons(a, ir, jr, urd);
+      T ul[4], ur[4];
+      Narrow(ul, uld);
+      Narrow(ur, urd);
+      C2T<T> L, R;
+      CompleteMasked(eq, L, ul, g.alpha[g.CellIndex(il, jl)] > 0.0);
+      CompleteMasked(eq, R, ur, g.alpha[g.CellIndex(ir, jr)] > 0.0);
+      T s0, s1;
+      EinfeldtMasked(eq, L, R, d, s0, s1);
+      const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
+      sm[d] = mx > sm[d] ? mx : sm[d];
+    }
+  }
+  for (int d = 0; d < 2; ++d) {
+    const double m = WarpMax(static_cast<double>(sm[d]));
+    if ((threadIdx.x & 31) == 0 && m > 0.0) AtomicMaxPositive(smax_out + d, m);
+  }
+}
+
+template <class T> cudaError_t LaunchKbnStates(const CcStateArgs& a, cudaStream_t s) {
+  const int64_t n = int64_t(a.g.nx + 2) * (a.g.ny + 2);
+  const int block = 128;
+  ReferenceStatesKernel<T><<<unsigned((n + block - 1) / block), block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <class T> cudaError_t LaunchKbnSweep(const CcSweepArgs& a, cudaStream_t s) {
+  const int nd = a.dir == 0 ? a.s.g.nx : a.s.g.ny;
+  const int nt = a.dir == 0 ? a.s.g.ny : a.s.g.nx;
+  const int block = 128;
+  const int seg = a.seg_len > 0 ? a.seg_len : nd;
+  CcSweepArgs b = a;
+  b.seg_len = seg;
+  dim3 grid(unsigned((nt + block - 1) / block), unsigned((nd + seg - 1) / seg));
+  KbnSweepKernel<T><<<grid, block, 0, s>>>(b);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t LaunchKbnStableDt(const CcStateArgs& a, unsigned long long* smax_out, Control* ctrl,
+                              cudaStream_t s) {
+  const int64_t n = int64_t(a.g.nx + 1) * (a.g.ny + 1);
+  const int block = 128;
+  KbnStableDtKernel<T><<<unsigned((n + block - 1) / block), block, 0, s>>>(a, smax_out, ctrl);
+  return cudaGetLastError();
+}
+
+}  // namespace cc
+}  // namespace fvs

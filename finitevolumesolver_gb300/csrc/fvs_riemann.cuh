@@ -98,14 +98,14 @@ __device__ __forceinline__ double DfSide(const SideFn& s, double d_exponent, dou
   return pow(q / s.p, d_exponent) / (s.rho * s.a);
 }
 
-// NewtonIteration from x0 (NewtonIteration.hpp:28-52), bounded.
-__device__ __forceinline__ void Newton(const SideFn& L, const SideFn& R, double du, double gm1,
-                                       double exponent, double d_exponent, double x0,
-                                       double tol, int max_iterations, double& x_out,
-                                       int& iterations, int& converged) {
-  // f(h) = f_right(h) + f_left(h) + du (ExactRiemannSolver.hpp:89)
+// NewtonIteration from x0 with f(x0) = fx0 already evaluated
+// (NewtonIteration.hpp:28-52), bounded.
+__device__ __forceinline__ void NewtonFrom(const SideFn& L, const SideFn& R, double du,
+                                           double gm1, double exponent, double d_exponent,
+                                           double x0, double fx0, double tol, int max_iterations,
+                                           double& x_out, int& iterations, int& converged) {
   double x = x0;
-  double fx = FSide(R, gm1, exponent, x) + FSide(L, gm1, exponent, x) + du;
+  double fx = fx0;
   int counter = 0;
   double err = fabs(fx);
   while (err > tol && counter < max_iterations) {
@@ -120,6 +120,17 @@ __device__ __forceinline__ void Newton(const SideFn& L, const SideFn& R, double 
   x_out = x;
   iterations = counter;
   converged = !(err > tol);
+}
+
+// NewtonIteration from x0 (NewtonIteration.hpp:28-52), bounded.
+__device__ __forceinline__ void Newton(const SideFn& L, const SideFn& R, double du, double gm1,
+                                       double exponent, double d_exponent, double x0,
+                                       double tol, int max_iterations, double& x_out,
+                                       int& iterations, int& converged) {
+  // f(h) = f_right(h) + f_left(h) + du (ExactRiemannSolver.hpp:89)
+  const double fx0 = FSide(R, gm1, exponent, x0) + FSide(L, gm1, exponent, x0) + du;
+  NewtonFrom(L, R, du, gm1, exponent, d_exponent, x0, fx0, tol, max_iterations, x_out,
+             iterations, converged);
 }
 
 template <int D>
@@ -161,10 +172,21 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
     // the wave strength and Newton needs zero or one step from it, keep
     // their start and never pay for the network.
     constexpr double kLearnedGate = 0.05;
-    const bool screened =
-        opt.guess == kGuessMlp &&
-        !(fabs(FSide(R, gm1, exponent, pv) + FSide(L, gm1, exponent, pv) + du) >
-          kLearnedGate * (L.a + R.a));
+    double f_pv = 0.0;
+    bool screened = false;
+    if (opt.guess == kGuessMlp) {
+      f_pv = FSide(R, gm1, exponent, pv) + FSide(L, gm1, exponent, pv) + du;
+      screened = !(fabs(f_pv) > kLearnedGate * (L.a + R.a));
+      if (screened || !opt.mlp) {
+        // PVRS/TR start, reusing the residual just evaluated
+        NewtonFrom(L, R, du, gm1, exponent, d_exponent, pv, f_pv, opt.tol, opt.max_iterations,
+                   st.p, st.iterations, st.converged);
+        const double fL = FSide(L, gm1, exponent, st.p);
+        const double fR = FSide(R, gm1, exponent, st.p);
+        st.u = 0.5 * (uL + uR) + 0.5 * (fR - fL);
+        return st;
+      }
+    }
     if (opt.guess == kGuessMlp && opt.mlp && !screened) {
       const double learned = mlp::GuessStarPressure(opt.mlp, L.rho, uL, L.p, L.a, R.rho, uR,
                                                     R.p, R.a);
@@ -185,8 +207,8 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
         st.fallback = 1;
         double x2;
         int it2, ok2;
-        Newton(L, R, du, gm1, exponent, d_exponent, pv, opt.tol, opt.max_iterations, x2, it2,
-               ok2);
+        NewtonFrom(L, R, du, gm1, exponent, d_exponent, pv, f_pv, opt.tol, opt.max_iterations,
+                   x2, it2, ok2);
         x = x2;
         it += it2;
         ok = ok2;

@@ -254,8 +254,10 @@ int fvs_solver_stream(fvs_solver* s, void** stream);
 /* Ghost layers of the cut-cell geometry arrays. */
 int fvs_cutcell_ghost_layers(void);
 /* Embeds the union of `ncircles` (1..16) circles, host array of (cx, cy, r)
- * triples, the body being their inside, into a rank-2 MUSCL-HLLE exact-FP64
- * solver whose cell (0, 0) has its lower-left corner at (x0, y0).  The FP64
+ * triples, the body being their inside, into a rank-2 MUSCL-HLLE solver
+ * (exact FP64, fast FP64, or mixed: FP32 reconstruction, fluxes, wall states
+ * and CFL speeds with FP64 state, fractions and update) whose cell (0, 0)
+ * has its lower-left corner at (x0, y0).  The FP64
  * geometry (volume / face fractions, normals, centroids, shielded fractions)
  * is computed on the device; from then on every sweep is the
  * KbnCutCellMethod update (include/fub/cutcell_method/KbnStabilisation.hpp:

@@ -72,3 +72,40 @@ def test_shock_over_circles_run_bit_exact(fvs, orc):
     np.testing.assert_array_equal(dts, ref_dts)
     np.testing.assert_array_equal(s.download(), out)
     s.close()
+
+
+def _totals(a):
+    return a.reshape(4, -1).sum(axis=1)
+
+
+@pytest.mark.parametrize("prec", ["fp64_fast", "mixed"])
+def test_flavours_track_exact_and_conserve(fvs, orc, prec):
+    """Fast FP64 stays within 1e-12 of the exact flavour; mixed within the
+    FP32 reconstruction error.  Periodic in x and y with the body inside the
+    domain: the volume-weighted mass and energy change only through the FP64
+    round-off of the cut-cell update (the wall flux carries no mass or
+    energy); 1e-11 relative over 10 steps of 16k cells."""
+    n = 128
+    circles = np.array([[0.5, 0.5, 0.15], [0.3, 0.7, 0.08]])
+    cons = workloads.random_state((n, n), 2, seed=9).reshape(4, 1, n, n)
+    ex = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "periodic")
+    ex.set_embedded_circles(circles)
+    geo = ex.cutcell_geometry()
+    G = geo["ghost"]
+    alpha = geo["alpha"][G:-G, G:-G]
+    cons = cons * (alpha > 0)[None, None]
+    ex.upload(cons)
+    st_e, dts_e = ex.run(cfl=0.5, t_end=10.0, max_steps=10, log_len=10)
+    s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "periodic", method=fvs.make_method(precision=prec))
+    s.set_embedded_circles(circles)
+    s.upload(cons)
+    st, dts = s.run(cfl=0.5, t_end=10.0, max_steps=10, log_len=10)
+    out, ref = s.download(), ex.download()
+    w = alpha[None, None]
+    l1 = float(np.abs(out[0] - ref[0]).mean())
+    assert l1 < (1e-12 if prec == "fp64_fast" else 2e-6), l1
+    t0 = (cons * w).reshape(4, -1).sum(axis=1)
+    t1 = (out * w).reshape(4, -1).sum(axis=1)
+    scale = (np.abs(cons) * w).reshape(4, -1).sum(axis=1)
+    drift = np.abs(t1 - t0) / scale
+    assert drift[0] < 1e-11 and drift[3] < 1e-11, drift
