@@ -432,7 +432,7 @@ def run_reference(args):
 def run_ours(args):
     import torch
     import finitevolumesolver_gb300 as fvs
-    from finitevolumesolver_gb300 import build, workloads
+    from finitevolumesolver_gb300 import build, partition, workloads
 
     rank, world, local = dist_env()
     if world > 1:
@@ -486,10 +486,7 @@ def run_ours(args):
         barrier()
         clk = clocks.stop() if clocks else None
         ms = ev0.elapsed_time(ev1)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = partition.slowest(ms)  # max over ranks (identity on one rank)
         assert st.steps == args.steps, "run stopped early"
         final = solver.download()
         # dominant kernel: the fused sweep; time single launches per direction
