@@ -140,6 +140,20 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
+def profile_value(name: str, key: str):
+    """A 'key: value' figure recorded in a profiles/ summary, or None."""
+    p = ROOT / "profiles" / name
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.strip().startswith(key + ":"):
+            try:
+                return float(ln.split(":", 1)[1])
+            except ValueError:
+                return None
+    return None
+
+
 def profile_traffic(name: str, cells: int):
     """DRAM bytes per sweep launch from an ncu capture of a smaller case:
     profiles/<name> records 'traffic_bytes_per_cell_update: <B>' (mean of the
@@ -596,7 +610,11 @@ def run_ours(args):
                          "traffic": traffic,
                          "kernel": "SweepMarchKernel (fused flux + update + CFL)",
                          "algorithmic_bytes_per_launch": algo_bytes,
-                         "launch_ms": main["sweep_s"] * 1e3, "peak_source": peaks["source"]},
+                         "launch_ms": main["sweep_s"] * 1e3, "peak_source": peaks["source"],
+                         "fp64_pipe_active_frac": profile_value(
+                             f"sweep_{args.precision}_160.md", "fp64_pipe_active_frac"),
+                         "note": "the FP64 flavours are bound by the FP64 pipe (2 FP64 "
+                                 "operations per SM and clock on GB300), not by HBM"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": state_bytes / args.steps,

@@ -252,6 +252,14 @@ class Solver:
         _capi.check(lib().fvs_solver_autotune(self._h, segs))
         return list(segs)[: self.rank]
 
+    def tuning(self):
+        """(segment cells, occupancy variant) per direction after autotune()."""
+        import numpy as np
+        seg = np.zeros(3, dtype=np.int32)
+        occ = np.zeros(3, dtype=np.int32)
+        _capi.check(lib().fvs_solver_tuning(self._h, seg.ctypes.data, occ.ctypes.data))
+        return seg[: self.rank].tolist(), occ[: self.rank].tolist()
+
     def set_cycle(self, cycle: int) -> None:
         _capi.check(lib().fvs_solver_set_cycle(self._h, int(cycle)))
 

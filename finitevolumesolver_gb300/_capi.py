@@ -93,6 +93,8 @@ def load() -> C.CDLL:
                                                 C.c_int, C.c_int, _DP, _VP]
     L.fvs_update_conservatively.argtypes = [_VP, Box, _VP, Box, _VP, Box, C.c_int, C.c_double,
                                             C.c_double, C.c_int, _VP]
+    L.fvs_update_conservatively_region.argtypes = [_VP, Box, Box, _VP, Box, _VP, Box, C.c_int,
+                                                   C.c_double, C.c_double, C.c_int, _VP]
     L.fvs_complete_from_cons.argtypes = [C.c_int, C.c_double, _VP, Box, _VP, Box, Box, _VP]
     L.fvs_solver_create.argtypes = [P(GridDesc), P(Method), P(_VP)]
     L.fvs_solver_destroy.argtypes = [_VP]
@@ -101,6 +103,7 @@ def load() -> C.CDLL:
     L.fvs_solver_state_device.argtypes = [_VP, P(_VP)]
     L.fvs_solver_set_tiling.argtypes = [_VP, C.c_int]
     L.fvs_solver_autotune.argtypes = [_VP, P(C.c_int)]
+    L.fvs_solver_tuning.argtypes = [_VP, _VP, _VP]
     L.fvs_solver_stable_dt.argtypes = [_VP, C.c_int, _DP]
     L.fvs_solver_sweep.argtypes = [_VP, C.c_int, C.c_double, _DP]
     L.fvs_solver_step.argtypes = [_VP, C.c_double, C.c_int]

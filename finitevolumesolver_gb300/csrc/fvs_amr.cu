@@ -63,12 +63,16 @@ struct LevelHost {
   int32_t slot_begin = 0, slot_end = 0;
   int block[2] = {128, 128};
   int grid[2] = {0, 0};
+  int occ[2] = {0, 0};  // occupancy variant of the mixed sweep
   std::string hist;
   int32_t Owner(int i, int j) const { return owner[size_t(int64_t(j) * n[0] + i)]; }
 };
 
 std::mutex g_tune_mutex;
-std::map<std::string, std::pair<int, int>> g_tuned;  // key -> (block, grid)
+struct Tuned {
+  int block, grid, occ;
+};
+std::map<std::string, Tuned> g_tuned;  // key -> launch shape
 
 }  // namespace
 
@@ -416,7 +420,7 @@ int Build(fvs_amr* a) {
 
 cudaError_t LaunchSweep(fvs_amr* a, int l, int d, const double* in, double* out,
                         double scale, const double* dt_ptr, unsigned long long* smax, int block,
-                        int grid) {
+                        int grid, int occ) {
   const LevelHost& Lv = a->L[size_t(l)];
   PatchSweepArgs s{};
   s.in = in;
@@ -439,7 +443,7 @@ cudaError_t LaunchSweep(fvs_amr* a, int l, int d, const double* in, double* out,
   case FVS_FP64_FAST:
     return LaunchPatchSweepFast(d, s, grid, block, a->stream);
   default:
-    return LaunchPatchSweepMixed(d, s, grid, block, a->stream);
+    return LaunchPatchSweepMixed(d, s, grid, block, occ, a->stream);
   }
 }
 
@@ -501,7 +505,7 @@ cudaError_t AdvanceLevel(fvs_amr* a, int l, int parity, int sub, int& counter) {
     const int d = seq[k];
     if ((e = FillGhosts(a, l, bufs[cur])) != cudaSuccess) return e;
     if ((e = LaunchSweep(a, l, d, bufs[cur], bufs[1 - cur], 0.5 / double(1 << l), &a->ctrl->dt,
-                         &a->ctrl->smax_sweep[counter++], Lv.block[d], Lv.grid[d])) !=
+                         &a->ctrl->smax_sweep[counter++], Lv.block[d], Lv.grid[d], Lv.occ[d])) !=
         cudaSuccess)
       return e;
     cur ^= 1;
@@ -802,40 +806,45 @@ int fvs_amr_autotune(fvs_amr* a, int32_t* configs) {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_tuned.find(key);
         if (it != g_tuned.end()) {
-          Lv.block[d] = it->second.first;
-          Lv.grid[d] = it->second.second;
+          Lv.block[d] = it->second.block;
+          Lv.grid[d] = it->second.grid;
+          Lv.occ[d] = it->second.occ;
           continue;
         }
       }
       float best = 1e30f;
-      int bb = 128, bg = Lv.grid[d];
-      for (int block : {64, 128}) {
-        const int full = std::max(1, (Lv.nrows[d] + block - 1) / block);
-        for (int bps : {1, 2, 4, 8, 16, 64}) {
-          const int grid = std::min(full, a->sms * bps);
-          float sum = 0.f;
-          for (int rep = 0; rep < 3; ++rep) {
-            AMR_CUDA(cudaEventRecord(e0, a->stream));
-            AMR_CUDA(LaunchSweep(a, l, d, Lv.A, Lv.B, 0.5, a->tune_dt, &a->ctrl->smax_sweep[0],
-                                 block, grid));
-            AMR_CUDA(cudaEventRecord(e1, a->stream));
-            AMR_CUDA(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            AMR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            if (rep > 0) sum += ms;
+      Tuned bt{128, Lv.grid[d], 0};
+      const bool mixed = a->m.precision == FVS_MIXED;
+      for (int occ : {0, 5}) {
+        if (occ && !mixed) continue;
+        for (int block : {64, 128}) {
+          const int full = std::max(1, (Lv.nrows[d] + block - 1) / block);
+          for (int bps : {1, 2, 4, 8, 16, 64}) {
+            const int grid = std::min(full, a->sms * bps);
+            float sum = 0.f;
+            for (int rep = 0; rep < 3; ++rep) {
+              AMR_CUDA(cudaEventRecord(e0, a->stream));
+              AMR_CUDA(LaunchSweep(a, l, d, Lv.A, Lv.B, 0.5, a->tune_dt, &a->ctrl->smax_sweep[0],
+                                   block, grid, occ));
+              AMR_CUDA(cudaEventRecord(e1, a->stream));
+              AMR_CUDA(cudaEventSynchronize(e1));
+              float ms = 0.f;
+              AMR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+              if (rep > 0) sum += ms;
+            }
+            if (sum < best) {
+              best = sum;
+              bt = {block, grid, occ};
+            }
+            if (grid == full) break;
           }
-          if (sum < best) {
-            best = sum;
-            bb = block;
-            bg = grid;
-          }
-          if (grid == full) break;
         }
       }
-      Lv.block[d] = bb;
-      Lv.grid[d] = bg;
+      Lv.block[d] = bt.block;
+      Lv.grid[d] = bt.grid;
+      Lv.occ[d] = bt.occ;
       std::lock_guard<std::mutex> lock(g_tune_mutex);
-      g_tuned[key] = {bb, bg};
+      g_tuned[key] = bt;
     }
   }
   cudaEventDestroy(e0);

@@ -116,8 +116,9 @@ cudaError_t LaunchPatchSweepExact(int dir, const PatchSweepArgs& a, int grid, in
                                   cudaStream_t s);
 cudaError_t LaunchPatchSweepFast(int dir, const PatchSweepArgs& a, int grid, int block,
                                  cudaStream_t s);
+// occupancy: 0 (registers as needed) or 5 (compiled for 5 resident blocks)
 cudaError_t LaunchPatchSweepMixed(int dir, const PatchSweepArgs& a, int grid, int block,
-                                  cudaStream_t s);
+                                  int occupancy, cudaStream_t s);
 cudaError_t LaunchPatchMaxSpeedExact(int dir, const MaxSpeedArgs& a, int grid, int block,
                                      cudaStream_t s);
 cudaError_t LaunchPatchMaxSpeedFast(int dir, const MaxSpeedArgs& a, int grid, int block,

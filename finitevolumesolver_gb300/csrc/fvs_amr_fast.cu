@@ -13,7 +13,8 @@ cudaError_t LaunchPatchSweepFast(int dir, const PatchSweepArgs& a, int grid, int
 }
 
 cudaError_t LaunchPatchSweepMixed(int dir, const PatchSweepArgs& a, int grid, int block,
-                                  cudaStream_t s) {
+                                  int occupancy, cudaStream_t s) {
+  if (occupancy == 5) return LaunchPatchSweepT<Mixed32PolicyOcc5>(dir, a, grid, block, s);
   return LaunchPatchSweepT<Mixed32Policy>(dir, a, grid, block, s);
 }
 

@@ -22,7 +22,7 @@ namespace fvs {
 namespace amr {
 
 template <int DIR, template <int> class PT>
-__global__ void __launch_bounds__(128) PatchSweepKernel(PatchSweepArgs a) {
+__global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(PatchSweepArgs a) {
   using P = PT<2>;
   using R = typename P::Real;
   constexpr int K = kComp;

@@ -188,6 +188,7 @@ struct fvs_solver {
   int dt_log_cap = 0;
   int seg_len = 0;
   int seg_tuned[3] = {0, 0, 0};  // autotuned cells per thread segment, per direction
+  int occ_tuned[3] = {0, 0, 0};  // autotuned occupancy variant (mixed), per direction
   int64_t cycle = 0;
   double t = 0.0;
   int64_t cells = 0;
@@ -278,6 +279,7 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
   a.bc = s->g.bc[dir];
   a.limiter = s->m.limiter;
   a.seg_len = SegLen(s, dir);
+  a.occupancy = s->occ_tuned[dir];
   a.gamma = s->m.gamma;
   a.dx = s->g.dx[dir];
   a.dt_ptr = dt_ptr;
@@ -502,28 +504,37 @@ int fvs_compute_stable_dt(const fvs_method* m, int rank, const double* states_de
   return FVS_OK;
 }
 
+int fvs_update_conservatively_region(double* next_dev, fvs_box next_box, fvs_box region,
+                                     const double* prev_dev, fvs_box prev_box,
+                                     const double* fluxes_dev, fvs_box face_box, int ncomp,
+                                     double dt, double dx, int dir, void* stream) {
+  if (dir < 0 || dir > 2) return Fail(FVS_ERR_INVALID, "direction out of range");
+  if (ncomp < 1) return Fail(FVS_ERR_INVALID, "ncomp must be positive");
+  if (!ValidBox(next_box) || !ValidBox(prev_box) || !ValidBox(face_box) || !ValidBox(region))
+    return Fail(FVS_ERR_INVALID, "invalid box");
+  if (Volume(region) == 0) return FVS_OK;
+  if (!Contains(next_box, region.lo, region.hi))
+    return Fail(FVS_ERR_INVALID, "next box does not cover the region");
+  if (!Contains(prev_box, region.lo, region.hi))
+    return Fail(FVS_ERR_INVALID, "prev box does not cover the region");
+  int hi[3] = {region.hi[0], region.hi[1], region.hi[2]};
+  hi[dir] += 1;
+  if (!Contains(face_box, region.lo, hi))
+    return Fail(FVS_ERR_INVALID, "face box does not cover the faces of the region");
+  if (int r = CheckDevice()) return r;
+  FVS_CUDA(fvs::LaunchPatchUpdate(next_dev, ToDesc(next_box), ToDesc(region), prev_dev,
+                                  ToDesc(prev_box), fluxes_dev, ToDesc(face_box), ncomp, dt,
+                                  dx, dir, static_cast<cudaStream_t>(stream)));
+  return FVS_OK;
+}
+
 int fvs_update_conservatively(double* next_dev, fvs_box next_box,
                               const double* prev_dev, fvs_box prev_box,
                               const double* fluxes_dev, fvs_box face_box,
                               int ncomp, double dt, double dx, int dir,
                               void* stream) {
-  if (dir < 0 || dir > 2) return Fail(FVS_ERR_INVALID, "direction out of range");
-  if (ncomp < 1) return Fail(FVS_ERR_INVALID, "ncomp must be positive");
-  if (!ValidBox(next_box) || !ValidBox(prev_box) || !ValidBox(face_box))
-    return Fail(FVS_ERR_INVALID, "invalid box");
-  if (Volume(next_box) == 0) return FVS_OK;
-  if (!Contains(prev_box, next_box.lo, next_box.hi))
-    return Fail(FVS_ERR_INVALID, "prev box does not cover next box");
-  int hi[3] = {next_box.hi[0], next_box.hi[1], next_box.hi[2]};
-  hi[dir] += 1;
-  if (!Contains(face_box, next_box.lo, hi))
-    return Fail(FVS_ERR_INVALID, "face box does not cover the faces of next box");
-  if (int r = CheckDevice()) return r;
-  FVS_CUDA(fvs::LaunchPatchUpdate(next_dev, ToDesc(next_box), prev_dev,
-                                  ToDesc(prev_box), fluxes_dev, ToDesc(face_box),
-                                  ncomp, dt, dx, dir,
-                                  static_cast<cudaStream_t>(stream)));
-  return FVS_OK;
+  return fvs_update_conservatively_region(next_dev, next_box, next_box, prev_dev, prev_box,
+                                          fluxes_dev, face_box, ncomp, dt, dx, dir, stream);
 }
 
 int fvs_complete_from_cons(int rank, double gamma, double* complete_dev,
@@ -628,9 +639,16 @@ int fvs_solver_set_tiling(fvs_solver* s, int seg_len) {
 
 int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
-  // Candidate segment lengths per direction, timed on the current state with
-  // a small dt (output goes to a spare buffer; the state is not changed).
+  // Candidate segment lengths per direction (and, for the mixed flavour,
+  // register/occupancy variants of the same kernel), timed on the current
+  // state with a small dt (output goes to a spare buffer; the state is not
+  // changed).
   const int cands[] = {16, 32, 64, 128, 256, 512};
+  const bool mixed = s->m.precision == FVS_MIXED && s->m.flux_method <= FVS_HLLE && !s->cc;
+  const int occs_mixed[] = {0, 4, 5};
+  const int occs_plain[] = {0};
+  const int* occs = mixed ? occs_mixed : occs_plain;
+  const int nocc = mixed ? 3 : 1;
   const int saved = s->seg_len;
   cudaEvent_t e0, e1;
   FVS_CUDA(cudaEventCreate(&e0));
@@ -645,27 +663,32 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   for (int d = 0; d < s->g.rank; ++d) {
     const int nd = s->g.n[d];
     float best = 1e30f;
-    int best_seg = 0;
-    for (int c : cands) {
-      if (c > 2 * nd && c != cands[0]) break;
-      s->seg_len = c;
-      float ms_sum = 0.f;
-      for (int rep = 0; rep < 3; ++rep) {
-        FVS_CUDA(cudaEventRecord(e0, s->stream));
-        FVS_CUDA(LaunchSweep(s, s->buf[s->cur], s->buf[out], d, nullptr, 1.0, dt,
-                             s->scratch_words, nullptr, -1, 0.0));
-        FVS_CUDA(cudaEventRecord(e1, s->stream));
-        FVS_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        FVS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        if (rep > 0) ms_sum += ms;
-      }
-      if (ms_sum < best) {
-        best = ms_sum;
-        best_seg = c;
+    int best_seg = 0, best_occ = 0;
+    for (int oi = 0; oi < nocc; ++oi) {
+      s->occ_tuned[d] = occs[oi];
+      for (int c : cands) {
+        if (c > 2 * nd && c != cands[0]) break;
+        s->seg_len = c;
+        float ms_sum = 0.f;
+        for (int rep = 0; rep < 3; ++rep) {
+          FVS_CUDA(cudaEventRecord(e0, s->stream));
+          FVS_CUDA(LaunchSweep(s, s->buf[s->cur], s->buf[out], d, nullptr, 1.0, dt,
+                               s->scratch_words, nullptr, -1, 0.0));
+          FVS_CUDA(cudaEventRecord(e1, s->stream));
+          FVS_CUDA(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          FVS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+          if (rep > 0) ms_sum += ms;
+        }
+        if (ms_sum < best) {
+          best = ms_sum;
+          best_seg = c;
+          best_occ = occs[oi];
+        }
       }
     }
     s->seg_tuned[d] = best_seg;
+    s->occ_tuned[d] = best_occ;
     if (seg_out) seg_out[d] = best_seg;
   }
   s->seg_len = saved;
@@ -673,6 +696,15 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   cudaEventDestroy(e1);
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   s->graphs.clear();
+  return FVS_OK;
+}
+
+int fvs_solver_tuning(fvs_solver* s, int32_t* seg, int32_t* occupancy) {
+  if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
+  for (int d = 0; d < 3; ++d) {
+    if (seg) seg[d] = s->seg_tuned[d];
+    if (occupancy) occupancy[d] = s->occ_tuned[d];
+  }
   return FVS_OK;
 }
 

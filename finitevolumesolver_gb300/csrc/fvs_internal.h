@@ -73,7 +73,8 @@ struct SweepArgs {
   int max_iterations;
   double tolerance;
   const float* mlp;     // learned-guess weights (guess == FVS_GUESS_MLP)
-  unsigned long long* stats_out;  // [2]: Newton iterations, non-converged faces
+  unsigned long long* stats_out;  // [3]: Newton iterations, non-converged, fallbacks
+  int occupancy;        // mixed flavour: 0 (registers as needed), 4 or 5 blocks per SM
 };
 
 // Stable-dt pass over all directions (max face speed per direction).
@@ -130,7 +131,7 @@ cudaError_t LaunchPatchStableDtExact(int method, int rank, double gamma,
                                      const double* states, BoxDesc cbox,
                                      int window_rule, int dir,
                                      unsigned long long* smax, cudaStream_t s);
-cudaError_t LaunchPatchUpdate(double* next, BoxDesc nbox, const double* prev,
+cudaError_t LaunchPatchUpdate(double* next, BoxDesc nbox, BoxDesc region, const double* prev,
                               BoxDesc pbox, const double* fluxes, BoxDesc fbox,
                               int ncomp, double dt, double dx, int dir,
                               cudaStream_t s);

@@ -277,13 +277,13 @@ cudaError_t LaunchPatchStableDtExact(int method, int rank, double gamma,
 
 // HyperbolicPatchIntegrator::UpdateConservatively
 // (src/HyperbolicPatchIntegrator.cpp:88-105): next = prev + dt/dx (F_L - F_R).
-__global__ void PatchUpdateKernel(double* next, BoxDesc nbox, View prev,
+__global__ void PatchUpdateKernel(double* next, BoxDesc nbox, BoxDesc region, View prev,
                                   View flux, int ncomp, double dt_dx, int dir) {
-  const int64_t ncell = int64_t(nbox.n[0]) * nbox.n[1] * nbox.n[2];
+  const int64_t ncell = int64_t(region.n[0]) * region.n[1] * region.n[2];
   const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (id >= ncell) return;
   int c[3];
-  Unflatten(id, nbox, c);
+  Unflatten(id, region, c);
   int r[3] = {c[0], c[1], c[2]};
   r[dir] += 1;
   View nv{next, nbox};
@@ -295,18 +295,17 @@ __global__ void PatchUpdateKernel(double* next, BoxDesc nbox, View prev,
   }
 }
 
-cudaError_t LaunchPatchUpdate(double* next, BoxDesc nbox, const double* prev,
+cudaError_t LaunchPatchUpdate(double* next, BoxDesc nbox, BoxDesc region, const double* prev,
                               BoxDesc pbox, const double* fluxes, BoxDesc fbox,
                               int ncomp, double dt, double dx, int dir,
                               cudaStream_t s) {
-  const int64_t ncell = int64_t(nbox.n[0]) * nbox.n[1] * nbox.n[2];
+  const int64_t ncell = int64_t(region.n[0]) * region.n[1] * region.n[2];
   if (ncell == 0) return cudaSuccess;
+  const double dt_dx = dt / dx;
   const int block = 256;
   const unsigned grid = static_cast<unsigned>((ncell + block - 1) / block);
-  const double dt_dx = dt / dx;
-  PatchUpdateKernel<<<grid, block, 0, s>>>(next, nbox, View{prev, pbox},
-                                           View{fluxes, fbox}, ncomp, dt_dx,
-                                           dir);
+  PatchUpdateKernel<<<grid, block, 0, s>>>(next, nbox, region, View{prev, pbox},
+                                           View{fluxes, fbox}, ncomp, dt_dx, dir);
   return cudaGetLastError();
 }
 

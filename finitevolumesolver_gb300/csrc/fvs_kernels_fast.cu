@@ -25,14 +25,25 @@ cudaError_t LaunchSweepFast(const SweepArgs& a, cudaStream_t s) {
   }
 }
 
-cudaError_t LaunchSweepMixed(const SweepArgs& a, cudaStream_t s) {
+template <template <int> class PT> cudaError_t LaunchSweepMixedT(const SweepArgs& a, cudaStream_t s) {
   switch (a.rank) {
   case 1:
-    return LaunchSweepT<1, Mixed32Policy>(a, s);
+    return LaunchSweepT<1, PT>(a, s);
   case 2:
-    return LaunchSweepT<2, Mixed32Policy>(a, s);
+    return LaunchSweepT<2, PT>(a, s);
   default:
-    return LaunchSweepT<3, Mixed32Policy>(a, s);
+    return LaunchSweepT<3, PT>(a, s);
+  }
+}
+
+cudaError_t LaunchSweepMixed(const SweepArgs& a, cudaStream_t s) {
+  switch (a.occupancy) {
+  case 4:
+    return LaunchSweepMixedT<Mixed32PolicyOcc4>(a, s);
+  case 5:
+    return LaunchSweepMixedT<Mixed32PolicyOcc5>(a, s);
+  default:
+    return LaunchSweepMixedT<Mixed32Policy>(a, s);
   }
 }
 

@@ -37,6 +37,7 @@ __device__ __forceinline__ GodunovGas MakeGodunovGas(double gamma, int guess, in
 template <int D, bool kMuscl> struct GodunovPolicyT {
   using Real = double;
   static constexpr bool kWarpX = false;
+  static constexpr int kMinBlocks = 1;
   using Gas = GodunovGas;
   using Rec = exact::Complete<D>;
   using Wave = exact::Complete<D>;

@@ -13,6 +13,7 @@ namespace fvs {
 template <int D> struct ExactPolicy {
   using Real = double;
   static constexpr bool kWarpX = false;
+  static constexpr int kMinBlocks = 1;
   using Gas = exact::Gas;
   using Wave = exact::CellWave;
   using Rec = exact::Complete<D>;

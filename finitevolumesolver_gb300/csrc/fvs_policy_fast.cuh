@@ -55,6 +55,7 @@ template <int D, typename T> struct FastBase {
   using Real = T;
   // the mixed flavour is memory-bound: its x sweep uses lanes along x
   static constexpr bool kWarpX = sizeof(T) == 4;
+  static constexpr int kMinBlocks = 1;
   using Gas = fast::Gas<T>;
   using Rec = fast::State<D, T>;
   using Wave = fast::Wave<T>;
@@ -114,5 +115,13 @@ template <int D, typename T> struct FastBase {
 
 template <int D> struct Fast64Policy : FastBase<D, double> {};
 template <int D> struct Mixed32Policy : FastBase<D, float> {};
+// The same arithmetic compiled for more resident blocks per SM (fewer
+// registers per thread, more warps to hide latency); the autotuner picks.
+template <int D> struct Mixed32PolicyOcc4 : FastBase<D, float> {
+  static constexpr int kMinBlocks = 4;
+};
+template <int D> struct Mixed32PolicyOcc5 : FastBase<D, float> {
+  static constexpr int kMinBlocks = 5;
+};
 
 }  // namespace fvs

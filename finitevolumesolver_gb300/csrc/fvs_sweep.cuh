@@ -100,7 +100,7 @@ struct NewtonStats {
 // between recR of the left cell and recL of the right cell (as double) and
 // the face's max signal speed of the input state (the CFL check).
 template <int D, int DIR, template <int> class PT>
-__global__ void __launch_bounds__(128) SweepMarchKernel(SweepArgs a) {
+__global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(SweepArgs a) {
   using P = PT<D>;
   constexpr int K = D + 2;
   const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
@@ -254,7 +254,7 @@ template <class R, int K> struct CellArr {
 // nx-1.  The arithmetic per face and cell is the policy's, exactly as in
 // SweepMarchKernel.
 template <int D, template <int> class PT>
-__global__ void __launch_bounds__(128) SweepXWarpKernel(SweepArgs a) {
+__global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(SweepArgs a) {
   using P = PT<D>;
   using R = typename P::Real;
   constexpr int K = D + 2;

@@ -162,6 +162,15 @@ int fvs_update_conservatively(double* next_dev, fvs_box next_box,
                               const double* fluxes_dev, fvs_box face_box,
                               int ncomp, double dt, double dx, int dir,
                               void* stream);
+/* The same update on `region`, a sub-box of next_box, with next laid out over
+ * next_box -- the reference's update through views of a larger FArrayBox
+ * (src/AMReX/TimeIntegrator.cpp:29-56 updates the cells enclosed by the flux
+ * box in place on the scratch).  next_dev may equal prev_dev (in place) when
+ * next_box == prev_box. */
+int fvs_update_conservatively_region(double* next_dev, fvs_box next_box, fvs_box region,
+                                     const double* prev_dev, fvs_box prev_box,
+                                     const double* fluxes_dev, fvs_box face_box, int ncomp,
+                                     double dt, double dx, int dir, void* stream);
 
 /* PerfectGas<D>::CompleteFromCons over `region` (src/equations/
  * PerfectGas.cpp:96-124; the scratch update of include/fub/AMReX/
@@ -222,6 +231,10 @@ int fvs_solver_set_tiling(fvs_solver* s, int seg_len);
  * the fastest per direction (used unless fvs_solver_set_tiling forces one).
  * seg_out (may be NULL) receives rank values.  Does not change the state. */
 int fvs_solver_autotune(fvs_solver* s, int* seg_out);
+/* The tuned segment lengths and (mixed flavour) occupancy variants per
+ * direction: 0 = registers as needed, 4 or 5 = compiled for that many
+ * resident 128-thread blocks per SM.  Either pointer may be NULL. */
+int fvs_solver_tuning(fvs_solver* s, int32_t* seg, int32_t* occupancy);
 /* Stable dt of the current state: dir = -1 for the minimum over all
  * directions (DimensionalSplitLevelIntegrator::ComputeStableDt). */
 int fvs_solver_stable_dt(fvs_solver* s, int dir, double* dt_out);

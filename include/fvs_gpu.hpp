@@ -71,11 +71,18 @@ struct Patch {
   void* stream;         // cudaStream_t
 };
 
-// Faces of `valid` in direction dir: valid grown by one face in dir.
-inline fvs_box FacesOf(const fvs_box& valid, int dir) {
-  fvs_box f = valid;
+// Faces of the cells `cells` in direction dir (AMReX surroundingNodes).
+inline fvs_box FacesOf(const fvs_box& cells, int dir) {
+  fvs_box f = cells;
   f.hi[dir] += 1;
   return f;
+}
+
+// Cells between the faces `faces` in direction dir (AMReX enclosedCells).
+inline fvs_box CellsOf(const fvs_box& faces, int dir) {
+  fvs_box c = faces;
+  c.hi[dir] -= 1;
+  return c;
 }
 
 template <class Adapter> class FluxMethod {
@@ -107,14 +114,15 @@ template <class Adapter> class FluxMethod {
     return Duration(dt);
   }
 
+  // Fluxes on every face of the patch's flux array (its box must leave the
+  // stencil inside the scratch box).
   template <class Context, class Direction>
   void ComputeNumericFluxes(Context& ctx, int level, Duration dt, Direction dir) {
     const int d = static_cast<int>(dir);
     const double dx = adapter_.CellSize(ctx, level, d);
     adapter_.ForEachPatch(ctx, level, d, [&](const Patch& p) {
-      Check(fvs_compute_numeric_fluxes(&m_, adapter_.Rank(), p.fluxes,
-                                       FacesOf(p.valid_box, d), p.scratch, p.scratch_box,
-                                       dt.count(), dx, d, p.stream));
+      Check(fvs_compute_numeric_fluxes(&m_, adapter_.Rank(), p.fluxes, p.flux_box, p.scratch,
+                                       p.scratch_box, dt.count(), dx, d, p.stream));
     });
   }
 
@@ -130,16 +138,18 @@ template <class Adapter> class TimeIntegrator {
  public:
   explicit TimeIntegrator(Adapter adapter = Adapter{}) : adapter_(std::move(adapter)) {}
 
-  // U' = U + dt/dx (F_i - F_{i+1}) on the valid cells, in place on the
-  // scratch's conservative components.
+  // U' = U + dt/dx (F_i - F_{i+1}) on the cells enclosed by the patch's
+  // flux box (src/AMReX/TimeIntegrator.cpp:29-56), in place on the scratch's
+  // conservative components.
   template <class Context, class Direction>
   void UpdateConservatively(Context& ctx, int level, Duration dt, Direction dir) {
     const int d = static_cast<int>(dir);
     const double dx = adapter_.CellSize(ctx, level, d);
     adapter_.ForEachPatch(ctx, level, d, [&](const Patch& p) {
-      Check(fvs_update_conservatively(p.scratch, p.scratch_box, p.scratch, p.scratch_box,
-                                      p.fluxes, p.flux_box, adapter_.Rank() + 2, dt.count(), dx,
-                                      d, p.stream));
+      Check(fvs_update_conservatively_region(p.scratch, p.scratch_box, CellsOf(p.flux_box, d),
+                                             p.scratch, p.scratch_box, p.fluxes, p.flux_box,
+                                             adapter_.Rank() + 2, dt.count(), dx, d,
+                                             p.stream));
     });
   }
 

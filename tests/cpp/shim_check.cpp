@@ -89,7 +89,11 @@ int WithGpu() {
   cudaMemcpy(out.data(), d_state, out.size() * sizeof(double), cudaMemcpyDeviceToHost);
   cudaFree(d_state);
   cudaFree(d_flux);
-  const double dt_expected = ctx.dx / (std::fabs(u) + c);
+  // Einfeldt speeds of two equal states: u -+ a_roe with the Roe sound speed
+  // of the total enthalpy, a_roe^2 = c^2 + (gamma - 1) v^2 / 2
+  // (src/equations/perfect_gas/EinfeldtSignalVelocities.hpp:25-62)
+  const double a_roe = std::sqrt(c * c + 0.5 * (gamma - 1.0) * v * v);
+  const double dt_expected = ctx.dx / (std::fabs(u) + a_roe);
   const double flux[4] = {rho * u, rho * u * u + p, rho * u * v, u * (E + p)};
   double err = std::fabs(dt - dt_expected) / dt_expected;
   for (int k = 0; k < 4; ++k)
