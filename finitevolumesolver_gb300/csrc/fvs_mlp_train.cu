@@ -17,6 +17,7 @@
 #include "fvs_mlp.cuh"
 #include "fvs_tcgen05.cuh"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 
 #include <cmath>
@@ -46,15 +47,25 @@ struct GemmArgs {
   int* error;
 };
 
+// Operands arrive by TMA: for every 8-element K slice of a chunk, one 2-D
+// tensor-map box of 16 bytes x rows lands as `rows` consecutive 16-byte rows,
+// i.e. a column of 8 x 16-byte core matrices.  In the canonical K-major
+// no-swizzle layout that is SBO = 128 bytes (next 8-row group) and LBO =
+// rows * 16 bytes (next K slice).  Rows beyond the tensor are zero-filled.
 template <int N>
-__global__ void __launch_bounds__(tc::kThreads) TcGemmKernel(GemmArgs a) {
-  extern __shared__ __align__(1024) uint8_t smem[];
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + tc::kTileM * tc::kChunkK * 2;
-  __shared__ uint64_t mbar;
+__global__ void __launch_bounds__(tc::kThreads)
+    TcGemmKernel(GemmArgs a, const __grid_constant__ CUtensorMap tmA,
+                 const __grid_constant__ CUtensorMap tmB) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full_bar, mma_bar;
   __shared__ uint32_t tmem_base;
+  const uint32_t raw = tc::SmemAddr(smem_raw);
+  uint8_t* sA = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+  uint8_t* sB = sA + tc::kTileM * tc::kChunkK * 2;
   constexpr uint32_t kCols = N < 32 ? 32 : N;
-  constexpr uint32_t kSbo = tc::kChunkK * 16;  // bytes between 8-row groups
+  constexpr uint32_t kSbo = 128;
+  constexpr uint32_t kLboA = tc::kTileM * 16;
+  constexpr uint32_t kLboB = N * 16;
   constexpr uint32_t kIdesc = tc::InstrDescBf16(tc::kTileM, N);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.x * tc::kTileM;
@@ -62,7 +73,8 @@ __global__ void __launch_bounds__(tc::kThreads) TcGemmKernel(GemmArgs a) {
   const int k_end = min(a.K, k_begin + a.k_per_cta);
   if (warp == 0) tc::TmemAlloc(&tmem_base, kCols);
   if (tid == 0) {
-    tc::MbarInit(&mbar, 1);
+    tc::MbarInit(&full_bar, 1);
+    tc::MbarInit(&mma_bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tc::FenceBeforeSync();
@@ -70,47 +82,48 @@ __global__ void __launch_bounds__(tc::kThreads) TcGemmKernel(GemmArgs a) {
   tc::FenceAfterSync();
   const uint32_t tmem = tmem_base;
   uint32_t phase = 0;
-  bool ok = true;  // CTA-uniform: decided with __syncthreads_or
+  bool ok = true;       // CTA-uniform: decided with __syncthreads_or
+  bool pending = false;  // copies or MMAs issued but not seen complete
   bool first = true;
   for (int kc = k_begin; kc < k_end && ok; kc += tc::kChunkK) {
-    const int kn = min(tc::kChunkK, k_end - kc);  // multiple of 16
-    const int cpr = kn / 8;                        // 16-byte chunks per row
-    for (int idx = tid; idx < tc::kTileM * cpr; idx += tc::kThreads) {
-      const int r = idx / cpr, c = idx % cpr;
-      const int grow = m0 + r;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if (grow < a.M)
-        v = *reinterpret_cast<const uint4*>(a.A + int64_t(grow) * a.lda + kc + c * 8);
-      *reinterpret_cast<uint4*>(sA + (r / 8) * kSbo + c * 128 + (r % 8) * 16) = v;
+    const int slices = min(tc::kChunkK, k_end - kc) / 8;
+    if (tid == 0) {
+      tc::MbarArriveExpectTx(&full_bar, uint32_t(slices) * (kLboA + kLboB));
+      for (int sl = 0; sl < slices; ++sl) {
+        tc::TmaLoad2D(sA + sl * kLboA, &tmA, kc + 8 * sl, m0, &full_bar);
+        tc::TmaLoad2D(sB + sl * kLboB, &tmB, kc + 8 * sl, 0, &full_bar);
+      }
     }
-    for (int idx = tid; idx < N * cpr; idx += tc::kThreads) {
-      const int r = idx / cpr, c = idx % cpr;
-      const uint4 v = *reinterpret_cast<const uint4*>(a.B + int64_t(r) * a.ldb + kc + c * 8);
-      *reinterpret_cast<uint4*>(sB + (r / 8) * kSbo + c * 128 + (r % 8) * 16) = v;
-    }
-    tc::FenceProxyAsync();
-    __syncthreads();
+    pending = true;
+    const bool landed = tc::MbarWait(&full_bar, phase, 1u << 22);
+    ok = !__syncthreads_or(landed ? 0 : 1);
+    if (!ok) break;
     if (tid == 0) {
       tc::FenceAfterSync();
       const uint32_t abase = tc::SmemAddr(sA), bbase = tc::SmemAddr(sB);
-      for (int ks = 0; ks < kn / 16; ++ks) {
-        const uint64_t ad = tc::SmemDesc(abase + ks * 256, 128, kSbo);
-        const uint64_t bd = tc::SmemDesc(bbase + ks * 256, 128, kSbo);
+      for (int ks = 0; ks < slices / 2; ++ks) {
+        const uint64_t ad = tc::SmemDesc(abase + 2 * ks * kLboA, kLboA, kSbo);
+        const uint64_t bd = tc::SmemDesc(bbase + 2 * ks * kLboB, kLboB, kSbo);
         tc::Mma(tmem, ad, bd, kIdesc, (first && ks == 0) ? 0u : 1u);
       }
-      tc::Commit(&mbar);
+      tc::Commit(&mma_bar);
     }
     first = false;
-    const bool done = tc::MbarWait(&mbar, phase, 1u << 22);
+    const bool done = tc::MbarWait(&mma_bar, phase, 1u << 22);
     tc::FenceAfterSync();
     ok = !__syncthreads_or(done ? 0 : 1);
-    if (ok) phase ^= 1u;
+    if (ok) {
+      phase ^= 1u;
+      pending = false;
+    }
   }
-  if (!ok) {
-    // The tensor core did not signal in time: record it, give the MMAs a
-    // second bounded chance to drain before the tensor memory is released.
+  if (!ok && pending) {
+    // A copy or the tensor core did not signal in time: record it and give
+    // the copies and MMAs of this chunk a second bounded chance to drain
+    // before shared and tensor memory are released.
     if (tid == 0 && a.error) atomicOr(a.error, 1);
-    tc::MbarWait(&mbar, phase, 1u << 22);
+    tc::MbarWait(&full_bar, phase, 1u << 22);
+    tc::MbarWait(&mma_bar, phase, 1u << 22);
   }
   if (ok && !first) {
     const int row = m0 + warp * 32 + lane;
@@ -135,18 +148,67 @@ __global__ void __launch_bounds__(tc::kThreads) TcGemmKernel(GemmArgs a) {
   if (warp == 0) tc::TmemDealloc(tmem, kCols);
 }
 
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver, found through the runtime (no
+// link-time dependency on libcuda).
+EncodeTiledFn EncodeTiled() {
+  static EncodeTiledFn fn = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// Tensor map of a row-major bf16 matrix [rows][inner] with row pitch `ld`
+// elements; boxes of 8 elements x box_rows rows.
+cudaError_t MakeOperandMap(CUtensorMap* m, const __nv_bfloat16* base, int inner, int rows, int ld,
+                           int box_rows) {
+  EncodeTiledFn fn = EncodeTiled();
+  if (!fn) return cudaErrorNotSupported;
+  const cuuint64_t dims[2] = {cuuint64_t(inner), cuuint64_t(rows)};
+  const cuuint64_t strides[1] = {cuuint64_t(ld) * 2};
+  const cuuint32_t box[2] = {8u, cuuint32_t(box_rows)};
+  const cuuint32_t estr[2] = {1u, 1u};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                        const_cast<__nv_bfloat16*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
 template <int N>
 cudaError_t LaunchGemm(const GemmArgs& a, int splits, cudaStream_t s) {
-  const size_t smem = size_t(tc::kTileM) * tc::kChunkK * 2 + size_t(N) * tc::kChunkK * 2;
+  // the operands' rows must start on 16-byte boundaries (TMA global strides)
+  if ((a.lda % 8) != 0 || (a.ldb % 8) != 0 || (reinterpret_cast<uintptr_t>(a.A) & 15) != 0 ||
+      (reinterpret_cast<uintptr_t>(a.B) & 15) != 0 || (a.K % 16) != 0 || (a.k_per_cta % 16) != 0)
+    return cudaErrorInvalidValue;
+  alignas(64) CUtensorMap tmA, tmB;
+  cudaError_t e = MakeOperandMap(&tmA, a.A, a.K, a.M, a.lda, tc::kTileM);
+  if (e == cudaSuccess) e = MakeOperandMap(&tmB, a.B, a.K, N, a.ldb, N);
+  if (e != cudaSuccess) return e;
+  const size_t smem = 1024 + size_t(tc::kTileM) * tc::kChunkK * 2 + size_t(N) * tc::kChunkK * 2;
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(TcGemmKernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(smem));
+    e = cudaFuncSetAttribute(TcGemmKernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(smem));
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
   dim3 grid(unsigned((a.M + tc::kTileM - 1) / tc::kTileM), unsigned(splits));
-  TcGemmKernel<N><<<grid, tc::kThreads, smem, s>>>(a);
+  TcGemmKernel<N><<<grid, tc::kThreads, smem, s>>>(a, tmA, tmB);
   return cudaGetLastError();
 }
 

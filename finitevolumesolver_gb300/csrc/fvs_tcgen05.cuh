@@ -4,17 +4,19 @@
 //   C[M x N] (+)= A[M x K] . B[N x K]^T      A, B bf16 (K contiguous), C fp32
 //
 // One CTA computes a 128 x N tile of C over a K range (split-K over
-// blockIdx.y accumulates with atomicAdd).  Per K chunk of 64 the 128 threads
-// copy the A and B tiles from global memory into shared memory in the
-// canonical no-swizzle K-major layout (8-row x 16-byte core matrices:
-// element (r, k) at (r/8)*SBO + (k/8)*LBO + (r%8)*16 + (k%8)*2 bytes with
-// LBO = 128 and SBO = 16*KC), make them visible to the tensor core's async
-// proxy, and one elected thread issues tcgen05.mma.cta_group::1.kind::f16
-// with M = 128, K = 16 per instruction.  tcgen05.commit arrives on an
-// mbarrier when the MMAs have completed; every wait on it is bounded and a
-// timeout sets an error flag instead of hanging.  The accumulator (128 lanes
-// x N fp32 columns of tensor memory) is read back with tcgen05.ld: warp w
-// reads lanes 32w..32w+31, i.e. rows 32w..32w+31 of the tile.
+// blockIdx.y accumulates with atomicAdd).  Per K chunk of 64 one thread
+// issues TMA loads (cp.async.bulk.tensor.2d) of the A and B tiles, one box of
+// 8 elements (16 bytes) x rows per 8-element K slice, which lands in shared
+// memory as the canonical no-swizzle K-major layout: 8-row x 16-byte core
+// matrices, element (r, k) at (k/8)*LBO + (r/8)*SBO + (r%8)*16 + (k%8)*2
+// bytes with SBO = 128 and LBO = rows*16.  The copies complete on an
+// mbarrier (expect_tx); then one thread issues
+// tcgen05.mma.cta_group::1.kind::f16 with M = 128, K = 16 per instruction,
+// and tcgen05.commit arrives on a second mbarrier when the MMAs have
+// completed.  Every wait is bounded and a timeout sets an error flag instead
+// of hanging.  The accumulator (128 lanes x N fp32 columns of tensor memory)
+// is read back with tcgen05.ld: warp w reads lanes 32w..32w+31, i.e. rows
+// 32w..32w+31 of the tile.
 #pragma once
 
 #include <cstdint>
@@ -108,6 +110,26 @@ __device__ __forceinline__ void FenceAfterSync() {
 }
 __device__ __forceinline__ void FenceProxyAsync() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// The next phase of `bar` completes once `bytes` of asynchronous copies
+// have landed (plus this one arrival).
+__device__ __forceinline__ void MbarArriveExpectTx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(SmemAddr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// TMA: box of a 2-D tensor map at element coordinates (x, y) into shared
+// memory, completing on `bar`.  x * element size must be a multiple of 16
+// bytes; rows outside the tensor are filled with zeros.
+__device__ __forceinline__ void TmaLoad2D(void* smem_dst, const void* tensor_map, int x, int y,
+                                          uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(SmemAddr(smem_dst)),
+      "l"(reinterpret_cast<uint64_t>(tensor_map)), "r"(x), "r"(y), "r"(SmemAddr(bar))
+      : "memory");
 }
 
 // 16 fp32 columns of this thread's TMEM lane starting at column `col`.
