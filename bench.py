@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--no-reports", action="store_true",
                     help="skip the secondary workloads (learned start value, 2-D Godunov, "
                          "2-D cut cells)")
-    ap.add_argument("--report", choices=["learned", "godunov", "amr", "cutcell"],
+    ap.add_argument("--report", choices=["sod", "learned", "godunov", "amr", "cutcell"],
                     help="run only this secondary workload and print its JSON report")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000)
     ap.add_argument("--mlp-epochs", type=int, default=24)
@@ -182,6 +182,36 @@ def cpu_reference_rate(n: int, steps: int, threads: int) -> dict:
     cons, dts, _ = g.run(m, cons, 0.8, 1e9, max_steps=steps, nthreads=threads)
     el = time.perf_counter() - t0
     return {"value": 6 * n ** 3 * steps / el, "seconds": el}
+
+
+def report_sod(args, torch, fvs, workloads):
+    """1-D Sod shock tube, 1024 cells, transmissive, MUSCL-Hancock/VanLeer +
+    HLLE, CFL 0.8, to t = 0.2: every flavour against the oracle, cell by cell."""
+    from oracle import build as obuild
+    obuild.build()
+    from oracle import oracle as orc
+    n = 1024
+    cons = workloads.sod_1d(n)
+    g = orc.Grid(1, [n], [1], [1.0 / n])
+    ref, ref_dts, _ = g.run(orc.method(), cons, 0.8, 0.2)
+    out = {"workload": "1D Sod shock tube, 1024 cells on [0, 1], transmissive, MUSCL-Hancock/"
+                       "VanLeer + HLLE, CFL 0.8, t = 0.2", "oracle_steps": len(ref_dts),
+           "flavours": {}}
+    for prec in ("fp64_exact", "fp64_fast", "mixed"):
+        s = fvs.Solver([n], [1.0 / n], "transmissive", method=fvs.make_method(precision=prec))
+        s.upload(cons)
+        t0 = time.perf_counter()
+        st, dts = s.run(cfl=0.8, t_end=0.2, log_len=4096)
+        el = time.perf_counter() - t0
+        res = s.download()
+        rel = np.abs(res - ref) / np.maximum(np.abs(ref), 1e-300)
+        out["flavours"][prec] = {
+            "steps": st.steps, "time": st.time, "wall_s": el,
+            "same_dt_sequence": bool(len(dts) == len(ref_dts) and np.array_equal(dts, ref_dts)),
+            "max_rel_diff_vs_oracle": float(rel.max()),
+            "bit_identical": bool(np.array_equal(res, ref))}
+        s.close()
+    return out
 
 
 def report_mlp(args, torch, fvs, workloads):
@@ -350,6 +380,8 @@ def report_amr(args, torch, fvs, workloads, peaks):
             out["flavours"][prec]["speedup_vs_fp64_exact"] = \
                 out["flavours"][prec]["cell_updates_per_s"] / base
     # CPU: the oracle's restatement, one coarse step of the same hierarchy
+    from oracle import build as obuild
+    obuild.build()
     from oracle import oracle as orc
     threads = orc.max_threads()
     t0 = time.perf_counter()
@@ -456,7 +488,9 @@ def run_ours(args):
     build.build()
     if args.report:
         peaks = load_peaks()
-        if args.report == "learned":
+        if args.report == "sod":
+            rep = report_sod(args, torch, fvs, workloads)
+        elif args.report == "learned":
             rep, _ = report_mlp(args, torch, fvs, workloads)
         elif args.report == "godunov":
             _, net = report_mlp(args, torch, fvs, workloads)
@@ -579,6 +613,10 @@ def run_ours(args):
     reports = None
     if rank == 0 and not args.no_reports:
         reports = {}
+        try:
+            reports["sod_1d"] = report_sod(args, torch, fvs, workloads)
+        except Exception as e:
+            reports["sod_1d"] = {"error": repr(e)}
         try:
             reports["learned_start_value"], net = report_mlp(args, torch, fvs, workloads)
         except Exception as e:  # report the failure, keep the headline
