@@ -31,7 +31,8 @@ __all__ = ["PerfectGas", "FluxMethod", "HyperbolicPatchIntegrator", "CompleteFro
            "Solver", "FvsError", "make_method", "box", "lib", "LearnedGuess",
            "riemann_features", "tc_gemm_bf16", "AmrSolver"]
 
-FLUX_METHODS = {"muscl_hlle": 0, "hlle": 1, "godunov": 2, "muscl_godunov": 3}
+FLUX_METHODS = {"muscl_hlle": 0, "hlle": 1, "godunov": 2, "muscl_godunov": 3, "hllem": 4,
+                "muscl_hllem": 5}
 LIMITERS = {"van_leer": 0, "minmod": 1, "none": 2}
 PRECISIONS = {"fp64_exact": 0, "fp64_fast": 1, "mixed": 2}
 GUESSES = {"mean": 0, "pvrs_tr": 1, "mlp": 2}
@@ -130,7 +131,7 @@ class FluxMethod:
         self.method = make_method(flux_method, limiter, precision, gamma=equation.gamma, **kw)
 
     def GetStencilWidth(self) -> int:
-        return 2 if self.method.flux_method in (0, 3) else 1
+        return 2 if self.method.flux_method in (0, 3, 5) else 1
 
     def ComputeNumericFluxes(self, fluxes, face_box, states, cell_box, dt, dx, dir,
                              stream=None) -> None:

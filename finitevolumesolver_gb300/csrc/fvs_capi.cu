@@ -71,7 +71,7 @@ int64_t Volume(const fvs_box& b) {
 int CheckMethod(const fvs_method* m, int rank) {
   if (!m) return Fail(FVS_ERR_INVALID, "method is NULL");
   if (rank < 1 || rank > 3) return Fail(FVS_ERR_INVALID, "rank must be 1, 2 or 3");
-  if (m->flux_method < 0 || m->flux_method > 3)
+  if (m->flux_method < 0 || m->flux_method > 5)
     return Fail(FVS_ERR_INVALID, "unknown flux method");
   if (m->limiter < 0 || m->limiter > 2) return Fail(FVS_ERR_INVALID, "unknown limiter");
   if (m->precision < 0 || m->precision > 2)
@@ -80,8 +80,12 @@ int CheckMethod(const fvs_method* m, int rank) {
   return FVS_OK;
 }
 
+bool IsGodunov(int method) { return method == FVS_GODUNOV || method == FVS_MUSCL_GODUNOV; }
+
 int StencilWidth(int method) {
-  return (method == FVS_MUSCL_HLLE || method == FVS_MUSCL_GODUNOV) ? 2 : 1;
+  return (method == FVS_MUSCL_HLLE || method == FVS_MUSCL_GODUNOV || method == FVS_MUSCL_HLLEM)
+             ? 2
+             : 1;
 }
 
 double BitsToDouble(unsigned long long b) {
@@ -296,6 +300,8 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
   a.stats_out = ctrl ? ctrl->newton : s->newton_words;
   if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
     return fvs::LaunchSweepGodunov(a, s->m.flux_method == FVS_MUSCL_GODUNOV, s->stream);
+  if (s->m.flux_method == FVS_HLLEM || s->m.flux_method == FVS_MUSCL_HLLEM)
+    return fvs::LaunchSweepHllem(a, s->m.flux_method == FVS_MUSCL_HLLEM, s->stream);
   switch (s->m.precision) {
   case FVS_FP64_EXACT:
     return fvs::LaunchSweepExact(a, s->stream);
@@ -327,6 +333,8 @@ cudaError_t LaunchStable(const fvs_solver* s, const double* in,
   if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
     return fvs::LaunchStableDtGodunov(a, s->m.guess, s->m.max_iterations, s->m.tolerance,
                                       s->m.mlp_params, s->stream);
+  if (s->m.flux_method == FVS_HLLEM || s->m.flux_method == FVS_MUSCL_HLLEM)
+    return fvs::LaunchStableDtHllem(a, s->stream);
   switch (s->m.precision) {
   case FVS_FP64_EXACT:
     return fvs::LaunchStableDtExact(a, s->stream);
@@ -450,7 +458,7 @@ int fvs_compute_numeric_fluxes(const fvs_method* m, int rank,
     return Fail(FVS_ERR_INVALID, "cell box does not cover the faces' stencils");
   if (m->precision != FVS_FP64_EXACT)
     return Fail(FVS_ERR_UNSUPPORTED, "patch-level calls run in exact FP64");
-  if (m->flux_method >= FVS_GODUNOV && m->guess == FVS_GUESS_MLP && !m->mlp_params)
+  if (IsGodunov(m->flux_method) && m->guess == FVS_GUESS_MLP && !m->mlp_params)
     return Fail(FVS_ERR_INVALID, "FVS_GUESS_MLP needs mlp_params");
   if (int r = CheckDevice()) return r;
   if (m->flux_method == FVS_GODUNOV || m->flux_method == FVS_MUSCL_GODUNOV) {
@@ -476,7 +484,7 @@ int fvs_compute_stable_dt(const fvs_method* m, int rank, const double* states_de
   if (!dt_out) return Fail(FVS_ERR_INVALID, "dt_out is NULL");
   if (window_rule != 0 && window_rule != 1)
     return Fail(FVS_ERR_INVALID, "window_rule must be 0 or 1");
-  if (m->flux_method >= FVS_GODUNOV && m->guess == FVS_GUESS_MLP && !m->mlp_params)
+  if (IsGodunov(m->flux_method) && m->guess == FVS_GUESS_MLP && !m->mlp_params)
     return Fail(FVS_ERR_INVALID, "FVS_GUESS_MLP needs mlp_params");
   if (int r = CheckDevice()) return r;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -561,10 +569,13 @@ int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
   if (!grid || !out) return Fail(FVS_ERR_INVALID, "NULL argument");
   if (int r = CheckMethod(m, grid->rank)) return r;
   if ((m->flux_method == FVS_HLLE))
-    return Fail(FVS_ERR_UNSUPPORTED, "the solver runs MUSCL-Hancock or Godunov fluxes");
-  if (m->flux_method >= FVS_GODUNOV && m->precision == FVS_MIXED)
+    return Fail(FVS_ERR_UNSUPPORTED, "the solver runs MUSCL-Hancock, HLLEM or Godunov fluxes");
+  if ((m->flux_method == FVS_HLLEM || m->flux_method == FVS_MUSCL_HLLEM) &&
+      m->precision != FVS_FP64_EXACT)
+    return Fail(FVS_ERR_UNSUPPORTED, "HLLEM runs in exact FP64");
+  if (IsGodunov(m->flux_method) && m->precision == FVS_MIXED)
     return Fail(FVS_ERR_UNSUPPORTED, "the exact Riemann solver runs in FP64");
-  if (m->flux_method >= FVS_GODUNOV && m->guess == FVS_GUESS_MLP && !m->mlp_params)
+  if (IsGodunov(m->flux_method) && m->guess == FVS_GUESS_MLP && !m->mlp_params)
     return Fail(FVS_ERR_INVALID, "FVS_GUESS_MLP needs mlp_params");
   for (int d = 0; d < 3; ++d) {
     const bool used = d < grid->rank;

@@ -95,6 +95,8 @@ void SetLastError(const std::string& msg);
 // Exact FP64 kernels (fvs_kernels_exact.cu, compiled with -fmad=false).
 cudaError_t LaunchSweepExact(const SweepArgs& a, cudaStream_t s);
 cudaError_t LaunchStableDtExact(const StableDtArgs& a, cudaStream_t s);
+cudaError_t LaunchSweepHllem(const SweepArgs& a, bool muscl, cudaStream_t s);
+cudaError_t LaunchStableDtHllem(const StableDtArgs& a, cudaStream_t s);
 
 // Fast FP64 and mixed FP32/FP64 kernels (fvs_kernels_fast.cu).
 cudaError_t LaunchSweepFast(const SweepArgs& a, cudaStream_t s);

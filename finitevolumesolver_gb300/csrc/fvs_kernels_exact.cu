@@ -3,9 +3,11 @@
 // Compiled with -fmad=false (see build.py): no FMA contraction, IEEE
 // division and sqrt, so every result is bit-identical to the reference's
 // x86-64 build of the same formulas.
+#include "fvs_hllem.cuh"
 #include "fvs_internal.h"
 #include "fvs_physics_exact.cuh"
 #include "fvs_policy_exact.cuh"
+#include "fvs_stable.cuh"
 #include "fvs_sweep.cuh"
 
 namespace fvs {
@@ -19,6 +21,91 @@ cudaError_t LaunchSweepExact(const SweepArgs& a, cudaStream_t s) {
   default:
     return LaunchSweepT<3, ExactPolicy>(a, s);
   }
+}
+
+// HLLEM (first order) and MUSCL-Hancock + HLLEM sweeps: the marching sweep
+// with Hllem<PerfectGas, Larrouturou> as the face flux and its stable-dt speed
+// as the CFL check (fvs_hllem.cuh).
+template <int D> struct HllemWave {
+  exact::Complete<D> q;
+  int dir;
+};
+
+template <int D, bool kMuscl> struct HllemPolicyT {
+  using Real = double;
+  static constexpr bool kWarpX = false;
+  static constexpr int kMinBlocks = 1;
+  using Gas = exact::Gas;
+  using Rec = exact::Complete<D>;
+  using Wave = HllemWave<D>;
+  using Stats = NoStats;
+  static __device__ __forceinline__ Gas MakeGas(double gamma) {
+    return ExactPolicy<D>::MakeGas(gamma);
+  }
+  static __device__ __forceinline__ Gas MakeGasFor(const SweepArgs& a) { return MakeGas(a.gamma); }
+  static __device__ __forceinline__ void ToCell(double* c, const double* u) {
+#pragma unroll
+    for (int k = 0; k < D + 2; ++k) c[k] = u[k];
+  }
+  static __device__ __forceinline__ void Predict(const Gas& eq, Rec& recL, Rec& recR,
+                                                 const double* q0, const double* q1,
+                                                 const double* q2, int limiter,
+                                                 double lambda_half, int dir) {
+    if constexpr (kMuscl) {
+      exact::MusclPredictBoth<D>(eq, recL, recR, q0, q1, q2, limiter, lambda_half, dir);
+    } else {
+      exact::CompleteFromCons<D>(eq, recL, q1);
+      recR = recL;
+    }
+  }
+  static __device__ __forceinline__ Wave MakeWave(const Gas& eq, const double* u, int dir) {
+    Wave w;
+    exact::CompleteFromCons<D>(eq, w.q, u);
+    w.dir = dir;
+    return w;
+  }
+  static __device__ __forceinline__ double FaceMaxSpeed(const Gas& eq, const Wave& wL,
+                                                        const Wave& wR) {
+    return exact::HllemMaxSpeed<D>(eq, wL.q, wR.q, wL.dir);
+  }
+  static __device__ __forceinline__ double Face(const Gas& eq, double* F, const Rec& L,
+                                                const Rec& R, const Wave& wL, const Wave& wR,
+                                                int dir, Stats&) {
+    exact::HllemFlux<D>(eq, F, L, R, dir);
+    return exact::HllemMaxSpeed<D>(eq, wL.q, wR.q, dir);
+  }
+};
+
+template <int D> struct HllemPolicy : HllemPolicyT<D, false> {};
+template <int D> struct MusclHllemPolicy : HllemPolicyT<D, true> {};
+
+cudaError_t LaunchSweepHllem(const SweepArgs& a, bool muscl, cudaStream_t s) {
+  switch (a.rank) {
+  case 1:
+    return muscl ? LaunchSweepT<1, MusclHllemPolicy>(a, s) : LaunchSweepT<1, HllemPolicy>(a, s);
+  case 2:
+    return muscl ? LaunchSweepT<2, MusclHllemPolicy>(a, s) : LaunchSweepT<2, HllemPolicy>(a, s);
+  default:
+    return muscl ? LaunchSweepT<3, MusclHllemPolicy>(a, s) : LaunchSweepT<3, HllemPolicy>(a, s);
+  }
+}
+
+cudaError_t LaunchStableDtHllem(const StableDtArgs& a, cudaStream_t s) {
+  const int64_t cells = int64_t(a.n[0]) * a.n[1] * a.n[2];
+  const int block = 256;
+  const unsigned grid = static_cast<unsigned>((cells + block - 1) / block);
+  switch (a.rank) {
+  case 1:
+    StableDtKernelT<1, HllemPolicy><<<grid, block, 0, s>>>(a);
+    break;
+  case 2:
+    StableDtKernelT<2, HllemPolicy><<<grid, block, 0, s>>>(a);
+    break;
+  default:
+    StableDtKernelT<3, HllemPolicy><<<grid, block, 0, s>>>(a);
+    break;
+  }
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
@@ -170,13 +257,16 @@ __global__ void PatchFluxKernel(int method, int limiter, double gamma,
   Unflatten(id, fbox, f);
   const exact::Gas eq = ExactPolicy<1>::MakeGas(gamma);
   double nf[K];
-  if (method == 1) {  // HLLE, stencil width 1
+  if (method == 1 || method == 4) {  // HLLE / HLLEM, stencil width 1
     int c0[3] = {f[0], f[1], f[2]};
     c0[dir] -= 1;
     const exact::Complete<D> L = LoadComplete<D>(st, c0[0], c0[1], c0[2]);
     const exact::Complete<D> R = LoadComplete<D>(st, f[0], f[1], f[2]);
-    exact::HllFlux<D>(eq, nf, L, R, dir);
-  } else {  // MUSCL-Hancock + HLLE, stencil width 2
+    if (method == 1)
+      exact::HllFlux<D>(eq, nf, L, R, dir);
+    else
+      exact::HllemFlux<D>(eq, nf, L, R, dir);
+  } else {  // MUSCL-Hancock + HLLE / HLLEM, stencil width 2
     double u[4][K];
     for (int s = 0; s < 4; ++s) {
       int c[3] = {f[0], f[1], f[2]};
@@ -190,7 +280,10 @@ __global__ void PatchFluxKernel(int method, int limiter, double gamma,
                                lambda_half, dir);
     exact::MusclPredictBoth<D>(eq, a1, b1, u[1], u[2], u[3], limiter,
                                lambda_half, dir);
-    exact::HllFlux<D>(eq, nf, b0, a1, dir);
+    if (method == 5)
+      exact::HllemFlux<D>(eq, nf, b0, a1, dir);
+    else
+      exact::HllFlux<D>(eq, nf, b0, a1, dir);
   }
   View fv{fluxes, fbox};
 #pragma unroll
@@ -228,7 +321,7 @@ cudaError_t LaunchPatchFluxesExact(int method, int limiter, int rank,
 // is the sequential tag (FluxMethod.hpp:295-314), 1 the simd tag
 // (FluxMethod.hpp:341-382).  Writes the max face speed; dt = dx / speed.
 template <int D>
-__global__ void PatchStableDtKernel(int w, double gamma, View st, BoxDesc wbox,
+__global__ void PatchStableDtKernel(int w, int hllem, double gamma, View st, BoxDesc wbox,
                                     int dir, unsigned long long* smax_out) {
   const int64_t nwin = int64_t(wbox.n[0]) * wbox.n[1] * wbox.n[2];
   const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -241,9 +334,13 @@ __global__ void PatchStableDtKernel(int w, double gamma, View st, BoxDesc wbox,
     c[dir] += 1;
     const exact::Complete<D> R = LoadComplete<D>(st, c[0], c[1], c[2]);
     const exact::Gas eq = ExactPolicy<1>::MakeGas(gamma);
-    double s0, s1;
-    exact::Einfeldt<D>(eq, L, R, dir, s0, s1);
-    s = exact::PMax(exact::PMax(0.0, fabs(s0)), fabs(s1));
+    if (hllem) {
+      s = exact::HllemMaxSpeed<D>(eq, L, R, dir);
+    } else {
+      double s0, s1;
+      exact::Einfeldt<D>(eq, L, R, dir, s0, s1);
+      s = exact::PMax(exact::PMax(0.0, fabs(s0)), fabs(s1));
+    }
   }
   s = WarpMax(s);
   if ((threadIdx.x & 31) == 0 && s > 0.0) AtomicMaxPositive(smax_out, s);
@@ -253,7 +350,8 @@ cudaError_t LaunchPatchStableDtExact(int method, int rank, double gamma,
                                      const double* states, BoxDesc cbox,
                                      int window_rule, int dir,
                                      unsigned long long* smax, cudaStream_t s) {
-  const int w = (method == 1) ? 1 : 2;
+  const int w = (method == 1 || method == 4) ? 1 : 2;
+  const int hllem = (method == 4 || method == 5) ? 1 : 0;
   BoxDesc wbox = cbox;
   wbox.n[dir] -= (window_rule == 0) ? 2 * w : 2 * w - 1;
   if (wbox.n[dir] <= 0) return cudaSuccess;
@@ -263,13 +361,13 @@ cudaError_t LaunchPatchStableDtExact(int method, int rank, double gamma,
   View st{states, cbox};
   switch (rank) {
   case 1:
-    PatchStableDtKernel<1><<<grid, block, 0, s>>>(w, gamma, st, wbox, dir, smax);
+    PatchStableDtKernel<1><<<grid, block, 0, s>>>(w, hllem, gamma, st, wbox, dir, smax);
     break;
   case 2:
-    PatchStableDtKernel<2><<<grid, block, 0, s>>>(w, gamma, st, wbox, dir, smax);
+    PatchStableDtKernel<2><<<grid, block, 0, s>>>(w, hllem, gamma, st, wbox, dir, smax);
     break;
   default:
-    PatchStableDtKernel<3><<<grid, block, 0, s>>>(w, gamma, st, wbox, dir, smax);
+    PatchStableDtKernel<3><<<grid, block, 0, s>>>(w, hllem, gamma, st, wbox, dir, smax);
     break;
   }
   return cudaGetLastError();

@@ -46,7 +46,9 @@ typedef enum fvs_flux_method {
   FVS_MUSCL_HLLE = 0,   /* MusclHancock<PerfectGas, Hll<Einfeldt>, Limiter> */
   FVS_HLLE = 1,         /* Hll<PerfectGas, EinfeldtSignalVelocities> */
   FVS_GODUNOV = 2,      /* Godunov<PerfectGas, ExactRiemannSolver> */
-  FVS_MUSCL_GODUNOV = 3 /* MusclHancock<PerfectGas, Godunov<Exact>, Limiter> */
+  FVS_MUSCL_GODUNOV = 3, /* MusclHancock<PerfectGas, Godunov<Exact>, Limiter> */
+  FVS_HLLEM = 4,        /* perfect_gas::Hllem<PerfectGas, Larrouturou = true> */
+  FVS_MUSCL_HLLEM = 5   /* MusclHancock<PerfectGas, Hllem, Limiter> (exact FP64) */
 } fvs_flux_method;
 
 typedef enum fvs_limiter {

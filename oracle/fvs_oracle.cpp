@@ -25,7 +25,7 @@ using namespace fvs_oracle;
 extern "C" {
 // Method description shared with the Python test helpers.
 struct orc_method {
-  int32_t method;   // kMusclHlle, kHlle, kGodunov, kMusclGodunov
+  int32_t method;   // kMusclHlle, kHlle, kGodunov, kMusclGodunov, kHllem, kMusclHllem
   int32_t limiter;  // kVanLeer, kMinMod, kNoLimiter
   int32_t guess;    // kGuessMean, kGuessPvrsTr
   int32_t max_iterations;
@@ -78,7 +78,7 @@ void LoadCons(double* u, const BoxView& v, int i, int j, int k) {
 inline void Shift(int* idx, int dir, int s) { idx[dir] += s; }
 
 int StencilWidth(int method) {
-  return (method == kMusclHlle || method == kMusclGodunov) ? 2 : 1;
+  return (method == kMusclHlle || method == kMusclGodunov || method == kMusclHllem) ? 2 : 1;
 }
 
 // The numeric flux of one face from the 2w cells of its stencil.
@@ -99,6 +99,10 @@ void FaceFlux(const Gas& eq, const orc_method& m, double* nf,
     HllFlux<D>(eq, nf, st[0], st[1], dir);
     return;
   }
+  if (m.method == kHllem) {
+    HllemFlux<D>(eq, nf, st[0], st[1], dir);
+    return;
+  }
   if (m.method == kGodunov) {
     int it = GodunovFlux<D>(eq, nf, st[0], st[1], dir, opt, 0.0, converged);
     if (iters) *iters = it;
@@ -112,6 +116,8 @@ void FaceFlux(const Gas& eq, const orc_method& m, double* nf,
   MusclPredict<D>(eq, rec1, u[1], u[2], u[3], m.limiter, lambda_half, dir, -1);
   if (m.method == kMusclHlle) {
     HllFlux<D>(eq, nf, rec0, rec1, dir);
+  } else if (m.method == kMusclHllem) {
+    HllemFlux<D>(eq, nf, rec0, rec1, dir);
   } else {
     int it = GodunovFlux<D>(eq, nf, rec0, rec1, dir, opt, 0.0, converged);
     if (iters) *iters = it;
@@ -133,6 +139,7 @@ double WindowDt(const Gas& eq, const orc_method& m, const Complete<D>* st,
     opt.max_iterations = m.max_iterations;
     return GodunovStableDt<D>(eq, L, R, dx, dir, opt);
   }
+  if (m.method == kHllem || m.method == kMusclHllem) return HllemStableDt<D>(eq, L, R, dx, dir);
   return HllStableDt<D>(eq, L, R, dx, dir);
 }
 
