@@ -12,7 +12,7 @@
 // delta = a_roe / (a_roe + |u_bar|), and the tangential momentum and
 // kinetic-energy fluxes are upwinded by the sign of the mass flux.  The 3-D
 // normal-momentum correction uses roeU[iy], as the reference does
-// (HllemMethod.hpp:1012-1013).
+// (HllemMethod.hpp:991-992).
 #pragma once
 
 #include "fvs_physics_exact.cuh"

@@ -314,7 +314,7 @@ inline void MusclPredict(const Gas& eq, Complete<D>& rec, const double* q0,
 // the reduced states is corrected along the second eigenvector, and the
 // tangential momentum and kinetic-energy fluxes are upwinded by the sign of
 // the mass flux.  The operation order is the reference's, including its 3-D
-// normal-momentum correction with roeU[iy] (HllemMethod.hpp:1012-1013).
+// normal-momentum correction with roeU[iy] (HllemMethod.hpp:991-992).
 template <int D>
 inline void HllemFlux(const Gas& eq, double* nf, const Complete<D>& left,
                       const Complete<D>& right, int ix) {
