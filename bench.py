@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64_fast",
-                    choices=["fp64_exact", "fp64_fast", "mixed"])
+                    choices=["fp64_exact", "fp64_fast", "fp64_df", "mixed"])
     ap.add_argument("--no-variants", action="store_true",
                     help="skip timing the other precision flavours")
     ap.add_argument("--n", type=int, default=256)
@@ -518,6 +518,7 @@ def run_ours(args):
         stream = torch.cuda.ExternalStream(solver.stream_handle())
         solver.upload(cons)
         segs = solver.autotune()
+        segs = {"segment_cells": segs, "occupancy_variant": solver.tuning()[1]}
         if args.warmup:
             solver.run(cfl=0.8, t_end=1e9, max_steps=args.warmup)
         clocks = ClockSampler(torch.cuda.current_device()) if with_clocks else None
@@ -577,7 +578,7 @@ def run_ours(args):
 
     variants = {}
     if not args.no_variants:
-        for prec in ("fp64_exact", "fp64_fast", "mixed"):
+        for prec in ("fp64_exact", "fp64_fast", "fp64_df", "mixed"):
             if prec == args.precision:
                 continue
             r = measure(prec, with_clocks=False)
@@ -640,7 +641,7 @@ def run_ours(args):
             "config": {"workload": f"3D perfect gas {n}^3 periodic, Strang MUSCL-Hancock/VanLeer"
                                    " + HLLE, CFL 0.8, seeded octants + Gaussian bumps",
                        "n": n, "precision": args.precision, "sweeps_per_step": 6,
-                       "autotuned_segment_cells": main["segs"],
+                       "autotuned": main["segs"],
                        "l2": "inputs larger than L2 (state 671 MB per copy)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": main["achieved"], "peak": peaks["hbm_gbs"],
@@ -662,7 +663,7 @@ def run_ours(args):
             "accuracy": accuracy(main["final"]),
             "variants": {k: {"value": v["value"], "ms_per_step": v["ms"] / args.steps,
                              "sweep_launch_ms": v["sweep_s"] * 1e3,
-                             "autotuned_segment_cells": v["segs"],
+                             "autotuned": v["segs"],
                              "hbm_frac": v["achieved"] / peaks["hbm_gbs"],
                              "accuracy": accuracy(v["final"])}
                          for k, v in variants.items()},

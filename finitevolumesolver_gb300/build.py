@@ -27,6 +27,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 UNITS = [
     ("fvs_kernels_exact.cu", ["-fmad=false"]),
     ("fvs_kernels_fast.cu", []),
+    ("fvs_kernels_df64.cu", []),
     ("fvs_kernels_godunov.cu", ["-fmad=false"]),
     ("fvs_kernels_cutcell.cu", ["-fmad=false"]),
     ("fvs_kernels_cutcell_mixed.cu", []),

@@ -589,6 +589,8 @@ int fvs_amr_create(const fvs_amr_desc* d, const fvs_method* m, fvs_amr** out) {
   }
   if (mm.flux_method != FVS_MUSCL_HLLE)
     return Fail(FVS_ERR_UNSUPPORTED, "AMR patch sets run MUSCL-Hancock + HLLE");
+  if (mm.precision < FVS_FP64_EXACT || mm.precision > FVS_MIXED)
+    return Fail(FVS_ERR_UNSUPPORTED, "AMR patch sets run in exact FP64, fast FP64 or mixed");
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
     cudaGetLastError();

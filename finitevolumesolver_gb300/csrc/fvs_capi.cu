@@ -74,7 +74,7 @@ int CheckMethod(const fvs_method* m, int rank) {
   if (m->flux_method < 0 || m->flux_method > 5)
     return Fail(FVS_ERR_INVALID, "unknown flux method");
   if (m->limiter < 0 || m->limiter > 2) return Fail(FVS_ERR_INVALID, "unknown limiter");
-  if (m->precision < 0 || m->precision > 2)
+  if (m->precision < 0 || m->precision > 3)
     return Fail(FVS_ERR_INVALID, "unknown precision");
   if (!(m->gamma > 1.0)) return Fail(FVS_ERR_INVALID, "gamma must exceed 1");
   return FVS_OK;
@@ -307,6 +307,8 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
     return fvs::LaunchSweepExact(a, s->stream);
   case FVS_FP64_FAST:
     return fvs::LaunchSweepFast(a, s->stream);
+  case FVS_FP64_DF:
+    return fvs::LaunchSweepDf64(a, s->stream);
   default:
     return fvs::LaunchSweepMixed(a, s->stream);
   }
@@ -340,6 +342,8 @@ cudaError_t LaunchStable(const fvs_solver* s, const double* in,
     return fvs::LaunchStableDtExact(a, s->stream);
   case FVS_FP64_FAST:
     return fvs::LaunchStableDtFast(a, s->stream);
+  case FVS_FP64_DF:
+    return fvs::LaunchStableDtDf64(a, s->stream);
   default:
     return fvs::LaunchStableDtMixed(a, s->stream);
   }
@@ -573,7 +577,8 @@ int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
   if ((m->flux_method == FVS_HLLEM || m->flux_method == FVS_MUSCL_HLLEM) &&
       m->precision != FVS_FP64_EXACT)
     return Fail(FVS_ERR_UNSUPPORTED, "HLLEM runs in exact FP64");
-  if (IsGodunov(m->flux_method) && m->precision == FVS_MIXED)
+  if (IsGodunov(m->flux_method) && m->precision != FVS_FP64_EXACT &&
+      m->precision != FVS_FP64_FAST)
     return Fail(FVS_ERR_UNSUPPORTED, "the exact Riemann solver runs in FP64");
   if (IsGodunov(m->flux_method) && m->guess == FVS_GUESS_MLP && !m->mlp_params)
     return Fail(FVS_ERR_INVALID, "FVS_GUESS_MLP needs mlp_params");
@@ -655,11 +660,14 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   // state with a small dt (output goes to a spare buffer; the state is not
   // changed).
   const int cands[] = {16, 32, 64, 128, 256, 512};
-  const bool mixed = s->m.precision == FVS_MIXED && s->m.flux_method <= FVS_HLLE && !s->cc;
+  const bool plain_hlle = s->m.flux_method <= FVS_HLLE && !s->cc;
+  const bool mixed = s->m.precision == FVS_MIXED && plain_hlle;
+  const bool df = s->m.precision == FVS_FP64_DF && plain_hlle;
   const int occs_mixed[] = {0, 4, 5};
+  const int occs_df[] = {0, 3};
   const int occs_plain[] = {0};
-  const int* occs = mixed ? occs_mixed : occs_plain;
-  const int nocc = mixed ? 3 : 1;
+  const int* occs = mixed ? occs_mixed : (df ? occs_df : occs_plain);
+  const int nocc = mixed ? 3 : (df ? 2 : 1);
   const int saved = s->seg_len;
   cudaEvent_t e0, e1;
   FVS_CUDA(cudaEventCreate(&e0));
@@ -727,6 +735,8 @@ int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int nc
   if (s->g.rank != 2) return Fail(FVS_ERR_UNSUPPORTED, "cut cells need a rank-2 grid");
   if (s->m.flux_method != FVS_MUSCL_HLLE)
     return Fail(FVS_ERR_UNSUPPORTED, "cut cells run MUSCL-Hancock + HLLE");
+  if (s->m.precision == FVS_FP64_DF)
+    return Fail(FVS_ERR_UNSUPPORTED, "cut cells run in exact FP64, fast FP64 or mixed precision");
   if (ncircles < 1 || ncircles > 16) return Fail(FVS_ERR_INVALID, "1 to 16 circles");
   for (int k = 0; k < ncircles; ++k)
     if (!(circles[3 * k + 2] > 0.0)) return Fail(FVS_ERR_INVALID, "circle radius must be > 0");

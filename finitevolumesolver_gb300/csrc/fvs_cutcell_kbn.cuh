@@ -21,6 +21,7 @@
 //   MakeRotation, Reflect      include/fub/ext/Eigen.hpp:104-115, src/equations/PerfectGas.cpp:240-252
 #pragma once
 
+#include "fvs_convert.cuh"
 #include "fvs_cutcell.h"
 #include "fvs_internal.h"
 #include "fvs_physics_exact.cuh"
@@ -278,7 +279,7 @@ __device__ __forceinline__ void LoadCons(const CcStateArgs& a, int i, int j, dou
 
 template <class T> __device__ __forceinline__ void Narrow(T* t, const double* u) {
 #pragma unroll
-  for (int k = 0; k < 4; ++k) t[k] = T(u[k]);
+  for (int k = 0; k < 4; ++k) t[k] = NarrowTo<T>(u[k]);
 }
 
 // KbnCutCellMethod::PreAdvanceHierarchy for the cut cells of [-1, n+1)^2.
@@ -299,16 +300,16 @@ template <class T> __global__ void ReferenceStatesKernel(CcStateArgs a) {
   const int64_t plane = int64_t(a.g.NX()) * a.g.NY();
   C2T<T> r;
   if (q.rho > T(0)) {
-    r = WallSolution(eq, q, T(a.g.normal[c]), T(a.g.normal[plane + c]));
+    r = WallSolution(eq, q, NarrowTo<T>(a.g.normal[c]), NarrowTo<T>(a.g.normal[plane + c]));
   } else {
     r = C2T<T>{T(0), {T(0), T(0)}, T(0), T(0), T(0)};
   }
-  a.refs[c] = r.rho;
-  a.refs[plane + c] = r.m[0];
-  a.refs[2 * plane + c] = r.m[1];
-  a.refs[3 * plane + c] = r.E;
-  a.refs[4 * plane + c] = r.p;
-  a.refs[5 * plane + c] = r.c;
+  a.refs[c] = Widen(r.rho);
+  a.refs[plane + c] = Widen(r.m[0]);
+  a.refs[2 * plane + c] = Widen(r.m[1]);
+  a.refs[3 * plane + c] = Widen(r.E);
+  a.refs[4 * plane + c] = Widen(r.p);
+  a.refs[5 * plane + c] = Widen(r.c);
 }
 
 // The fused KBN sweep: one thread marches one grid line (segment) along
@@ -342,7 +343,7 @@ template <class T> __global__ void __launch_bounds__(128) KbnSweepKernel(CcSweep
     const int t = static_cast<int>(t64);
     const GasT<T> eq = MakeGasT<T>(a.s.gamma);
     const double dx = a.dx;
-    const T lambda_half = T(0.5 * split_dt / dx);
+    const T lambda_half = NarrowTo<T>(0.5 * split_dt / dx);
     const double dt_dx = split_dt / dx;
     const int64_t plane = int64_t(g.NX()) * g.NY();
     const int64_t cs = int64_t(g.nx) * g.ny;
@@ -380,20 +381,21 @@ template <class T> __global__ void __launch_bounds__(128) KbnSweepKernel(CcSweep
       for (int k = 0; k < 4; ++k) fb[k] = 0.0;
       if (!g.cut[ci]) return;
       C2T<T> ref;
-      ref.rho = T(a.s.refs[ci]);
-      ref.m[0] = T(a.s.refs[plane + ci]);
-      ref.m[1] = T(a.s.refs[2 * plane + ci]);
-      ref.E = T(a.s.refs[3 * plane + ci]);
-      ref.p = T(a.s.refs[4 * plane + ci]);
-      ref.c = T(a.s.refs[5 * plane + ci]);
+      ref.rho = NarrowTo<T>(a.s.refs[ci]);
+      ref.m[0] = NarrowTo<T>(a.s.refs[plane + ci]);
+      ref.m[1] = NarrowTo<T>(a.s.refs[2 * plane + ci]);
+      ref.E = NarrowTo<T>(a.s.refs[3 * plane + ci]);
+      ref.p = NarrowTo<T>(a.s.refs[4 * plane + ci]);
+      ref.c = NarrowTo<T>(a.s.refs[5 * plane + ci]);
       C2T<T> q;
       CompleteMasked(eq, q, u, g.alpha[ci] > 0.0);
       T f[4];
       FluxT(f, ref, dir);
-      const C2T<T> sol = WallSolution(eq, q, T(g.normal[ci]), T(g.normal[plane + ci]));
+      const C2T<T> sol =
+          WallSolution(eq, q, NarrowTo<T>(g.normal[ci]), NarrowTo<T>(g.normal[plane + ci]));
       f[1 + dir] += sol.p - ref.p;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) fb[k] = double(f[k]);
+      for (int k = 0; k < 4; ++k) fb[k] = Widen(f[k]);
     };
     auto center_of = [&](int c) {
       int i, j;
@@ -433,7 +435,7 @@ template <class T> __global__ void __launch_bounds__(128) KbnSweepKernel(CcSweep
           T f[4];
           HllMasked(eq, f, recR_prev, recL, dir);
 #pragma unroll
-          for (int k = 0; k < 4; ++k) F.f[k] = double(f[k]);
+          for (int k = 0; k < 4; ++k) F.f[k] = Widen(f[k]);
           T s0, s1;
           EinfeldtMasked(eq, q_prev, q, dir, s0, s1);
           const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));

@@ -74,7 +74,8 @@ struct SweepArgs {
   double tolerance;
   const float* mlp;     // learned-guess weights (guess == FVS_GUESS_MLP)
   unsigned long long* stats_out;  // [3]: Newton iterations, non-converged, fallbacks
-  int occupancy;        // mixed flavour: 0 (registers as needed), 4 or 5 blocks per SM
+  int occupancy;        // 0 (registers as needed) or the resident blocks per SM a
+                        // variant is compiled for (mixed: 4, 5; double-float: 3)
 };
 
 // Stable-dt pass over all directions (max face speed per direction).
@@ -96,6 +97,8 @@ void SetLastError(const std::string& msg);
 cudaError_t LaunchSweepExact(const SweepArgs& a, cudaStream_t s);
 cudaError_t LaunchStableDtExact(const StableDtArgs& a, cudaStream_t s);
 cudaError_t LaunchSweepHllem(const SweepArgs& a, bool muscl, cudaStream_t s);
+cudaError_t LaunchSweepDf64(const SweepArgs& a, cudaStream_t s);
+cudaError_t LaunchStableDtDf64(const StableDtArgs& a, cudaStream_t s);
 cudaError_t LaunchStableDtHllem(const StableDtArgs& a, cudaStream_t s);
 
 // Fast FP64 and mixed FP32/FP64 kernels (fvs_kernels_fast.cu).

@@ -91,21 +91,7 @@ cudaError_t LaunchSweepHllem(const SweepArgs& a, bool muscl, cudaStream_t s) {
 }
 
 cudaError_t LaunchStableDtHllem(const StableDtArgs& a, cudaStream_t s) {
-  const int64_t cells = int64_t(a.n[0]) * a.n[1] * a.n[2];
-  const int block = 256;
-  const unsigned grid = static_cast<unsigned>((cells + block - 1) / block);
-  switch (a.rank) {
-  case 1:
-    StableDtKernelT<1, HllemPolicy><<<grid, block, 0, s>>>(a);
-    break;
-  case 2:
-    StableDtKernelT<2, HllemPolicy><<<grid, block, 0, s>>>(a);
-    break;
-  default:
-    StableDtKernelT<3, HllemPolicy><<<grid, block, 0, s>>>(a);
-    break;
-  }
-  return cudaGetLastError();
+  return LaunchStableDtT<HllemPolicy>(a, s);
 }
 
 // ---------------------------------------------------------------------------

@@ -60,7 +60,9 @@ typedef enum fvs_limiter {
 typedef enum fvs_precision {
   FVS_FP64_EXACT = 0, /* reference operation order, no FMA: bit-identical */
   FVS_FP64_FAST = 1,  /* FP64 with FMA and shared reciprocals (<= 1e-12 rel) */
-  FVS_MIXED = 2       /* FP32 reconstruction/flux, FP64 state and update */
+  FVS_MIXED = 2,      /* FP32 reconstruction/flux, FP64 state and update */
+  FVS_FP64_DF = 3     /* MUSCL-HLLE in double-float (FP32 pairs, ~48 bits) on the
+                         FP32 pipes, FP64 state and update (uniform grids) */
 } fvs_precision;
 
 typedef enum fvs_guess {
@@ -233,9 +235,9 @@ int fvs_solver_set_tiling(fvs_solver* s, int seg_len);
  * the fastest per direction (used unless fvs_solver_set_tiling forces one).
  * seg_out (may be NULL) receives rank values.  Does not change the state. */
 int fvs_solver_autotune(fvs_solver* s, int* seg_out);
-/* The tuned segment lengths and (mixed flavour) occupancy variants per
- * direction: 0 = registers as needed, 4 or 5 = compiled for that many
- * resident 128-thread blocks per SM.  Either pointer may be NULL. */
+/* The tuned segment lengths and occupancy variants per direction: 0 =
+ * registers as needed, 3 (double-float), 4 or 5 (mixed) = compiled for that
+ * many resident 128-thread blocks per SM.  Either pointer may be NULL. */
 int fvs_solver_tuning(fvs_solver* s, int32_t* seg, int32_t* occupancy);
 /* Stable dt of the current state: dir = -1 for the minimum over all
  * directions (DimensionalSplitLevelIntegrator::ComputeStableDt). */

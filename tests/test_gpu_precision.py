@@ -1,6 +1,7 @@
 """GPU tests of the fast FP64 and the mixed-precision flavours.
 
-fast FP64 ("fp64_fast"): per call within 1e-12 relative per cell of the
+fast FP64 ("fp64_fast") and double-float ("fp64_df"): per call within 1e-12
+relative per cell of the
 oracle (the tolerance stated for the plain FP64 path: FMA contraction and
 reordered divisions), with an absolute floor of 1e-12 x the component's
 max |value| for components that cross zero (momenta).
@@ -37,14 +38,15 @@ GRIDS = [
 ]
 
 
+@pytest.mark.parametrize("prec", ["fp64_fast", "fp64_df"])
 @pytest.mark.parametrize("rank,n,bc", GRIDS)
-def test_fast_fp64_sweeps_and_steps(fvs, orc, rank, n, bc):
+def test_fast_fp64_sweeps_and_steps(fvs, orc, rank, n, bc, prec):
     cons = workloads.random_state(tuple(reversed(n)), rank, seed=7 + rank, v=0.6)
     cons = cons.reshape([rank + 2] + [1] * (3 - rank) + list(reversed(n)))
     dx = [0.1, 0.07, 0.05][:rank]
     g = orc.Grid(rank, n, bc, dx)
     m = orc.method()
-    s = fvs.Solver(n, dx, bc, method=fvs.make_method(precision="fp64_fast"))
+    s = fvs.Solver(n, dx, bc, method=fvs.make_method(precision=prec))
     s.upload(cons)
     dt_ref = g.stable_dt(m, cons)
     assert s.ComputeStableDt(-1) == pytest.approx(dt_ref, rel=RTOL_FP64)
@@ -61,13 +63,14 @@ def test_fast_fp64_sweeps_and_steps(fvs, orc, rank, n, bc):
     s.close()
 
 
-def test_fast_fp64_octants_run(fvs, orc):
+@pytest.mark.parametrize("prec", ["fp64_fast", "fp64_df"])
+def test_fast_fp64_octants_run(fvs, orc, prec):
     n = 32
     cons = workloads.octants_3d(n, seed=5)
     dx = [1.0 / n] * 3
     g = orc.Grid(3, [n] * 3, [0, 0, 0], dx)
     ref, ref_dts, _ = g.run(orc.method(), cons, 0.8, 10.0, max_steps=4)
-    s = fvs.Solver([n] * 3, dx, "periodic", method=fvs.make_method(precision="fp64_fast"))
+    s = fvs.Solver([n] * 3, dx, "periodic", method=fvs.make_method(precision=prec))
     s.upload(cons)
     st, dts = s.run(cfl=0.8, t_end=10.0, max_steps=4, log_len=8)
     assert st.steps == 4
