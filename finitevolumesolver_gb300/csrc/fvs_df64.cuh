@@ -89,12 +89,14 @@ __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) { return a * b + c; 
 namespace fast {
 
 template <> struct Math<df64> {
-  // 1/a: the FP32 reciprocal refined by two Newton steps in double-float
-  // (y <- y + y (1 - a y)); each step doubles the correct bits (24 -> 48).
+  // 1/a: y = 1/a.hi rounded to nearest, the residual r = 1 - a y from FMAs
+  // (for a correctly rounded y, 1 - a.hi y is exact in FP32), and
+  // 1/a = y / (1 - r) = y (1 + r + r^2 + ...) with the correction y (r + r^2)
+  // in the low word: relative error ~ r^3 + 2^-48.
   static __device__ __forceinline__ df64 Rcp(df64 a) {
-    df64 y(__frcp_rn(a.hi), 0.0f);
-    y = y + y * (df64(1) - a * y);
-    return y + y * (df64(1) - a * y);
+    const float y = __frcp_rn(a.hi);
+    const float r = __fmaf_rn(-a.lo, y, __fmaf_rn(-a.hi, y, 1.0f));
+    return dfops::QuickTwoSum(y, __fmul_rn(y, __fmaf_rn(r, r, r)));
   }
   static __device__ __forceinline__ df64 Div(df64 a, df64 b) {
     // quotient from the reciprocal plus one residual correction
@@ -102,13 +104,15 @@ template <> struct Math<df64> {
     const df64 q = a * y;
     return q + (a - b * q) * y;
   }
-  // 1/sqrt(a), a > 0: the FP32 estimate refined by two Newton steps
-  // (y <- y + y (1 - a y^2) / 2).
+  // 1/sqrt(a), a > 0: y = rsqrt(a.hi), r = 1 - a y^2 in double-float, and
+  // 1/sqrt(a) = y (1 - r)^(-1/2) = y (1 + r/2 + 3 r^2/8 + ...); the
+  // correction goes to the low word.
   static __device__ __forceinline__ df64 Rsqrt(df64 a) {
-    df64 y(rsqrtf(a.hi), 0.0f);
-    const df64 half(0.5f, 0.0f);
-    y = y + (half * y) * (df64(1) - a * (y * y));
-    return y + (half * y) * (df64(1) - a * (y * y));
+    const float y = rsqrtf(a.hi);
+    const df64 t = df64(y, 0.0f) * df64(y, 0.0f);
+    const df64 r = df64(1) - a * t;
+    const float c = __fmaf_rn(__fmul_rn(0.375f, r.hi), r.hi, __fmul_rn(0.5f, r.hi));
+    return dfops::QuickTwoSum(y, __fmul_rn(y, c));
   }
   // sqrt(a) for a >= 0 (0 for a <= 0): s = a y and one correction
   // s + (a - s^2) y / 2.
