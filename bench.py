@@ -367,7 +367,7 @@ def report_amr(args, torch, fvs, workloads, peaks):
             "ms_per_coarse_step": ms / max(st.steps, 1), "cell_updates_per_s": rate,
             "restarts": st.restarts,
             "hbm_frac_algorithmic": rate * 64 / 1e9 / peaks["hbm_gbs"],
-            "launch_shapes_block_grid": cfg.tolist()}
+            "launch_block_grid_threads_per_row": cfg.tolist()}
         a.close()
     if "fp64_exact" in finals:
         parts_ref = h.split(finals["fp64_exact"])

@@ -469,12 +469,13 @@ class AmrSolver:
                                       C.byref(st)))
         return st, log[:min(log_len, st.steps)].copy()
 
-    def set_launch(self, level, dir, block, grid) -> None:
+    def set_launch(self, level, dir, block, grid, threads_per_row=1) -> None:
         _capi.check(lib().fvs_amr_set_launch(self._h, int(level), int(dir), int(block),
-                                             int(grid)))
+                                             int(grid), int(threads_per_row)))
 
     def autotune(self):
+        """Tuned [level][direction][block, grid, threads per row]."""
         import numpy as np
-        cfg = np.zeros((int(self.hier.nlevels), 2, 2), dtype=np.int32)
+        cfg = np.zeros((int(self.hier.nlevels), 2, 3), dtype=np.int32)
         _capi.check(lib().fvs_amr_autotune(self._h, cfg.ctypes.data))
         return cfg

@@ -127,7 +127,7 @@ def load() -> C.CDLL:
     L.fvs_amr_stream.argtypes = [_VP, P(_VP)]
     L.fvs_amr_stable_dt.argtypes = [_VP, _DP]
     L.fvs_amr_run.argtypes = [_VP, C.c_double, C.c_double, C.c_int, _DP, C.c_int, P(RunStats)]
-    L.fvs_amr_set_launch.argtypes = [_VP, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.fvs_amr_set_launch.argtypes = [_VP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
     L.fvs_amr_autotune.argtypes = [_VP, _VP]
     L.fvs_mlp_param_count.restype = C.c_int
     L.fvs_mlp_create.argtypes = [C.c_uint64, P(_VP)]

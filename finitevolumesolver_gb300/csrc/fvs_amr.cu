@@ -53,6 +53,9 @@ struct LevelHost {
   double* backup = nullptr;
   Row* rows[2] = {nullptr, nullptr};
   int32_t nrows[2] = {0, 0};
+  Seg* segs[2][kSplits] = {};
+  int32_t nsegs[2][kSplits] = {};
+  int split[2] = {0, 0};  // index into kSplitOf
   Cap* caps[2] = {nullptr, nullptr};
   Ghost* ghosts = nullptr;
   int32_t nghosts = 0;
@@ -70,7 +73,7 @@ struct LevelHost {
 
 std::mutex g_tune_mutex;
 struct Tuned {
-  int block, grid, occ;
+  int block, grid, occ, split;
 };
 std::map<std::string, Tuned> g_tuned;  // key -> launch shape
 
@@ -378,8 +381,37 @@ int Build(fvs_amr* a) {
     AMR_CUDA(a->Alloc(&Lv.B, n));
     AMR_CUDA(a->Alloc(&Lv.backup, n));
     for (int d = 0; d < 2; ++d) {
-      AMR_CUDA(a->Upload(&Lv.rows[d], rows_h[d][size_t(l)]));
-      AMR_CUDA(a->Upload(&Lv.caps[d], caps_flat[d][size_t(l)]));
+      const std::vector<Row>& R = rows_h[d][size_t(l)];
+      const std::vector<Cap>& flat = caps_flat[d][size_t(l)];
+      AMR_CUDA(a->Upload(&Lv.rows[d], R));
+      AMR_CUDA(a->Upload(&Lv.caps[d], flat));
+      // the rows split into 1, 2 or 4 segments (threads per row)
+      for (int si = 0; si < kSplits; ++si) {
+        std::vector<Seg> segs;
+        for (size_t r = 0; r < R.size(); ++r) {
+          const int nn = R[r].n;
+          const int parts = std::max(1, std::min(kSplitOf[si], nn));
+          const int32_t cb = r > 0 ? R[r - 1].cap_end : 0, ce = R[r].cap_end;
+          int32_t c = cb;
+          for (int k = 0; k < parts; ++k) {
+            Seg sg{};
+            sg.base = R[r].base;
+            sg.stride = R[r].stride;
+            sg.j0 = int32_t(int64_t(k) * nn / parts);
+            sg.j1 = int32_t(int64_t(k + 1) * nn / parts);
+            sg.cap_begin = c;
+            if (k + 1 < parts) {
+              while (c < ce && flat[size_t(c)].face < sg.j1) ++c;
+            } else {
+              c = ce;
+            }
+            sg.cap_end = c;
+            segs.push_back(sg);
+          }
+        }
+        Lv.nsegs[d][si] = int32_t(segs.size());
+        AMR_CUDA(a->Upload(&Lv.segs[d][si], segs));
+      }
     }
     AMR_CUDA(a->Upload(&Lv.ghosts, ghosts_h[size_t(l)]));
     Lv.nghosts = int32_t(ghosts_h[size_t(l)].size());
@@ -394,7 +426,7 @@ int Build(fvs_amr* a) {
       Lv.hist += std::to_string(kv.first.first) + "x" + std::to_string(kv.first.second) + ":" +
                  std::to_string(kv.second) + ",";
     for (int d = 0; d < 2; ++d)
-      Lv.grid[d] = std::max(1, std::min((Lv.nrows[d] + 127) / 128, a->sms * 4));
+      Lv.grid[d] = std::max(1, std::min((Lv.nsegs[d][0] + 127) / 128, a->sms * 4));
   }
   AMR_CUDA(a->Alloc(&a->reg, size_t(std::max(a->nslots, 1)) * 3 * kComp));
   AMR_CUDA(a->Upload(&a->signs, signs_h));
@@ -420,14 +452,14 @@ int Build(fvs_amr* a) {
 
 cudaError_t LaunchSweep(fvs_amr* a, int l, int d, const double* in, double* out,
                         double scale, const double* dt_ptr, unsigned long long* smax, int block,
-                        int grid, int occ) {
+                        int grid, int occ, int split) {
   const LevelHost& Lv = a->L[size_t(l)];
   PatchSweepArgs s{};
   s.in = in;
   s.out = out;
   s.ncells = int32_t(Lv.ncells);
-  s.rows = Lv.rows[d];
-  s.nrows = Lv.nrows[d];
+  s.segs = Lv.segs[d][split];
+  s.nsegs = Lv.nsegs[d][split];
   s.caps = Lv.caps[d];
   s.reg = a->reg;
   s.gamma = a->m.gamma;
@@ -505,7 +537,8 @@ cudaError_t AdvanceLevel(fvs_amr* a, int l, int parity, int sub, int& counter) {
     const int d = seq[k];
     if ((e = FillGhosts(a, l, bufs[cur])) != cudaSuccess) return e;
     if ((e = LaunchSweep(a, l, d, bufs[cur], bufs[1 - cur], 0.5 / double(1 << l), &a->ctrl->dt,
-                         &a->ctrl->smax_sweep[counter++], Lv.block[d], Lv.grid[d], Lv.occ[d])) !=
+                         &a->ctrl->smax_sweep[counter++], Lv.block[d], Lv.grid[d], Lv.occ[d],
+                         Lv.split[d])) !=
         cudaSuccess)
       return e;
     cur ^= 1;
@@ -779,14 +812,20 @@ int fvs_amr_run(fvs_amr* a, double cfl, double t_end, int max_steps, double* dt_
   return FVS_OK;
 }
 
-int fvs_amr_set_launch(fvs_amr* a, int level, int dir, int block, int grid) {
+int fvs_amr_set_launch(fvs_amr* a, int level, int dir, int block, int grid,
+                       int threads_per_row) {
   if (!a || level < 0 || level >= a->nlevels || dir < 0 || dir > 1)
     return Fail(FVS_ERR_INVALID, "bad level or direction");
   if (block != 32 && block != 64 && block != 128)
     return Fail(FVS_ERR_INVALID, "block must be 32, 64 or 128");
   if (grid < 1) return Fail(FVS_ERR_INVALID, "grid must be positive");
+  int si = -1;
+  for (int k = 0; k < kSplits; ++k)
+    if (kSplitOf[k] == threads_per_row) si = k;
+  if (si < 0) return Fail(FVS_ERR_INVALID, "threads per row must be 1, 2, 4 or 8");
   a->L[size_t(level)].block[dir] = block;
   a->L[size_t(level)].grid[dir] = grid;
+  a->L[size_t(level)].split[dir] = si;
   DropGraphs(a);
   return FVS_OK;
 }
@@ -811,40 +850,45 @@ int fvs_amr_autotune(fvs_amr* a, int32_t* configs) {
           Lv.block[d] = it->second.block;
           Lv.grid[d] = it->second.grid;
           Lv.occ[d] = it->second.occ;
+          Lv.split[d] = it->second.split;
           continue;
         }
       }
       float best = 1e30f;
-      Tuned bt{128, Lv.grid[d], 0};
+      Tuned bt{128, Lv.grid[d], 0, 0};
       const bool mixed = a->m.precision == FVS_MIXED;
-      for (int occ : {0, 5}) {
-        if (occ && !mixed) continue;
-        for (int block : {64, 128}) {
-          const int full = std::max(1, (Lv.nrows[d] + block - 1) / block);
-          for (int bps : {1, 2, 4, 8, 16, 64}) {
-            const int grid = std::min(full, a->sms * bps);
-            float sum = 0.f;
-            for (int rep = 0; rep < 3; ++rep) {
-              AMR_CUDA(cudaEventRecord(e0, a->stream));
-              AMR_CUDA(LaunchSweep(a, l, d, Lv.A, Lv.B, 0.5, a->tune_dt, &a->ctrl->smax_sweep[0],
-                                   block, grid, occ));
-              AMR_CUDA(cudaEventRecord(e1, a->stream));
-              AMR_CUDA(cudaEventSynchronize(e1));
-              float ms = 0.f;
-              AMR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-              if (rep > 0) sum += ms;
+      for (int si = 0; si < kSplits; ++si) {
+        if (si > 0 && Lv.nsegs[d][si] == Lv.nsegs[d][si - 1]) continue;  // rows too short
+        for (int occ : {0, 5}) {
+          if (occ && !mixed) continue;
+          for (int block : {64, 128}) {
+            const int full = std::max(1, (Lv.nsegs[d][si] + block - 1) / block);
+            for (int bps : {1, 2, 4, 8, 16, 64}) {
+              const int grid = std::min(full, a->sms * bps);
+              float sum = 0.f;
+              for (int rep = 0; rep < 3; ++rep) {
+                AMR_CUDA(cudaEventRecord(e0, a->stream));
+                AMR_CUDA(LaunchSweep(a, l, d, Lv.A, Lv.B, 0.5, a->tune_dt,
+                                     &a->ctrl->smax_sweep[0], block, grid, occ, si));
+                AMR_CUDA(cudaEventRecord(e1, a->stream));
+                AMR_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                AMR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                if (rep > 0) sum += ms;
+              }
+              if (sum < best) {
+                best = sum;
+                bt = {block, grid, occ, si};
+              }
+              if (grid == full) break;
             }
-            if (sum < best) {
-              best = sum;
-              bt = {block, grid, occ};
-            }
-            if (grid == full) break;
           }
         }
       }
       Lv.block[d] = bt.block;
       Lv.grid[d] = bt.grid;
       Lv.occ[d] = bt.occ;
+      Lv.split[d] = bt.split;
       std::lock_guard<std::mutex> lock(g_tune_mutex);
       g_tuned[key] = bt;
     }
@@ -854,8 +898,9 @@ int fvs_amr_autotune(fvs_amr* a, int32_t* configs) {
   if (configs)
     for (int l = 0; l < a->nlevels; ++l)
       for (int d = 0; d < 2; ++d) {
-        configs[(l * 2 + d) * 2] = a->L[size_t(l)].block[d];
-        configs[(l * 2 + d) * 2 + 1] = a->L[size_t(l)].grid[d];
+        configs[(l * 2 + d) * 3] = a->L[size_t(l)].block[d];
+        configs[(l * 2 + d) * 3 + 1] = a->L[size_t(l)].grid[d];
+        configs[(l * 2 + d) * 3 + 2] = kSplitOf[a->L[size_t(l)].split[d]];
       }
   DropGraphs(a);
   return FVS_OK;

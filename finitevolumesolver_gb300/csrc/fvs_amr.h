@@ -30,6 +30,21 @@ struct Row {
   int32_t cap_end;  // captures of this row: [previous row's cap_end, cap_end)
 };
 
+// A segment [j0, j1) of a row, the work item of a sweep thread: it computes
+// the faces j0..j1 and updates the cells j0..j1-1.  A row split into S
+// segments gives S threads per row (the autotuner picks S).  The segment's
+// register captures are caps[cap_begin, cap_end): faces in [j0, j1), and face
+// n for the row's last segment.
+struct Seg {
+  int32_t base;
+  int32_t stride;
+  int32_t j0, j1;
+  int32_t cap_begin, cap_end;
+};
+
+constexpr int kSplits = 4;  // rows are offered split into 1, 2, 4 or 8 segments
+constexpr int kSplitOf[kSplits] = {1, 2, 4, 8};
+
 // A flux-register capture: face `face` (0..n, between cells face-1 and face)
 // of a row adds dt_split * F to register entry `dst` (K doubles).
 struct Cap {
@@ -87,8 +102,8 @@ struct PatchSweepArgs {
   const double* in;
   double* out;
   int32_t ncells;  // component stride of the level
-  const Row* rows;
-  int32_t nrows;
+  const Seg* segs;
+  int32_t nsegs;
   const Cap* caps;
   double* reg;     // register entries of the captures
   double gamma;

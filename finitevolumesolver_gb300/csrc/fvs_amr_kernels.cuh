@@ -1,11 +1,11 @@
 // fvs_amr_kernels.cuh -- kernels of the batched AMR patch update (2-D).
 //
 // PatchSweepKernel: one persistent launch per level and sweep.  Each thread
-// takes rows of the level's row list (grid-stride) and marches along a row
+// takes segments of the level's rows (grid-stride) and marches along them
 // with the same three-cell window, policy arithmetic and update as the
-// uniform grid's SweepMarchKernel (fvs_sweep.cuh): for a row of n interior
-// cells it reads the ghosted cells -2..n+1 of the input buffer, computes the
-// n+1 faces, writes the n updated interior cells to the output buffer,
+// uniform grid's SweepMarchKernel (fvs_sweep.cuh): for a segment [j0, j1) of
+// a row it reads the ghosted cells j0-2..j1+1 of the input buffer, computes
+// the faces j0..j1, writes the updated cells j0..j1-1 to the output buffer,
 // accumulates dt_split * F into the flux-register entries of the row's
 // captured faces (each entry belongs to exactly one face, so no atomics and
 // a deterministic sum) and reduces the row's max signal speed for the
@@ -36,12 +36,12 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
   R smax = R(0);
   int status = 0;
   typename P::Stats stats;
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.nrows;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.nsegs;
        r += gridDim.x * blockDim.x) {
-    const Row w = a.rows[r];
-    int cap = r > 0 ? a.rows[r - 1].cap_end : 0;
+    const Seg w = a.segs[r];
+    int cap = w.cap_begin;
     int next_face = cap < w.cap_end ? a.caps[cap].face : INT_MAX;
-    const int n = w.n;
+    const int j0 = w.j0, j1 = w.j1;
     auto load = [&](double* u, int j) {
       const int64_t off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
 #pragma unroll
@@ -49,23 +49,23 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
     };
     double dm[K], dc[K], dp[K], dn[K];
     R cm[K], cc[K], cp[K];
-    load(dm, -2);
-    load(dc, -1);
-    load(dn, 0);
+    load(dm, j0 - 2);
+    load(dc, j0 - 1);
+    load(dn, j0);
     P::ToCell(cm, dm);
     P::ToCell(cc, dc);
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
     double F_prev[K];
-    for (int j = -1; j <= n; ++j) {
+    for (int j = j0 - 1; j <= j1; ++j) {
 #pragma unroll
       for (int c = 0; c < K; ++c) dp[c] = dn[c];
-      if (j + 2 <= n + 1) load(dn, j + 2);
+      if (j + 2 <= j1 + 1) load(dn, j + 2);
       P::ToCell(cp, dp);
       typename P::Rec recL, recR;
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
       const typename P::Wave wv = P::MakeWave(eq, cc, DIR);
-      if (j >= 0) {
+      if (j >= j0) {
         double F[K];
         const R s = P::Face(eq, F, recR_prev, recL, w_prev, wv, DIR, stats);
         smax = s > smax ? s : smax;
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
           ++cap;
           next_face = cap < w.cap_end ? a.caps[cap].face : INT_MAX;
         }
-        if (j > 0) {
+        if (j > j0) {
           const int64_t off = int64_t(w.base) + int64_t(j - 1 + kGhost) * w.stride;
 #pragma unroll
           for (int c = 0; c < K; ++c) {
@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
 template <template <int> class PT>
 cudaError_t LaunchPatchSweepT(int dir, const PatchSweepArgs& a, int grid, int block,
                               cudaStream_t s) {
-  if (a.nrows == 0) return cudaSuccess;
+  if (a.nsegs == 0) return cudaSuccess;
   if (dir == 0)
     PatchSweepKernel<0, PT><<<grid, block, 0, s>>>(a);
   else

@@ -348,14 +348,17 @@ int fvs_amr_stable_dt(fvs_amr* a, double* dt);
  * its start with cfl times 2^l times the failing level's dt. */
 int fvs_amr_run(fvs_amr* a, double cfl, double t_end, int max_steps, double* dt_log,
                 int log_len, fvs_run_stats* stats);
-/* Persistent launch shape (threads per block, blocks) of a level's sweeps
- * in direction dir. */
-int fvs_amr_set_launch(fvs_amr* a, int level, int dir, int block, int grid);
+/* Persistent launch shape of a level's sweeps in direction dir: threads per
+ * block, blocks, and threads per patch row (1, 2, 4 or 8: each row split into
+ * that many segments). */
+int fvs_amr_set_launch(fvs_amr* a, int level, int dir, int block, int grid, int threads_per_row);
 /* Times the sweeps of every level and direction for a set of launch shapes
- * and keeps the fastest; results are cached per process under the key
- * (precision, direction, the level's patch-size histogram), so hierarchies
- * with the same histogram reuse them.  configs (may be NULL) receives
- * [nlevels][2 directions][block, grid]. */
+ * (threads per row, threads per block, blocks, and for the mixed flavour a
+ * register/occupancy variant) and keeps the fastest; results are cached per
+ * process under the key (precision, direction, the level's patch-size
+ * histogram), so hierarchies with the same histogram reuse them.  configs
+ * (may be NULL) receives [nlevels][2 directions][block, grid, threads per
+ * row]. */
 int fvs_amr_autotune(fvs_amr* a, int32_t* configs);
 
 /* ---- Learned start value of the exact Riemann solver ------------------- */

@@ -63,17 +63,18 @@ def test_three_level_blast_bit_exact(fvs, orc, n0, target):
 def test_launch_shape_and_autotune_do_not_change_results(fvs, orc):
     h, cons = workloads.amr_blast_2d(64, 3, target=80, sizes=(8, 16))
     ref, _, _ = orc.amr_run(h, cons, 0.8, 10.0, max_steps=4)
-    a = fvs.AmrSolver(h)
-    for l in range(3):
-        for d in range(2):
-            a.set_launch(l, d, 32, 3)
-    a.upload(cons)
-    a.run(cfl=0.8, t_end=10.0, max_steps=4)
-    np.testing.assert_array_equal(a.download(), ref)
+    for tpr in (1, 2, 4, 8):
+        a = fvs.AmrSolver(h)
+        for l in range(3):
+            for d in range(2):
+                a.set_launch(l, d, 32, 3, tpr)
+        a.upload(cons)
+        a.run(cfl=0.8, t_end=10.0, max_steps=4)
+        np.testing.assert_array_equal(a.download(), ref)
     b = fvs.AmrSolver(h)
     b.upload(cons)
     cfg = b.autotune()
-    assert cfg.shape == (3, 2, 2) and (cfg > 0).all()
+    assert cfg.shape == (3, 2, 3) and (cfg > 0).all()
     b.run(cfl=0.8, t_end=10.0, max_steps=4)
     np.testing.assert_array_equal(b.download(), ref)
 
