@@ -197,18 +197,23 @@ def report_sod(args, torch, fvs, workloads):
     out = {"workload": "1D Sod shock tube, 1024 cells on [0, 1], transmissive, MUSCL-Hancock/"
                        "VanLeer + HLLE, CFL 0.8, t = 0.2", "oracle_steps": len(ref_dts),
            "flavours": {}}
-    for prec in ("fp64_exact", "fp64_fast", "mixed"):
+    for prec in ("fp64_exact", "fp64_fast", "fp64_df", "mixed"):
         s = fvs.Solver([n], [1.0 / n], "transmissive", method=fvs.make_method(precision=prec))
         s.upload(cons)
         t0 = time.perf_counter()
         st, dts = s.run(cfl=0.8, t_end=0.2, log_len=4096)
         el = time.perf_counter() - t0
         res = s.download()
-        rel = np.abs(res - ref) / np.maximum(np.abs(ref), 1e-300)
+        # |a - b| / (|b| + max |b| of the component): relative per cell, with
+        # the component's scale as the floor for values crossing zero (momentum)
+        scale = np.abs(ref).reshape(ref.shape[0], -1).max(axis=1)
+        scale = scale.reshape((-1,) + (1,) * (ref.ndim - 1))
+        rel = np.abs(res - ref) / (np.abs(ref) + scale)
         out["flavours"][prec] = {
             "steps": st.steps, "time": st.time, "wall_s": el,
             "same_dt_sequence": bool(len(dts) == len(ref_dts) and np.array_equal(dts, ref_dts)),
             "max_rel_diff_vs_oracle": float(rel.max()),
+            "l1_density_vs_oracle": float(np.abs(res[0] - ref[0]).mean()),
             "bit_identical": bool(np.array_equal(res, ref))}
         s.close()
     return out
