@@ -32,7 +32,7 @@ __all__ = ["PerfectGas", "FluxMethod", "HyperbolicPatchIntegrator", "CompleteFro
            "riemann_features", "tc_gemm_bf16", "AmrSolver"]
 
 FLUX_METHODS = {"muscl_hlle": 0, "hlle": 1, "godunov": 2, "muscl_godunov": 3, "hllem": 4,
-                "muscl_hllem": 5}
+                "muscl_hllem": 5, "muscl_char": 6, "muscl_prim": 7}
 LIMITERS = {"van_leer": 0, "minmod": 1, "none": 2}
 PRECISIONS = {"fp64_exact": 0, "fp64_fast": 1, "mixed": 2, "fp64_df": 3}
 GUESSES = {"mean": 0, "pvrs_tr": 1, "mlp": 2}
@@ -123,7 +123,10 @@ class PerfectGas:
 
 class FluxMethod:
     """fub::FluxMethod<Base> for Base in MusclHancock<PerfectGas, Hll<Einfeldt>,
-    Limiter> (the default), Hll<PerfectGas, Einfeldt>, Godunov<ExactRiemannSolver>."""
+    Limiter> (the default), Hll<PerfectGas, Einfeldt>, Godunov<ExactRiemannSolver>,
+    MusclHancock<PerfectGas, Godunov>, perfect_gas::Hllem, MusclHancock<PerfectGas,
+    Hllem>, perfect_gas::MusclHancockCharacteristic and perfect_gas::MusclHancockPrim
+    (names in FLUX_METHODS)."""
 
     def __init__(self, equation: PerfectGas, flux_method="muscl_hlle", limiter="van_leer",
                  precision="fp64_exact", **kw):
@@ -131,7 +134,7 @@ class FluxMethod:
         self.method = make_method(flux_method, limiter, precision, gamma=equation.gamma, **kw)
 
     def GetStencilWidth(self) -> int:
-        return 2 if self.method.flux_method in (0, 3, 5) else 1
+        return 1 if self.method.flux_method in (1, 2, 4) else 2
 
     def ComputeNumericFluxes(self, fluxes, face_box, states, cell_box, dt, dx, dir,
                              stream=None) -> None:

@@ -71,9 +71,15 @@ int64_t Volume(const fvs_box& b) {
 int CheckMethod(const fvs_method* m, int rank) {
   if (!m) return Fail(FVS_ERR_INVALID, "method is NULL");
   if (rank < 1 || rank > 3) return Fail(FVS_ERR_INVALID, "rank must be 1, 2 or 3");
-  if (m->flux_method < 0 || m->flux_method > 5)
+  if (m->flux_method < 0 || m->flux_method > 7)
     return Fail(FVS_ERR_INVALID, "unknown flux method");
   if (m->limiter < 0 || m->limiter > 2) return Fail(FVS_ERR_INVALID, "unknown limiter");
+  // the characteristic method limits with VanLeer's two-slope functor only,
+  // the primitive one with its own fixed limiter
+  if ((m->flux_method == FVS_MUSCL_CHAR || m->flux_method == FVS_MUSCL_PRIM) &&
+      m->limiter != FVS_VAN_LEER)
+    return Fail(FVS_ERR_UNSUPPORTED, "the characteristic and primitive reconstructions "
+                                     "take no limiter choice (FVS_VAN_LEER)");
   if (m->precision < 0 || m->precision > 3)
     return Fail(FVS_ERR_INVALID, "unknown precision");
   if (!(m->gamma > 1.0)) return Fail(FVS_ERR_INVALID, "gamma must exceed 1");
@@ -83,9 +89,24 @@ int CheckMethod(const fvs_method* m, int rank) {
 bool IsGodunov(int method) { return method == FVS_GODUNOV || method == FVS_MUSCL_GODUNOV; }
 
 int StencilWidth(int method) {
-  return (method == FVS_MUSCL_HLLE || method == FVS_MUSCL_GODUNOV || method == FVS_MUSCL_HLLEM)
-             ? 2
-             : 1;
+  return (method == FVS_HLLE || method == FVS_GODUNOV || method == FVS_HLLEM) ? 1 : 2;
+}
+
+// Methods whose face flux is Hllem: none, conservative, characteristic or
+// primitive reconstruction in front of it (-1 for the others).
+int HllemRecon(int method) {
+  switch (method) {
+  case FVS_HLLEM:
+    return 0;
+  case FVS_MUSCL_HLLEM:
+    return 1;
+  case FVS_MUSCL_CHAR:
+    return 2;
+  case FVS_MUSCL_PRIM:
+    return 3;
+  default:
+    return -1;
+  }
 }
 
 double BitsToDouble(unsigned long long b) {
@@ -300,8 +321,8 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
   a.stats_out = ctrl ? ctrl->newton : s->newton_words;
   if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
     return fvs::LaunchSweepGodunov(a, s->m.flux_method == FVS_MUSCL_GODUNOV, s->stream);
-  if (s->m.flux_method == FVS_HLLEM || s->m.flux_method == FVS_MUSCL_HLLEM)
-    return fvs::LaunchSweepHllem(a, s->m.flux_method == FVS_MUSCL_HLLEM, s->stream);
+  if (HllemRecon(s->m.flux_method) >= 0)
+    return fvs::LaunchSweepHllem(a, HllemRecon(s->m.flux_method), s->stream);
   switch (s->m.precision) {
   case FVS_FP64_EXACT:
     return fvs::LaunchSweepExact(a, s->stream);
@@ -329,14 +350,14 @@ cudaError_t LaunchStable(const fvs_solver* s, const double* in,
   }
   a.rank = s->g.rank;
   a.rule = s->g.dt_rule;
+  a.width = StencilWidth(s->m.flux_method);
   a.gamma = s->m.gamma;
   a.smax_out = smax_out;
   a.ctrl = ctrl;
   if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
     return fvs::LaunchStableDtGodunov(a, s->m.guess, s->m.max_iterations, s->m.tolerance,
                                       s->m.mlp_params, s->stream);
-  if (s->m.flux_method == FVS_HLLEM || s->m.flux_method == FVS_MUSCL_HLLEM)
-    return fvs::LaunchStableDtHllem(a, s->stream);
+  if (HllemRecon(s->m.flux_method) >= 0) return fvs::LaunchStableDtHllem(a, s->stream);
   switch (s->m.precision) {
   case FVS_FP64_EXACT:
     return fvs::LaunchStableDtExact(a, s->stream);
@@ -574,8 +595,7 @@ int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
   if (int r = CheckMethod(m, grid->rank)) return r;
   if ((m->flux_method == FVS_HLLE))
     return Fail(FVS_ERR_UNSUPPORTED, "the solver runs MUSCL-Hancock, HLLEM or Godunov fluxes");
-  if ((m->flux_method == FVS_HLLEM || m->flux_method == FVS_MUSCL_HLLEM) &&
-      m->precision != FVS_FP64_EXACT)
+  if (HllemRecon(m->flux_method) >= 0 && m->precision != FVS_FP64_EXACT)
     return Fail(FVS_ERR_UNSUPPORTED, "HLLEM runs in exact FP64");
   if (IsGodunov(m->flux_method) && m->precision != FVS_FP64_EXACT &&
       m->precision != FVS_FP64_FAST)

@@ -85,6 +85,7 @@ struct StableDtArgs {
   int rank;
   int bc[3];
   int rule;             // 0 all faces, 1 reference MFIter tiles of 8 in y/z
+  int width;            // stencil width of the method (windows of 2 width cells)
   double gamma;
   unsigned long long* smax_out;  // [rank]
   Control* ctrl;
@@ -96,7 +97,9 @@ void SetLastError(const std::string& msg);
 // Exact FP64 kernels (fvs_kernels_exact.cu, compiled with -fmad=false).
 cudaError_t LaunchSweepExact(const SweepArgs& a, cudaStream_t s);
 cudaError_t LaunchStableDtExact(const StableDtArgs& a, cudaStream_t s);
-cudaError_t LaunchSweepHllem(const SweepArgs& a, bool muscl, cudaStream_t s);
+// recon: 0 none (HLLEM), 1 conservative MUSCL-Hancock, 2 characteristic,
+// 3 primitive reconstruction
+cudaError_t LaunchSweepHllem(const SweepArgs& a, int recon, cudaStream_t s);
 cudaError_t LaunchSweepDf64(const SweepArgs& a, cudaStream_t s);
 cudaError_t LaunchStableDtDf64(const StableDtArgs& a, cudaStream_t s);
 cudaError_t LaunchStableDtHllem(const StableDtArgs& a, cudaStream_t s);

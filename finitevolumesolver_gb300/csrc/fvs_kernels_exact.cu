@@ -5,6 +5,7 @@
 // x86-64 build of the same formulas.
 #include "fvs_hllem.cuh"
 #include "fvs_internal.h"
+#include "fvs_recon_hllem.cuh"
 #include "fvs_physics_exact.cuh"
 #include "fvs_policy_exact.cuh"
 #include "fvs_stable.cuh"
@@ -23,15 +24,19 @@ cudaError_t LaunchSweepExact(const SweepArgs& a, cudaStream_t s) {
   }
 }
 
-// HLLEM (first order) and MUSCL-Hancock + HLLEM sweeps: the marching sweep
-// with Hllem<PerfectGas, Larrouturou> as the face flux and its stable-dt speed
-// as the CFL check (fvs_hllem.cuh).
+// HLLEM sweeps: the marching sweep with Hllem<PerfectGas, Larrouturou> as
+// the face flux and its stable-dt speed as the CFL check (fvs_hllem.cuh),
+// after one of four reconstructions: none (first order), MUSCL-Hancock of
+// the conservative variables, the characteristic or the primitive
+// reconstruction of the perfect gas (fvs_recon_hllem.cuh).
 template <int D> struct HllemWave {
   exact::Complete<D> q;
   int dir;
 };
 
-template <int D, bool kMuscl> struct HllemPolicyT {
+enum HllemRecon : int { kReconNone = 0, kReconCons = 1, kReconChar = 2, kReconPrim = 3 };
+
+template <int D, int kRecon> struct HllemPolicyT {
   using Real = double;
   static constexpr bool kWarpX = false;
   static constexpr int kMinBlocks = 1;
@@ -51,8 +56,19 @@ template <int D, bool kMuscl> struct HllemPolicyT {
                                                  const double* q0, const double* q1,
                                                  const double* q2, int limiter,
                                                  double lambda_half, int dir) {
-    if constexpr (kMuscl) {
+    if constexpr (kRecon == kReconCons) {
       exact::MusclPredictBoth<D>(eq, recL, recR, q0, q1, q2, limiter, lambda_half, dir);
+    } else if constexpr (kRecon == kReconChar || kRecon == kReconPrim) {
+      // dt/dx: lambda_half is (0.5 dt)/dx, so doubling it is exact
+      const double lambda = 2.0 * lambda_half;
+      exact::Complete<D> s0, s1, s2;
+      exact::CompleteFromCons<D>(eq, s0, q0);
+      exact::CompleteFromCons<D>(eq, s1, q1);
+      exact::CompleteFromCons<D>(eq, s2, q2);
+      if constexpr (kRecon == kReconChar)
+        exact::CharPredictBoth<D>(eq, recL, recR, s0, s1, s2, lambda, dir);
+      else
+        exact::PrimPredictBoth<D>(eq, recL, recR, s0, s1, s2, lambda, dir);
     } else {
       exact::CompleteFromCons<D>(eq, recL, q1);
       recR = recL;
@@ -76,17 +92,33 @@ template <int D, bool kMuscl> struct HllemPolicyT {
   }
 };
 
-template <int D> struct HllemPolicy : HllemPolicyT<D, false> {};
-template <int D> struct MusclHllemPolicy : HllemPolicyT<D, true> {};
+template <int D> struct HllemPolicy : HllemPolicyT<D, kReconNone> {};
+template <int D> struct MusclHllemPolicy : HllemPolicyT<D, kReconCons> {};
+template <int D> struct CharHllemPolicy : HllemPolicyT<D, kReconChar> {};
+template <int D> struct PrimHllemPolicy : HllemPolicyT<D, kReconPrim> {};
 
-cudaError_t LaunchSweepHllem(const SweepArgs& a, bool muscl, cudaStream_t s) {
+template <template <int> class PT>
+cudaError_t LaunchSweepRanks(const SweepArgs& a, cudaStream_t s) {
   switch (a.rank) {
   case 1:
-    return muscl ? LaunchSweepT<1, MusclHllemPolicy>(a, s) : LaunchSweepT<1, HllemPolicy>(a, s);
+    return LaunchSweepT<1, PT>(a, s);
   case 2:
-    return muscl ? LaunchSweepT<2, MusclHllemPolicy>(a, s) : LaunchSweepT<2, HllemPolicy>(a, s);
+    return LaunchSweepT<2, PT>(a, s);
   default:
-    return muscl ? LaunchSweepT<3, MusclHllemPolicy>(a, s) : LaunchSweepT<3, HllemPolicy>(a, s);
+    return LaunchSweepT<3, PT>(a, s);
+  }
+}
+
+cudaError_t LaunchSweepHllem(const SweepArgs& a, int recon, cudaStream_t s) {
+  switch (recon) {
+  case kReconCons:
+    return LaunchSweepRanks<MusclHllemPolicy>(a, s);
+  case kReconChar:
+    return LaunchSweepRanks<CharHllemPolicy>(a, s);
+  case kReconPrim:
+    return LaunchSweepRanks<PrimHllemPolicy>(a, s);
+  default:
+    return LaunchSweepRanks<HllemPolicy>(a, s);
   }
 }
 
@@ -150,7 +182,7 @@ __global__ void __launch_bounds__(256) StableDtKernel(StableDtArgs a) {
       const int faces = (idx[d] == nd - 1) ? 2 : 1;
       for (int fi = 0; fi < faces; ++fi) {
         const int f = idx[d] + fi;
-        if (a.rule == 1 && d > 0 && !ReferenceTileFace(f, nd, 2)) continue;
+        if (a.rule == 1 && d > 0 && !ReferenceTileFace(f, nd, a.width)) continue;
         if (fi == 1 && a.bc[d] == 0) continue;  // periodic: face n == face 0
         const int other = BcIndex(fi == 0 ? f - 1 : f, nd, a.bc[d]);
         int oidx[3] = {i, j, k};
@@ -252,7 +284,27 @@ __global__ void PatchFluxKernel(int method, int limiter, double gamma,
       exact::HllFlux<D>(eq, nf, L, R, dir);
     else
       exact::HllemFlux<D>(eq, nf, L, R, dir);
-  } else {  // MUSCL-Hancock + HLLE / HLLEM, stencil width 2
+  } else if (method == 6 || method == 7) {
+    // characteristic / primitive reconstruction + HLLEM, stencil width 2
+    // (MusclHancockCharacteristicMethod.hpp:303-317,
+    // MusclHancockPrimMethod.hpp:59-182), from the stored complete states
+    const double lambda = dt / dx;
+    exact::Complete<D> q[4];
+    for (int s = 0; s < 4; ++s) {
+      int c[3] = {f[0], f[1], f[2]};
+      c[dir] += s - 2;
+      q[s] = LoadComplete<D>(st, c[0], c[1], c[2]);
+    }
+    exact::Complete<D> a0, b0, a1, b1;
+    if (method == 6) {
+      exact::CharPredictBoth<D>(eq, a0, b0, q[0], q[1], q[2], lambda, dir);
+      exact::CharPredictBoth<D>(eq, a1, b1, q[1], q[2], q[3], lambda, dir);
+    } else {
+      exact::PrimPredictBoth<D>(eq, a0, b0, q[0], q[1], q[2], lambda, dir);
+      exact::PrimPredictBoth<D>(eq, a1, b1, q[1], q[2], q[3], lambda, dir);
+    }
+    exact::HllemFlux<D>(eq, nf, b0, a1, dir);
+  } else {  // MUSCL-Hancock (conservative) + HLLE / HLLEM, stencil width 2
     double u[4][K];
     for (int s = 0; s < 4; ++s) {
       int c[3] = {f[0], f[1], f[2]};
@@ -260,8 +312,8 @@ __global__ void PatchFluxKernel(int method, int limiter, double gamma,
 #pragma unroll
       for (int q = 0; q < K; ++q) u[s][q] = st(q, c[0], c[1], c[2]);
     }
-    const double lambda_half = 0.5 * dt / dx;
     exact::Complete<D> a0, b0, a1, b1;
+    const double lambda_half = 0.5 * dt / dx;
     exact::MusclPredictBoth<D>(eq, a0, b0, u[0], u[1], u[2], limiter,
                                lambda_half, dir);
     exact::MusclPredictBoth<D>(eq, a1, b1, u[1], u[2], u[3], limiter,
@@ -337,7 +389,7 @@ cudaError_t LaunchPatchStableDtExact(int method, int rank, double gamma,
                                      int window_rule, int dir,
                                      unsigned long long* smax, cudaStream_t s) {
   const int w = (method == 1 || method == 4) ? 1 : 2;
-  const int hllem = (method == 4 || method == 5) ? 1 : 0;
+  const int hllem = (method >= 4) ? 1 : 0;
   BoxDesc wbox = cbox;
   wbox.n[dir] -= (window_rule == 0) ? 2 * w : 2 * w - 1;
   if (wbox.n[dir] <= 0) return cudaSuccess;

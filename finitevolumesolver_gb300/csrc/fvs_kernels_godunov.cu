@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(256) GodunovStableDtKernel(StableDtArgs a, int
       const int faces = (idx[d] == nd - 1) ? 2 : 1;
       for (int fi = 0; fi < faces; ++fi) {
         const int f = idx[d] + fi;
-        if (a.rule == 1 && d > 0 && !ReferenceTileFaceT(f, nd, 1)) continue;
+        if (a.rule == 1 && d > 0 && !ReferenceTileFaceT(f, nd, a.width)) continue;
         if (fi == 1 && a.bc[d] == 0) continue;
         int oidx[3] = {idx[0], idx[1], idx[2]};
         oidx[d] = BcIndex(fi == 0 ? f - 1 : f, nd, a.bc[d]);

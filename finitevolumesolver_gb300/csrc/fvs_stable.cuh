@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(256) StableDtKernelT(StableDtArgs a) {
       const int faces = (idx[d] == nd - 1) ? 2 : 1;
       for (int fi = 0; fi < faces; ++fi) {
         const int f = idx[d] + fi;
-        if (a.rule == 1 && d > 0 && !ReferenceTileFaceT(f, nd, 2)) continue;
+        if (a.rule == 1 && d > 0 && !ReferenceTileFaceT(f, nd, a.width)) continue;
         if (fi == 1 && a.bc[d] == 0) continue;  // periodic: face n == face 0
         const int other = BcIndex(fi == 0 ? f - 1 : f, nd, a.bc[d]);
         int oidx[3] = {i, j, k};

@@ -48,7 +48,14 @@ typedef enum fvs_flux_method {
   FVS_GODUNOV = 2,      /* Godunov<PerfectGas, ExactRiemannSolver> */
   FVS_MUSCL_GODUNOV = 3, /* MusclHancock<PerfectGas, Godunov<Exact>, Limiter> */
   FVS_HLLEM = 4,        /* perfect_gas::Hllem<PerfectGas, Larrouturou = true> */
-  FVS_MUSCL_HLLEM = 5   /* MusclHancock<PerfectGas, Hllem, Limiter> (exact FP64) */
+  FVS_MUSCL_HLLEM = 5,  /* MusclHancock<PerfectGas, Hllem, Limiter> (exact FP64) */
+  FVS_MUSCL_CHAR = 6,   /* perfect_gas::MusclHancockCharacteristic<Rank>: characteristic
+                           reconstruction + Hllem (exact FP64, van Leer only);
+                           src/equations/perfect_gas/MusclHancockCharacteristicMethod.hpp */
+  FVS_MUSCL_PRIM = 7    /* perfect_gas::MusclHancockPrim<Dim>: primitive reconstruction
+                           with its own limiter + Hllem (exact FP64; limiter must be
+                           FVS_VAN_LEER, the default);
+                           src/equations/perfect_gas/MusclHancockPrimMethod.hpp */
 } fvs_flux_method;
 
 typedef enum fvs_limiter {

@@ -25,7 +25,8 @@ using namespace fvs_oracle;
 extern "C" {
 // Method description shared with the Python test helpers.
 struct orc_method {
-  int32_t method;   // kMusclHlle, kHlle, kGodunov, kMusclGodunov, kHllem, kMusclHllem
+  int32_t method;   // kMusclHlle, kHlle, kGodunov, kMusclGodunov, kHllem, kMusclHllem,
+                    // kMusclChar, kMusclPrim
   int32_t limiter;  // kVanLeer, kMinMod, kNoLimiter
   int32_t guess;    // kGuessMean, kGuessPvrsTr
   int32_t max_iterations;
@@ -78,7 +79,7 @@ void LoadCons(double* u, const BoxView& v, int i, int j, int k) {
 inline void Shift(int* idx, int dir, int s) { idx[dir] += s; }
 
 int StencilWidth(int method) {
-  return (method == kMusclHlle || method == kMusclGodunov || method == kMusclHllem) ? 2 : 1;
+  return (method == kHlle || method == kGodunov || method == kHllem) ? 1 : 2;
 }
 
 // The numeric flux of one face from the 2w cells of its stencil.
@@ -106,6 +107,23 @@ void FaceFlux(const Gas& eq, const orc_method& m, double* nf,
   if (m.method == kGodunov) {
     int it = GodunovFlux<D>(eq, nf, st[0], st[1], dir, opt, 0.0, converged);
     if (iters) *iters = it;
+    return;
+  }
+  if (m.method == kMusclChar || m.method == kMusclPrim) {
+    // MusclHancockCharacteristic / MusclHancockPrim: reconstruct the two
+    // inner cells, then Hllem (MusclHancockCharacteristicMethod.hpp:303-317,
+    // MusclHancockPrimMethod.hpp:59-182); the stable dt is Hllem's on the
+    // inner pair (:354-358, :35-40).
+    const double lambda = dt / dx;
+    Complete<D> rec0, rec1;
+    if (m.method == kMusclChar) {
+      CharPredict<D>(eq, rec0, st, lambda, dir, 1.0);
+      CharPredict<D>(eq, rec1, st + 1, lambda, dir, -1.0);
+    } else {
+      PrimPredict<D>(eq, rec0, st, lambda, dir, +1);
+      PrimPredict<D>(eq, rec1, st + 1, lambda, dir, -1);
+    }
+    HllemFlux<D>(eq, nf, rec0, rec1, dir);
     return;
   }
   const double lambda_half = 0.5 * dt / dx;
@@ -139,7 +157,9 @@ double WindowDt(const Gas& eq, const orc_method& m, const Complete<D>* st,
     opt.max_iterations = m.max_iterations;
     return GodunovStableDt<D>(eq, L, R, dx, dir, opt);
   }
-  if (m.method == kHllem || m.method == kMusclHllem) return HllemStableDt<D>(eq, L, R, dx, dir);
+  if (m.method == kHllem || m.method == kMusclHllem || m.method == kMusclChar ||
+      m.method == kMusclPrim)
+    return HllemStableDt<D>(eq, L, R, dx, dir);
   return HllStableDt<D>(eq, L, R, dx, dir);
 }
 

@@ -469,13 +469,130 @@ inline double HllemStableDt(const Gas& eq, const Complete<D>& L, const Complete<
   return dx / maxS;
 }
 
+// MusclHancockCharacteristic<Rank>: one side of the characteristic
+// reconstruction, array path (src/equations/perfect_gas/
+// MusclHancockCharacteristicMethod.hpp:51-64 ComputeAmplitudes, :77-85
+// Recombine, :108-128 ComputeSlopes, :170-180 DoTimeStep, :235-256
+// Reconstruct; src/equations/PerfectGas.cpp:160-174 CompleteFromPrim).  s[0..2] are the
+// cell's left neighbour, the cell and its right neighbour; sign = +1 gives
+// the state at the cell's right face ("is_right_side" 0), -1 at its left
+// face.  Primitive velocities are three-vectors (zero beyond D) indexed by
+// ix, iy = (ix+1)%3, iz = (iy+1)%3, as the reference's Primitives are.
+// The slopes of the five amplitudes are limited with VanLeer's functor
+// (MusclHancockMethod.hpp:137-149), the only limiter the method accepts.
+template <int D>
+inline void CharPredict(const Gas& eq, Complete<D>& rec, const Complete<D>* s,
+                        double lambda, int ix, double sign) {
+  const int iy = (ix + 1) % 3;
+  const int iz = (iy + 1) % 3;
+  const Complete<D>& q = s[1];
+  const double rho = q.rho;
+  const double u = q.m[ix] / rho;
+  const double c = q.c;
+  const double rhoc = rho * c;
+  const double ooc2 = 1.0 / (c * c);
+  double v[3][3];
+  for (int k = 0; k < 3; ++k)
+    for (int d = 0; d < 3; ++d) v[k][d] = d < D ? s[k].m[d] / s[k].rho : 0.0;
+  double amp[2][5];
+  for (int h = 0; h < 2; ++h) {
+    const Complete<D>& l = s[h];
+    const Complete<D>& r = s[h + 1];
+    const double dp = r.p - l.p;
+    const double du = v[h + 1][ix] - v[h][ix];
+    const double drho = r.rho - l.rho;
+    amp[h][0] = dp - rhoc * du;    // minus
+    amp[h][1] = drho - ooc2 * dp;  // zero
+    amp[h][2] = dp + rhoc * du;    // plus
+    amp[h][3] = v[h + 1][iy] - v[h][iy];
+    amp[h][4] = v[h + 1][iz] - v[h][iz];
+  }
+  double slope[5];
+  for (int k = 0; k < 5; ++k) slope[k] = VanLeer(amp[0][k], amp[1][k]);
+  const double minus = sign * 0.5 * slope[0] * (1.0 - sign * lambda * (u - c));
+  const double zero = sign * 0.5 * slope[1] * (1.0 - sign * lambda * u);
+  const double plus = sign * 0.5 * slope[2] * (1.0 - sign * lambda * (u + c));
+  const double dv = sign * 0.5 * slope[3] * (1.0 - sign * lambda * u);
+  const double dw = sign * 0.5 * slope[4] * (1.0 - sign * lambda * u);
+  double dvel[3];
+  const double dpres = 0.5 * (minus + plus);
+  const double drho = ooc2 * dpres + zero;
+  dvel[ix] = 0.5 * (plus - minus) / rhoc;
+  dvel[iy] = dv;
+  dvel[iz] = dw;
+  const double w_rho = drho + rho;
+  const double w_p = dpres + q.p;
+  rec.rho = w_rho;
+  for (int d = 0; d < D; ++d) rec.m[d] = w_rho * (dvel[d] + q.m[d] / q.rho);
+  rec.p = w_p;
+  const double e_kin = KineticEnergy<D>(rec.rho, rec.m);
+  rec.E = e_kin + w_p * eq.gamma_minus_1_inv;
+  rec.c = std::sqrt(eq.gamma * rec.p / rec.rho);
+}
+
+// The slope limiter of MusclHancockPrim<Dim>::ComputeNumericFlux
+// (src/equations/perfect_gas/MusclHancockPrimMethod.hpp:63-77): the van
+// Leer function of the smaller of the two one-sided ratios to the central
+// difference, times the central difference; flat below |dq| = 1e-12.
+inline double PrimLimiter(double qL, double qM, double qR) {
+  const double delta_q = 0.5 * (qR - qL);
+  const bool is_relevant = std::abs(delta_q) > 1e-12;
+  const double dq = is_relevant ? delta_q : 1.0;
+  const double rL = is_relevant ? (qM - qL) / dq : 0.0;
+  const double rR = is_relevant ? (qR - qM) / dq : 0.0;
+  const bool is_positive = rL > 0.0 && rR > 0.0;
+  const double r = is_positive ? PMin(rL, rR) : 0.0;
+  const double r_1 = 2.0 * r / (1.0 + r);
+  const double r_2 = 0.5 * (r + 1.0);
+  const double sigma = r < 1.0 ? r_1 : r_2;
+  return sigma * delta_q;
+}
+
+// MusclHancockPrim<Dim>: the Hancock-predicted primitive state of the cell
+// s[1] at its right face (side = +1, the "_l" formulas) or its left face
+// (side = -1, the "_r" formulas), array path
+// (src/equations/perfect_gas/MusclHancockPrimMethod.hpp:78-175).
+template <int D>
+inline void PrimPredict(const Gas& eq, Complete<D>& rec, const Complete<D>* s,
+                        double lambda, int d, int side) {
+  double u[3][D];
+  for (int k = 0; k < 3; ++k)
+    for (int i = 0; i < D; ++i) u[k][i] = s[k].m[i] / s[k].rho;
+  const double rho = s[1].rho, p = s[1].p, a = s[1].c;
+  const double drho = PrimLimiter(s[0].rho, rho, s[2].rho);
+  const double dp = PrimLimiter(s[0].p, p, s[2].p);
+  double du[D];
+  for (int i = 0; i < D; ++i) du[i] = PrimLimiter(u[0][i], u[1][i], u[2][i]);
+  const double* ul = u[1];
+  double rec_rho, rec_p, rec_u[D];
+  if (side > 0) {
+    rec_rho = rho + 0.5 * (drho - lambda * (ul[d] * drho + rho * du[d]));
+    rec_p = p + 0.5 * (dp - lambda * (rho * a * a * du[d] + ul[d] * dp));
+    for (int i = 0; i < D; ++i)
+      rec_u[i] = ul[i] + 0.5 * (du[i] - lambda * (ul[d] * du[i]));
+  } else {
+    rec_rho = rho - 0.5 * (drho + lambda * (ul[d] * drho + rho * du[d]));
+    rec_p = p - 0.5 * (dp + lambda * (rho * a * a * du[d] + ul[d] * dp));
+    for (int i = 0; i < D; ++i)
+      rec_u[i] = ul[i] - 0.5 * (du[i] + lambda * (ul[d] * du[i]));
+  }
+  rec_u[d] -= 0.5 * lambda * dp / rho;
+  rec.rho = rec_rho;
+  for (int i = 0; i < D; ++i) rec.m[i] = rec_rho * rec_u[i];
+  rec.p = rec_p;
+  rec.c = std::sqrt(eq.gamma * rec_p / rec_rho);
+  rec.E = 0.5 * rec_rho * SquaredNorm<D>(rec_u) + rec_p * eq.gamma_minus_1_inv;
+}
+
 enum Method : int {
   kMusclHlle = 0,
   kHlle = 1,
   kGodunov = 2,
   kMusclGodunov = 3,
-  kHllem = 4,      // Hllem<PerfectGas, Larrouturou>
-  kMusclHllem = 5  // MusclHancock<PerfectGas, Hllem, Limiter>
+  kHllem = 4,       // Hllem<PerfectGas, Larrouturou>
+  kMusclHllem = 5,  // MusclHancock<PerfectGas, Hllem, Limiter>
+  kMusclChar = 6,   // perfect_gas::MusclHancockCharacteristic (HLLEM base)
+  kMusclPrim = 7    // perfect_gas::MusclHancockPrim (HLLEM base)
 };
 
 }  // namespace fvs_oracle
