@@ -95,7 +95,10 @@ template <class Adapter> class FluxMethod {
   }
 
   int GetStencilWidth() const {
-    return (m_.flux_method == FVS_MUSCL_HLLE || m_.flux_method == FVS_MUSCL_GODUNOV) ? 2 : 1;
+    return (m_.flux_method == FVS_HLLE || m_.flux_method == FVS_GODUNOV ||
+            m_.flux_method == FVS_HLLEM)
+               ? 1
+               : 2;
   }
 
   // min over the level's patches of FluxMethod::ComputeStableDt (simd window
