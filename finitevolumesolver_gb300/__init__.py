@@ -215,6 +215,10 @@ class Solver:
         _capi.check(lib().fvs_solver_download(self._h, a.ctypes.data))
         return a
 
+    def write_plotfile(self, directory) -> None:
+        """AMReX plotfile of the current state (fub::amrex::PlotfileOutput)."""
+        _capi.check(lib().fvs_solver_write_plotfile(self._h, str(directory).encode()))
+
     def state_device_ptr(self) -> int:
         p = C.c_void_p()
         _capi.check(lib().fvs_solver_state_device(self._h, C.byref(p)))
@@ -442,6 +446,10 @@ class AmrSolver:
         a = np.empty(self.size, dtype=np.float64)
         _capi.check(lib().fvs_amr_download(self._h, a.ctypes.data))
         return a
+
+    def write_plotfile(self, directory) -> None:
+        """AMReX plotfile of every level (fub::amrex::PlotfileOutput)."""
+        _capi.check(lib().fvs_amr_write_plotfile(self._h, str(directory).encode()))
 
     def info(self):
         import numpy as np

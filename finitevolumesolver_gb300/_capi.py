@@ -20,6 +20,7 @@ FVS_ERR_DT_TOO_LARGE = 3
 FVS_ERR_UNSUPPORTED = 4
 FVS_ERR_NO_DEVICE = 5
 FVS_ERR_STATE = 6
+FVS_ERR_IO = 7
 
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "DT_TOO_LARGE", 4: "UNSUPPORTED",
                 5: "NO_DEVICE", 6: "STATE"}
@@ -100,6 +101,7 @@ def load() -> C.CDLL:
     L.fvs_solver_destroy.argtypes = [_VP]
     L.fvs_solver_upload.argtypes = [_VP, _VP]
     L.fvs_solver_download.argtypes = [_VP, _VP]
+    L.fvs_solver_write_plotfile.argtypes = [_VP, C.c_char_p]
     L.fvs_solver_state_device.argtypes = [_VP, P(_VP)]
     L.fvs_solver_set_tiling.argtypes = [_VP, C.c_int]
     L.fvs_solver_autotune.argtypes = [_VP, P(C.c_int)]
@@ -123,6 +125,7 @@ def load() -> C.CDLL:
     L.fvs_amr_destroy.argtypes = [_VP]
     L.fvs_amr_upload.argtypes = [_VP, _VP]
     L.fvs_amr_download.argtypes = [_VP, _VP]
+    L.fvs_amr_write_plotfile.argtypes = [_VP, C.c_char_p]
     L.fvs_amr_info.argtypes = [_VP, _VP, _VP, _VP]
     L.fvs_amr_stream.argtypes = [_VP, P(_VP)]
     L.fvs_amr_stable_dt.argtypes = [_VP, _DP]

@@ -37,6 +37,7 @@ UNITS = [
     ("fvs_amr.cu", []),
     ("fvs_amr_exact.cu", ["-fmad=false"]),
     ("fvs_amr_fast.cu", []),
+    ("fvs_plotfile.cpp", []),
 ]
 
 

@@ -19,6 +19,7 @@
 #include "../../include/fvs_gpu.h"
 #include "fvs_amr.h"
 #include "fvs_internal.h"
+#include "fvs_plotfile.h"
 
 #include <algorithm>
 #include <cmath>
@@ -719,6 +720,76 @@ int fvs_amr_download(fvs_amr* a, double* host) {
       for (int j = 0; j < P.n[1]; ++j)
         for (int i = 0; i < P.n[0]; ++i)
           host[off++] = v[size_t(c * N + a->SI(int(p), P.lo[0] + i, P.lo[1] + j))];
+  }
+  return FVS_OK;
+}
+
+int fvs_amr_write_plotfile(fvs_amr* a, const char* dir) {
+  if (!a || !dir || !*dir) return Fail(FVS_ERR_INVALID, "NULL argument");
+  fvs::plot::Plotfile pf;
+  pf.dir = dir;
+  pf.dim = 2;
+  pf.time = a->t;
+  pf.vars = fvs::plot::CompleteNames(2);
+  for (int d = 0; d < 2; ++d) pf.prob_hi[d] = a->n0[d] * a->dx0;
+  std::vector<std::vector<int>> members(static_cast<size_t>(a->nlevels));
+  for (size_t p = 0; p < a->patches.size(); ++p)
+    members[size_t(a->patches[p].level)].push_back(int(p));
+  for (int l = 0; l < a->nlevels; ++l) {
+    const LevelHost& LH = a->L[size_t(l)];
+    fvs::plot::Level L{};
+    for (int d = 0; d < 3; ++d) {
+      L.domain.lo[d] = 0;
+      L.domain.hi[d] = d < 2 ? LH.n[d] - 1 : 0;
+      L.dx[d] = d < 2 ? LH.dx : 1.0;
+    }
+    L.step = static_cast<int>(a->cycle << l);
+    L.ratio_to_next = 2;
+    for (int p : members[size_t(l)]) {
+      const PatchHost& P = a->patches[size_t(p)];
+      fvs::plot::Box b{};
+      for (int d = 0; d < 2; ++d) {
+        b.lo[d] = P.lo[d];
+        b.hi[d] = P.lo[d] + P.n[d] - 1;
+      }
+      L.boxes.push_back(b);
+    }
+    pf.levels.push_back(L);
+  }
+  if (std::string e = fvs::plot::WriteHeader(pf); !e.empty()) return Fail(FVS_ERR_IO, e);
+  constexpr int kOut = 6;  // Complete components in 2-D
+  for (int l = 0; l < a->nlevels; ++l) {
+    const LevelHost& LH = a->L[size_t(l)];
+    const int64_t N = LH.ncells;
+    double* dq = nullptr;
+    AMR_CUDA(cudaMallocAsync(&dq, size_t(N) * kOut * sizeof(double), a->stream));
+    // Complete state of every storage cell of the level (the level arrays are
+    // component-major over N cells, read here as an N x 1 x 1 box)
+    fvs::BoxDesc box{{0, 0, 0}, {static_cast<int>(N), 1, 1}};
+    cudaError_t ce =
+        fvs::LaunchPatchCompleteFromCons(2, a->m.gamma, dq, box, LH.A, box, box, a->stream);
+    std::vector<double> q(size_t(N) * kOut);
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(q.data(), dq, q.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                           a->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(a->stream);
+    cudaFreeAsync(dq, a->stream);
+    if (ce != cudaSuccess) return Fail(FVS_ERR_CUDA, cudaGetErrorString(ce));
+    fvs::plot::LevelWriter w(pf, l);
+    std::vector<double> fab;
+    int bi = 0;
+    for (int p : members[size_t(l)]) {
+      const PatchHost& P = a->patches[size_t(p)];
+      const int64_t n = int64_t(P.n[0]) * P.n[1];
+      fab.resize(size_t(n) * kOut);
+      size_t off = 0;
+      for (int c = 0; c < kOut; ++c)
+        for (int j = 0; j < P.n[1]; ++j)
+          for (int i = 0; i < P.n[0]; ++i)
+            fab[off++] = q[size_t(c * N + a->SI(p, P.lo[0] + i, P.lo[1] + j))];
+      if (std::string e = w.Append(bi++, fab.data()); !e.empty()) return Fail(FVS_ERR_IO, e);
+    }
+    if (std::string e = w.Finish(); !e.empty()) return Fail(FVS_ERR_IO, e);
   }
   return FVS_OK;
 }

@@ -4,7 +4,9 @@
 #include "../../include/fvs_gpu.h"
 #include "fvs_cutcell.h"
 #include "fvs_internal.h"
+#include "fvs_plotfile.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -658,6 +660,88 @@ int fvs_solver_download(fvs_solver* s, double* cons_host) {
   FVS_CUDA(cudaMemcpyAsync(cons_host, s->buf[s->cur], bytes, cudaMemcpyDeviceToHost,
                            s->stream));
   FVS_CUDA(cudaStreamSynchronize(s->stream));
+  return FVS_OK;
+}
+
+int fvs_solver_write_plotfile(fvs_solver* s, const char* dir) {
+  if (!s || !dir || !*dir) return Fail(FVS_ERR_INVALID, "NULL argument");
+  const int rank = s->g.rank;
+  fvs::plot::Plotfile pf;
+  pf.dir = dir;
+  pf.dim = rank;
+  pf.time = s->t;
+  pf.vars = fvs::plot::CompleteNames(rank);
+  if (s->cc) {
+    pf.vars.push_back("Boundary_X");
+    pf.vars.push_back("Boundary_Y");
+    pf.vars.push_back("vfrac");
+  }
+  const int ncomp = static_cast<int>(pf.vars.size());
+  fvs::plot::Level L{};
+  for (int d = 0; d < 3; ++d) {
+    L.domain.lo[d] = 0;
+    L.domain.hi[d] = s->g.n[d] - 1;
+    L.dx[d] = d < rank ? s->g.dx[d] : 1.0;
+    pf.prob_hi[d] = d < rank ? s->g.n[d] * s->g.dx[d] : 1.0;
+  }
+  L.step = static_cast<int>(s->cycle);
+  L.ratio_to_next = 2;
+  // slabs of the slowest direction, at most 2^21 cells each
+  const int slow = rank - 1;
+  const int64_t plane = s->cells / s->g.n[slow];
+  const int per = static_cast<int>(std::max<int64_t>(
+      1, std::min<int64_t>(s->g.n[slow], (int64_t(1) << 21) / plane)));
+  for (int z0 = 0; z0 < s->g.n[slow]; z0 += per) {
+    fvs::plot::Box b = L.domain;
+    b.lo[slow] = z0;
+    b.hi[slow] = std::min(s->g.n[slow] - 1, z0 + per - 1);
+    L.boxes.push_back(b);
+  }
+  pf.levels.push_back(L);
+  if (std::string e = fvs::plot::WriteHeader(pf); !e.empty()) return Fail(FVS_ERR_IO, e);
+  if (int r = CheckDevice()) return r;
+  const int64_t max_cells = plane * per;
+  const size_t bytes = size_t(max_cells) * size_t(ncomp) * sizeof(double);
+  double* dbuf = nullptr;
+  double* hbuf = nullptr;
+  FVS_CUDA(cudaMallocAsync(&dbuf, bytes, s->stream));
+  if (cudaMallocHost(&hbuf, bytes) != cudaSuccess) {
+    cudaFreeAsync(dbuf, s->stream);
+    return Fail(FVS_ERR_CUDA, "cudaMallocHost failed for the plotfile buffer");
+  }
+  fvs::plot::LevelWriter w(pf, 0);
+  std::string err;
+  cudaError_t ce = cudaSuccess;
+  const double* cons = s->buf[s->cur];
+  for (size_t bi = 0; bi < pf.levels[0].boxes.size() && err.empty() && ce == cudaSuccess;
+       ++bi) {
+    const fvs::plot::Box& b = pf.levels[0].boxes[bi];
+    const int64_t n = b.Cells(3);
+    if (s->cc) {
+      ce = fvs::LaunchCutCellPlotData(s->ccg, cons, s->m.gamma, b.lo[1], b.hi[1] - b.lo[1] + 1,
+                                      dbuf, s->stream);
+    } else {
+      fvs::BoxDesc q{}, u{};
+      for (int d = 0; d < 3; ++d) {
+        q.lo[d] = b.lo[d];
+        q.n[d] = b.hi[d] - b.lo[d] + 1;
+        u.lo[d] = 0;
+        u.n[d] = s->g.n[d];
+      }
+      ce = fvs::LaunchPatchCompleteFromCons(rank, s->m.gamma, dbuf, q, cons, u, q, s->stream);
+    }
+    if (ce == cudaSuccess)
+      ce = cudaMemcpyAsync(hbuf, dbuf, size_t(n) * size_t(ncomp) * sizeof(double),
+                           cudaMemcpyDeviceToHost, s->stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(s->stream);
+    if (ce == cudaSuccess) err = w.Append(static_cast<int>(bi), hbuf);
+  }
+  if (err.empty() && ce == cudaSuccess) err = w.Finish();
+  cudaFreeAsync(dbuf, s->stream);
+  cudaStreamSynchronize(s->stream);
+  cudaFreeHost(hbuf);
+  if (ce != cudaSuccess) return Fail(FVS_ERR_CUDA, cudaGetErrorString(ce));
+  if (!err.empty()) return Fail(FVS_ERR_IO, err);
   return FVS_OK;
 }
 

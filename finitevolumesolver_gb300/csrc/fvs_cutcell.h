@@ -78,6 +78,10 @@ struct CcSweepArgs {
 
 cudaError_t LaunchCutCellGeometry(const CcGeomArgs& a, const CcGeom& g, cudaStream_t s);
 cudaError_t LaunchCutCellReferenceStates(const CcStateArgs& a, cudaStream_t s);
+// Plotfile components of rows [j0, j0 + rows): masked Complete (6),
+// Boundary_X, Boundary_Y, vfrac; [9][rows][nx].
+cudaError_t LaunchCutCellPlotData(const CcGeom& g, const double* cons, double gamma, int j0,
+                                  int rows, double* out, cudaStream_t s);
 // Fast FP64 (precision 1) and mixed (precision 2) flavours of the KBN kernels.
 cudaError_t LaunchCutCellReferenceStatesT(int precision, const CcStateArgs& a, cudaStream_t s);
 cudaError_t LaunchCutCellSweepT(int precision, const CcSweepArgs& a, cudaStream_t s);

@@ -177,4 +177,51 @@ cudaError_t LaunchCutCellStableDt(const CcStateArgs& a, unsigned long long* smax
   return cc::LaunchKbnStableDt<double>(a, smax_out, ctrl, s);
 }
 
+namespace cc {
+
+// Plotfile data of rows [j0, j0 + rows) of the cut-cell grid, component-major
+// over the nx x rows box: the Complete state masked by alpha > 0
+// (include/fub/AMReX/cutcell/Reconstruction.hpp:76-157), Boundary_X and
+// Boundary_Y (AMReX's boundary normal of cut cells, 0 < alpha < 1, the
+// negative of fub's GetBoundaryNormal, src/CutCellData.cpp:90-105; 0
+// elsewhere), and vfrac, the components the reference's cut-cell
+// WritePlotFile (include/fub/AMReX/cutcell/PatchHierarchy.hpp:265-314) and
+// AMReX's EB plotfile writer put out.
+__global__ void PlotDataKernel(CcGeom g, const double* __restrict__ in, double gamma, int j0,
+                               int rows, double* __restrict__ out) {
+  const int64_t n = int64_t(g.nx) * rows;
+  const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (id >= n) return;
+  const int i = static_cast<int>(id % g.nx);
+  const int j = j0 + static_cast<int>(id / g.nx);
+  const int64_t cs = int64_t(g.nx) * g.ny;
+  const int64_t cell = int64_t(j) * g.nx + i;
+  double u[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) u[c] = in[c * cs + cell];
+  const int64_t gi = g.CellIndex(i, j);
+  const double alpha = g.alpha[gi];
+  const GasT<double> eq = MakeGasT<double>(gamma);
+  C2T<double> q;
+  CompleteMasked(eq, q, u, alpha > 0.0);
+  const bool cut = alpha > 0.0 && alpha < 1.0;
+  const int64_t gc = int64_t(g.NX()) * g.NY();
+  const double v[9] = {q.rho, q.m[0], q.m[1], q.E, q.p, q.c,
+                       cut ? -g.normal[gi] : 0.0, cut ? -g.normal[gc + gi] : 0.0, alpha};
+#pragma unroll
+  for (int c = 0; c < 9; ++c) out[c * n + id] = v[c];
+}
+
+}  // namespace cc
+
+cudaError_t LaunchCutCellPlotData(const CcGeom& g, const double* cons, double gamma, int j0,
+                                  int rows, double* out, cudaStream_t s) {
+  const int64_t n = int64_t(g.nx) * rows;
+  if (n == 0) return cudaSuccess;
+  const int block = 256;
+  cc::PlotDataKernel<<<unsigned((n + block - 1) / block), block, 0, s>>>(g, cons, gamma, j0,
+                                                                         rows, out);
+  return cudaGetLastError();
+}
+
 }  // namespace fvs

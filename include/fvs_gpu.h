@@ -39,7 +39,8 @@ typedef enum fvs_status {
   FVS_ERR_DT_TOO_LARGE = 3,   /* a per-sweep CFL check failed */
   FVS_ERR_UNSUPPORTED = 4,    /* method / precision not available here */
   FVS_ERR_NO_DEVICE = 5,      /* no CUDA device */
-  FVS_ERR_STATE = 6           /* non-positive density / non-finite state */
+  FVS_ERR_STATE = 6,          /* non-positive density / non-finite state */
+  FVS_ERR_IO = 7              /* a file or directory could not be written */
 } fvs_status;
 
 typedef enum fvs_flux_method {
@@ -234,6 +235,17 @@ int fvs_solver_upload(fvs_solver* s, const double* cons_host);
 int fvs_solver_download(fvs_solver* s, double* cons_host);
 /* Device pointer of the current state (valid until the next call). */
 int fvs_solver_state_device(fvs_solver* s, double** cons_dev);
+/* Writes the current state as an AMReX plotfile directory `dir` (created if
+ * missing; its files are overwritten): the Complete state (Density,
+ * Momentum_d (Momentum in 1-D), Energy, Pressure, SpeedOfSound) computed on
+ * the device, one level whose boxes are slabs of the slowest direction of at
+ * most 2^21 cells, the solver's time and step count.  With cut cells the
+ * state is masked by alpha > 0 and Boundary_X, Boundary_Y and vfrac follow.
+ * Replaces fub::amrex::PlotfileOutput / WritePlotFile
+ * (include/fub/AMReX/output/WritePlotfiles.hpp:33-56,
+ * include/fub/AMReX/PatchHierarchy.hpp:278-315,
+ * include/fub/AMReX/cutcell/PatchHierarchy.hpp:265-314). */
+int fvs_solver_write_plotfile(fvs_solver* s, const char* dir);
 /* Threads per block / cells per thread segment of the sweep kernels
  * (0 = automatic). */
 int fvs_solver_set_tiling(fvs_solver* s, int seg_len);
@@ -342,6 +354,9 @@ int fvs_amr_destroy(fvs_amr* a);
  * [4][ny][nx] (FArrayBox layout of the patch box). */
 int fvs_amr_upload(fvs_amr* a, const double* host);
 int fvs_amr_download(fvs_amr* a, double* host);
+/* AMReX plotfile of every level (one box per patch, in patch order; level l
+ * has step count 2^l times the coarse steps), as fvs_solver_write_plotfile. */
+int fvs_amr_write_plotfile(fvs_amr* a, const char* dir);
 /* Interior cells and storage cells (with ghosts) per level, and the number
  * of coarse-fine register faces.  Any pointer may be NULL. */
 int fvs_amr_info(fvs_amr* a, int64_t* cells_per_level, int64_t* storage_per_level,
