@@ -47,21 +47,21 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * N + off);
     };
-    double dm[K], dc[K], dp[K], dn[K];
+    // the update re-reads the FP64 state of cell j-1 (an L1 hit) instead of
+    // carrying a window of FP64 states in registers
+    double dn[K];
     R cm[K], cc[K], cp[K];
-    load(dm, j0 - 2);
-    load(dc, j0 - 1);
+    load(dn, j0 - 2);
+    P::ToCell(cm, dn);
+    load(dn, j0 - 1);
+    P::ToCell(cc, dn);
     load(dn, j0);
-    P::ToCell(cm, dm);
-    P::ToCell(cc, dc);
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
     double F_prev[K];
     for (int j = j0 - 1; j <= j1; ++j) {
-#pragma unroll
-      for (int c = 0; c < K; ++c) dp[c] = dn[c];
+      P::ToCell(cp, dn);
       if (j + 2 <= j1 + 1) load(dn, j + 2);
-      P::ToCell(cp, dp);
       typename P::Rec recL, recR;
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
       const typename P::Wave wv = P::MakeWave(eq, cc, DIR);
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
           const int64_t off = int64_t(w.base) + int64_t(j - 1 + kGhost) * w.stride;
 #pragma unroll
           for (int c = 0; c < K; ++c) {
-            const double v = dm[c] + dt_dx * (F_prev[c] - F[c]);
+            const double v = __ldg(in + c * N + off) + dt_dx * (F_prev[c] - F[c]);
             out[c * N + off] = v;
             if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
           }
@@ -92,8 +92,6 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
       w_prev = wv;
 #pragma unroll
       for (int c = 0; c < K; ++c) {
-        dm[c] = dc[c];
-        dc[c] = dp[c];
         cm[c] = cc[c];
         cc[c] = cp[c];
       }

@@ -147,23 +147,23 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * cs + off);
     };
-    // double window for the update, compute-precision window for the rest;
-    // the loads run one cell ahead of the arithmetic (dn is the next "up")
-    double dm[K], dc[K], dp[K], dn[K];
+    // compute-precision window of three cells; the FP64 loads run one cell
+    // ahead of the arithmetic (dn is the next "up").  The update of cell j-1
+    // re-reads its FP64 state (loaded two iterations earlier, an L1 hit)
+    // instead of carrying a window of FP64 states in registers.
+    double dn[K];
     R cm[K], cc[K], cp[K];
-    load(dm, j0 - 2);
-    load(dc, j0 - 1);
+    load(dn, j0 - 2);
+    P::ToCell(cm, dn);
+    load(dn, j0 - 1);
+    P::ToCell(cc, dn);
     load(dn, j0);
-    P::ToCell(cm, dm);
-    P::ToCell(cc, dc);
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
     double F_prev[K];
     for (int j = j0 - 1; j <= j1; ++j) {
-#pragma unroll
-      for (int c = 0; c < K; ++c) dp[c] = dn[c];
+      P::ToCell(cp, dn);
       if (j + 2 <= j1 + 1) load(dn, j + 2);
-      P::ToCell(cp, dp);
       typename P::Rec recL, recR;
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
       const typename P::Wave w = P::MakeWave(eq, cc, DIR);
@@ -172,11 +172,11 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
         const R s = P::Face(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
         smax = s > smax ? s : smax;
         if (j > j0) {
-          // cell j-1: U' = U + dt/dx (F_{j-1} - F_j)
+          // cell j-1 (inside [0, nd)): U' = U + dt/dx (F_{j-1} - F_j)
           const int64_t off = base + int64_t(j - 1) * stride;
 #pragma unroll
           for (int c = 0; c < K; ++c) {
-            const double v = dm[c] + dt_dx * (F_prev[c] - F[c]);
+            const double v = __ldg(in + c * cs + off) + dt_dx * (F_prev[c] - F[c]);
             out[c * cs + off] = v;
             // non-positive density: sign bit set or zero (integer test)
             if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
@@ -189,8 +189,6 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
       w_prev = w;
 #pragma unroll
       for (int c = 0; c < K; ++c) {
-        dm[c] = dc[c];
-        dc[c] = dp[c];
         cm[c] = cc[c];
         cc[c] = cp[c];
       }
@@ -314,13 +312,11 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(Sweep
   typename P::Rec carry_rec = ShflIdx(wrecR, 31);
   typename P::Wave carry_w = ShflIdx(wW, 31);
   Cell carry_c = ShflIdx(Cw, 31);
-  Dbl carry_u = ShflIdx(Uw, 31);
   Dbl carry_f;
 #pragma unroll
   for (int c = 0; c < K; ++c) carry_f.v[c] = Fw[c];
   carry_f = ShflIdx(carry_f, 31);
 
-  Dbl U = U0;
   Cell C = C0;
   const int nchunks = (nx + 31) / 32;
   Dbl Unext;  // the chunk after the next one is loaded one iteration early
@@ -354,18 +350,15 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(Sweep
 #pragma unroll
     for (int c = 0; c < K; ++c) Fd.v[c] = F[c];
     Dbl Fm = ShflUp(Fd, 1);
-    Dbl Um = ShflUp(U, 1);
-    if (lane == 0) {
-      Fm = carry_f;
-      Um = carry_u;
-    }
-    // update cell x-1 (lane 0 of chunk 0: cell -1, i.e. nx-1 on a periodic row)
+    if (lane == 0) Fm = carry_f;
+    // update cell x-1 (lane 0 of chunk 0: cell -1, i.e. nx-1 on a periodic row);
+    // its FP64 state is re-read (a coalesced L1 hit) rather than shuffled
     const bool upd = valid && (x >= 1 || periodic);
     if (upd) {
       const int64_t off = base + BcIndex(x - 1, nx, a.bc);
 #pragma unroll
       for (int c = 0; c < K; ++c) {
-        const double v = Um.v[c] + dt_dx * (Fm.v[c] - Fd.v[c]);
+        const double v = __ldg(in + c * cs + off) + dt_dx * (Fm.v[c] - Fd.v[c]);
         out[c * cs + off] = v;
         if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
       }
@@ -375,9 +368,7 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(Sweep
     carry_rec = ShflIdx(recR, last);
     carry_w = ShflIdx(W, last);
     carry_c = ShflIdx(C, last);
-    carry_u = ShflIdx(U, last);
     carry_f = ShflIdx(Fd, last);
-    U = Un;
     C = Cn;
   }
   if (!periodic) {
@@ -392,7 +383,7 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(Sweep
       const int64_t off = base + (nx - 1);
 #pragma unroll
       for (int c = 0; c < K; ++c) {
-        const double v = carry_u.v[c] + dt_dx * (carry_f.v[c] - F[c]);
+        const double v = __ldg(in + c * cs + off) + dt_dx * (carry_f.v[c] - F[c]);
         out[c * cs + off] = v;
         if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
       }
