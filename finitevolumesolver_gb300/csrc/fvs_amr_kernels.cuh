@@ -97,8 +97,8 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
       }
     }
   }
-  const double smax_w = WarpMax(static_cast<double>(smax));
-  if ((threadIdx.x & 31) == 0 && smax_w > 0.0) AtomicMaxPositive(a.smax_out, smax_w);
+  const double smax_d = static_cast<double>(smax);
+  BlockMaxAtomic<1>(a.smax_out, &smax_d);
   if (status) atomicOr(&a.ctrl->step_status, status);
 }
 
@@ -132,8 +132,8 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
       wl = wr;
     }
   }
-  const double smax_w = WarpMax(static_cast<double>(smax));
-  if ((threadIdx.x & 31) == 0 && smax_w > 0.0) AtomicMaxPositive(a.smax_out, smax_w);
+  const double smax_d = static_cast<double>(smax);
+  BlockMaxAtomic<1>(a.smax_out, &smax_d);
 }
 
 template <template <int> class PT>

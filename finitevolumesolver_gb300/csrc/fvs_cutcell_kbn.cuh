@@ -330,13 +330,15 @@ template <class T> __global__ void __launch_bounds__(128) KbnSweepKernel(CcSweep
   const int j0 = blockIdx.y * a.seg_len;
   const int j1 = min(nd, j0 + a.seg_len);
   const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
+  bool run = true;
   if (a.ctrl) {
-    if (a.ctrl->abort || a.ctrl->done) return;
+    if (a.ctrl->abort || a.ctrl->done) run = false;
     if (a.prev_check >= 0) {
       const double smax = BitsToDouble(a.ctrl->smax_check[a.prev_check]);
-      if (a.prev_dx / smax < split_dt) return;
+      if (a.prev_dx / smax < split_dt) run = false;
     }
   }
+  if (!BlockAll(run)) return;
   T smax = T(0);
   int status = 0;
   if (t64 < nt) {
@@ -516,8 +518,8 @@ template <class T> __global__ void __launch_bounds__(128) KbnSweepKernel(CcSweep
       ac = ap;
     }
   }
-  const double m = WarpMax(static_cast<double>(smax));
-  if ((threadIdx.x & 31) == 0 && a.smax_out && m > 0.0) AtomicMaxPositive(a.smax_out, m);
+  const double smax_d = static_cast<double>(smax);
+  BlockMaxAtomic<1>(a.smax_out, &smax_d);
   if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
 }
 
@@ -525,12 +527,13 @@ template <class T> __global__ void __launch_bounds__(128) KbnSweepKernel(CcSweep
 // (KbnStabilisation.hpp:275-345).
 template <class T>
 __global__ void KbnStableDtKernel(CcStateArgs a, unsigned long long* smax_out, Control* ctrl) {
-  if (ctrl && (ctrl->abort || ctrl->done)) return;
+  if (!BlockAll(!(ctrl && (ctrl->abort || ctrl->done)))) return;
   const CcGeom& g = a.g;
   const int w = g.nx + 1, h = g.ny + 1;
-  const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   T sm[2] = {T(0), T(0)};
-  if (id < int64_t(w) * h) {
+  // grid-stride over faces; one atomic per block and direction at the end
+  for (int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; id < int64_t(w) * h;
+       id += int64_t(gridDim.x) * blockDim.x) {
     const int i = static_cast<int>(id % w), j = static_cast<int>(id / w);
     const GasT<T> eq = MakeGasT<T>(a.gamma);
     for (int d = 0; d < 2; ++d) {
@@ -556,10 +559,8 @@ __global__ void KbnStableDtKernel(CcStateArgs a, unsigned long long* smax_out, C
       sm[d] = mx > sm[d] ? mx : sm[d];
     }
   }
-  for (int d = 0; d < 2; ++d) {
-    const double m = WarpMax(static_cast<double>(sm[d]));
-    if ((threadIdx.x & 31) == 0 && m > 0.0) AtomicMaxPositive(smax_out + d, m);
-  }
+  const double smd[2] = {static_cast<double>(sm[0]), static_cast<double>(sm[1])};
+  BlockMaxAtomic<2>(smax_out, smd);
 }
 
 template <class T> cudaError_t LaunchKbnStates(const CcStateArgs& a, cudaStream_t s) {
@@ -586,7 +587,7 @@ cudaError_t LaunchKbnStableDt(const CcStateArgs& a, unsigned long long* smax_out
                               cudaStream_t s) {
   const int64_t n = int64_t(a.g.nx + 1) * (a.g.ny + 1);
   const int block = 128;
-  KbnStableDtKernel<T><<<unsigned((n + block - 1) / block), block, 0, s>>>(a, smax_out, ctrl);
+  KbnStableDtKernel<T><<<GridStrideBlocks(n, block, 16), block, 0, s>>>(a, smax_out, ctrl);
   return cudaGetLastError();
 }
 

@@ -153,11 +153,12 @@ __global__ void __launch_bounds__(256) StableDtKernel(StableDtArgs a) {
   constexpr int K = D + 2;
   const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
   const int64_t cs = int64_t(nx) * ny * nz;
-  const int64_t cell = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (a.ctrl && (a.ctrl->abort || a.ctrl->done)) return;
+  if (!BlockAll(!(a.ctrl && (a.ctrl->abort || a.ctrl->done)))) return;
   const exact::Gas eq = ExactPolicy<1>::MakeGas(a.gamma);
   double smax[3] = {0.0, 0.0, 0.0};
-  if (cell < cs) {
+  // grid-stride over cells; one atomic per block and direction at the end
+  for (int64_t cell = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; cell < cs;
+       cell += int64_t(gridDim.x) * blockDim.x) {
     const int i = static_cast<int>(cell % nx);
     const int j = static_cast<int>((cell / nx) % ny);
     const int k = static_cast<int>(cell / (int64_t(nx) * ny));
@@ -199,17 +200,13 @@ __global__ void __launch_bounds__(256) StableDtKernel(StableDtArgs a) {
       }
     }
   }
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const double m = WarpMax(smax[d]);
-    if ((threadIdx.x & 31) == 0 && m > 0.0) AtomicMaxPositive(a.smax_out + d, m);
-  }
+  BlockMaxAtomic<D>(a.smax_out, smax);
 }
 
 cudaError_t LaunchStableDtExact(const StableDtArgs& a, cudaStream_t s) {
   const int64_t cells = int64_t(a.n[0]) * a.n[1] * a.n[2];
   const int block = 256;
-  const unsigned grid = static_cast<unsigned>((cells + block - 1) / block);
+  const unsigned grid = GridStrideBlocks(cells, block, 8);
   switch (a.rank) {
   case 1:
     StableDtKernel<1><<<grid, block, 0, s>>>(a);

@@ -105,11 +105,12 @@ __global__ void __launch_bounds__(256) GodunovStableDtKernel(StableDtArgs a, int
   constexpr int K = D + 2;
   const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
   const int64_t cs = int64_t(nx) * ny * nz;
-  const int64_t cell = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (a.ctrl && (a.ctrl->abort || a.ctrl->done)) return;
+  if (!BlockAll(!(a.ctrl && (a.ctrl->abort || a.ctrl->done)))) return;
   const GodunovGas g = MakeGodunovGas(a.gamma, guess, max_it, tol, mlp);
   double smax[3] = {0.0, 0.0, 0.0};
-  if (cell < cs) {
+  // grid-stride over cells; one atomic per block and direction at the end
+  for (int64_t cell = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; cell < cs;
+       cell += int64_t(gridDim.x) * blockDim.x) {
     const int idx[3] = {static_cast<int>(cell % nx), static_cast<int>((cell / nx) % ny),
                         static_cast<int>(cell / (int64_t(nx) * ny))};
     double u[K];
@@ -141,18 +142,14 @@ __global__ void __launch_bounds__(256) GodunovStableDtKernel(StableDtArgs a, int
       }
     }
   }
-#pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const double m = WarpMax(smax[d]);
-    if ((threadIdx.x & 31) == 0 && m > 0.0) AtomicMaxPositive(a.smax_out + d, m);
-  }
+  BlockMaxAtomic<D>(a.smax_out, smax);
 }
 
 cudaError_t LaunchStableDtGodunov(const StableDtArgs& a, int guess, int max_it, double tol,
                                   const float* mlp, cudaStream_t s) {
   const int64_t cells = int64_t(a.n[0]) * a.n[1] * a.n[2];
   const int block = 256;
-  const unsigned grid = static_cast<unsigned>((cells + block - 1) / block);
+  const unsigned grid = GridStrideBlocks(cells, block, 8);
   switch (a.rank) {
   case 1:
     GodunovStableDtKernel<1><<<grid, block, 0, s>>>(a, guess, max_it, tol, mlp);

@@ -262,6 +262,24 @@ __device__ __forceinline__ Wave<T> MakeWave(const Gas<T>& eq, const T* u, int di
   return Wave<T>{s.sq, s.u, s.h, s.a};
 }
 
+// The waves of a cell in the D directions from one preparation: the same
+// operations as Prepare (so each wave equals MakeWave's), with the
+// direction-free part (sqrt(rho), 1/rho, h, a) computed once.
+template <int D, typename T>
+__device__ __forceinline__ void MakeWaves(const Gas<T>& eq, const T* u, Wave<T>* w) {
+  using M = Math<T>;
+  const T rho = u[0];
+  const T rs = M::Rsqrt(rho);
+  const T ir = rs * rs;
+  const T sq = rho * rs;
+  const T ke = T(0.5) * SquaredNorm<D, T>(u + 1) * ir;
+  const T p = (u[1 + D] - ke) * eq.gm1;
+  const T h = (u[1 + D] + p) * ir;
+  const T a = M::Sqrt(eq.gamma * p * ir);
+#pragma unroll
+  for (int d = 0; d < D; ++d) w[d] = Wave<T>{sq, u[1 + d] * ir, h, a};
+}
+
 template <typename T>
 __device__ __forceinline__ T FaceMaxSpeed(const Gas<T>& eq, const Wave<T>& L, const Wave<T>& R) {
   T sL, sR;

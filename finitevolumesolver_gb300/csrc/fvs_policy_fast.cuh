@@ -74,6 +74,9 @@ template <int D, typename T> struct FastBase {
   static __device__ __forceinline__ Wave MakeWave(const Gas& eq, const T* u, int dir) {
     return fast::MakeWave<D, T>(eq, u, dir);
   }
+  static __device__ __forceinline__ void MakeWaves(const Gas& eq, const T* u, Wave* w) {
+    fast::MakeWaves<D, T>(eq, u, w);
+  }
   static __device__ __forceinline__ T FaceMaxSpeed(const Gas& eq, const Wave& L,
                                                    const Wave& R) {
     return fast::FaceMaxSpeed<T>(eq, L, R);

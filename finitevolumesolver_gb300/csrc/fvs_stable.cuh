@@ -9,6 +9,9 @@
 // face speed per direction; dt = dx / speed is formed once on the host/device.
 #pragma once
 
+#include <algorithm>
+#include <type_traits>
+
 #include "fvs_internal.h"
 #include "fvs_sweep.cuh"
 
@@ -40,11 +43,12 @@ __global__ void __launch_bounds__(256) StableDtKernelT(StableDtArgs a) {
   constexpr int K = D + 2;
   const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
   const int64_t cs = int64_t(nx) * ny * nz;
-  const int64_t cell = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (a.ctrl && (a.ctrl->abort || a.ctrl->done)) return;
+  if (!BlockAll(!(a.ctrl && (a.ctrl->abort || a.ctrl->done)))) return;
   const typename P::Gas eq = P::MakeGas(a.gamma);
   double smax[3] = {0.0, 0.0, 0.0};
-  if (cell < cs) {
+  // grid-stride over cells; one atomic per block and direction at the end
+  for (int64_t cell = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; cell < cs;
+       cell += int64_t(gridDim.x) * blockDim.x) {
     const int i = static_cast<int>(cell % nx);
     const int j = static_cast<int>((cell / nx) % ny);
     const int k = static_cast<int>(cell / (int64_t(nx) * ny));
@@ -79,29 +83,128 @@ __global__ void __launch_bounds__(256) StableDtKernelT(StableDtArgs a) {
       }
     }
   }
+  BlockMaxAtomic<D>(a.smax_out, smax);
+}
+
+// The waves of one cell in the three directions: a policy with a shared
+// preparation (MakeWaves) computes the direction-free part once, any other
+// policy calls MakeWave per direction.
+template <class P, class = void> struct WavesOf {
+  static __device__ __forceinline__ void Get(const typename P::Gas& eq,
+                                             const typename P::Real* u,
+                                             typename P::Wave* w) {
 #pragma unroll
-  for (int d = 0; d < D; ++d) {
-    const double m = WarpMax(smax[d]);
-    if ((threadIdx.x & 31) == 0 && m > 0.0) AtomicMaxPositive(a.smax_out + d, m);
+    for (int d = 0; d < 3; ++d) w[d] = P::MakeWave(eq, u, d);
   }
+};
+template <class P> struct WavesOf<P, std::void_t<decltype(&P::MakeWaves)>> {
+  static __device__ __forceinline__ void Get(const typename P::Gas& eq,
+                                             const typename P::Real* u,
+                                             typename P::Wave* w) {
+    P::MakeWaves(eq, u, w);
+  }
+};
+
+// Stable dt of a 3-D grid with every cell loaded and its waves computed once
+// (the faces and their speeds are those of StableDtKernelT): a warp covers
+// 31 cells of an x row (lane 0 holds the left neighbour of the first) and
+// marches along z over `seg` planes, keeping the previous plane's z waves in
+// registers; the x neighbour comes by a shuffle and the y neighbour (j-1) of
+// each cell is loaded once more.  One atomic per block and direction.
+template <template <int> class PT>
+__global__ void __launch_bounds__(256) StableDtMarch3Kernel(StableDtArgs a, int seg) {
+  using P = PT<3>;
+  using R = typename P::Real;
+  using W = typename P::Wave;
+  constexpr int K = 5;
+  const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
+  const int64_t cs = int64_t(nx) * ny * nz;
+  if (!BlockAll(!(a.ctrl && (a.ctrl->abort || a.ctrl->done)))) return;
+  const typename P::Gas eq = P::MakeGas(a.gamma);
+  double smax[3] = {0.0, 0.0, 0.0};
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int xw = (nx + 30) / 31;
+  const int zseg = (nz + seg - 1) / seg;
+  if (gw < int64_t(xw) * ny * zseg) {  // warp-uniform
+    const int wx = static_cast<int>(gw % xw);
+    const int64_t r = gw / xw;
+    const int j = static_cast<int>(r % ny);
+    const int k0 = static_cast<int>(r / ny) * seg;
+    const int k1 = min(nz, k0 + seg);
+    const int i = wx * 31 + lane - 1;
+    const bool own = lane >= 1 && i < nx;
+    const int ic = BcIndex(i, nx, a.bc[0]);  // lane 0: the left neighbour
+    const int jm = BcIndex(j - 1, ny, a.bc[1]);
+    auto load = [&](int jj, int kk, R* u) {
+      const int64_t off = (int64_t(kk) * ny + jj) * nx + ic;
+      double ud[K];
+#pragma unroll
+      for (int c = 0; c < K; ++c) ud[c] = __ldg(a.in + c * cs + off);
+      P::ToCell(u, ud);
+    };
+    auto take = [&](double& m, R s) {
+      const double v = static_cast<double>(s);
+      m = v > m ? v : m;
+    };
+    const bool ytile = !(a.rule == 1 && !ReferenceTileFaceT(j, ny, a.width));
+    const bool ytop = j == ny - 1 && a.bc[1] != 0 &&
+                      !(a.rule == 1 && !ReferenceTileFaceT(ny, ny, a.width));
+    W wz_prev;
+    {
+      R u[K];
+      load(j, BcIndex(k0 - 1, nz, a.bc[2]), u);
+      wz_prev = P::MakeWave(eq, u, 2);
+    }
+    for (int k = k0; k < k1; ++k) {
+      R u[K];
+      load(j, k, u);
+      W w[3];
+      WavesOf<P>::Get(eq, u, w);
+      const W wl = ShflUp(w[0], 1);
+      if (own) {
+        // x: face i (i-1, i); face nx of a transmissive row (nx-1, nx-1)
+        take(smax[0], P::FaceMaxSpeed(eq, wl, w[0]));
+        if (i == nx - 1 && a.bc[0] != 0) take(smax[0], P::FaceMaxSpeed(eq, w[0], w[0]));
+        // y: face j (j-1, j); face ny of a transmissive column
+        if (ytile) {
+          R v[K];
+          load(jm, k, v);
+          take(smax[1], P::FaceMaxSpeed(eq, P::MakeWave(eq, v, 1), w[1]));
+        }
+        if (ytop) take(smax[1], P::FaceMaxSpeed(eq, w[1], w[1]));
+        // z: face k (k-1, k); face nz of a transmissive column
+        if (!(a.rule == 1 && !ReferenceTileFaceT(k, nz, a.width)))
+          take(smax[2], P::FaceMaxSpeed(eq, wz_prev, w[2]));
+        if (k == nz - 1 && a.bc[2] != 0 && !(a.rule == 1 && !ReferenceTileFaceT(nz, nz, a.width)))
+          take(smax[2], P::FaceMaxSpeed(eq, w[2], w[2]));
+      }
+      wz_prev = w[2];
+    }
+  }
+  BlockMaxAtomic<3>(a.smax_out, smax);
 }
 
 template <template <int> class PT>
 cudaError_t LaunchStableDtT(const StableDtArgs& a, cudaStream_t s) {
   const int64_t cells = int64_t(a.n[0]) * a.n[1] * a.n[2];
   const int block = 256;
-  const unsigned grid = static_cast<unsigned>((cells + block - 1) / block);
-  switch (a.rank) {
-  case 1:
-    StableDtKernelT<1, PT><<<grid, block, 0, s>>>(a);
-    break;
-  case 2:
-    StableDtKernelT<2, PT><<<grid, block, 0, s>>>(a);
-    break;
-  default:
-    StableDtKernelT<3, PT><<<grid, block, 0, s>>>(a);
-    break;
+  if (a.rank == 3) {
+    // enough warps for about two waves of the GPU, planes split accordingly
+    const int64_t rows = int64_t((a.n[0] + 30) / 31) * a.n[1];
+    const int64_t want = int64_t(GridStrideBlocks(int64_t(1) << 40, block, 8)) * (block / 32) * 2;
+    const int64_t zseg = std::max<int64_t>(1, std::min<int64_t>(a.n[2], (want + rows - 1) / rows));
+    const int seg = static_cast<int>((a.n[2] + zseg - 1) / zseg);
+    const int64_t warps = rows * ((a.n[2] + seg - 1) / seg);
+    const unsigned grid = static_cast<unsigned>((warps * 32 + block - 1) / block);
+    StableDtMarch3Kernel<PT><<<grid, block, 0, s>>>(a, seg);
+    return cudaGetLastError();
   }
+  const unsigned grid = GridStrideBlocks(cells, block, 8);
+  if (a.rank == 1)
+    StableDtKernelT<1, PT><<<grid, block, 0, s>>>(a);
+  else
+    StableDtKernelT<2, PT><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -54,6 +54,53 @@ __device__ __forceinline__ double BitsToDouble(unsigned long long b) {
   return __longlong_as_double(static_cast<long long>(b));
 }
 
+// True on every thread of the block iff `pred` holds on every thread of it:
+// a kernel that returns on !BlockAll(...) leaves no thread of a block behind
+// a later barrier.
+__device__ __forceinline__ bool BlockAll(bool pred) { return __syncthreads_and(pred) != 0; }
+
+// Max over the thread block of per-thread values v[0..N) (each >= 0), then
+// one atomic max per word and block (words may be NULL).  Every thread of
+// the block calls it exactly once per kernel; one atomic per block instead
+// of one per warp keeps the same-address atomic traffic small.
+template <int N>
+__device__ __forceinline__ void BlockMaxAtomic(unsigned long long* words, const double* v) {
+  __shared__ double part[N][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int d = 0; d < N; ++d) {
+    const double m = WarpMax(v[d]);
+    if (lane == 0) part[d][warp] = m;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int d = 0; d < N; ++d) {
+      double m = lane < nw ? part[d][lane] : 0.0;
+      m = WarpMax(m);
+      if (lane == 0 && words && m > 0.0) AtomicMaxPositive(words + d, m);
+    }
+  }
+}
+
+// Blocks of a grid-stride launch over `work` items: enough to fill every SM
+// `per_sm` times, no more than the work needs.
+inline unsigned GridStrideBlocks(int64_t work, int block, int per_sm) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0)
+      sms = n;
+    else
+      sms = 152;
+  }
+  const int64_t need = (work + block - 1) / block;
+  const int64_t cap = int64_t(sms) * per_sm;
+  return static_cast<unsigned>(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
 // Returns false when this sweep must not run (run aborted / finished, or the
 // previous sweep's CFL check failed).
 __device__ __forceinline__ bool SweepGate(const SweepArgs& a, double split_dt) {
@@ -115,7 +162,7 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
   const int j1 = min(nd, j0 + a.seg_len);
 
   const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
-  if (!SweepGate(a, split_dt)) return;
+  if (!BlockAll(SweepGate(a, split_dt))) return;
   const bool active = t < ntrans;
 
   int64_t base, stride;
@@ -195,10 +242,8 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
     }
   }
   stats.Flush(a.stats_out);
-  const double smax_w = WarpMax(static_cast<double>(smax));
-  if ((threadIdx.x & 31) == 0) {
-    if (a.smax_out && smax_w > 0.0) AtomicMaxPositive(a.smax_out, smax_w);
-  }
+  const double smax_d = static_cast<double>(smax);
+  BlockMaxAtomic<1>(a.smax_out, &smax_d);
   if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
 }
 
@@ -252,7 +297,9 @@ template <class R, int K> struct CellArr {
 // nx-1.  The arithmetic per face and cell is the policy's, exactly as in
 // SweepMarchKernel.
 template <int D, template <int> class PT>
-__global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(SweepArgs a) {
+__device__ __forceinline__ void XWarpRow(const SweepArgs& a, int64_t row, double split_dt,
+                                         typename PT<D>::Real& smax, int& status,
+                                         typename PT<D>::Stats& stats) {
   using P = PT<D>;
   using R = typename P::Real;
   constexpr int K = D + 2;
@@ -260,12 +307,7 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(Sweep
   using Dbl = CellArr<double, K>;
   const int nx = a.n[0];
   const int64_t cs = int64_t(nx) * a.n[1] * a.n[2];
-  const int64_t rows = int64_t(a.n[1]) * a.n[2];
   const int lane = threadIdx.x & 31;
-  const int64_t row = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
-  if (!SweepGate(a, split_dt)) return;
-  if (row >= rows) return;  // warp-uniform
   const int64_t base = row * nx;
   const bool periodic = (a.bc == 0);
   const typename P::Gas eq = P::MakeGasFor(a);
@@ -283,9 +325,6 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(Sweep
     P::ToCell(c.v, u.v);
     return c;
   };
-  R smax = R(0);
-  int status = 0;
-  typename P::Stats stats;
 
   // ---- warm-up: cells -3..-1 in lanes 29..31, cell 0 from the first chunk
   Dbl U0;
@@ -389,9 +428,34 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(Sweep
       }
     }
   }
+}
+
+// The kernel: one row per warp.  A block whose warps all have a row reduces
+// their max signal speed before one atomic; the last block of a grid whose
+// row count is not a multiple of the warps per block returns its idle warps
+// early and reduces per warp (no barrier after the return).
+template <int D, template <int> class PT>
+__global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(SweepArgs a) {
+  using P = PT<D>;
+  using R = typename P::Real;
+  const int64_t rows = int64_t(a.n[1]) * a.n[2];
+  const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
+  if (!BlockAll(SweepGate(a, split_dt))) return;
+  R smax = R(0);
+  int status = 0;
+  typename P::Stats stats;
+  const int64_t row = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const bool full_block = int64_t(blockIdx.x + 1) * (blockDim.x >> 5) <= rows;  // block-uniform
+  if (row >= rows) return;  // only in a block that is not full
+  XWarpRow<D, PT>(a, row, split_dt, smax, status, stats);
   stats.Flush(a.stats_out);
-  const double smax_w = WarpMax(static_cast<double>(smax));
-  if (lane == 0 && a.smax_out && smax_w > 0.0) AtomicMaxPositive(a.smax_out, smax_w);
+  const double smax_d = static_cast<double>(smax);
+  if (full_block) {
+    BlockMaxAtomic<1>(a.smax_out, &smax_d);
+  } else {
+    const double m = WarpMax(smax_d);
+    if ((threadIdx.x & 31) == 0 && a.smax_out && m > 0.0) AtomicMaxPositive(a.smax_out, m);
+  }
   if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
 }
 
