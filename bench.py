@@ -63,6 +63,11 @@ def parse():
     ap.add_argument("--amr-flavours", default="fp64_exact,fp64_fast,mixed")
     ap.add_argument("--cutcell-n", type=int, default=1024)
     ap.add_argument("--cutcell-steps", type=int, default=400)
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="profiling aid: run this many Strang steps of the --n workload in "
+                         "--precision with the default launch shapes (no autotuner, no "
+                         "timing) and exit; the first sweep launches are then the x, y, z "
+                         "sweeps of step 1")
     return ap.parse_args()
 
 
@@ -510,6 +515,16 @@ def run_ours(args):
     n = args.n
     cells = n ** 3
     cons = workloads.octants_3d(n)
+    if args.profile_steps > 0:
+        solver = fvs.Solver([n] * 3, [1.0 / n] * 3, "periodic",
+                            method=fvs.make_method(precision=args.precision))
+        solver.upload(cons)
+        st, _ = solver.run(cfl=0.8, t_end=1e9, max_steps=args.profile_steps)
+        solver.close()
+        if rank == 0:
+            print(json.dumps({"profile_steps": st.steps, "n": n, "precision": args.precision}),
+                  flush=True)
+        return
     peaks = load_peaks()
     algo_bytes = 16 * (3 + 2) * cells  # state read once + written once, FP64
 

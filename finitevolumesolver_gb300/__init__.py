@@ -232,6 +232,10 @@ class Solver:
     def set_tiling(self, seg_len: int) -> None:
         _capi.check(lib().fvs_solver_set_tiling(self._h, int(seg_len)))
 
+    def set_launch(self, dir, seg_len=0, variant=0) -> None:
+        """Force direction dir's segment length and launch variant."""
+        _capi.check(lib().fvs_solver_set_launch(self._h, int(dir), int(seg_len), int(variant)))
+
     def set_embedded_circles(self, circles, x0=0.0, y0=0.0) -> None:
         """Union of circles (rows cx, cy, r; the body is their inside) as an
         embedded boundary: the solver switches to the KBN cut-cell update."""

@@ -104,6 +104,7 @@ def load() -> C.CDLL:
     L.fvs_solver_write_plotfile.argtypes = [_VP, C.c_char_p]
     L.fvs_solver_state_device.argtypes = [_VP, P(_VP)]
     L.fvs_solver_set_tiling.argtypes = [_VP, C.c_int]
+    L.fvs_solver_set_launch.argtypes = [_VP, C.c_int, C.c_int, C.c_int]
     L.fvs_solver_autotune.argtypes = [_VP, P(C.c_int)]
     L.fvs_solver_tuning.argtypes = [_VP, _VP, _VP]
     L.fvs_solver_stable_dt.argtypes = [_VP, C.c_int, _DP]

@@ -757,6 +757,24 @@ int fvs_solver_set_tiling(fvs_solver* s, int seg_len) {
   return FVS_OK;
 }
 
+int fvs_solver_set_launch(fvs_solver* s, int dir, int seg_len, int variant) {
+  if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
+  if (dir < 0 || dir >= s->g.rank) return Fail(FVS_ERR_INVALID, "direction out of range");
+  if (seg_len < 0) return Fail(FVS_ERR_INVALID, "segment length must be >= 0");
+  const bool plain_hlle = s->m.flux_method <= FVS_HLLE && !s->cc;
+  bool ok = variant == 0;
+  if (s->m.precision == FVS_MIXED && plain_hlle)
+    ok = variant == 0 || variant == 4 || variant == 5 ||
+         (dir == 0 && (variant == 10 || variant == 14 || variant == 15));
+  if (s->m.precision == FVS_FP64_DF && plain_hlle) ok = variant == 0 || variant == 3;
+  if (!ok) return Fail(FVS_ERR_INVALID, "no such launch variant for this method");
+  s->seg_tuned[dir] = seg_len;
+  s->occ_tuned[dir] = variant;
+  for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
+  s->graphs.clear();
+  return FVS_OK;
+}
+
 int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   if (!s) return Fail(FVS_ERR_INVALID, "NULL solver");
   // Candidate segment lengths per direction (and, for the mixed flavour,
@@ -767,11 +785,11 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   const bool plain_hlle = s->m.flux_method <= FVS_HLLE && !s->cc;
   const bool mixed = s->m.precision == FVS_MIXED && plain_hlle;
   const bool df = s->m.precision == FVS_FP64_DF && plain_hlle;
+  // mixed x sweeps: lanes-along-x kernel (0, 4, 5) or marching kernel (10, 14, 15)
+  const int occs_mixed_x[] = {0, 4, 5, 10, 14, 15};
   const int occs_mixed[] = {0, 4, 5};
   const int occs_df[] = {0, 3};
   const int occs_plain[] = {0};
-  const int* occs = mixed ? occs_mixed : (df ? occs_df : occs_plain);
-  const int nocc = mixed ? 3 : (df ? 2 : 1);
   const int saved = s->seg_len;
   cudaEvent_t e0, e1;
   FVS_CUDA(cudaEventCreate(&e0));
@@ -785,12 +803,17 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   const int out = (s->cur + 1) % 3;
   for (int d = 0; d < s->g.rank; ++d) {
     const int nd = s->g.n[d];
+    const int* occs = mixed ? (d == 0 ? occs_mixed_x : occs_mixed) : (df ? occs_df : occs_plain);
+    const int nocc = mixed ? (d == 0 ? 6 : 3) : (df ? 2 : 1);
     float best = 1e30f;
     int best_seg = 0, best_occ = 0;
     for (int oi = 0; oi < nocc; ++oi) {
       s->occ_tuned[d] = occs[oi];
+      // the lanes-along-x kernel has no segment length: one candidate
+      const bool warp_x = mixed && d == 0 && occs[oi] < 10;
       for (int c : cands) {
         if (c > 2 * nd && c != cands[0]) break;
+        if (warp_x && c != cands[0]) break;
         s->seg_len = c;
         float ms_sum = 0.f;
         for (int rep = 0; rep < 3; ++rep) {

@@ -75,7 +75,8 @@ struct SweepArgs {
   const float* mlp;     // learned-guess weights (guess == FVS_GUESS_MLP)
   unsigned long long* stats_out;  // [3]: Newton iterations, non-converged, fallbacks
   int occupancy;        // 0 (registers as needed) or the resident blocks per SM a
-                        // variant is compiled for (mixed: 4, 5; double-float: 3)
+                        // variant is compiled for (mixed: 4, 5; double-float: 3);
+                        // mixed x sweeps: + 10 for the marching kernel in x
 };
 
 // Stable-dt pass over all directions (max face speed per direction).

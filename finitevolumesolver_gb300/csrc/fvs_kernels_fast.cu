@@ -36,8 +36,20 @@ template <template <int> class PT> cudaError_t LaunchSweepMixedT(const SweepArgs
   }
 }
 
+// occupancy: 0, 4, 5 = register/occupancy variant (x sweeps with lanes along
+// x); 10, 14, 15 = the same variants with the marching kernel in x.
 cudaError_t LaunchSweepMixed(const SweepArgs& a, cudaStream_t s) {
-  switch (a.occupancy) {
+  if (a.dir == 0 && a.occupancy >= 10) {
+    switch (a.occupancy) {
+    case 14:
+      return LaunchSweepMixedT<Mixed32PolicyMarchXOcc4>(a, s);
+    case 15:
+      return LaunchSweepMixedT<Mixed32PolicyMarchXOcc5>(a, s);
+    default:
+      return LaunchSweepMixedT<Mixed32PolicyMarchX>(a, s);
+    }
+  }
+  switch (a.occupancy % 10) {
   case 4:
     return LaunchSweepMixedT<Mixed32PolicyOcc4>(a, s);
   case 5:

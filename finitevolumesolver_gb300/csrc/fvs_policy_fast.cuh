@@ -93,5 +93,18 @@ template <int D> struct Mixed32PolicyOcc4 : FastBase<D, float> {
 template <int D> struct Mixed32PolicyOcc5 : FastBase<D, float> {
   static constexpr int kMinBlocks = 5;
 };
+// The mixed flavour with the marching kernel in x as well (a thread walks a
+// row; each row's loads are reused from L1 instead of exchanged by shuffles).
+template <int D> struct Mixed32PolicyMarchX : FastBase<D, float> {
+  static constexpr bool kWarpX = false;
+};
+template <int D> struct Mixed32PolicyMarchXOcc4 : FastBase<D, float> {
+  static constexpr bool kWarpX = false;
+  static constexpr int kMinBlocks = 4;
+};
+template <int D> struct Mixed32PolicyMarchXOcc5 : FastBase<D, float> {
+  static constexpr bool kWarpX = false;
+  static constexpr int kMinBlocks = 5;
+};
 
 }  // namespace fvs

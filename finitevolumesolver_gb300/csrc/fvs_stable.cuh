@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) StableDtKernelT(StableDtArgs a) {
   const int64_t cs = int64_t(nx) * ny * nz;
   if (!BlockAll(!(a.ctrl && (a.ctrl->abort || a.ctrl->done)))) return;
   const typename P::Gas eq = P::MakeGas(a.gamma);
-  double smax[3] = {0.0, 0.0, 0.0};
+  R smr[3] = {R(0), R(0), R(0)};  // in the policy's precision (no FP64 work per face)
   // grid-stride over cells; one atomic per block and direction at the end
   for (int64_t cell = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; cell < cs;
        cell += int64_t(gridDim.x) * blockDim.x) {
@@ -77,12 +77,14 @@ __global__ void __launch_bounds__(256) StableDtKernelT(StableDtArgs a) {
         for (int c = 0; c < K; ++c) vd[c] = __ldg(a.in + c * cs + ocell);
         P::ToCell(v, vd);
         const typename P::Wave wo = P::MakeWave(eq, v, d);
-        const double s = static_cast<double>((fi == 0) ? P::FaceMaxSpeed(eq, wo, w)
-                                                       : P::FaceMaxSpeed(eq, w, wo));
-        smax[d] = s > smax[d] ? s : smax[d];
+        const R s = (fi == 0) ? P::FaceMaxSpeed(eq, wo, w) : P::FaceMaxSpeed(eq, w, wo);
+        smr[d] = s > smr[d] ? s : smr[d];
       }
     }
   }
+  double smax[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) smax[d] = static_cast<double>(smr[d]);
   BlockMaxAtomic<D>(a.smax_out, smax);
 }
 
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(256) StableDtMarch3Kernel(StableDtArgs a, int 
   const int64_t cs = int64_t(nx) * ny * nz;
   if (!BlockAll(!(a.ctrl && (a.ctrl->abort || a.ctrl->done)))) return;
   const typename P::Gas eq = P::MakeGas(a.gamma);
-  double smax[3] = {0.0, 0.0, 0.0};
+  R smr[3] = {R(0), R(0), R(0)};  // in the policy's precision (no FP64 work per face)
   const int lane = threadIdx.x & 31;
   const int64_t gw = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
   const int xw = (nx + 30) / 31;
@@ -143,10 +145,7 @@ __global__ void __launch_bounds__(256) StableDtMarch3Kernel(StableDtArgs a, int 
       for (int c = 0; c < K; ++c) ud[c] = __ldg(a.in + c * cs + off);
       P::ToCell(u, ud);
     };
-    auto take = [&](double& m, R s) {
-      const double v = static_cast<double>(s);
-      m = v > m ? v : m;
-    };
+    auto take = [&](R& m, R v) { m = v > m ? v : m; };
     const bool ytile = !(a.rule == 1 && !ReferenceTileFaceT(j, ny, a.width));
     const bool ytop = j == ny - 1 && a.bc[1] != 0 &&
                       !(a.rule == 1 && !ReferenceTileFaceT(ny, ny, a.width));
@@ -164,24 +163,26 @@ __global__ void __launch_bounds__(256) StableDtMarch3Kernel(StableDtArgs a, int 
       const W wl = ShflUp(w[0], 1);
       if (own) {
         // x: face i (i-1, i); face nx of a transmissive row (nx-1, nx-1)
-        take(smax[0], P::FaceMaxSpeed(eq, wl, w[0]));
-        if (i == nx - 1 && a.bc[0] != 0) take(smax[0], P::FaceMaxSpeed(eq, w[0], w[0]));
+        take(smr[0], P::FaceMaxSpeed(eq, wl, w[0]));
+        if (i == nx - 1 && a.bc[0] != 0) take(smr[0], P::FaceMaxSpeed(eq, w[0], w[0]));
         // y: face j (j-1, j); face ny of a transmissive column
         if (ytile) {
           R v[K];
           load(jm, k, v);
-          take(smax[1], P::FaceMaxSpeed(eq, P::MakeWave(eq, v, 1), w[1]));
+          take(smr[1], P::FaceMaxSpeed(eq, P::MakeWave(eq, v, 1), w[1]));
         }
-        if (ytop) take(smax[1], P::FaceMaxSpeed(eq, w[1], w[1]));
+        if (ytop) take(smr[1], P::FaceMaxSpeed(eq, w[1], w[1]));
         // z: face k (k-1, k); face nz of a transmissive column
         if (!(a.rule == 1 && !ReferenceTileFaceT(k, nz, a.width)))
-          take(smax[2], P::FaceMaxSpeed(eq, wz_prev, w[2]));
+          take(smr[2], P::FaceMaxSpeed(eq, wz_prev, w[2]));
         if (k == nz - 1 && a.bc[2] != 0 && !(a.rule == 1 && !ReferenceTileFaceT(nz, nz, a.width)))
-          take(smax[2], P::FaceMaxSpeed(eq, w[2], w[2]));
+          take(smr[2], P::FaceMaxSpeed(eq, w[2], w[2]));
       }
       wz_prev = w[2];
     }
   }
+  const double smax[3] = {static_cast<double>(smr[0]), static_cast<double>(smr[1]),
+                          static_cast<double>(smr[2])};
   BlockMaxAtomic<3>(a.smax_out, smax);
 }
 

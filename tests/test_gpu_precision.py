@@ -147,3 +147,36 @@ def test_mixed_x_sweep_matches_marching_kernel(fvs, bc, nx):
     np.testing.assert_array_equal(a[0, 0], b[0, 0].T)
     np.testing.assert_array_equal(a[1, 0], b[2, 0].T)
     np.testing.assert_array_equal(a[3, 0], b[3, 0].T)
+
+
+@pytest.mark.parametrize("xvariant", [0, 4, 5, 10, 14, 15])
+def test_mixed_launch_variants(fvs, orc, xvariant):
+    """Every launch variant of the mixed x sweep (lanes along x or marching,
+    three register budgets) gives the same accuracy and conservation, and the
+    y/z variants run too."""
+    n = 40
+    cons = workloads.octants_3d(n, seed=12)
+    dx = [1.0 / n] * 3
+    g = orc.Grid(3, [n] * 3, [0, 0, 0], dx)
+    m = orc.method()
+    s = fvs.Solver([n] * 3, dx, "periodic", method=fvs.make_method(precision="mixed"))
+    s.set_launch(0, 16, xvariant)
+    s.set_launch(1, 16, xvariant % 10)
+    s.set_launch(2, 32, xvariant % 10)
+    assert s.tuning()[1] == [xvariant, xvariant % 10, xvariant % 10]
+    s.upload(cons)
+    dt = 0.8 * g.stable_dt(m, cons)
+    s.step(dt, 0)
+    out = s.download()
+    ref = g.step(m, cons, dt, 0)
+    l1 = np.abs(out[0] - ref[0]).mean() / np.abs(ref[0]).mean()
+    assert l1 < 2e-7, l1
+    s.upload(cons)
+    s.run(cfl=0.8, t_end=10.0, max_steps=6)
+    tot0 = cons.reshape(5, -1).sum(1)
+    scale = np.abs(cons).reshape(5, -1).sum(1)
+    tot = s.download().reshape(5, -1).sum(1)
+    assert np.all(np.abs(tot - tot0) <= 1e-13 * scale)
+    with pytest.raises(fvs.FvsError):
+        s.set_launch(1, 16, 10)  # the marching-x variants exist for x only
+    s.close()
