@@ -420,6 +420,7 @@ def report_cutcell(args, torch, fvs, workloads):
         s.set_embedded_circles(circles)
         stream = torch.cuda.ExternalStream(s.stream_handle())
         s.upload(cons)
+        s.autotune()
         s.run(cfl=0.5, t_end=1e9, max_steps=3)
         s.upload(cons)
         torch.cuda.synchronize()

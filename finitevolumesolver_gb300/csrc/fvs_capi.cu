@@ -801,6 +801,8 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   }
   dt = std::isfinite(dt) ? 0.1 * dt : 1e-6;
   const int out = (s->cur + 1) % 3;
+  // cut cells: the sweeps read the wall reference states of the current state
+  if (s->cc) FVS_CUDA(CcReferenceStates(s, s->buf[s->cur]));
   for (int d = 0; d < s->g.rank; ++d) {
     const int nd = s->g.n[d];
     const int* occs = mixed ? (d == 0 ? occs_mixed_x : occs_mixed) : (df ? occs_df : occs_plain);

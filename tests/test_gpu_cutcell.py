@@ -60,12 +60,15 @@ def test_sweeps_bit_exact(fvs, orc, n, circles):
     s.close()
 
 
-def test_shock_over_circles_run_bit_exact(fvs, orc):
+@pytest.mark.parametrize("tuned", [False, True])
+def test_shock_over_circles_run_bit_exact(fvs, orc, tuned):
     n = 96
     circles, cons = workloads.shock_circles_2d(n, seed=5)
     ref = orc.CutCellGeometry(n, n, circles)
     s = solver_with(fvs, n, circles)
     s.upload(cons)
+    if tuned:  # the autotuner times cut-cell sweeps on the live state, leaving it unchanged
+        s.autotune()
     st, dts = s.run(cfl=0.5, t_end=10.0, max_steps=6, log_len=8)
     out, ref_dts, rs = ref.run(cons, 0.5, 10.0, max_steps=6)
     assert st.steps == 6 and st.restarts == rs
