@@ -56,9 +56,10 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
     load(dn, j0 - 1);
     P::ToCell(cc, dn);
     load(dn, j0);
+    using FluxT = typename FluxOf<P>::type;
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
-    double F_prev[K];
+    FluxT F_prev[K];
     for (int j = j0 - 1; j <= j1; ++j) {
       P::ToCell(cp, dn);
       if (j + 2 <= j1 + 1) load(dn, j + 2);
@@ -66,13 +67,13 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
       const typename P::Wave wv = P::MakeWave(eq, cc, DIR);
       if (j >= j0) {
-        double F[K];
-        const R s = P::Face(eq, F, recR_prev, recL, w_prev, wv, DIR, stats);
+        FluxT F[K];
+        const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, wv, DIR, stats);
         smax = s > smax ? s : smax;
         if (j == next_face) {
           double* dst = a.reg + int64_t(a.caps[cap].dst) * K;
 #pragma unroll
-          for (int c = 0; c < K; ++c) dst[c] = dst[c] + split_dt * F[c];
+          for (int c = 0; c < K; ++c) dst[c] = dst[c] + split_dt * FluxWiden(F[c]);
           ++cap;
           next_face = cap < w.cap_end ? a.caps[cap].face : INT_MAX;
         }
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
           const int64_t off = int64_t(w.base) + int64_t(j - 1 + kGhost) * w.stride;
 #pragma unroll
           for (int c = 0; c < K; ++c) {
-            const double v = __ldg(in + c * N + off) + dt_dx * (F_prev[c] - F[c]);
+            const double v = __ldg(in + c * N + off) + dt_dx * FluxDiff(F_prev[c], F[c]);
             out[c * N + off] = v;
             if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
           }

@@ -52,6 +52,13 @@ template <int D, typename T> struct FastBase {
     fast::PredictBoth<D, T>(eq, recL, recR, q0, q1, q2, limiter, T(lambda_half), dir);
   }
   using Stats = NoStats;
+  // the mixed flavour hands its FP32 fluxes to the sweep unwidened
+  static constexpr bool kFloatFlux = sizeof(T) == 4;
+  static __device__ __forceinline__ T FaceR(const Gas& eq, T* f, const Rec& L, const Rec& R,
+                                            const Wave& wL, const Wave& wR, int dir, Stats&) {
+    fast::HllFlux<D, T>(eq, f, L, R, dir);
+    return fast::FaceMaxSpeed<T>(eq, wL, wR);
+  }
   static __device__ __forceinline__ T Face(const Gas& eq, double* F, const Rec& L,
                                            const Rec& R, const Wave& wL, const Wave& wR,
                                            int dir, Stats&) {

@@ -20,6 +20,9 @@
 // evaluated once (the reference evaluates it for both faces of the cell).
 #pragma once
 
+#include <type_traits>
+
+#include "fvs_convert.cuh"
 #include "fvs_internal.h"
 
 #include <cstring>
@@ -115,6 +118,38 @@ __device__ __forceinline__ bool SweepGate(const SweepArgs& a, double split_dt) {
   return true;
 }
 
+// Policies whose face fluxes are computed in FP32 (the mixed flavour) hand
+// them to the sweep in FP32 (kFloatFlux); all others in FP64.
+template <class P, class = void> struct FluxOf {
+  using type = double;
+};
+template <class P> struct FluxOf<P, std::enable_if_t<P::kFloatFlux>> {
+  using type = float;
+};
+
+template <class P, class F>
+__device__ __forceinline__ typename P::Real SweepFace(const typename P::Gas& eq, F* flux,
+                                                      const typename P::Rec& L,
+                                                      const typename P::Rec& R,
+                                                      const typename P::Wave& wL,
+                                                      const typename P::Wave& wR, int dir,
+                                                      typename P::Stats& stats) {
+  if constexpr (std::is_same_v<F, float>) {
+    return P::FaceR(eq, flux, L, R, wL, wR, dir, stats);
+  } else {
+    return P::Face(eq, flux, L, R, wL, wR, dir, stats);
+  }
+}
+
+// F_L - F_R in FP64 for the conservative update: FP32 fluxes are widened
+// (exactly, on the integer pipe) and subtracted in FP64.
+__device__ __forceinline__ double FluxDiff(double a, double b) { return a - b; }
+__device__ __forceinline__ double FluxDiff(float a, float b) {
+  return FloatToDoubleBits(a) - FloatToDoubleBits(b);
+}
+__device__ __forceinline__ double FluxWiden(double a) { return a; }
+__device__ __forceinline__ double FluxWiden(float a) { return FloatToDoubleBits(a); }
+
 // Counters of the exact Riemann solver (Newton iterations, faces whose
 // Newton iteration did not converge); empty for the HLLE policies.
 struct NoStats {
@@ -205,9 +240,10 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
     load(dn, j0 - 1);
     P::ToCell(cc, dn);
     load(dn, j0);
+    using FluxT = typename FluxOf<P>::type;
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
-    double F_prev[K];
+    FluxT F_prev[K];
     for (int j = j0 - 1; j <= j1; ++j) {
       P::ToCell(cp, dn);
       if (j + 2 <= j1 + 1) load(dn, j + 2);
@@ -215,15 +251,15 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
       const typename P::Wave w = P::MakeWave(eq, cc, DIR);
       if (j >= j0) {
-        double F[K];
-        const R s = P::Face(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
+        FluxT F[K];
+        const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
         smax = s > smax ? s : smax;
         if (j > j0) {
           // cell j-1 (inside [0, nd)): U' = U + dt/dx (F_{j-1} - F_j)
           const int64_t off = base + int64_t(j - 1) * stride;
 #pragma unroll
           for (int c = 0; c < K; ++c) {
-            const double v = __ldg(in + c * cs + off) + dt_dx * (F_prev[c] - F[c]);
+            const double v = __ldg(in + c * cs + off) + dt_dx * FluxDiff(F_prev[c], F[c]);
             out[c * cs + off] = v;
             // non-positive density: sign bit set or zero (integer test)
             if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
@@ -344,14 +380,16 @@ __device__ __forceinline__ void XWarpRow(const SweepArgs& a, int64_t row, double
   // face -1 (between cells -2 and -1), used to update cell -1 on a periodic row
   const typename P::Rec wrecRm = ShflUp(wrecR, 1);
   const typename P::Wave wWm = ShflUp(wW, 1);
-  double Fw[K];
+  using FluxT = typename FluxOf<P>::type;
+  using Flx = CellArr<FluxT, K>;
+  FluxT Fw[K];
   typename P::Stats wstats;
-  P::Face(eq, Fw, wrecRm, wrecL, wWm, wW, 0, wstats);
+  SweepFace<P>(eq, Fw, wrecRm, wrecL, wWm, wW, 0, wstats);
   // carries into chunk 0 (from lane 31 = cell -1)
   typename P::Rec carry_rec = ShflIdx(wrecR, 31);
   typename P::Wave carry_w = ShflIdx(wW, 31);
   Cell carry_c = ShflIdx(Cw, 31);
-  Dbl carry_f;
+  Flx carry_f;
 #pragma unroll
   for (int c = 0; c < K; ++c) carry_f.v[c] = Fw[c];
   carry_f = ShflIdx(carry_f, 31);
@@ -382,13 +420,10 @@ __device__ __forceinline__ void XWarpRow(const SweepArgs& a, int64_t row, double
       recRm = carry_rec;
       Wm = carry_w;
     }
-    double F[K];
-    const R sp = P::Face(eq, F, recRm, recL, Wm, W, 0, stats);
+    Flx Fd;
+    const R sp = SweepFace<P>(eq, Fd.v, recRm, recL, Wm, W, 0, stats);
     if (valid) smax = sp > smax ? sp : smax;
-    Dbl Fd;
-#pragma unroll
-    for (int c = 0; c < K; ++c) Fd.v[c] = F[c];
-    Dbl Fm = ShflUp(Fd, 1);
+    Flx Fm = ShflUp(Fd, 1);
     if (lane == 0) Fm = carry_f;
     // update cell x-1 (lane 0 of chunk 0: cell -1, i.e. nx-1 on a periodic row);
     // its FP64 state is re-read (a coalesced L1 hit) rather than shuffled
@@ -397,7 +432,7 @@ __device__ __forceinline__ void XWarpRow(const SweepArgs& a, int64_t row, double
       const int64_t off = base + BcIndex(x - 1, nx, a.bc);
 #pragma unroll
       for (int c = 0; c < K; ++c) {
-        const double v = __ldg(in + c * cs + off) + dt_dx * (Fm.v[c] - Fd.v[c]);
+        const double v = __ldg(in + c * cs + off) + dt_dx * FluxDiff(Fm.v[c], Fd.v[c]);
         out[c * cs + off] = v;
         if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
       }
@@ -415,14 +450,14 @@ __device__ __forceinline__ void XWarpRow(const SweepArgs& a, int64_t row, double
     typename P::Rec recL, recR;
     P::Predict(eq, recL, recR, carry_c.v, carry_c.v, carry_c.v, a.limiter, lambda_half, 0);
     const typename P::Wave W = P::MakeWave(eq, carry_c.v, 0);
-    double F[K];
-    const R sp = P::Face(eq, F, carry_rec, recL, carry_w, W, 0, stats);
+    FluxT F[K];
+    const R sp = SweepFace<P>(eq, F, carry_rec, recL, carry_w, W, 0, stats);
     if (lane == 0) {
       smax = sp > smax ? sp : smax;
       const int64_t off = base + (nx - 1);
 #pragma unroll
       for (int c = 0; c < K; ++c) {
-        const double v = __ldg(in + c * cs + off) + dt_dx * (carry_f.v[c] - F[c]);
+        const double v = __ldg(in + c * cs + off) + dt_dx * FluxDiff(carry_f.v[c], F[c]);
         out[c * cs + off] = v;
         if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
       }
