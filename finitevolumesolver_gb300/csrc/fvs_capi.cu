@@ -293,6 +293,7 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
     c.ctrl = ctrl;
     c.prev_check = prev_check;
     c.prev_dx = prev_dx;
+    c.occupancy = s->occ_tuned[dir];
     return s->m.precision == FVS_FP64_EXACT
                ? fvs::LaunchCutCellSweep(c, s->stream)
                : fvs::LaunchCutCellSweepT(s->m.precision, c, s->stream);
@@ -767,6 +768,7 @@ int fvs_solver_set_launch(fvs_solver* s, int dir, int seg_len, int variant) {
     ok = variant == 0 || variant == 4 || variant == 5 ||
          (dir == 0 && (variant == 10 || variant == 14 || variant == 15));
   if (s->m.precision == FVS_FP64_DF && plain_hlle) ok = variant == 0 || variant == 3;
+  if (s->cc) ok = variant == 0 || variant == (s->m.precision == FVS_MIXED ? 4 : 3);
   if (!ok) return Fail(FVS_ERR_INVALID, "no such launch variant for this method");
   s->seg_tuned[dir] = seg_len;
   s->occ_tuned[dir] = variant;
@@ -790,6 +792,10 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   const int occs_mixed[] = {0, 4, 5};
   const int occs_df[] = {0, 3};
   const int occs_plain[] = {0};
+  // cut cells: the KBN sweep in its default and its higher-occupancy build
+  const int occs_cc64[] = {0, 3};
+  const int occs_cc32[] = {0, 4};
+  const bool cc32 = s->cc && s->m.precision == FVS_MIXED;
   const int saved = s->seg_len;
   cudaEvent_t e0, e1;
   FVS_CUDA(cudaEventCreate(&e0));
@@ -805,8 +811,9 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   if (s->cc) FVS_CUDA(CcReferenceStates(s, s->buf[s->cur]));
   for (int d = 0; d < s->g.rank; ++d) {
     const int nd = s->g.n[d];
-    const int* occs = mixed ? (d == 0 ? occs_mixed_x : occs_mixed) : (df ? occs_df : occs_plain);
-    const int nocc = mixed ? (d == 0 ? 6 : 3) : (df ? 2 : 1);
+    const int* occs = mixed ? (d == 0 ? occs_mixed_x : occs_mixed)
+                            : (df ? occs_df : (s->cc ? (cc32 ? occs_cc32 : occs_cc64) : occs_plain));
+    const int nocc = mixed ? (d == 0 ? 6 : 3) : ((df || s->cc) ? 2 : 1);
     float best = 1e30f;
     int best_seg = 0, best_occ = 0;
     for (int oi = 0; oi < nocc; ++oi) {

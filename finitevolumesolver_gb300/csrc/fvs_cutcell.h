@@ -74,6 +74,8 @@ struct CcSweepArgs {
   Control* ctrl;
   int prev_check;
   double prev_dx;
+  int occupancy;  // 0, or resident 128-thread blocks per SM the kernel is compiled for
+                  // (FP64: 3, FP32 reconstruction: 4)
 };
 
 cudaError_t LaunchCutCellGeometry(const CcGeomArgs& a, const CcGeom& g, cudaStream_t s);

@@ -321,7 +321,8 @@ struct FaceData {
   double beta, us, sL, sR;
 };
 
-template <class T> __global__ void __launch_bounds__(128) KbnSweepKernel(CcSweepArgs a) {
+template <class T, int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a) {
   const CcGeom& g = a.s.g;
   const int dir = a.dir;
   const int nd = dir == 0 ? g.nx : g.ny;
@@ -578,7 +579,13 @@ template <class T> cudaError_t LaunchKbnSweep(const CcSweepArgs& a, cudaStream_t
   CcSweepArgs b = a;
   b.seg_len = seg;
   dim3 grid(unsigned((nt + block - 1) / block), unsigned((nd + seg - 1) / seg));
-  KbnSweepKernel<T><<<grid, block, 0, s>>>(b);
+  // register/occupancy variant: the default, or compiled for 3 (FP64) / 4 (FP32)
+  // resident blocks per SM (spilling a little)
+  constexpr int kMore = sizeof(T) == 4 ? 4 : 3;
+  if (a.occupancy == kMore)
+    KbnSweepKernel<T, kMore><<<grid, block, 0, s>>>(b);
+  else
+    KbnSweepKernel<T, 1><<<grid, block, 0, s>>>(b);
   return cudaGetLastError();
 }
 

@@ -60,15 +60,18 @@ def test_sweeps_bit_exact(fvs, orc, n, circles):
     s.close()
 
 
-@pytest.mark.parametrize("tuned", [False, True])
-def test_shock_over_circles_run_bit_exact(fvs, orc, tuned):
+@pytest.mark.parametrize("launch", ["default", "tuned", "occupancy3"])
+def test_shock_over_circles_run_bit_exact(fvs, orc, launch):
     n = 96
     circles, cons = workloads.shock_circles_2d(n, seed=5)
     ref = orc.CutCellGeometry(n, n, circles)
     s = solver_with(fvs, n, circles)
     s.upload(cons)
-    if tuned:  # the autotuner times cut-cell sweeps on the live state, leaving it unchanged
+    if launch == "tuned":  # timed on the live state, which it leaves unchanged
         s.autotune()
+    elif launch == "occupancy3":  # the KBN sweep built for 3 blocks per SM
+        s.set_launch(0, 16, 3)
+        s.set_launch(1, 32, 3)
     st, dts = s.run(cfl=0.5, t_end=10.0, max_steps=6, log_len=8)
     out, ref_dts, rs = ref.run(cons, 0.5, 10.0, max_steps=6)
     assert st.steps == 6 and st.restarts == rs
@@ -82,7 +85,8 @@ def _totals(a):
 
 
 @pytest.mark.parametrize("prec", ["fp64_fast", "mixed"])
-def test_flavours_track_exact_and_conserve(fvs, orc, prec):
+@pytest.mark.parametrize("variant", [False, True])
+def test_flavours_track_exact_and_conserve(fvs, orc, prec, variant):
     """Fast FP64 stays within 1e-12 of the exact flavour; mixed within the
     FP32 reconstruction error.  Periodic in x and y with the body inside the
     domain: the volume-weighted mass and energy change only through the FP64
@@ -101,6 +105,9 @@ def test_flavours_track_exact_and_conserve(fvs, orc, prec):
     st_e, dts_e = ex.run(cfl=0.5, t_end=10.0, max_steps=10, log_len=10)
     s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "periodic", method=fvs.make_method(precision=prec))
     s.set_embedded_circles(circles)
+    if variant:  # the KBN sweep's higher-occupancy build
+        for d in (0, 1):
+            s.set_launch(d, 32, 4 if prec == "mixed" else 3)
     s.upload(cons)
     st, dts = s.run(cfl=0.5, t_end=10.0, max_steps=10, log_len=10)
     out, ref = s.download(), ex.download()
