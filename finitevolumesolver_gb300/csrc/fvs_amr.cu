@@ -485,11 +485,13 @@ cudaError_t LaunchMaxSpeed(fvs_amr* a, int l, int d) {
   MaxSpeedArgs s{};
   s.in = Lv.A;
   s.ncells = int32_t(Lv.ncells);
-  s.rows = Lv.rows[d];
-  s.nrows = Lv.nrows[d];
+  s.segs = Lv.segs[d][kSplits - 1];  // rows in 8 segments
+  s.nsegs = Lv.nsegs[d][kSplits - 1];
   s.gamma = a->m.gamma;
   s.smax_out = &a->ctrl->smax_stable[l][d];
-  const int grid = Lv.grid[d], block = Lv.block[d];
+  const int block = 128;
+  const int grid = static_cast<int>(std::max<int64_t>(
+      1, std::min<int64_t>((int64_t(s.nsegs) + block - 1) / block, int64_t(a->sms) * 16)));
   switch (a->m.precision) {
   case FVS_FP64_EXACT:
     return LaunchPatchMaxSpeedExact(d, s, grid, block, a->stream);

@@ -118,8 +118,8 @@ struct PatchSweepArgs {
 struct MaxSpeedArgs {
   const double* in;
   int32_t ncells;
-  const Row* rows;
-  int32_t nrows;
+  const Seg* segs;  // the level's rows in this direction, split into segments
+  int32_t nsegs;
   double gamma;
   unsigned long long* smax_out;
 };

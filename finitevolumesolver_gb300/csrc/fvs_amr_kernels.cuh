@@ -104,7 +104,9 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
 }
 
 // Max signal speed over the faces 0..n of every row (the stable dt of the
-// level in that direction is dx / max).
+// level in that direction is dx / max): a segment [j0, j1) of a row takes
+// the faces j0..j1 (neighbouring segments share a face; the max does not
+// mind), so short segments give every row several threads.
 template <int DIR, template <int> class PT>
 __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
   using P = PT<2>;
@@ -113,9 +115,9 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
   const typename P::Gas eq = P::MakeGas(a.gamma);
   const int64_t N = a.ncells;
   R smax = R(0);
-  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.nrows;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.nsegs;
        r += gridDim.x * blockDim.x) {
-    const Row w = a.rows[r];
+    const Seg w = a.segs[r];
     auto wave = [&](int j) {
       const int64_t off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
       double u[K];
@@ -125,8 +127,8 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
       P::ToCell(v, u);
       return P::MakeWave(eq, v, DIR);
     };
-    typename P::Wave wl = wave(-1);
-    for (int f = 0; f <= w.n; ++f) {
+    typename P::Wave wl = wave(w.j0 - 1);
+    for (int f = w.j0; f <= w.j1; ++f) {
       const typename P::Wave wr = wave(f);
       const R s = P::FaceMaxSpeed(eq, wl, wr);
       smax = s > smax ? s : smax;
@@ -151,7 +153,7 @@ cudaError_t LaunchPatchSweepT(int dir, const PatchSweepArgs& a, int grid, int bl
 template <template <int> class PT>
 cudaError_t LaunchPatchMaxSpeedT(int dir, const MaxSpeedArgs& a, int grid, int block,
                                  cudaStream_t s) {
-  if (a.nrows == 0) return cudaSuccess;
+  if (a.nsegs == 0) return cudaSuccess;
   if (dir == 0)
     PatchMaxSpeedKernel<0, PT><<<grid, block, 0, s>>>(a);
   else
