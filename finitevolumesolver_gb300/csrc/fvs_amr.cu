@@ -58,8 +58,8 @@ struct LevelHost {
   int32_t nsegs[2][kSplits] = {};
   int split[2] = {0, 0};  // index into kSplitOf
   Cap* caps[2] = {nullptr, nullptr};
-  Ghost* ghosts = nullptr;
-  int32_t nghosts = 0;
+  Ghost* ghosts[2] = {nullptr, nullptr};  // the x-side and the y-side strips
+  int32_t nghosts[2] = {0, 0};
   RefluxCell* reflux = nullptr;
   int32_t nreflux = 0;
   AvgDown* avg = nullptr;
@@ -222,13 +222,16 @@ int Build(fvs_amr* a) {
     }
   }
 
-  // ghost gathers
-  std::vector<std::vector<Ghost>> ghosts_h(static_cast<size_t>(nl));
+  // ghost gathers, per level and side: a sweep along d reads only the strips
+  // at the ends of its rows (the d-side strips)
+  std::vector<std::vector<Ghost>> ghosts_h[2];
+  ghosts_h[0].resize(static_cast<size_t>(nl));
+  ghosts_h[1].resize(static_cast<size_t>(nl));
   for (int l = 0; l < nl; ++l) {
     const LevelHost& L = a->L[size_t(l)];
     for (int p : L.patches) {
       const PatchHost& P = a->patches[size_t(p)];
-      auto add = [&](int li, int lj) -> int {
+      auto add = [&](int side, int li, int lj) -> int {
         const int gi = P.lo[0] + li, gj = P.lo[1] + lj;
         const int si = a->MapCoord(gi, L.n[0], 0), sj = a->MapCoord(gj, L.n[1], 1);
         Ghost g{};
@@ -246,22 +249,23 @@ int Build(fvs_amr* a) {
                             std::to_string(l) + " has no coarser cell under it");
           g.src = -a->SI(co, si >> 1, sj >> 1) - 1;
         }
-        ghosts_h[size_t(l)].push_back(g);
+        ghosts_h[side][size_t(l)].push_back(g);
         return FVS_OK;
       };
       for (int lj = 0; lj < P.n[1]; ++lj)
         for (int g = 1; g <= kGhost; ++g) {
-          if (int r = add(-g, lj)) return r;
-          if (int r = add(P.n[0] - 1 + g, lj)) return r;
+          if (int r = add(0, -g, lj)) return r;
+          if (int r = add(0, P.n[0] - 1 + g, lj)) return r;
         }
       for (int li = 0; li < P.n[0]; ++li)
         for (int g = 1; g <= kGhost; ++g) {
-          if (int r = add(li, -g)) return r;
-          if (int r = add(li, P.n[1] - 1 + g)) return r;
+          if (int r = add(1, li, -g)) return r;
+          if (int r = add(1, li, P.n[1] - 1 + g)) return r;
         }
     }
-    std::sort(ghosts_h[size_t(l)].begin(), ghosts_h[size_t(l)].end(),
-              [](const Ghost& x, const Ghost& y) { return x.dst < y.dst; });
+    for (int side = 0; side < 2; ++side)
+      std::sort(ghosts_h[side][size_t(l)].begin(), ghosts_h[side][size_t(l)].end(),
+                [](const Ghost& x, const Ghost& y) { return x.dst < y.dst; });
   }
 
   // coarse-fine faces (register slots), captures, reflux and average-down
@@ -414,8 +418,10 @@ int Build(fvs_amr* a) {
         AMR_CUDA(a->Upload(&Lv.segs[d][si], segs));
       }
     }
-    AMR_CUDA(a->Upload(&Lv.ghosts, ghosts_h[size_t(l)]));
-    Lv.nghosts = int32_t(ghosts_h[size_t(l)].size());
+    for (int side = 0; side < 2; ++side) {
+      AMR_CUDA(a->Upload(&Lv.ghosts[side], ghosts_h[side][size_t(l)]));
+      Lv.nghosts[side] = int32_t(ghosts_h[side][size_t(l)].size());
+    }
     AMR_CUDA(a->Upload(&Lv.reflux, reflux_h[size_t(l)]));
     Lv.nreflux = int32_t(reflux_h[size_t(l)].size());
     AMR_CUDA(a->Upload(&Lv.avg, avg_h[size_t(l)]));
@@ -502,11 +508,19 @@ cudaError_t LaunchMaxSpeed(fvs_amr* a, int l, int d) {
   }
 }
 
-cudaError_t FillGhosts(fvs_amr* a, int l, double* buf) {
+// Refills the ghost strips of level l on side `side` (0: x ends of the rows,
+// 1: y ends), or both for side < 0.
+cudaError_t FillGhosts(fvs_amr* a, int l, double* buf, int side = -1) {
   const LevelHost& Lv = a->L[size_t(l)];
   const LevelHost* C = l > 0 ? &a->L[size_t(l - 1)] : nullptr;
-  return LaunchGhostFill(buf, int32_t(Lv.ncells), C ? C->A : nullptr,
-                         C ? int32_t(C->ncells) : 0, Lv.ghosts, Lv.nghosts, a->stream);
+  for (int sd = 0; sd < 2; ++sd) {
+    if (side >= 0 && sd != side) continue;
+    const cudaError_t e = LaunchGhostFill(buf, int32_t(Lv.ncells), C ? C->A : nullptr,
+                                          C ? int32_t(C->ncells) : 0, Lv.ghosts[sd],
+                                          Lv.nghosts[sd], a->stream);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 LevelDx Dx(const fvs_amr* a) {
@@ -538,7 +552,7 @@ cudaError_t AdvanceLevel(fvs_amr* a, int l, int parity, int sub, int& counter) {
   int cur = 0;
   for (int k = 0; k < 4; ++k) {
     const int d = seq[k];
-    if ((e = FillGhosts(a, l, bufs[cur])) != cudaSuccess) return e;
+    if ((e = FillGhosts(a, l, bufs[cur], d)) != cudaSuccess) return e;
     if ((e = LaunchSweep(a, l, d, bufs[cur], bufs[1 - cur], 0.5 / double(1 << l), &a->ctrl->dt,
                          &a->ctrl->smax_sweep[counter++], Lv.block[d], Lv.grid[d], Lv.occ[d],
                          Lv.split[d])) !=
