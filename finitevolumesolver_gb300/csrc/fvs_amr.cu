@@ -1,21 +1,23 @@
 // fvs_amr.cu -- host side of the batched AMR patch update (2-D, ratio 2).
 //
 // Builds, once per hierarchy, every table the device needs: the rows of the
-// patches per level and direction (the work of one persistent sweep launch),
-// the ghost-cell gather lists (same-level copies, piecewise-constant
-// injection from the coarser level, boundary conditions), the flux-register
-// captures, the reflux lists and the average-down lists.  A coarse step --
-// ghost fill, stable dt of every level, dt selection, the fine-first
-// subcycled Strang sweeps of all levels, refluxing, average-down and the
-// per-sweep CFL checks -- is one CUDA graph (one per parity of the cycle
-// counter, which fixes the direction order).  The semantics follow
+// patches per level and direction (the work of one persistent sweep launch)
+// with the sources of their halo cells (same-level cells after the boundary
+// condition's mapping, or piecewise-constant injection from the coarser
+// level), the flux-register captures, the reflux lists and the average-down
+// lists.  A coarse step -- stable dt of every level, dt selection, the
+// fine-first subcycled Strang sweeps of all levels, refluxing, average-down
+// and the per-sweep CFL checks -- is one CUDA graph (one per parity of the
+// cycle counter, which fixes the direction order).  The semantics follow
 // SubcycleFineFirstSolver (include/fub/solver/SubcycleFineFirstSolver.hpp:
 // 100-191) and DimensionalSplitLevelIntegrator (include/fub/solver/
 // DimensionalSplitLevelIntegrator.hpp:204-276) with these rules of this
-// library: every sweep refills its level's ghost cells (so a level split
-// into patches advances exactly like one uniform grid), and a fine level's
-// ghost cells outside that level are injected from the coarser level's
-// state at the start of the coarse step (fine levels advance first).
+// library: every sweep sees its level's ghost cells as they are at that
+// sweep (it reads a row's halo from the neighbouring patch's current cells,
+// so a level split into patches advances exactly like one uniform grid), and
+// a fine level's ghost cells outside that level are injected from the
+// coarser level's state at the start of the coarse step (fine levels advance
+// first).
 #include "../../include/fvs_gpu.h"
 #include "fvs_amr.h"
 #include "fvs_internal.h"
@@ -58,8 +60,6 @@ struct LevelHost {
   int32_t nsegs[2][kSplits] = {};
   int split[2] = {0, 0};  // index into kSplitOf
   Cap* caps[2] = {nullptr, nullptr};
-  Ghost* ghosts[2] = {nullptr, nullptr};  // the x-side and the y-side strips
-  int32_t nghosts[2] = {0, 0};
   RefluxCell* reflux = nullptr;
   int32_t nreflux = 0;
   AvgDown* avg = nullptr;
@@ -222,50 +222,43 @@ int Build(fvs_amr* a) {
     }
   }
 
-  // ghost gathers, per level and side: a sweep along d reads only the strips
-  // at the ends of its rows (the d-side strips)
-  std::vector<std::vector<Ghost>> ghosts_h[2];
-  ghosts_h[0].resize(static_cast<size_t>(nl));
-  ghosts_h[1].resize(static_cast<size_t>(nl));
+  // halo sources of every row end: the cell a ghost fill would copy into the
+  // halo (same level after the boundary condition's mapping, else the
+  // coarser cell under it); also checks the nesting of the patches
   for (int l = 0; l < nl; ++l) {
     const LevelHost& L = a->L[size_t(l)];
     for (int p : L.patches) {
       const PatchHost& P = a->patches[size_t(p)];
-      auto add = [&](int side, int li, int lj) -> int {
+      auto src_of = [&](int li, int lj, int32_t& src) -> int {
         const int gi = P.lo[0] + li, gj = P.lo[1] + lj;
         const int si = a->MapCoord(gi, L.n[0], 0), sj = a->MapCoord(gj, L.n[1], 1);
-        Ghost g{};
-        g.dst = P.block_start + (lj + kGhost) * P.pitch + (li + kGhost);
         const int32_t o = L.Owner(si, sj);
         if (o >= 0) {
-          g.src = a->SI(o, si, sj);
-        } else {
-          if (l == 0) return Fail(FVS_ERR_INVALID, "level 0 does not cover the domain");
-          const LevelHost& C = a->L[size_t(l - 1)];
-          const int32_t co = C.Owner(si >> 1, sj >> 1);
-          if (co < 0)
-            return Fail(FVS_ERR_INVALID,
-                        "patches are not properly nested: a ghost cell of level " +
-                            std::to_string(l) + " has no coarser cell under it");
-          g.src = -a->SI(co, si >> 1, sj >> 1) - 1;
+          src = a->SI(o, si, sj);
+          return FVS_OK;
         }
-        ghosts_h[side][size_t(l)].push_back(g);
+        if (l == 0) return Fail(FVS_ERR_INVALID, "level 0 does not cover the domain");
+        const LevelHost& C = a->L[size_t(l - 1)];
+        const int32_t co = C.Owner(si >> 1, sj >> 1);
+        if (co < 0)
+          return Fail(FVS_ERR_INVALID,
+                      "patches are not properly nested: a ghost cell of level " +
+                          std::to_string(l) + " has no coarser cell under it");
+        src = -a->SI(co, si >> 1, sj >> 1) - 1;
         return FVS_OK;
       };
-      for (int lj = 0; lj < P.n[1]; ++lj)
-        for (int g = 1; g <= kGhost; ++g) {
-          if (int r = add(0, -g, lj)) return r;
-          if (int r = add(0, P.n[0] - 1 + g, lj)) return r;
+      for (int d = 0; d < 2; ++d) {
+        const int nt = P.n[1 - d], nd = P.n[d];
+        for (int t = 0; t < nt; ++t) {
+          Row& r = rows_h[d][size_t(l)][size_t(P.row_offset[d] + t)];
+          const int pos[4] = {-2, -1, nd, nd + 1};
+          for (int h = 0; h < 4; ++h) {
+            const int li = d == 0 ? pos[h] : t, lj = d == 0 ? t : pos[h];
+            if (int e = src_of(li, lj, r.halo[h])) return e;
+          }
         }
-      for (int li = 0; li < P.n[0]; ++li)
-        for (int g = 1; g <= kGhost; ++g) {
-          if (int r = add(1, li, -g)) return r;
-          if (int r = add(1, li, P.n[1] - 1 + g)) return r;
-        }
+      }
     }
-    for (int side = 0; side < 2; ++side)
-      std::sort(ghosts_h[side][size_t(l)].begin(), ghosts_h[side][size_t(l)].end(),
-                [](const Ghost& x, const Ghost& y) { return x.dst < y.dst; });
   }
 
   // coarse-fine faces (register slots), captures, reflux and average-down
@@ -402,6 +395,8 @@ int Build(fvs_amr* a) {
             Seg sg{};
             sg.base = R[r].base;
             sg.stride = R[r].stride;
+            sg.n = nn;
+            for (int h = 0; h < 4; ++h) sg.halo[h] = R[r].halo[h];
             sg.j0 = int32_t(int64_t(k) * nn / parts);
             sg.j1 = int32_t(int64_t(k + 1) * nn / parts);
             sg.cap_begin = c;
@@ -417,10 +412,6 @@ int Build(fvs_amr* a) {
         Lv.nsegs[d][si] = int32_t(segs.size());
         AMR_CUDA(a->Upload(&Lv.segs[d][si], segs));
       }
-    }
-    for (int side = 0; side < 2; ++side) {
-      AMR_CUDA(a->Upload(&Lv.ghosts[side], ghosts_h[side][size_t(l)]));
-      Lv.nghosts[side] = int32_t(ghosts_h[side][size_t(l)].size());
     }
     AMR_CUDA(a->Upload(&Lv.reflux, reflux_h[size_t(l)]));
     Lv.nreflux = int32_t(reflux_h[size_t(l)].size());
@@ -465,6 +456,12 @@ cudaError_t LaunchSweep(fvs_amr* a, int l, int d, const double* in, double* out,
   s.in = in;
   s.out = out;
   s.ncells = int32_t(Lv.ncells);
+  // halo cells injected from the coarser level's state at the start of the
+  // coarse step (finer levels advance first, so its A buffer still holds it)
+  if (l > 0) {
+    s.coarse = a->L[size_t(l - 1)].A;
+    s.coarse_ncells = int32_t(a->L[size_t(l - 1)].ncells);
+  }
   s.segs = Lv.segs[d][split];
   s.nsegs = Lv.nsegs[d][split];
   s.caps = Lv.caps[d];
@@ -491,6 +488,10 @@ cudaError_t LaunchMaxSpeed(fvs_amr* a, int l, int d) {
   MaxSpeedArgs s{};
   s.in = Lv.A;
   s.ncells = int32_t(Lv.ncells);
+  if (l > 0) {
+    s.coarse = a->L[size_t(l - 1)].A;
+    s.coarse_ncells = int32_t(a->L[size_t(l - 1)].ncells);
+  }
   s.segs = Lv.segs[d][kSplits - 1];  // rows in 8 segments
   s.nsegs = Lv.nsegs[d][kSplits - 1];
   s.gamma = a->m.gamma;
@@ -506,21 +507,6 @@ cudaError_t LaunchMaxSpeed(fvs_amr* a, int l, int d) {
   default:
     return LaunchPatchMaxSpeedMixed(d, s, grid, block, a->stream);
   }
-}
-
-// Refills the ghost strips of level l on side `side` (0: x ends of the rows,
-// 1: y ends), or both for side < 0.
-cudaError_t FillGhosts(fvs_amr* a, int l, double* buf, int side = -1) {
-  const LevelHost& Lv = a->L[size_t(l)];
-  const LevelHost* C = l > 0 ? &a->L[size_t(l - 1)] : nullptr;
-  for (int sd = 0; sd < 2; ++sd) {
-    if (side >= 0 && sd != side) continue;
-    const cudaError_t e = LaunchGhostFill(buf, int32_t(Lv.ncells), C ? C->A : nullptr,
-                                          C ? int32_t(C->ncells) : 0, Lv.ghosts[sd],
-                                          Lv.nghosts[sd], a->stream);
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
 }
 
 LevelDx Dx(const fvs_amr* a) {
@@ -552,7 +538,6 @@ cudaError_t AdvanceLevel(fvs_amr* a, int l, int parity, int sub, int& counter) {
   int cur = 0;
   for (int k = 0; k < 4; ++k) {
     const int d = seq[k];
-    if ((e = FillGhosts(a, l, bufs[cur], d)) != cudaSuccess) return e;
     if ((e = LaunchSweep(a, l, d, bufs[cur], bufs[1 - cur], 0.5 / double(1 << l), &a->ctrl->dt,
                          &a->ctrl->smax_sweep[counter++], Lv.block[d], Lv.grid[d], Lv.occ[d],
                          Lv.split[d])) !=
@@ -583,8 +568,6 @@ cudaError_t EnqueueStep(fvs_amr* a, int parity) {
   e = cudaMemsetAsync(&a->ctrl->smax_stable[0][0], 0,
                       sizeof(a->ctrl->smax_stable) + sizeof(a->ctrl->smax_sweep), a->stream);
   if (e != cudaSuccess) return e;
-  for (int l = 0; l < a->nlevels; ++l)
-    if ((e = FillGhosts(a, l, a->L[size_t(l)].A)) != cudaSuccess) return e;
   for (int l = 0; l < a->nlevels; ++l)
     for (int d = 0; d < 2; ++d)
       if ((e = LaunchMaxSpeed(a, l, d)) != cudaSuccess) return e;
@@ -834,7 +817,6 @@ int fvs_amr_stable_dt(fvs_amr* a, double* dt) {
   if (!a || !dt) return Fail(FVS_ERR_INVALID, "NULL argument");
   AMR_CUDA(cudaMemsetAsync(&a->ctrl->smax_stable[0][0], 0, sizeof(a->ctrl->smax_stable),
                            a->stream));
-  for (int l = 0; l < a->nlevels; ++l) AMR_CUDA(FillGhosts(a, l, a->L[size_t(l)].A));
   for (int l = 0; l < a->nlevels; ++l)
     for (int d = 0; d < 2; ++d) AMR_CUDA(LaunchMaxSpeed(a, l, d));
   unsigned long long bits[kMaxLevels][2];
@@ -921,7 +903,6 @@ int fvs_amr_autotune(fvs_amr* a, int32_t* configs) {
   if (!a) return Fail(FVS_ERR_INVALID, "NULL argument");
   const double dt_small = 1e-9;
   AMR_CUDA(cudaMemcpy(a->tune_dt, &dt_small, sizeof dt_small, cudaMemcpyHostToDevice));
-  for (int l = 0; l < a->nlevels; ++l) AMR_CUDA(FillGhosts(a, l, a->L[size_t(l)].A));
   cudaEvent_t e0, e1;
   AMR_CUDA(cudaEventCreate(&e0));
   AMR_CUDA(cudaEventCreate(&e1));

@@ -22,12 +22,17 @@ constexpr int kComp = 4;  // rho, m_x, m_y, E
 // per coarse step at most 4 sweeps on each of 1 + 2 + 4 + 8 level subcycles
 constexpr int kMaxSweeps = 4 * 15;
 
+// Where a sweep reads a row's halo cells (positions -2, -1, n, n+1 along the
+// row): cell `src` of the same level's current buffer (src >= 0) or cell
+// -src-1 of the next coarser level (piecewise-constant injection).  Reading
+// them there at sweep time is the ghost fill of the row's two end strips.
 // One row (x sweep) or column (y sweep) of one patch.
 struct Row {
   int32_t base;     // storage index of the row's first ghost cell (interior -2)
   int32_t stride;   // 1 for x rows, the patch pitch for y columns
   int32_t n;        // interior cells
   int32_t cap_end;  // captures of this row: [previous row's cap_end, cap_end)
+  int32_t halo[4];  // sources of the halo cells -2, -1, n, n+1
 };
 
 // A segment [j0, j1) of a row, the work item of a sweep thread: it computes
@@ -40,6 +45,8 @@ struct Seg {
   int32_t stride;
   int32_t j0, j1;
   int32_t cap_begin, cap_end;
+  int32_t n;        // the row's interior cells
+  int32_t halo[4];  // the row's halo sources (Row::halo)
 };
 
 constexpr int kSplits = 4;  // rows are offered split into 1, 2, 4 or 8 segments
@@ -52,12 +59,6 @@ struct Cap {
   int32_t dst;
 };
 
-// Ghost cell `dst` of a level takes the value of cell `src` of the same
-// level (src >= 0) or of cell -src-1 of the next coarser level.
-struct Ghost {
-  int32_t dst;
-  int32_t src;
-};
 
 // Reflux of one coarse cell from `count` register slots starting at
 // `first`; the slot's sign is +1 for the cell's low face, -1 for its high face.
@@ -102,6 +103,8 @@ struct PatchSweepArgs {
   const double* in;
   double* out;
   int32_t ncells;  // component stride of the level
+  const double* coarse;   // the next coarser level's state (halo injection)
+  int32_t coarse_ncells;
   const Seg* segs;
   int32_t nsegs;
   const Cap* caps;
@@ -118,6 +121,8 @@ struct PatchSweepArgs {
 struct MaxSpeedArgs {
   const double* in;
   int32_t ncells;
+  const double* coarse;
+  int32_t coarse_ncells;
   const Seg* segs;  // the level's rows in this direction, split into segments
   int32_t nsegs;
   double gamma;
@@ -140,8 +145,6 @@ cudaError_t LaunchPatchMaxSpeedFast(int dir, const MaxSpeedArgs& a, int grid, in
                                     cudaStream_t s);
 cudaError_t LaunchPatchMaxSpeedMixed(int dir, const MaxSpeedArgs& a, int grid, int block,
                                      cudaStream_t s);
-cudaError_t LaunchGhostFill(double* dst, int32_t n_dst, const double* coarse, int32_t n_coarse,
-                            const Ghost* g, int32_t count, cudaStream_t s);
 cudaError_t LaunchReflux(double* coarse, int32_t n_coarse, const double* reg,
                          const RefluxCell* cells, int32_t ncells, const float* signs, double dx,
                          cudaStream_t s);

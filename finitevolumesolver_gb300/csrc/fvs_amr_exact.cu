@@ -20,31 +20,6 @@ cudaError_t LaunchPatchMaxSpeedExact(int dir, const MaxSpeedArgs& a, int grid, i
   return LaunchPatchMaxSpeedT<ExactPolicy>(dir, a, grid, block, s);
 }
 
-// Ghost cells from the level's own interior cells or the coarser level.
-__global__ void GhostFillKernel(double* dst, int32_t n_dst, const double* coarse,
-                                int32_t n_coarse, const Ghost* g, int32_t count) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= count) return;
-  const Ghost e = g[i];
-  if (e.src >= 0) {
-#pragma unroll
-    for (int c = 0; c < kComp; ++c)
-      dst[int64_t(c) * n_dst + e.dst] = dst[int64_t(c) * n_dst + e.src];
-  } else {
-    const int32_t src = -e.src - 1;
-#pragma unroll
-    for (int c = 0; c < kComp; ++c)
-      dst[int64_t(c) * n_dst + e.dst] = coarse[int64_t(c) * n_coarse + src];
-  }
-}
-
-cudaError_t LaunchGhostFill(double* dst, int32_t n_dst, const double* coarse, int32_t n_coarse,
-                            const Ghost* g, int32_t count, cudaStream_t s) {
-  if (count == 0) return cudaSuccess;
-  GhostFillKernel<<<(count + 255) / 256, 256, 0, s>>>(dst, n_dst, coarse, n_coarse, g, count);
-  return cudaGetLastError();
-}
-
 // U += s * (0.5 * (F1 + F2) - Fc) / dx for each register slot of the cell,
 // in slot order (register entry 3k: coarse sum, 3k+1 and 3k+2: the fine
 // sub-faces' sums).

@@ -9,8 +9,9 @@
 // accumulates dt_split * F into the flux-register entries of the row's
 // captured faces (each entry belongs to exactly one face, so no atomics and
 // a deterministic sum) and reduces the row's max signal speed for the
-// per-sweep CFL check.  Ghost cells are refilled from the level's gather
-// table before every sweep (GhostFillKernel).
+// per-sweep CFL check.  The halo cells at the ends of a row are read where
+// they live (Seg::halo): the same level's current buffer or the coarser
+// level, which is the ghost fill of those strips at sweep time.
 #pragma once
 
 #include <climits>
@@ -43,9 +44,22 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
     int next_face = cap < w.cap_end ? a.caps[cap].face : INT_MAX;
     const int j0 = w.j0, j1 = w.j1;
     auto load = [&](double* u, int j) {
-      const int64_t off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
+      const double* src = in;
+      int64_t off, cs = N;
+      if (j >= 0 && j < w.n) {
+        off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
+      } else {  // halo cell: its source in this level or the coarser one
+        const int32_t g = w.halo[j < 0 ? j + 2 : j - w.n + 2];
+        if (g >= 0) {
+          off = g;
+        } else {
+          off = -int64_t(g) - 1;
+          src = a.coarse;
+          cs = a.coarse_ncells;
+        }
+      }
 #pragma unroll
-      for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * N + off);
+      for (int c = 0; c < K; ++c) u[c] = __ldg(src + c * cs + off);
     };
     // the update re-reads the FP64 state of cell j-1 (an L1 hit) instead of
     // carrying a window of FP64 states in registers
@@ -119,11 +133,24 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
        r += gridDim.x * blockDim.x) {
     const Seg w = a.segs[r];
     auto wave = [&](int j) {
-      const int64_t off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
+      const double* src = a.in;
+      int64_t off, cs = N;
+      if (j >= 0 && j < w.n) {
+        off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
+      } else {  // halo cell (j = -1 or n)
+        const int32_t g = w.halo[j < 0 ? j + 2 : j - w.n + 2];
+        if (g >= 0) {
+          off = g;
+        } else {
+          off = -int64_t(g) - 1;
+          src = a.coarse;
+          cs = a.coarse_ncells;
+        }
+      }
       double u[K];
       R v[K];
 #pragma unroll
-      for (int c = 0; c < K; ++c) u[c] = __ldg(a.in + c * N + off);
+      for (int c = 0; c < K; ++c) u[c] = __ldg(src + c * cs + off);
       P::ToCell(v, u);
       return P::MakeWave(eq, v, DIR);
     };
