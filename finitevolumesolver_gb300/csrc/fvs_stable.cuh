@@ -108,78 +108,89 @@ template <class P> struct WavesOf<P, std::void_t<decltype(&P::MakeWaves)>> {
 };
 
 // Stable dt of a 3-D grid with every cell loaded and its waves computed once
-// (the faces and their speeds are those of StableDtKernelT): a warp covers
-// 31 cells of an x row (lane 0 holds the left neighbour of the first) and
-// marches along z over `seg` planes, keeping the previous plane's z waves in
-// registers; the x neighbour comes by a shuffle and the y neighbour (j-1) of
-// each cell is loaded once more.  One atomic per block and direction.
+// (the faces and their speeds are those of StableDtKernelT).  A block of 8
+// warps covers 8 consecutive y rows of one 31-cell x range and marches along
+// z over `seg` planes: lane 0 of a warp holds the left neighbour of the
+// warp's first cell (x faces by a shuffle), the previous plane's z waves stay
+// in registers, and the y waves pass from each warp to the next through
+// shared memory (double-buffered, one barrier per plane); only the block's
+// first warp loads the row below the block.  One atomic per block and
+// direction.  Every block is full (rows past ny compute a clamped row and
+// take no faces), so all its threads reach every barrier.
+constexpr int kDtRows = 8;
+
 template <template <int> class PT>
-__global__ void __launch_bounds__(256) StableDtMarch3Kernel(StableDtArgs a, int seg) {
+__global__ void __launch_bounds__(32 * kDtRows) StableDtMarch3Kernel(StableDtArgs a, int seg) {
   using P = PT<3>;
   using R = typename P::Real;
   using W = typename P::Wave;
   constexpr int K = 5;
+  __shared__ W ywave[2][kDtRows][32];
   const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
   const int64_t cs = int64_t(nx) * ny * nz;
   if (!BlockAll(!(a.ctrl && (a.ctrl->abort || a.ctrl->done)))) return;
   const typename P::Gas eq = P::MakeGas(a.gamma);
   R smr[3] = {R(0), R(0), R(0)};  // in the policy's precision (no FP64 work per face)
-  const int lane = threadIdx.x & 31;
-  const int64_t gw = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int xw = (nx + 30) / 31;
-  const int zseg = (nz + seg - 1) / seg;
-  if (gw < int64_t(xw) * ny * zseg) {  // warp-uniform
-    const int wx = static_cast<int>(gw % xw);
-    const int64_t r = gw / xw;
-    const int j = static_cast<int>(r % ny);
-    const int k0 = static_cast<int>(r / ny) * seg;
-    const int k1 = min(nz, k0 + seg);
-    const int i = wx * 31 + lane - 1;
-    const bool own = lane >= 1 && i < nx;
-    const int ic = BcIndex(i, nx, a.bc[0]);  // lane 0: the left neighbour
-    const int jm = BcIndex(j - 1, ny, a.bc[1]);
-    auto load = [&](int jj, int kk, R* u) {
-      const int64_t off = (int64_t(kk) * ny + jj) * nx + ic;
-      double ud[K];
+  const int jblocks = (ny + kDtRows - 1) / kDtRows;
+  const int wx = static_cast<int>(blockIdx.x % xw);
+  const int jb = static_cast<int>((blockIdx.x / xw) % jblocks);
+  const int k0 = static_cast<int>(blockIdx.x / (int64_t(xw) * jblocks)) * seg;
+  const int k1 = min(nz, k0 + seg);
+  const int j = jb * kDtRows + warp;
+  const bool jvalid = j < ny;
+  const int jc = jvalid ? j : ny - 1;
+  const int i = wx * 31 + lane - 1;
+  const bool own = jvalid && lane >= 1 && i < nx;
+  const int ic = BcIndex(i, nx, a.bc[0]);  // lane 0: the left neighbour
+  const int jbelow = BcIndex(jb * kDtRows - 1, ny, a.bc[1]);
+  auto load = [&](int jj, int kk, R* u) {
+    const int64_t off = (int64_t(kk) * ny + jj) * nx + ic;
+    double ud[K];
 #pragma unroll
-      for (int c = 0; c < K; ++c) ud[c] = __ldg(a.in + c * cs + off);
-      P::ToCell(u, ud);
-    };
-    auto take = [&](R& m, R v) { m = v > m ? v : m; };
-    const bool ytile = !(a.rule == 1 && !ReferenceTileFaceT(j, ny, a.width));
-    const bool ytop = j == ny - 1 && a.bc[1] != 0 &&
-                      !(a.rule == 1 && !ReferenceTileFaceT(ny, ny, a.width));
-    W wz_prev;
-    {
-      R u[K];
-      load(j, BcIndex(k0 - 1, nz, a.bc[2]), u);
-      wz_prev = P::MakeWave(eq, u, 2);
+    for (int c = 0; c < K; ++c) ud[c] = __ldg(a.in + c * cs + off);
+    P::ToCell(u, ud);
+  };
+  auto take = [&](R& m, R v) { m = v > m ? v : m; };
+  const bool ytile = !(a.rule == 1 && !ReferenceTileFaceT(j, ny, a.width));
+  const bool ytop = j == ny - 1 && a.bc[1] != 0 &&
+                    !(a.rule == 1 && !ReferenceTileFaceT(ny, ny, a.width));
+  W wz_prev;
+  {
+    R u[K];
+    load(jc, BcIndex(k0 - 1, nz, a.bc[2]), u);
+    wz_prev = P::MakeWave(eq, u, 2);
+  }
+  for (int k = k0; k < k1; ++k) {
+    R u[K];
+    load(jc, k, u);
+    W w[3];
+    WavesOf<P>::Get(eq, u, w);
+    ywave[k & 1][warp][lane] = w[1];
+    W wy_below;
+    if (warp == 0) {  // the row below the block
+      R v[K];
+      load(jbelow, k, v);
+      wy_below = P::MakeWave(eq, v, 1);
     }
-    for (int k = k0; k < k1; ++k) {
-      R u[K];
-      load(j, k, u);
-      W w[3];
-      WavesOf<P>::Get(eq, u, w);
-      const W wl = ShflUp(w[0], 1);
-      if (own) {
-        // x: face i (i-1, i); face nx of a transmissive row (nx-1, nx-1)
-        take(smr[0], P::FaceMaxSpeed(eq, wl, w[0]));
-        if (i == nx - 1 && a.bc[0] != 0) take(smr[0], P::FaceMaxSpeed(eq, w[0], w[0]));
-        // y: face j (j-1, j); face ny of a transmissive column
-        if (ytile) {
-          R v[K];
-          load(jm, k, v);
-          take(smr[1], P::FaceMaxSpeed(eq, P::MakeWave(eq, v, 1), w[1]));
-        }
-        if (ytop) take(smr[1], P::FaceMaxSpeed(eq, w[1], w[1]));
-        // z: face k (k-1, k); face nz of a transmissive column
-        if (!(a.rule == 1 && !ReferenceTileFaceT(k, nz, a.width)))
-          take(smr[2], P::FaceMaxSpeed(eq, wz_prev, w[2]));
-        if (k == nz - 1 && a.bc[2] != 0 && !(a.rule == 1 && !ReferenceTileFaceT(nz, nz, a.width)))
-          take(smr[2], P::FaceMaxSpeed(eq, w[2], w[2]));
-      }
-      wz_prev = w[2];
+    const W wl = ShflUp(w[0], 1);
+    __syncthreads();
+    if (warp > 0) wy_below = ywave[k & 1][warp - 1][lane];
+    if (own) {
+      // x: face i (i-1, i); face nx of a transmissive row (nx-1, nx-1)
+      take(smr[0], P::FaceMaxSpeed(eq, wl, w[0]));
+      if (i == nx - 1 && a.bc[0] != 0) take(smr[0], P::FaceMaxSpeed(eq, w[0], w[0]));
+      // y: face j (j-1, j); face ny of a transmissive column
+      if (ytile) take(smr[1], P::FaceMaxSpeed(eq, wy_below, w[1]));
+      if (ytop) take(smr[1], P::FaceMaxSpeed(eq, w[1], w[1]));
+      // z: face k (k-1, k); face nz of a transmissive column
+      if (!(a.rule == 1 && !ReferenceTileFaceT(k, nz, a.width)))
+        take(smr[2], P::FaceMaxSpeed(eq, wz_prev, w[2]));
+      if (k == nz - 1 && a.bc[2] != 0 && !(a.rule == 1 && !ReferenceTileFaceT(nz, nz, a.width)))
+        take(smr[2], P::FaceMaxSpeed(eq, w[2], w[2]));
     }
+    wz_prev = w[2];
   }
   const double smax[3] = {static_cast<double>(smr[0]), static_cast<double>(smr[1]),
                           static_cast<double>(smr[2])};
@@ -191,14 +202,15 @@ cudaError_t LaunchStableDtT(const StableDtArgs& a, cudaStream_t s) {
   const int64_t cells = int64_t(a.n[0]) * a.n[1] * a.n[2];
   const int block = 256;
   if (a.rank == 3) {
-    // enough warps for about two waves of the GPU, planes split accordingly
-    const int64_t rows = int64_t((a.n[0] + 30) / 31) * a.n[1];
-    const int64_t want = int64_t(GridStrideBlocks(int64_t(1) << 40, block, 8)) * (block / 32) * 2;
-    const int64_t zseg = std::max<int64_t>(1, std::min<int64_t>(a.n[2], (want + rows - 1) / rows));
+    // blocks of kDtRows x rows; enough blocks for about two waves of the GPU,
+    // the planes split accordingly; every block full (see the kernel)
+    const int64_t tiles = int64_t((a.n[0] + 30) / 31) * ((a.n[1] + kDtRows - 1) / kDtRows);
+    const int64_t want = int64_t(GridStrideBlocks(int64_t(1) << 40, 32 * kDtRows, 8)) * 2;
+    const int64_t zseg =
+        std::max<int64_t>(1, std::min<int64_t>(a.n[2], (want + tiles - 1) / tiles));
     const int seg = static_cast<int>((a.n[2] + zseg - 1) / zseg);
-    const int64_t warps = rows * ((a.n[2] + seg - 1) / seg);
-    const unsigned grid = static_cast<unsigned>((warps * 32 + block - 1) / block);
-    StableDtMarch3Kernel<PT><<<grid, block, 0, s>>>(a, seg);
+    const unsigned grid = static_cast<unsigned>(tiles * ((a.n[2] + seg - 1) / seg));
+    StableDtMarch3Kernel<PT><<<grid, 32 * kDtRows, 0, s>>>(a, seg);
     return cudaGetLastError();
   }
   const unsigned grid = GridStrideBlocks(cells, block, 8);
