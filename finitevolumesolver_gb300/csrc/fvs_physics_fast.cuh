@@ -18,10 +18,14 @@
 // reconstruction and flux.
 //
 // Reciprocal and reciprocal square root in FP64 start from the PTX
-// rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64 estimates and refine them with
-// Newton-Raphson iterations (x_{k+1} = x_k (2 - a x_k) for 1/a, and
-// x_{k+1} = x_k (3 - a x_k^2) / 2 for 1/sqrt(a)); each iteration doubles the
-// number of correct bits.
+// rcp.approx.ftz.f64 / rsqrt.approx.ftz.f64 estimates (measured on GB300: at
+// most 2^-20 relative error) and refine them with one third-order step from
+// the series of the exact value in the residual r of the estimate y0:
+//   1/a       = y0 / (1 - r),        r = 1 - a y0:   y0 (1 + r + r^2 + ...)
+//   1/sqrt(a) = y0 (1 - r)^(-1/2),   r = 1 - a y0^2: y0 (1 + r/2 + 3 r^2/8 + ...)
+// truncated after the r^2 term, so the refined value is off by ~r^3 < 2^-60
+// (a few ulp after rounding).  a/b = a * (1/b) and sqrt(a) = a * (1/sqrt(a))
+// then carry about one more ulp.
 #pragma once
 
 #include <cstdint>
@@ -42,39 +46,24 @@ template <> struct Math<double> {
     asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(a));
     return y;
   }
-  // 1/a to ~full precision: two Newton steps from the hardware estimate.
+  // 1/a: y0 (1 + r + r^2), r = 1 - a y0.
   static __device__ __forceinline__ double Rcp(double a) {
-    double y = RcpSeed(a);
-    double e = fma(-a, y, 1.0);
-    y = fma(y, e, y);
-    e = fma(-a, y, 1.0);
-    return fma(y, e, y);
+    const double y = RcpSeed(a);
+    const double r = fma(-a, y, 1.0);
+    return fma(y, fma(r, r, r), y);
   }
-  // a/b: quotient from a refined reciprocal plus one residual correction.
-  static __device__ __forceinline__ double Div(double a, double b) {
-    double y = RcpSeed(b);
-    double e = fma(-b, y, 1.0);
-    y = fma(y, e, y);
-    const double q = a * y;
-    const double r = fma(-b, q, a);
-    return fma(r, y, q);
-  }
-  // 1/sqrt(a), a > 0: two Newton steps.
+  // a/b as a times the refined reciprocal.
+  static __device__ __forceinline__ double Div(double a, double b) { return a * Rcp(b); }
+  // 1/sqrt(a), a > 0: y0 (1 + r (1/2 + 3 r/8)), r = 1 - a y0^2.
   static __device__ __forceinline__ double Rsqrt(double a) {
-    double y = RsqrtSeed(a);
-    const double ha = 0.5 * a;
-    double t = y * y;
-    y = y * fma(-ha, t, 1.5);
-    t = y * y;
-    return y * fma(-ha, t, 1.5);
+    const double y = RsqrtSeed(a);
+    const double r = fma(-a, y * y, 1.0);
+    return fma(y * r, fma(0.375, r, 0.5), y);
   }
   // sqrt(a) for a >= 0 (0 for a <= 0).
   static __device__ __forceinline__ double Sqrt(double a) {
     if (!(a > 0.0)) return 0.0;
-    const double y = Rsqrt(a);
-    const double s = a * y;
-    const double r = fma(-s, s, a);
-    return fma(r, 0.5 * y, s);
+    return a * Rsqrt(a);
   }
 };
 
