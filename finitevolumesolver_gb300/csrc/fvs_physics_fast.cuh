@@ -184,26 +184,28 @@ __device__ __forceinline__ void HllFlux(const Gas<T>& eq, T* nf, const State<D, 
   T ds = sR - sL;
   ds = (ds > T(0)) ? ds : T(1);
   const T ids = Math<T>::Rcp(ds);
+  // (sR fL - sL fR + sL sR (qR - qL)) / ds with the three weights divided once
+  const T wL = sR * ids, wR = sL * ids, wq = sLsR * ids;
   T qL[K], qR[K];
   ConsOf<D, T>(qL, L);
   ConsOf<D, T>(qR, R);
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    const T num = fma(sLsR, qR[k] - qL[k], fma(sR, fL[k], -sL * fR[k]));
-    nf[k] = num * ids;
-  }
+  for (int k = 0; k < K; ++k) nf[k] = fma(wL, fL[k], fma(-wR, fR[k], wq * (qR[k] - qL[k])));
 }
 
+// Half the limited slope (what the predictor adds and subtracts).  Van Leer:
+// (2 sL sR / (sL + sR)) / 2 = sL sR / (sL + sR), the factors 2 and 1/2 being
+// exact they are left out.
 template <typename T>
-__device__ __forceinline__ T LimitedSlope(int limiter, T qL, T qM, T qR) {
+__device__ __forceinline__ T HalfSlope(int limiter, T qL, T qM, T qR) {
   const T sL = qM - qL;
   const T sR = qR - qM;
   if (limiter == 0) {  // van Leer
-    const T c = T(2) * sL * sR;
+    const T c = sL * sR;
     return (c > T(0)) ? Math<T>::Div(c, sL + sR) : T(0);
   }
   if (limiter == 1) {  // MinMod
-    return (sR > T(0)) ? Max(T(0), Min(sL, sR)) : Min(T(0), Max(sL, sR));
+    return T(0.5) * ((sR > T(0)) ? Max(T(0), Min(sL, sR)) : Min(T(0), Max(sL, sR)));
   }
   return T(0);
 }
@@ -218,7 +220,7 @@ __device__ __forceinline__ void PredictBoth(const Gas<T>& eq, State<D, T>& recL,
   T uL[K], uR[K];
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    const T hs = T(0.5) * LimitedSlope<T>(limiter, q0[k], q1[k], q2[k]);
+    const T hs = HalfSlope<T>(limiter, q0[k], q1[k], q2[k]);
     uL[k] = q1[k] - hs;
     uR[k] = q1[k] + hs;
   }
