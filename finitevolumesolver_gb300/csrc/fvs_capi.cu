@@ -137,6 +137,7 @@ struct StepPlan {
   double frac;  // split dt = frac * dt
   int rank;
   double dxd[3];
+  int skip0;    // sweep 0 takes its check's speed from the stable-dt pass
 };
 
 // RunSimulation's dt selection (include/fub/RunSimulation.hpp:125-131):
@@ -171,6 +172,9 @@ __global__ void BeginStepKernel(Control* c, StepPlan plan) {
   }
   c->dt = dt;
   for (int q = 0; q < 6; ++q) c->smax_check[q] = 0ull;
+  // the first sweep's input is the state the stable-dt pass just measured,
+  // over the same faces: its check uses that pass's speed in its direction
+  if (plan.skip0) c->smax_check[0] = c->smax_stable[plan.dir[0]];
   c->step_status = 0;
 }
 
@@ -277,7 +281,8 @@ cudaError_t CcReferenceStates(const fvs_solver* s, const double* in) {
 cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
                         int dir, const double* dt_ptr, double dt_scale,
                         double dt_value, unsigned long long* smax_out,
-                        fvs::Control* ctrl, int prev_check, double prev_dx) {
+                        fvs::Control* ctrl, int prev_check, double prev_dx,
+                        bool skip_cfl = false) {
   if (s->cc) {
     fvs::CcSweepArgs c{};
     c.s = MakeCcState(s, in);
@@ -322,6 +327,7 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
   a.tolerance = s->m.tolerance;
   a.mlp = s->m.mlp_params;
   a.stats_out = ctrl ? ctrl->newton : s->newton_words;
+  a.skip_cfl = skip_cfl ? 1 : 0;
   if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
     return fvs::LaunchSweepGodunov(a, s->m.flux_method == FVS_MUSCL_GODUNOV, s->stream);
   if (HllemRecon(s->m.flux_method) >= 0)
@@ -398,6 +404,13 @@ fvs::StepPlan MakePlan(const fvs_solver* s, int64_t cycle) {
   }
   for (int i = 0; i < p.nsweeps; ++i) p.dx[i] = s->g.dx[p.dir[i]];
   p.rank = D;
+  // HLL and HLLEM sweeps measure the same face speeds as the stable-dt pass
+  // when that pass takes every face (dt rule 0); cut cells, the exact Riemann
+  // solver's sweeps and the mixed flavour keep their own
+  p.skip0 = (!s->cc && s->g.dt_rule == 0 && !IsGodunov(s->m.flux_method) &&
+             s->m.precision != FVS_MIXED)
+                ? 1
+                : 0;
   for (int d = 0; d < 3; ++d) p.dxd[d] = s->g.dx[d];
   return p;
 }
@@ -419,9 +432,10 @@ cudaError_t EnqueueStep(fvs_solver* s, int start, int64_t cycle, int step_in_bat
   const int X = (start + 1) % 3, Y = (start + 2) % 3;
   int src = start, dst = X;
   for (int q = 0; q < plan.nsweeps; ++q) {
+    const bool skip = q == 0 && plan.skip0;
     e = LaunchSweep(s, s->buf[src], s->buf[dst], plan.dir[q], &s->ctrl->dt,
-                    plan.frac, 0.0, &s->ctrl->smax_check[q], s->ctrl,
-                    q > 0 ? q - 1 : -1, q > 0 ? plan.dx[q - 1] : 0.0);
+                    plan.frac, 0.0, skip ? nullptr : &s->ctrl->smax_check[q], s->ctrl,
+                    q > 0 ? q - 1 : -1, q > 0 ? plan.dx[q - 1] : 0.0, skip);
     if (e != cudaSuccess) return e;
     src = dst;
     dst = (dst == X) ? Y : X;

@@ -74,6 +74,9 @@ struct SweepArgs {
   double tolerance;
   const float* mlp;     // learned-guess weights (guess == FVS_GUESS_MLP)
   unsigned long long* stats_out;  // [3]: Newton iterations, non-converged, fallbacks
+  // the first sweep of a step: its input's face speeds are the stable-dt
+  // pass's, so the sweep computes no cell waves and no CFL speeds
+  int skip_cfl;
   int occupancy;        // 0 (registers as needed) or the resident blocks per SM a
                         // variant is compiled for (mixed: 4, 5; double-float: 3);
                         // mixed x sweeps: + 10 for the marching kernel in x

@@ -84,6 +84,10 @@ template <int D, int kRecon> struct HllemPolicyT {
                                                         const Wave& wR) {
     return exact::HllemMaxSpeed<D>(eq, wL.q, wR.q, wL.dir);
   }
+  static __device__ __forceinline__ void FluxOnly(const Gas& eq, double* F, const Rec& L,
+                                                  const Rec& R, int dir) {
+    exact::HllemFlux<D>(eq, F, L, R, dir);
+  }
   static __device__ __forceinline__ double Face(const Gas& eq, double* F, const Rec& L,
                                                 const Rec& R, const Wave& wL, const Wave& wR,
                                                 int dir, Stats&) {

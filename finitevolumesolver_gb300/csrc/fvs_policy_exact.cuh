@@ -39,6 +39,10 @@ template <int D> struct ExactPolicy {
                                lambda_half, dir);
   }
   using Stats = NoStats;
+  static __device__ __forceinline__ void FluxOnly(const Gas& eq, double* F, const Rec& L,
+                                                  const Rec& R, int dir) {
+    exact::HllFlux<D>(eq, F, L, R, dir);
+  }
   static __device__ __forceinline__ double Face(const Gas& eq, double* F, const Rec& L,
                                                 const Rec& R, const Wave& wL,
                                                 const Wave& wR, int dir, Stats&) {

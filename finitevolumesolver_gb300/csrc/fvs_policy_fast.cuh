@@ -59,6 +59,15 @@ template <int D, typename T> struct FastBase {
     fast::HllFlux<D, T>(eq, f, L, R, dir);
     return fast::FaceMaxSpeed<T>(eq, wL, wR);
   }
+  // the face flux alone (no CFL speed): FP64 (widened) and compute precision
+  static __device__ __forceinline__ void FluxOnly(const Gas& eq, double* F, const Rec& L,
+                                                  const Rec& R, int dir) {
+    HllFlux(eq, F, L, R, dir);
+  }
+  static __device__ __forceinline__ void FluxOnlyR(const Gas& eq, T* f, const Rec& L,
+                                                   const Rec& R, int dir) {
+    fast::HllFlux<D, T>(eq, f, L, R, dir);
+  }
   static __device__ __forceinline__ T Face(const Gas& eq, double* F, const Rec& L,
                                            const Rec& R, const Wave& wL, const Wave& wR,
                                            int dir, Stats&) {

@@ -127,6 +127,8 @@ template <class P> struct FluxOf<P, std::enable_if_t<P::kFloatFlux>> {
   using type = float;
 };
 
+template <class P> using FluxOfArg = typename FluxOf<P>::type;
+
 template <class P, class F>
 __device__ __forceinline__ typename P::Real SweepFace(const typename P::Gas& eq, F* flux,
                                                       const typename P::Rec& L,
@@ -138,6 +140,27 @@ __device__ __forceinline__ typename P::Real SweepFace(const typename P::Gas& eq,
     return P::FaceR(eq, flux, L, R, wL, wR, dir, stats);
   } else {
     return P::Face(eq, flux, L, R, wL, wR, dir, stats);
+  }
+}
+
+// Policies that can compute a face flux without its CFL speed (FluxOnly):
+// the first sweep of a step then takes its input's face speeds from the
+// stable-dt pass over the same state and skips the cell waves.
+// (FP64-flux policies only: the mixed flavour's sweeps are bound by memory
+// and its FP64 update, and the extra path would cost them registers.)
+template <class P, class = void> struct HasFluxOnly : std::false_type {};
+template <class P>
+struct HasFluxOnly<P, std::void_t<decltype(&P::FluxOnly)>>
+    : std::bool_constant<std::is_same_v<typename FluxOf<P>::type, double>> {};
+
+template <class P, class F>
+__device__ __forceinline__ void SweepFluxOnly(const typename P::Gas& eq, F* flux,
+                                              const typename P::Rec& L,
+                                              const typename P::Rec& R, int dir) {
+  if constexpr (std::is_same_v<F, float>) {
+    P::FluxOnlyR(eq, flux, L, R, dir);
+  } else {
+    P::FluxOnly(eq, flux, L, R, dir);
   }
 }
 
@@ -199,6 +222,7 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
   const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
   if (!BlockAll(SweepGate(a, split_dt))) return;
   const bool active = t < ntrans;
+  const bool skip_cfl = HasFluxOnly<P>::value && a.skip_cfl != 0;
 
   int64_t base, stride;
   if (DIR == 0) {
@@ -249,11 +273,21 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
       if (j + 2 <= j1 + 1) load(dn, j + 2);
       typename P::Rec recL, recR;
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
-      const typename P::Wave w = P::MakeWave(eq, cc, DIR);
+      typename P::Wave w{};
+      if (!skip_cfl) w = P::MakeWave(eq, cc, DIR);
       if (j >= j0) {
         FluxT F[K];
-        const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
-        smax = s > smax ? s : smax;
+        if constexpr (HasFluxOnly<P>::value) {
+          if (skip_cfl) {
+            SweepFluxOnly<P>(eq, F, recR_prev, recL, DIR);
+          } else {
+            const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
+            smax = s > smax ? s : smax;
+          }
+        } else {
+          const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
+          smax = s > smax ? s : smax;
+        }
         if (j > j0) {
           // cell j-1 (inside [0, nd)): U' = U + dt/dx (F_{j-1} - F_j)
           const int64_t off = base + int64_t(j - 1) * stride;
@@ -376,18 +410,34 @@ __device__ __forceinline__ void XWarpRow(const SweepArgs& a, int64_t row, double
   if (lane == 0) Cwm = Cw;
   typename P::Rec wrecL, wrecR;
   P::Predict(eq, wrecL, wrecR, Cwm.v, Cw.v, Cwp.v, a.limiter, lambda_half, 0);
-  typename P::Wave wW = P::MakeWave(eq, Cw.v, 0);
+  const bool skip_cfl = HasFluxOnly<P>::value && a.skip_cfl != 0;  // warp-uniform
+  // faces with or without their CFL speed (see HasFluxOnly)
+  auto face = [&](FluxOfArg<P>* F, const typename P::Rec& L, const typename P::Rec& Rr,
+                  const typename P::Wave& wl, const typename P::Wave& wr,
+                  typename P::Stats& st) -> R {
+    if constexpr (HasFluxOnly<P>::value) {
+      if (skip_cfl) {
+        SweepFluxOnly<P>(eq, F, L, Rr, 0);
+        return R(0);
+      }
+    }
+    return SweepFace<P>(eq, F, L, Rr, wl, wr, 0, st);
+  };
+  typename P::Wave wW{};
+  if (!skip_cfl) wW = P::MakeWave(eq, Cw.v, 0);
   // face -1 (between cells -2 and -1), used to update cell -1 on a periodic row
   const typename P::Rec wrecRm = ShflUp(wrecR, 1);
-  const typename P::Wave wWm = ShflUp(wW, 1);
+  typename P::Wave wWm{};
+  if (!skip_cfl) wWm = ShflUp(wW, 1);
   using FluxT = typename FluxOf<P>::type;
   using Flx = CellArr<FluxT, K>;
   FluxT Fw[K];
   typename P::Stats wstats;
-  SweepFace<P>(eq, Fw, wrecRm, wrecL, wWm, wW, 0, wstats);
+  face(Fw, wrecRm, wrecL, wWm, wW, wstats);
   // carries into chunk 0 (from lane 31 = cell -1)
   typename P::Rec carry_rec = ShflIdx(wrecR, 31);
-  typename P::Wave carry_w = ShflIdx(wW, 31);
+  typename P::Wave carry_w{};
+  if (!skip_cfl) carry_w = ShflIdx(wW, 31);
   Cell carry_c = ShflIdx(Cw, 31);
   Flx carry_f;
 #pragma unroll
@@ -413,15 +463,17 @@ __device__ __forceinline__ void XWarpRow(const SweepArgs& a, int64_t row, double
     if (lane == 0) Cm = carry_c;
     typename P::Rec recL, recR;
     P::Predict(eq, recL, recR, Cm.v, C.v, Cp.v, a.limiter, lambda_half, 0);
-    const typename P::Wave W = P::MakeWave(eq, C.v, 0);
+    typename P::Wave W{};
+    if (!skip_cfl) W = P::MakeWave(eq, C.v, 0);
     typename P::Rec recRm = ShflUp(recR, 1);
-    typename P::Wave Wm = ShflUp(W, 1);
+    typename P::Wave Wm{};
+    if (!skip_cfl) Wm = ShflUp(W, 1);
     if (lane == 0) {
       recRm = carry_rec;
       Wm = carry_w;
     }
     Flx Fd;
-    const R sp = SweepFace<P>(eq, Fd.v, recRm, recL, Wm, W, 0, stats);
+    const R sp = face(Fd.v, recRm, recL, Wm, W, stats);
     if (valid) smax = sp > smax ? sp : smax;
     Flx Fm = ShflUp(Fd, 1);
     if (lane == 0) Fm = carry_f;
@@ -440,7 +492,7 @@ __device__ __forceinline__ void XWarpRow(const SweepArgs& a, int64_t row, double
     // carries: the chunk's last cell
     const int last = min(31, nx - 1 - x0);
     carry_rec = ShflIdx(recR, last);
-    carry_w = ShflIdx(W, last);
+    if (!skip_cfl) carry_w = ShflIdx(W, last);
     carry_c = ShflIdx(C, last);
     carry_f = ShflIdx(Fd, last);
     C = Cn;
@@ -449,9 +501,10 @@ __device__ __forceinline__ void XWarpRow(const SweepArgs& a, int64_t row, double
     // face nx and cell nx-1 of a transmissive row (cells >= nx copy nx-1)
     typename P::Rec recL, recR;
     P::Predict(eq, recL, recR, carry_c.v, carry_c.v, carry_c.v, a.limiter, lambda_half, 0);
-    const typename P::Wave W = P::MakeWave(eq, carry_c.v, 0);
+    typename P::Wave W{};
+    if (!skip_cfl) W = P::MakeWave(eq, carry_c.v, 0);
     FluxT F[K];
-    const R sp = SweepFace<P>(eq, F, carry_rec, recL, carry_w, W, 0, stats);
+    const R sp = face(F, carry_rec, recL, carry_w, W, stats);
     if (lane == 0) {
       smax = sp > smax ? sp : smax;
       const int64_t off = base + (nx - 1);
