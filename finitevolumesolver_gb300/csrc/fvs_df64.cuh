@@ -98,12 +98,8 @@ template <> struct Math<df64> {
     const float r = __fmaf_rn(-a.lo, y, __fmaf_rn(-a.hi, y, 1.0f));
     return dfops::QuickTwoSum(y, __fmul_rn(y, __fmaf_rn(r, r, r)));
   }
-  static __device__ __forceinline__ df64 Div(df64 a, df64 b) {
-    // quotient from the reciprocal plus one residual correction
-    const df64 y = Rcp(b);
-    const df64 q = a * y;
-    return q + (a - b * q) * y;
-  }
+  // a/b as a times the reciprocal (relative error ~2^-46)
+  static __device__ __forceinline__ df64 Div(df64 a, df64 b) { return a * Rcp(b); }
   // 1/sqrt(a), a > 0: y = rsqrt(a.hi), r = 1 - a y^2 in double-float, and
   // 1/sqrt(a) = y (1 - r)^(-1/2) = y (1 + r/2 + 3 r^2/8 + ...); the
   // correction goes to the low word.
@@ -114,13 +110,11 @@ template <> struct Math<df64> {
     const float c = __fmaf_rn(__fmul_rn(0.375f, r.hi), r.hi, __fmul_rn(0.5f, r.hi));
     return dfops::QuickTwoSum(y, __fmul_rn(y, c));
   }
-  // sqrt(a) for a >= 0 (0 for a <= 0): s = a y and one correction
-  // s + (a - s^2) y / 2.
+  // sqrt(a) for a >= 0 (0 for a <= 0): a times the reciprocal square root
+  // (relative error ~2^-46).
   static __device__ __forceinline__ df64 Sqrt(df64 a) {
     if (!(a.hi > 0.0f)) return df64(0);
-    const df64 y = Rsqrt(a);
-    const df64 s = a * y;
-    return s + (a - s * s) * (df64(0.5f, 0.0f) * y);
+    return a * Rsqrt(a);
   }
 };
 
