@@ -208,6 +208,9 @@ __global__ void __launch_bounds__(256) StableDtKernel(StableDtArgs a) {
 }
 
 cudaError_t LaunchStableDtExact(const StableDtArgs& a, cudaStream_t s) {
+  // 3-D: the marching pass (each cell completed once), with the same face
+  // speeds as StableDtKernel
+  if (a.rank == 3) return LaunchStableDtT<ExactPolicy>(a, s);
   const int64_t cells = int64_t(a.n[0]) * a.n[1] * a.n[2];
   const int block = 256;
   const unsigned grid = GridStrideBlocks(cells, block, 8);

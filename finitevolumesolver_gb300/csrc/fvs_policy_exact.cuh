@@ -53,6 +53,21 @@ template <int D> struct ExactPolicy {
                                                   int dir) {
     return exact::MakeCellWave<D>(eq, u, dir);
   }
+  // the waves of all D directions from one CompleteFromCons (each equal to
+  // MakeWave's: the same operations)
+  static __device__ __forceinline__ void MakeWaves(const Gas& eq, const double* u, Wave* w) {
+    exact::Complete<D> q;
+    exact::CompleteFromCons<D>(eq, q, u);
+    const double sq = sqrt(q.rho);
+    const double h = (q.E + q.p) / q.rho;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      w[d].sq = sq;
+      w[d].u = q.m[d] / q.rho;
+      w[d].h = h;
+      w[d].a = q.c;
+    }
+  }
   static __device__ __forceinline__ double FaceMaxSpeed(const Gas& eq, const Wave& wL,
                                                         const Wave& wR) {
     return exact::FaceMaxSpeed(eq, wL, wR);
