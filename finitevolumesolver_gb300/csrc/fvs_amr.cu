@@ -54,7 +54,6 @@ struct LevelHost {
   double* A = nullptr;
   double* B = nullptr;
   double* backup = nullptr;
-  Row* rows[2] = {nullptr, nullptr};
   int32_t nrows[2] = {0, 0};
   Seg* segs[2][kSplits] = {};
   int32_t nsegs[2][kSplits] = {};
@@ -381,7 +380,6 @@ int Build(fvs_amr* a) {
     for (int d = 0; d < 2; ++d) {
       const std::vector<Row>& R = rows_h[d][size_t(l)];
       const std::vector<Cap>& flat = caps_flat[d][size_t(l)];
-      AMR_CUDA(a->Upload(&Lv.rows[d], R));
       AMR_CUDA(a->Upload(&Lv.caps[d], flat));
       // the rows split into 1, 2 or 4 segments (threads per row)
       for (int si = 0; si < kSplits; ++si) {
