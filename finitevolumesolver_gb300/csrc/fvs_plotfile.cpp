@@ -131,7 +131,9 @@ std::string LevelWriter::Append(int b, const double* data) {
   const Box& box = L.boxes[size_t(b)];
   const int64_t n = box.Cells(pf_.dim);
   const int ncomp = static_cast<int>(pf_.vars.size());
-  offsets_.push_back(static_cast<int64_t>(std::ftell(f_)));
+  const long pos = std::ftell(f_);
+  if (pos < 0) return error_ = "cannot tell the position in the level data file";
+  offsets_.push_back(static_cast<int64_t>(pos));
   std::ostringstream h;
   // IEEE double, little-endian byte order (the native order of both hosts)
   h << "FAB ((8, (64 11 52 0 1 12 0 1023)),(8, (8 7 6 5 4 3 2 1)))";
