@@ -299,7 +299,7 @@ def report_mlp(args, torch, fvs, workloads):
     }, net
 
 
-def report_godunov(args, torch, fvs, workloads, net):
+def report_godunov(args, torch, fvs, workloads, net, peaks=None):
     """2-D first-order Godunov with the exact Riemann solver on an n^2
     four-quadrant problem drawn from the sampled distribution, Strang
     splitting, for the three Newton start values."""
@@ -327,8 +327,11 @@ def report_godunov(args, torch, fvs, workloads, net):
         ms = a.elapsed_time(b)
         it, fail, fb = s.newton_stats(fallbacks=True)
         faces = st.steps * 4 * (n + 1) * n
+        rate = 4 * n * n * st.steps / (ms / 1e3)
         out[guess] = {"steps": st.steps, "ms_per_step": ms / max(st.steps, 1),
-                      "cell_updates_per_s": 4 * n * n * st.steps / (ms / 1e3),
+                      "cell_updates_per_s": rate,
+                      "hbm_frac_algorithmic": (rate * 64 / 1e9 / peaks["hbm_gbs"]
+                                               if peaks else None),
                       "newton_iterations_per_interface": it / faces,
                       "fallback_rate": fb / faces, "not_converged": fail}
         finals[guess] = s.download()
@@ -403,7 +406,7 @@ def report_amr(args, torch, fvs, workloads, peaks):
     return out
 
 
-def report_cutcell(args, torch, fvs, workloads):
+def report_cutcell(args, torch, fvs, workloads, peaks=None):
     """2-D KBN h-box cut cells: Mach 2 shock over 8 seeded circles on n^2,
     Strang MUSCL-Hancock/VanLeer + HLLE, in the exact FP64, fast FP64 and
     mixed flavours; L1 density error against exact FP64 (which is the
@@ -437,9 +440,13 @@ def report_cutcell(args, torch, fvs, workloads):
             G = geo["ghost"]
             alpha = geo["alpha"][G:-G, G:-G]
             out["cut_cells"] = int(geo["cut"][G:-G, G:-G].sum())
+        rate = 4 * n * n * st.steps / (ms / 1e3)
         out["flavours"][prec] = {
             "steps": st.steps, "restarts": st.restarts, "ms_per_step": ms / max(st.steps, 1),
-            "cell_updates_per_s": 4 * n * n * st.steps / (ms / 1e3)}
+            "cell_updates_per_s": rate}
+        if peaks:
+            # 64 B state + 64 B geometry (alpha, beta, shielded weights, x_B, normal)
+            out["flavours"][prec]["hbm_frac_algorithmic"] = rate * 128 / 1e9 / peaks["hbm_gbs"]
         s.close()
     ref = finals["fp64_exact"]
     w = alpha[None, None]
@@ -505,11 +512,11 @@ def run_ours(args):
             rep, _ = report_mlp(args, torch, fvs, workloads)
         elif args.report == "godunov":
             _, net = report_mlp(args, torch, fvs, workloads)
-            rep = report_godunov(args, torch, fvs, workloads, net)
+            rep = report_godunov(args, torch, fvs, workloads, net, peaks)
         elif args.report == "amr":
             rep = report_amr(args, torch, fvs, workloads, peaks)
         else:
-            rep = report_cutcell(args, torch, fvs, workloads)
+            rep = report_cutcell(args, torch, fvs, workloads, peaks)
         if rank == 0:
             print(json.dumps({"report": args.report, **rep}), flush=True)
         return
@@ -644,9 +651,11 @@ def run_ours(args):
         except Exception as e:  # report the failure, keep the headline
             reports["learned_start_value"] = {"error": repr(e)}
             net = None
-        for key, fn in (("godunov_2d", lambda: report_godunov(args, torch, fvs, workloads, net)),
+        for key, fn in (("godunov_2d", lambda: report_godunov(args, torch, fvs, workloads, net,
+                                                              peaks)),
                         ("amr_2d", lambda: report_amr(args, torch, fvs, workloads, peaks)),
-                        ("cutcell_2d", lambda: report_cutcell(args, torch, fvs, workloads))):
+                        ("cutcell_2d", lambda: report_cutcell(args, torch, fvs, workloads,
+                                                              peaks))):
             try:
                 reports[key] = fn()
             except Exception as e:
