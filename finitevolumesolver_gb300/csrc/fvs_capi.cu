@@ -840,6 +840,8 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
         s->seg_len = c;
         float ms_sum = 0.f;
         for (int rep = 0; rep < 3; ++rep) {
+          // the sweep's max slot starts at zero, as in a step
+          FVS_CUDA(cudaMemsetAsync(s->scratch_words, 0, sizeof(unsigned long long), s->stream));
           FVS_CUDA(cudaEventRecord(e0, s->stream));
           FVS_CUDA(LaunchSweep(s, s->buf[s->cur], s->buf[out], d, nullptr, 1.0, dt,
                                s->scratch_words, nullptr, -1, 0.0));

@@ -13,7 +13,8 @@ namespace fvs {
 template <int D> struct ExactPolicy {
   using Real = double;
   static constexpr bool kWarpX = false;
-  static constexpr int kMinBlocks = 1;
+  static constexpr int kMinBlocks = 3;  // at most 168 registers
+  static constexpr bool kEinfeldtCfl = true;  // CFL speeds screened in FP32
   using Gas = exact::Gas;
   using Wave = exact::CellWave;
   using Rec = exact::Complete<D>;

@@ -23,6 +23,8 @@ template <int D, typename T> struct FastBase {
   // the mixed flavour is memory-bound: its x sweep uses lanes along x
   static constexpr bool kWarpX = sizeof(T) == 4;
   static constexpr int kMinBlocks = 1;
+  // FP64 and double-float: the sweep screens the Einfeldt CFL speeds in FP32
+  static constexpr bool kEinfeldtCfl = sizeof(T) != 4;
   using Gas = fast::Gas<T>;
   using Rec = fast::State<D, T>;
   using Wave = fast::Wave<T>;
@@ -99,7 +101,10 @@ template <int D, typename T> struct FastBase {
   }
 };
 
-template <int D> struct Fast64Policy : FastBase<D, double> {};
+// three resident blocks of 128 threads (at most 168 registers)
+template <int D> struct Fast64Policy : FastBase<D, double> {
+  static constexpr int kMinBlocks = 3;
+};
 template <int D> struct Mixed32Policy : FastBase<D, float> {};
 // The same arithmetic compiled for more resident blocks per SM (fewer
 // registers per thread, more warps to hide latency); the autotuner picks.

@@ -24,6 +24,7 @@
 
 #include "fvs_convert.cuh"
 #include "fvs_internal.h"
+#include "fvs_physics_fast.cuh"
 
 #include <cstring>
 
@@ -164,6 +165,76 @@ __device__ __forceinline__ void SweepFluxOnly(const typename P::Gas& eq, F* flux
   }
 }
 
+// Filtered CFL maximum.  For policies whose CFL speed is the Einfeldt speed
+// of the two cell states of a face (kEinfeldtCfl), a sweep evaluates that
+// speed in the policy's arithmetic only on faces that can hold the sweep's
+// maximum.  Every face first gets an FP32 speed s32 from the FP32-rounded
+// states and a bound on its error:
+//   |s - s32| <= s32 / 1024 + sqrt(max(h_L, h_R)) / 64 + 2^-24,
+// h = (E + p) / rho.  The relative term covers the roundings and the
+// approximate FP32 reciprocals and square roots; the h term covers the
+// cancellations in p = (gamma - 1)(E - e_kin) and in the Roe sound speed,
+// whose absolute errors are below sqrt(c eps h) with c eps < 1e-5 for
+// 1 < gamma <= 2; the constant covers underflow.  The bound holds for cells
+// with 2^-30 <= rho <= 2^30, |m| <= 2^30, |E| <= 2^40 and a positive FP32
+// pressure (no FP32 overflow; underflow errors far below 2^-24); any other
+// face is evaluated.  A face is skipped when s32 plus its error bound is
+// below a threshold that is itself a lower bound of an evaluated face's
+// exact speed (the lane's own maximum and the sweep's maximum published so
+// far, rounded down to FP32), so every skipped face is strictly slower than
+// an evaluated one and the sweep's maximum is the same number, bit for bit.
+// Warps publish their maximum to the sweep's max slot every kCflSyncRows
+// rows and read it back, so later blocks start with the maximum of earlier
+// ones.  The slot must start at zero (or at an evaluated speed of the same
+// sweep).
+template <class P, class = void> struct FilteredCfl : std::false_type {};
+template <class P>
+struct FilteredCfl<P, std::enable_if_t<P::kEinfeldtCfl>> : std::true_type {};
+
+constexpr float kCflRel = 1.0f + 1.0f / 1024.0f;
+constexpr float kCflScale = 1.0f / 64.0f;
+constexpr float kCflAbs = 0x1p-24f;
+constexpr int kCflSyncRows = 8;
+
+template <class R> __device__ __forceinline__ float CflToF32(const R& x) {
+  if constexpr (std::is_same_v<R, double>) {
+    return DoubleToFloatBits(x);
+  } else {
+    return x.hi;  // double-float: its leading FP32 word
+  }
+}
+
+// FP32 cell values inside the range of the error bound above.
+template <int D> __device__ __forceinline__ bool CflInRange(const float* u) {
+  bool ok = u[0] >= 0x1p-30f && u[0] <= 0x1p30f && fabsf(u[1 + D]) <= 0x1p40f;
+#pragma unroll
+  for (int d = 0; d < D; ++d) ok = ok && fabsf(u[1 + d]) <= 0x1p30f;
+  return ok;
+}
+
+// An FP32 number not above x >= 0 (x rounded to nearest, then lowered by
+// more than the rounding; capped at 2^100 so that it stays finite).
+__device__ __forceinline__ float CflFloatBelow(double x) {
+  return fminf(DoubleToFloatBits(x) * (1.0f - 0x1p-22f), 0x1p100f);
+}
+
+// The warp's maximum of the lanes' `mine` (non-negative), folded into the
+// sweep's max slot `slot` by one atomic of the first active lane; returns
+// the slot's new value to every lane of `amask`.
+__device__ __forceinline__ double CflSync(unsigned long long* slot, double mine,
+                                          unsigned amask) {
+  const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(mine));
+  const unsigned bhi = static_cast<unsigned>(b >> 32);
+  const unsigned mhi = __reduce_max_sync(amask, bhi);
+  const unsigned mlo = __reduce_max_sync(amask, bhi == mhi ? static_cast<unsigned>(b) : 0u);
+  const unsigned long long w = (static_cast<unsigned long long>(mhi) << 32) | mlo;
+  const int leader = __ffs(amask) - 1;
+  unsigned long long g = 0;
+  if ((threadIdx.x & 31) == leader) g = atomicMax(slot, w);
+  g = __shfl_sync(amask, g, leader);
+  return __longlong_as_double(static_cast<long long>(g > w ? g : w));
+}
+
 // F_L - F_R in FP64 for the conservative update: FP32 fluxes are widened
 // (exactly, on the integer pipe) and subtracted in FP64.
 __device__ __forceinline__ double FluxDiff(double a, double b) { return a - b; }
@@ -223,6 +294,10 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
   if (!BlockAll(SweepGate(a, split_dt))) return;
   const bool active = t < ntrans;
   const bool skip_cfl = HasFluxOnly<P>::value && a.skip_cfl != 0;
+  constexpr bool kFilter = FilteredCfl<P>::value && HasFluxOnly<P>::value;
+  const unsigned amask = __ballot_sync(0xffffffffu, active);
+  // the FP32 screen's error bound is stated for 1 < gamma <= 2
+  const bool screen = kFilter && !skip_cfl && a.gamma > 1.0 && a.gamma <= 2.0;
 
   int64_t base, stride;
   if (DIR == 0) {
@@ -268,16 +343,59 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
     FluxT F_prev[K];
+    fast::Gas<float> g32;
+    g32.gamma = static_cast<float>(a.gamma);
+    g32.gm1 = static_cast<float>(a.gamma - 1.0);
+    fast::Wave<float> v_prev{};
+    bool ok_prev = false;
+    bool have_prev = false;  // w_prev holds the exact wave of cell j-1
+    // skip threshold: a lower bound of an evaluated face's exact speed
+    float thr = 0.0f;
+    if (kFilter && !skip_cfl && a.smax_out) thr = CflFloatBelow(CflSync(a.smax_out, 0.0, amask));
     for (int j = j0 - 1; j <= j1; ++j) {
+      if constexpr (kFilter) {
+        // the CFL speed of face j (cells j-1, j), before the reconstruction
+        // so that its registers are free
+        if (!skip_cfl) {
+          float c32[K];
+#pragma unroll
+          for (int c = 0; c < K; ++c) c32[c] = CflToF32(cc[c]);
+          const fast::Wave<float> v = fast::MakeWave<D, float>(g32, c32, DIR);
+          const bool ok = screen && CflInRange<D>(c32) && v.a > 0.0f;
+          if (j >= j0) {
+            const float s32 = fast::FaceMaxSpeed<float>(g32, v_prev, v);
+            const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
+            const float bound = fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs));
+            const bool need = !(ok && ok_prev && bound < thr);
+            if (__any_sync(amask, need)) {
+              // the whole warp evaluates (the same instructions as some lanes)
+              const typename P::Wave wl = have_prev ? w_prev : P::MakeWave(eq, cm, DIR);
+              w_prev = P::MakeWave(eq, cc, DIR);
+              const R s = P::FaceMaxSpeed(eq, wl, w_prev);
+              smax = s > smax ? s : smax;
+              thr = fmaxf(thr, CflFloatBelow(static_cast<double>(smax)));
+              have_prev = true;
+            } else {
+              have_prev = false;
+            }
+            if (a.smax_out && ((j - j0) % kCflSyncRows) == kCflSyncRows - 1)
+              thr = fmaxf(thr, CflFloatBelow(CflSync(a.smax_out, static_cast<double>(smax), amask)));
+          }
+          ok_prev = ok;
+          v_prev = v;
+        }
+      }
       P::ToCell(cp, dn);
       if (j + 2 <= j1 + 1) load(dn, j + 2);
       typename P::Rec recL, recR;
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
       typename P::Wave w{};
-      if (!skip_cfl) w = P::MakeWave(eq, cc, DIR);
+      if (!kFilter && !skip_cfl) w = P::MakeWave(eq, cc, DIR);
       if (j >= j0) {
         FluxT F[K];
-        if constexpr (HasFluxOnly<P>::value) {
+        if constexpr (kFilter) {
+          SweepFluxOnly<P>(eq, F, recR_prev, recL, DIR);
+        } else if constexpr (HasFluxOnly<P>::value) {
           if (skip_cfl) {
             SweepFluxOnly<P>(eq, F, recR_prev, recL, DIR);
           } else {
@@ -303,7 +421,7 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
         for (int c = 0; c < K; ++c) F_prev[c] = F[c];
       }
       recR_prev = recR;
-      w_prev = w;
+      if constexpr (!kFilter) w_prev = w;
 #pragma unroll
       for (int c = 0; c < K; ++c) {
         cm[c] = cc[c];

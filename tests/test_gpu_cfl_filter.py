@@ -1,0 +1,158 @@
+"""The sweeps' CFL maximum under the FP32 screen of the exact, fast and
+double-float flavours.
+
+A sweep evaluates a face's Einfeldt speed in the flavour's own arithmetic only
+where an FP32 estimate plus its error bound reaches the largest speed found so
+far, so its maximum must still be the same number as the unscreened one.  The
+stable-dt pass evaluates every face with the same arithmetic: over the same
+faces its per-direction dt equals the sweep's level dt bit for bit, and for
+the exact flavour both equal the oracle's
+(DimensionalSplitLevelIntegrator.hpp:240-245 checks exactly this number).
+The states put many faces within rounding of the maximum, carry hypersonic
+normal and tangential flow (the cancellations the error bound covers), hold
+densities and energies outside the screen's range, or use a gamma outside
+(1, 2], where the screen is off."""
+import zlib
+
+import numpy as np
+import pytest
+
+from finitevolumesolver_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+FLAVOURS = ["fp64_exact", "fp64_fast", "fp64_df"]
+
+
+def plateau(shape, rank, rng):
+    # one uniform state with relative noise 1e-12 and one faster cell: the
+    # maximum sits on two faces among thousands within 1e-11 of it
+    r = 1.0 + 1e-12 * rng.standard_normal(shape)
+    p = 1.0 + 1e-12 * rng.standard_normal(shape)
+    vel = [0.3 + 1e-12 * rng.standard_normal(shape) for _ in range(rank)]
+    cons = workloads.cons_from_prim(r, vel, p)
+    idx = tuple(s // 3 for s in shape)
+    cons[(rank + 1,) + idx] *= 1.0 + 1e-9
+    return cons
+
+
+def hypersonic(shape, rank, rng):
+    # Mach ~1e3 along x (normal for x sweeps, tangential for the others)
+    r = rng.uniform(0.5, 1.5, shape)
+    p = rng.uniform(0.5, 1.5, shape)
+    vel = [1.2e3 * (1.0 + 0.01 * rng.standard_normal(shape))]
+    vel += [rng.uniform(-0.5, 0.5, shape) for _ in range(rank - 1)]
+    return workloads.cons_from_prim(r, vel, p)
+
+
+def hypersonic_mixed(shape, rank, rng):
+    # Mach up to ~1e4 in every direction, pressures over six decades
+    r = np.exp(rng.uniform(-3, 3, shape))
+    p = np.exp(rng.uniform(-7, 7, shape))
+    vel = [rng.uniform(-3e3, 3e3, shape) for _ in range(rank)]
+    return workloads.cons_from_prim(r, vel, p)
+
+
+def scaled(shape, rank, rng):
+    # densities, momenta and energies times 1e-34 or 1e34 (outside the
+    # screen's range) next to ordinary cells of the same velocity and
+    # temperature, so the maximum can sit on either kind
+    cons = workloads.random_state(shape, rank, seed=int(rng.integers(1 << 30)))
+    flat = cons.reshape(rank + 2, -1)
+    n = flat.shape[1]
+    pick = rng.choice(n, size=(2, max(1, n // 20)), replace=False)
+    flat[:, pick[0]] *= 1e-34
+    flat[:, pick[1]] *= 1e34
+    return cons
+
+
+def hot_and_light(shape, rank, rng):
+    # a few cells with E beyond 2^40 (very hot) and a few light cells (density
+    # and momentum times 1e-12, the same pressure: sound 1e6 times faster)
+    cons = workloads.random_state(shape, rank, seed=int(rng.integers(1 << 30)))
+    flat = cons.reshape(rank + 2, -1)
+    n = flat.shape[1]
+    pick = rng.choice(n, size=(2, max(1, n // 200)), replace=False)
+    flat[rank + 1, pick[0]] *= 1e15
+    ke = 0.5 * (flat[1:1 + rank, pick[1]] ** 2).sum(axis=0) / flat[0, pick[1]]
+    flat[rank + 1, pick[1]] -= ke * (1.0 - 1e-12)
+    flat[:1 + rank, pick[1]] *= 1e-12
+    return cons
+
+
+def cold(shape, rank, rng):
+    # nearly pressureless gas: sound speeds ~1e-6, speeds ~1e-3
+    r = rng.uniform(0.5, 1.5, shape)
+    p = 1e-12 * rng.uniform(0.5, 1.5, shape)
+    vel = [1e-3 * rng.uniform(-1, 1, shape) for _ in range(rank)]
+    return workloads.cons_from_prim(r, vel, p)
+
+
+STATES = {"plateau": plateau, "hypersonic": hypersonic, "hypersonic_mixed": hypersonic_mixed,
+          "scaled": scaled, "hot_and_light": hot_and_light, "cold": cold}
+GRIDS = [(1, [1000]), (2, [150, 41]), (3, [40, 34, 37])]
+
+
+def check_sweeps(fvs, orc, rank, n, cons, prec, gamma=1.4, seg=0, oracle=True):
+    dx = [0.1, 0.07, 0.05][:rank]
+    m = fvs.make_method(precision=prec, gamma=gamma)
+    s = fvs.Solver(n, dx, "periodic", method=m)
+    s.set_tiling(seg)
+    g = orc.Grid(rank, n, [0] * rank, dx) if oracle else None
+    for d in range(rank):
+        s.upload(cons)
+        ref = s.ComputeStableDt(d)
+        assert np.isfinite(ref) and ref > 0
+        if g is not None and prec == "fp64_exact":
+            assert ref == g.stable_dt(orc.method(), cons, d, 0)
+        s.upload(cons)
+        level = s.sweep(d, 1e-3 * ref)
+        assert level == ref, (d, level, ref)
+    s.close()
+
+
+@pytest.mark.parametrize("prec", FLAVOURS)
+@pytest.mark.parametrize("state", sorted(STATES))
+@pytest.mark.parametrize("rank,n", GRIDS)
+def test_sweep_max_equals_stable_dt(fvs, orc, rank, n, state, prec):
+    rng = np.random.default_rng(zlib.crc32(f"{rank}{state}".encode()))
+    shape = tuple(reversed(n))
+    cons = STATES[state](shape, rank, rng)
+    cons = cons.reshape([rank + 2] + [1] * (3 - rank) + list(shape))
+    check_sweeps(fvs, orc, rank, n, cons, prec)
+
+
+@pytest.mark.parametrize("seg", [3, 8, 17])
+def test_sweep_max_segments(fvs, orc, seg):
+    # short segments: the warps' running maxima meet through the sweep's slot
+    rng = np.random.default_rng(11)
+    n = [40, 34, 37]
+    cons = hypersonic_mixed(tuple(reversed(n)), 3, rng)
+    for prec in FLAVOURS:
+        check_sweeps(fvs, orc, 3, n, cons, prec, seg=seg)
+
+
+def test_sweep_max_many_blocks(fvs, orc):
+    # 96^3: several waves of blocks, later ones start from the published max
+    rng = np.random.default_rng(3)
+    n = [96, 96, 96]
+    cons = workloads.octants_3d(96, seed=4)
+    check_sweeps(fvs, orc, 3, n, cons, "fp64_exact")
+    check_sweeps(fvs, orc, 3, n, plateau(tuple(reversed(n)), 3, rng), "fp64_exact")
+    check_sweeps(fvs, orc, 3, n, hypersonic(tuple(reversed(n)), 3, rng), "fp64_fast",
+                 oracle=False)
+
+
+@pytest.mark.parametrize("gamma", [1.0 + 1e-3, 5.0 / 3.0, 2.0, 2.5, 4.0])
+def test_sweep_max_gamma(fvs, orc, gamma):
+    # the screen covers 1 < gamma <= 2 and is off above; the oracle's gas has
+    # gamma 1.4, so these compare the sweep with the stable-dt pass only
+    rng = np.random.default_rng(int(gamma * 1000))
+    n = [40, 34, 37]
+    shape = tuple(reversed(n))
+    r = rng.uniform(0.5, 1.5, shape)
+    p = np.exp(rng.uniform(-4, 4, shape))
+    vel = [rng.uniform(-50, 50, shape) for _ in range(3)]
+    cons = workloads.cons_from_prim(r, vel, p, gamma=gamma)
+    for prec in FLAVOURS:
+        check_sweeps(fvs, orc, 3, n, cons, prec, gamma=gamma, oracle=False)
