@@ -426,6 +426,9 @@ cudaError_t EnqueueStep(fvs_solver* s, int start, int64_t cycle, int step_in_bat
     e = CcReferenceStates(s, s->buf[start]);
     if (e != cudaSuccess) return e;
   }
+  // the pass's max slots start at zero (its screened speeds need it)
+  e = cudaMemsetAsync(s->ctrl->smax_stable, 0, sizeof(s->ctrl->smax_stable), s->stream);
+  if (e != cudaSuccess) return e;
   e = LaunchStable(s, s->buf[start], s->ctrl->smax_stable, s->ctrl);
   if (e != cudaSuccess) return e;
   fvs::BeginStepKernel<<<1, 1, 0, s->stream>>>(s->ctrl, plan);

@@ -197,6 +197,158 @@ __global__ void __launch_bounds__(32 * kDtRows) StableDtMarch3Kernel(StableDtArg
   BlockMaxAtomic<3>(a.smax_out, smax);
 }
 
+// StableDtMarch3Kernel with the CFL speeds screened in FP32 (FilteredCfl
+// policies, 1 < gamma <= 2): the same blocks, marching and faces; the FP32
+// waves pass between lanes (x), warps (y, shared memory) and planes (z), and
+// a direction's exact speeds are evaluated only by warps holding a face of
+// that direction whose FP32 speed plus error bound reaches the direction's
+// threshold (the lane's own maximum and the pass's maximum published so far,
+// every kCflSyncRows planes).  The exact waves of a face's other cell come
+// from a shuffle (x) or a reload of its state (y, z; L1 hits).  Cells outside
+// the bound's range carry h = inf, so their faces are always evaluated.  The
+// per-direction maxima are the same numbers as the unscreened kernel's, bit
+// for bit; the max slots must start at zero (or at an exact speed of the same
+// state).
+template <template <int> class PT>
+__global__ void __launch_bounds__(32 * kDtRows) StableDtScreen3Kernel(StableDtArgs a, int seg) {
+  using P = PT<3>;
+  using R = typename P::Real;
+  using W = typename P::Wave;
+  using V = fast::Wave<float>;
+  constexpr int K = 5;
+  constexpr unsigned kAll = 0xffffffffu;
+  __shared__ V ycell[2][kDtRows][32];
+  const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
+  const int64_t cs = int64_t(nx) * ny * nz;
+  if (!BlockAll(!(a.ctrl && (a.ctrl->abort || a.ctrl->done)))) return;
+  const typename P::Gas eq = P::MakeGas(a.gamma);
+  fast::Gas<float> g32;
+  g32.gamma = static_cast<float>(a.gamma);
+  g32.gm1 = static_cast<float>(a.gamma - 1.0);
+  R smr[3] = {R(0), R(0), R(0)};
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int xw = (nx + 30) / 31;
+  const int jblocks = (ny + kDtRows - 1) / kDtRows;
+  const int wx = static_cast<int>(blockIdx.x % xw);
+  const int jb = static_cast<int>((blockIdx.x / xw) % jblocks);
+  const int k0 = static_cast<int>(blockIdx.x / (int64_t(xw) * jblocks)) * seg;
+  const int k1 = min(nz, k0 + seg);
+  const int j = jb * kDtRows + warp;
+  const bool jvalid = j < ny;
+  const int jc = jvalid ? j : ny - 1;
+  const int i = wx * 31 + lane - 1;
+  const bool own = jvalid && lane >= 1 && i < nx;
+  const int ic = BcIndex(i, nx, a.bc[0]);  // lane 0: the left neighbour
+  const int jbelow = BcIndex(jb * kDtRows - 1, ny, a.bc[1]);
+  const int jn = warp > 0 ? j - 1 : jbelow;  // the row below this warp's (own lanes)
+  auto load = [&](int jj, int kk, R* u) {
+    const int64_t off = (int64_t(kk) * ny + jj) * nx + ic;
+    double ud[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) ud[c] = __ldg(a.in + c * cs + off);
+    P::ToCell(u, ud);
+  };
+  // FP32 waves of a cell in the three directions; h = inf outside the range
+  auto screen_waves = [&](const R* u, V* v) {
+    float c32[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) c32[c] = CflToF32(u[c]);
+    fast::MakeWaves<3, float>(g32, c32, v);
+    const bool ok = CflInRange<3>(c32) && v[0].a > 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d].h = ok ? v[d].h : __int_as_float(0x7f800000);
+  };
+  auto bound = [&](const V& l, const V& r) {
+    const float s32 = fast::FaceMaxSpeed<float>(g32, l, r);
+    const float sh = fast::Math<float>::Sqrt(fmaxf(l.h, r.h));
+    return fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs));
+  };
+  auto take = [&](R& m, R v) { m = v > m ? v : m; };
+  const bool ytile = !(a.rule == 1 && !ReferenceTileFaceT(j, ny, a.width));
+  const bool ytop = j == ny - 1 && a.bc[1] != 0 &&
+                    !(a.rule == 1 && !ReferenceTileFaceT(ny, ny, a.width));
+  float thr[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) thr[d] = CflFloatBelow(CflSync(a.smax_out + d, 0.0, kAll));
+  V vz_prev;
+  {
+    R u[K];
+    load(jc, BcIndex(k0 - 1, nz, a.bc[2]), u);
+    V v[3];
+    screen_waves(u, v);
+    vz_prev = v[2];
+  }
+  for (int k = k0; k < k1; ++k) {
+    R u[K];
+    load(jc, k, u);
+    V v[3];
+    screen_waves(u, v);
+    ycell[k & 1][warp][lane] = v[1];
+    V vy_below;
+    if (warp == 0) {  // the row below the block
+      R ub[K];
+      load(jbelow, k, ub);
+      V vb[3];
+      screen_waves(ub, vb);
+      vy_below = vb[1];
+    }
+    const V vl = ShflUp(v[0], 1);
+    __syncthreads();
+    if (warp > 0) vy_below = ycell[k & 1][warp - 1][lane];
+    const bool zface = !(a.rule == 1 && !ReferenceTileFaceT(k, nz, a.width));
+    const bool ztop = k == nz - 1 && a.bc[2] != 0 &&
+                      !(a.rule == 1 && !ReferenceTileFaceT(nz, nz, a.width));
+    const bool xtop = i == nx - 1 && a.bc[0] != 0;
+    bool need[3] = {false, false, false};
+    if (own) {
+      need[0] = !(bound(vl, v[0]) < thr[0]) || (xtop && !(bound(v[0], v[0]) < thr[0]));
+      need[1] = (ytile && !(bound(vy_below, v[1]) < thr[1])) ||
+                (ytop && !(bound(v[1], v[1]) < thr[1]));
+      need[2] = (zface && !(bound(vz_prev, v[2]) < thr[2])) ||
+                (ztop && !(bound(v[2], v[2]) < thr[2]));
+    }
+    const bool any_x = __any_sync(kAll, need[0]);
+    const bool any_y = __any_sync(kAll, need[1]);
+    const bool any_z = __any_sync(kAll, need[2]);
+    if (any_x || any_y || any_z) {
+      // exact speeds of the warp's faces in the directions that need them
+      W w[3];
+      WavesOf<P>::Get(eq, u, w);
+      if (any_x) {
+        const W wl = ShflUp(w[0], 1);
+        if (own) {
+          take(smr[0], P::FaceMaxSpeed(eq, wl, w[0]));
+          if (xtop) take(smr[0], P::FaceMaxSpeed(eq, w[0], w[0]));
+        }
+      }
+      if (any_y && own) {
+        R ub[K];
+        load(jn, k, ub);
+        if (ytile) take(smr[1], P::FaceMaxSpeed(eq, P::MakeWave(eq, ub, 1), w[1]));
+        if (ytop) take(smr[1], P::FaceMaxSpeed(eq, w[1], w[1]));
+      }
+      if (any_z && own) {
+        R uz[K];
+        load(jc, BcIndex(k - 1, nz, a.bc[2]), uz);
+        if (zface) take(smr[2], P::FaceMaxSpeed(eq, P::MakeWave(eq, uz, 2), w[2]));
+        if (ztop) take(smr[2], P::FaceMaxSpeed(eq, w[2], w[2]));
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) thr[d] = fmaxf(thr[d], CflFloatBelow(static_cast<double>(smr[d])));
+    }
+    if (((k - k0) % kCflSyncRows) == kCflSyncRows - 1) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        thr[d] = fmaxf(thr[d], CflFloatBelow(CflSync(a.smax_out + d,
+                                                     static_cast<double>(smr[d]), kAll)));
+    }
+    vz_prev = v[2];
+  }
+  const double smax[3] = {static_cast<double>(smr[0]), static_cast<double>(smr[1]),
+                          static_cast<double>(smr[2])};
+  BlockMaxAtomic<3>(a.smax_out, smax);
+}
+
 template <template <int> class PT>
 cudaError_t LaunchStableDtT(const StableDtArgs& a, cudaStream_t s) {
   const int64_t cells = int64_t(a.n[0]) * a.n[1] * a.n[2];
@@ -210,6 +362,12 @@ cudaError_t LaunchStableDtT(const StableDtArgs& a, cudaStream_t s) {
         std::max<int64_t>(1, std::min<int64_t>(a.n[2], (want + tiles - 1) / tiles));
     const int seg = static_cast<int>((a.n[2] + zseg - 1) / zseg);
     const unsigned grid = static_cast<unsigned>(tiles * ((a.n[2] + seg - 1) / seg));
+    if constexpr (FilteredCfl<PT<3>>::value) {
+      if (a.gamma > 1.0 && a.gamma <= 2.0 && a.smax_out) {
+        StableDtScreen3Kernel<PT><<<grid, 32 * kDtRows, 0, s>>>(a, seg);
+        return cudaGetLastError();
+      }
+    }
     StableDtMarch3Kernel<PT><<<grid, 32 * kDtRows, 0, s>>>(a, seg);
     return cudaGetLastError();
   }

@@ -70,7 +70,9 @@ typedef enum fvs_precision {
   FVS_FP64_FAST = 1,  /* FP64 with FMA and shared reciprocals (<= 1e-12 rel) */
   FVS_MIXED = 2,      /* FP32 reconstruction/flux, FP64 state and update */
   FVS_FP64_DF = 3     /* MUSCL-HLLE in double-float (FP32 pairs, ~48 bits) on the
-                         FP32 pipes, FP64 state and update (uniform grids) */
+                         FP32 pipes, FP64 state and update (uniform grids); FP32's
+                         exponent range: states and products such as rho u^2 within
+                         about 1e-30 .. 1e30 */
 } fvs_precision;
 
 typedef enum fvs_guess {

@@ -4,10 +4,12 @@ double-float flavours.
 A sweep evaluates a face's Einfeldt speed in the flavour's own arithmetic only
 where an FP32 estimate plus its error bound reaches the largest speed found so
 far, so its maximum must still be the same number as the unscreened one.  The
-stable-dt pass evaluates every face with the same arithmetic: over the same
-faces its per-direction dt equals the sweep's level dt bit for bit, and for
-the exact flavour both equal the oracle's
-(DimensionalSplitLevelIntegrator.hpp:240-245 checks exactly this number).
+stable-dt pass computes the same face speeds with the same arithmetic (its
+3-D kernel screened the same way, its 1-D and 2-D kernels not): over the same
+faces its per-direction dt equals the sweep's level dt bit for bit, for the
+exact flavour both equal the oracle's
+(DimensionalSplitLevelIntegrator.hpp:240-245 checks exactly this number), and
+for the fast and double-float flavours they agree with it to 1e-12.
 The states put many faces within rounding of the maximum, carry hypersonic
 normal and tangential flow (the cancellations the error bound covers), hold
 densities and energies outside the screen's range, or use a gamma outside
@@ -103,8 +105,12 @@ def check_sweeps(fvs, orc, rank, n, cons, prec, gamma=1.4, seg=0, oracle=True):
         s.upload(cons)
         ref = s.ComputeStableDt(d)
         assert np.isfinite(ref) and ref > 0
-        if g is not None and prec == "fp64_exact":
-            assert ref == g.stable_dt(orc.method(), cons, d, 0)
+        if g is not None:
+            want = g.stable_dt(orc.method(), cons, d, 0)
+            if prec == "fp64_exact":
+                assert ref == want
+            else:
+                assert ref == pytest.approx(want, rel=1e-12)
         s.upload(cons)
         level = s.sweep(d, 1e-3 * ref)
         assert level == ref, (d, level, ref)
@@ -115,6 +121,8 @@ def check_sweeps(fvs, orc, rank, n, cons, prec, gamma=1.4, seg=0, oracle=True):
 @pytest.mark.parametrize("state", sorted(STATES))
 @pytest.mark.parametrize("rank,n", GRIDS)
 def test_sweep_max_equals_stable_dt(fvs, orc, rank, n, state, prec):
+    if state == "scaled" and prec == "fp64_df":
+        pytest.skip("double-float has FP32's exponent range: rho u^2 of 1e34 overflows")
     rng = np.random.default_rng(zlib.crc32(f"{rank}{state}".encode()))
     shape = tuple(reversed(n))
     cons = STATES[state](shape, rank, rng)
