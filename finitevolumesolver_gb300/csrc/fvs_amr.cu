@@ -933,6 +933,9 @@ int fvs_amr_autotune(fvs_amr* a, int32_t* configs) {
               const int grid = std::min(full, a->sms * bps);
               float sum = 0.f;
               for (int rep = 0; rep < 3; ++rep) {
+                // the sweep's max slot starts at zero, as in a step
+                AMR_CUDA(cudaMemsetAsync(&a->ctrl->smax_sweep[0], 0, sizeof(unsigned long long),
+                                         a->stream));
                 AMR_CUDA(cudaEventRecord(e0, a->stream));
                 AMR_CUDA(LaunchSweep(a, l, d, Lv.A, Lv.B, 0.5, a->tune_dt,
                                      &a->ctrl->smax_sweep[0], block, grid, occ, si));

@@ -12,6 +12,16 @@
 // per-sweep CFL check.  The halo cells at the ends of a row are read where
 // they live (Seg::halo): the same level's current buffer or the coarser
 // level, which is the ghost fill of those strips at sweep time.
+//
+// For FilteredCfl policies (exact and fast FP64) both kernels screen the CFL
+// speeds in FP32 as the uniform sweeps do (fvs_sweep.cuh): a face's exact
+// speed is evaluated only when its FP32 speed plus error bound reaches the
+// thread's threshold.  The rows of a warp can differ in length, so the
+// decisions are per thread (no warp votes); the threshold is the thread's own
+// maximum and the launch's max slot, read at every segment start, and a
+// thread publishes its maximum at a segment end when it exceeds the slot
+// value it read.  The maxima are the same numbers, bit for bit; the max slots
+// must start at zero (or at an exact speed of the same sweep).
 #pragma once
 
 #include <climits>
@@ -37,9 +47,20 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
   R smax = R(0);
   int status = 0;
   typename P::Stats stats;
+  constexpr bool kFilter = FilteredCfl<P>::value && HasFluxOnly<P>::value;
+  const bool screen = kFilter && a.gamma > 1.0 && a.gamma <= 2.0;
+  fast::Gas<float> g32;
+  g32.gamma = static_cast<float>(a.gamma);
+  g32.gm1 = static_cast<float>(a.gamma - 1.0);
+  float thr = 0.0f;
+  unsigned long long known = 0;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.nsegs;
        r += gridDim.x * blockDim.x) {
     const Seg w = a.segs[r];
+    if constexpr (kFilter) {
+      known = *reinterpret_cast<volatile unsigned long long*>(a.smax_out);
+      thr = fmaxf(thr, CflFloatBelow(__longlong_as_double(static_cast<long long>(known))));
+    }
     int cap = w.cap_begin;
     int next_face = cap < w.cap_end ? a.caps[cap].face : INT_MAX;
     const int j0 = w.j0, j1 = w.j1;
@@ -74,16 +95,48 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
     FluxT F_prev[K];
+    fast::Wave<float> v_prev{};
+    bool ok_prev = false;
+    bool have_prev = false;  // w_prev holds the exact wave of cell j-1
     for (int j = j0 - 1; j <= j1; ++j) {
+      if constexpr (kFilter) {
+        float c32[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) c32[c] = CflToF32(cc[c]);
+        const fast::Wave<float> v = fast::MakeWave<2, float>(g32, c32, DIR);
+        const bool ok = screen && CflInRange<2>(c32) && v.a > 0.0f;
+        if (j >= j0) {
+          const float s32 = fast::FaceMaxSpeed<float>(g32, v_prev, v);
+          const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
+          const float bound = fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs));
+          if (!(ok && ok_prev && bound < thr)) {
+            const typename P::Wave wl = have_prev ? w_prev : P::MakeWave(eq, cm, DIR);
+            w_prev = P::MakeWave(eq, cc, DIR);
+            const R s = P::FaceMaxSpeed(eq, wl, w_prev);
+            smax = s > smax ? s : smax;
+            thr = fmaxf(thr, CflFloatBelow(static_cast<double>(smax)));
+            have_prev = true;
+          } else {
+            have_prev = false;
+          }
+        }
+        ok_prev = ok;
+        v_prev = v;
+      }
       P::ToCell(cp, dn);
       if (j + 2 <= j1 + 1) load(dn, j + 2);
       typename P::Rec recL, recR;
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
-      const typename P::Wave wv = P::MakeWave(eq, cc, DIR);
+      typename P::Wave wv{};
+      if constexpr (!kFilter) wv = P::MakeWave(eq, cc, DIR);
       if (j >= j0) {
         FluxT F[K];
-        const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, wv, DIR, stats);
-        smax = s > smax ? s : smax;
+        if constexpr (kFilter) {
+          SweepFluxOnly<P>(eq, F, recR_prev, recL, DIR);
+        } else {
+          const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, wv, DIR, stats);
+          smax = s > smax ? s : smax;
+        }
         if (j == next_face) {
           double* dst = a.reg + int64_t(a.caps[cap].dst) * K;
 #pragma unroll
@@ -104,12 +157,17 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
         for (int c = 0; c < K; ++c) F_prev[c] = F[c];
       }
       recR_prev = recR;
-      w_prev = wv;
+      if constexpr (!kFilter) w_prev = wv;
 #pragma unroll
       for (int c = 0; c < K; ++c) {
         cm[c] = cc[c];
         cc[c] = cp[c];
       }
+    }
+    if constexpr (kFilter) {
+      const unsigned long long b =
+          static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(smax)));
+      if (b > known) atomicMax(a.smax_out, b);
     }
   }
   const double smax_d = static_cast<double>(smax);
@@ -128,11 +186,18 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
   constexpr int K = kComp;
   const typename P::Gas eq = P::MakeGas(a.gamma);
   const int64_t N = a.ncells;
+  constexpr bool kFilter = FilteredCfl<P>::value;
+  const bool screen = kFilter && a.gamma > 1.0 && a.gamma <= 2.0;
+  fast::Gas<float> g32;
+  g32.gamma = static_cast<float>(a.gamma);
+  g32.gm1 = static_cast<float>(a.gamma - 1.0);
+  float thr = 0.0f;
+  unsigned long long known = 0;
   R smax = R(0);
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.nsegs;
        r += gridDim.x * blockDim.x) {
     const Seg w = a.segs[r];
-    auto wave = [&](int j) {
+    auto cell = [&](int j, R* v) {
       const double* src = a.in;
       int64_t off, cs = N;
       if (j >= 0 && j < w.n) {
@@ -148,18 +213,69 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
         }
       }
       double u[K];
-      R v[K];
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(src + c * cs + off);
       P::ToCell(v, u);
-      return P::MakeWave(eq, v, DIR);
     };
-    typename P::Wave wl = wave(w.j0 - 1);
-    for (int f = w.j0; f <= w.j1; ++f) {
-      const typename P::Wave wr = wave(f);
-      const R s = P::FaceMaxSpeed(eq, wl, wr);
-      smax = s > smax ? s : smax;
-      wl = wr;
+    if constexpr (kFilter) {
+      known = *reinterpret_cast<volatile unsigned long long*>(a.smax_out);
+      thr = fmaxf(thr, CflFloatBelow(__longlong_as_double(static_cast<long long>(known))));
+      // FP32 screen (see the file comment): the exact waves of a face only
+      // when its bound reaches the threshold
+      auto screen_wave = [&](const R* u, bool& ok) {
+        float c32[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) c32[c] = CflToF32(u[c]);
+        const fast::Wave<float> v = fast::MakeWave<2, float>(g32, c32, DIR);
+        ok = screen && CflInRange<2>(c32) && v.a > 0.0f;
+        return v;
+      };
+      R ul[K];
+      cell(w.j0 - 1, ul);
+      bool ok_l;
+      fast::Wave<float> vl = screen_wave(ul, ok_l);
+      typename P::Wave wl;
+      bool have_l = false;
+      for (int f = w.j0; f <= w.j1; ++f) {
+        R ur[K];
+        cell(f, ur);
+        bool ok_r;
+        const fast::Wave<float> vr = screen_wave(ur, ok_r);
+        const float s32 = fast::FaceMaxSpeed<float>(g32, vl, vr);
+        const float sh = fast::Math<float>::Sqrt(fmaxf(vl.h, vr.h));
+        const float bound = fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs));
+        if (!(ok_l && ok_r && bound < thr)) {
+          if (!have_l) wl = P::MakeWave(eq, ul, DIR);
+          const typename P::Wave wr = P::MakeWave(eq, ur, DIR);
+          const R s = P::FaceMaxSpeed(eq, wl, wr);
+          smax = s > smax ? s : smax;
+          thr = fmaxf(thr, CflFloatBelow(static_cast<double>(smax)));
+          wl = wr;
+          have_l = true;
+        } else {
+          have_l = false;
+        }
+#pragma unroll
+        for (int c = 0; c < K; ++c) ul[c] = ur[c];
+        vl = vr;
+        ok_l = ok_r;
+      }
+      const unsigned long long b =
+          static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(smax)));
+      if (b > known) atomicMax(a.smax_out, b);
+    } else {
+      auto wave = [&](int j) {
+        R v[K];
+        cell(j, v);
+        return P::MakeWave(eq, v, DIR);
+      };
+      typename P::Wave wl = wave(w.j0 - 1);
+      for (int f = w.j0; f <= w.j1; ++f) {
+        const typename P::Wave wr = wave(f);
+        const R s = P::FaceMaxSpeed(eq, wl, wr);
+        smax = s > smax ? s : smax;
+        wl = wr;
+      }
     }
   }
   const double smax_d = static_cast<double>(smax);

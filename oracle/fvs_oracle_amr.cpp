@@ -167,11 +167,14 @@ struct Hier {
           }
           CompleteFromCons<kD>(eq, a, ua);
           CompleteFromCons<kD>(eq, b, ub);
-          // HllStableDt = dx / max(|sL|, |sR|); the speed itself here
+          // the face speed of HllStableDt (fvs_oracle.hpp; HllMethod.hpp:
+          // 337-347) with its NaN rule: a NaN sound speed (negative
+          // pressure) gives either |sR| or NaN, and NaN face speeds are
+          // skipped by the max, as in the uniform-grid restatement
           double sL, sR;
           Einfeldt<kD>(eq, a, b, d, sL, sR);
-          const double s = std::max(std::abs(sL), std::abs(sR));
-          smax = std::max(smax, s);
+          const double s = PMax(PMax(0.0, std::abs(sL)), std::abs(sR));
+          smax = s > smax ? s : smax;
         }
       }
     }

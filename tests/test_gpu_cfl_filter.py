@@ -164,3 +164,23 @@ def test_sweep_max_gamma(fvs, orc, gamma):
     cons = workloads.cons_from_prim(r, vel, p, gamma=gamma)
     for prec in FLAVOURS:
         check_sweeps(fvs, orc, 3, n, cons, prec, gamma=gamma, oracle=False)
+
+
+@pytest.mark.parametrize("state", ["hypersonic", "plateau", "cold"])
+def test_amr_screened_speeds_bit_exact(fvs, orc, state):
+    # the AMR patch sweeps and max-speed passes screen their speeds per thread:
+    # a three-level hierarchy filled with the state, patch by patch, runs the
+    # oracle's dt sequence and state bit for bit (exact FP64)
+    h, _ = workloads.amr_blast_2d(64, 3, target=80, sizes=(8, 16))
+    rng = np.random.default_rng(zlib.crc32(state.encode()))
+    parts = []
+    for x0, y0, x1, y1 in h.boxes:
+        parts.append(STATES[state]((y1 - y0, x1 - x0), 2, rng).reshape(-1))
+    cons = np.concatenate(parts)
+    a = fvs.AmrSolver(h)
+    a.upload(cons)
+    st, dts = a.run(cfl=0.8, t_end=10.0, max_steps=3, log_len=4)
+    ref, ref_dts, rs = orc.amr_run(h, cons, 0.8, 10.0, max_steps=3)
+    assert st.steps == 3 and st.restarts == rs
+    np.testing.assert_array_equal(dts, ref_dts)
+    np.testing.assert_array_equal(a.download(), ref)
