@@ -3,7 +3,9 @@
 // speeds:
 //   T = double in a -fmad=false translation unit: the exact flavour, bit for
 //     bit the CPU oracle's restatement of the reference;
-//   T = double with FMA contraction: the fast FP64 flavour;
+//   T = double with FMA contraction and the refined reciprocals and
+//     reciprocal square roots of fvs_physics_fast.cuh (math policy CcFast):
+//     the fast FP64 flavour, within 1e-12 of the exact one;
 //   T = float: the mixed flavour -- masked MUSCL-Hancock, HLL/Einfeldt,
 //     boundary (wall) states and CFL speeds in FP32; the state, the face
 //     fractions, the h-box flux combination and the cut-cell update in FP64.
@@ -30,9 +32,32 @@
 namespace fvs {
 namespace cc {
 
-template <class T> struct GasT {
+// Arithmetic of the physics below: IEEE quotients and square roots (CcIeee:
+// the exact flavour, and FP32 for the mixed one) or the fast FP64 flavour's
+// (CcFast: quotients as products with a reciprocal refined from the
+// rcp.approx seed, square roots as a times its refined reciprocal square
+// root; each within 2 ulp; the square root of a non-positive number is 0).
+// The policy is a template argument of every kernel and launcher, so the
+// exact and the fast FP64 instantiations, compiled with different flags in
+// different translation units, never share a symbol.
+struct CcIeee {
+  static constexpr bool kFast = false;
+  template <class T> static __device__ __forceinline__ T Div(T a, T b) { return a / b; }
+  template <class T> static __device__ __forceinline__ T Sqrt(T a) { return sqrt(a); }
+};
+struct CcFast {
+  static constexpr bool kFast = true;
+  static __device__ __forceinline__ double Div(double a, double b) {
+    return fast::Math<double>::Div(a, b);
+  }
+  static __device__ __forceinline__ double Rcp(double a) { return fast::Math<double>::Rcp(a); }
+  static __device__ __forceinline__ double Sqrt(double a) { return fast::Math<double>::Sqrt(a); }
+};
+
+template <class T, class M = CcIeee> struct GasT {
   T gamma;
   T gamma_minus_1_inv;
+  T gm1;  // gamma - 1 (fast flavour: p = e_int * (gamma - 1))
 };
 
 template <class T> struct C2T {
@@ -46,30 +71,38 @@ template <class T> struct C2T {
 template <class T> __device__ __forceinline__ T PMinT(T a, T b) { return a < b ? a : b; }
 template <class T> __device__ __forceinline__ T PMaxT(T a, T b) { return a > b ? a : b; }
 
-template <class T> __device__ __forceinline__ GasT<T> MakeGasT(double gamma) {
-  GasT<T> g;
+template <class T, class M = CcIeee> __device__ __forceinline__ GasT<T, M> MakeGasT(double gamma) {
+  GasT<T, M> g;
   g.gamma = T(gamma);
   g.gamma_minus_1_inv = T(1.0 / (gamma - 1.0));
+  g.gm1 = T(gamma - 1.0);
   return g;
 }
 
 // PerfectGas<2>::CompleteFromCons (PerfectGas.cpp:96-110): e_kin = 0.5 |m|^2
 // / rho, p = (E - e_kin) / gamma_minus_1_inv, c = sqrt(gamma p / rho).
-template <class T>
-__device__ __forceinline__ void CompleteT(const GasT<T>& eq, C2T<T>& q, const T* u) {
+template <class T, class M>
+__device__ __forceinline__ void CompleteT(const GasT<T, M>& eq, C2T<T>& q, const T* u) {
   q.rho = u[0];
   q.m[0] = u[1];
   q.m[1] = u[2];
   q.E = u[3];
-  const T e_kin = T(0.5) * (q.m[0] * q.m[0] + q.m[1] * q.m[1]) / q.rho;
-  const T e_int = q.E - e_kin;
-  q.p = e_int / eq.gamma_minus_1_inv;
-  q.c = sqrt(eq.gamma * q.p / q.rho);
+  if constexpr (M::kFast) {
+    const T ir = M::Rcp(q.rho);
+    const T e_kin = T(0.5) * (q.m[0] * q.m[0] + q.m[1] * q.m[1]) * ir;
+    q.p = (q.E - e_kin) * eq.gm1;
+    q.c = M::Sqrt(eq.gamma * q.p * ir);
+  } else {
+    const T e_kin = T(0.5) * (q.m[0] * q.m[0] + q.m[1] * q.m[1]) / q.rho;
+    const T e_int = q.E - e_kin;
+    q.p = e_int / eq.gamma_minus_1_inv;
+    q.c = sqrt(eq.gamma * q.p / q.rho);
+  }
 }
 
 // PerfectGas<2>::Flux (PerfectGas.cpp:52-64).
-template <class T> __device__ __forceinline__ void FluxT(T* f, const C2T<T>& q, int dir) {
-  const T velocity = q.m[dir] / q.rho;
+template <class M, class T> __device__ __forceinline__ void FluxT(T* f, const C2T<T>& q, int dir) {
+  const T velocity = M::Div(q.m[dir], q.rho);
   f[0] = q.m[dir];
   f[1] = velocity * q.m[0];
   f[2] = velocity * q.m[1];
@@ -78,29 +111,29 @@ template <class T> __device__ __forceinline__ void FluxT(T* f, const C2T<T>& q, 
 }
 
 // EinfeldtSignalVelocities (scalar, EinfeldtSignalVelocities.hpp:25-62).
-template <class T>
-__device__ __forceinline__ void EinfeldtT(const GasT<T>& eq, const C2T<T>& L, const C2T<T>& R,
-                                          int dir, T& sL, T& sR) {
+template <class T, class M>
+__device__ __forceinline__ void EinfeldtT(const GasT<T, M>& eq, const C2T<T>& L,
+                                          const C2T<T>& R, int dir, T& sL, T& sR) {
   const T rhoL = L.rho;
   const T rhoR = R.rho;
-  const T sqRhoL = sqrt(rhoL);
-  const T sqRhoR = sqrt(rhoR);
-  const T oosqRhoSum = T(1) / (sqRhoL + sqRhoR);
-  const T uL = L.m[dir] / rhoL;
-  const T uR = R.m[dir] / rhoR;
+  const T sqRhoL = M::Sqrt(rhoL);
+  const T sqRhoR = M::Sqrt(rhoR);
+  const T oosqRhoSum = M::Div(T(1), sqRhoL + sqRhoR);
+  const T uL = M::Div(L.m[dir], rhoL);
+  const T uR = M::Div(R.m[dir], rhoR);
   const T roeU = (uL * sqRhoL + uR * sqRhoR) * oosqRhoSum;
-  const T hL = (L.E + L.p) / rhoL;
-  const T hR = (R.E + R.p) / rhoR;
+  const T hL = M::Div(L.E + L.p, rhoL);
+  const T hR = M::Div(R.E + R.p, rhoR);
   const T roeH = (hL * sqRhoL + hR * sqRhoR) * oosqRhoSum;
   const T roeA2 = (eq.gamma - T(1)) * (roeH - T(0.5) * roeU * roeU);
-  const T roeA = sqrt(roeA2);
+  const T roeA = M::Sqrt(roeA2);
   sL = PMinT(uL - L.c, roeU - roeA);
   sR = PMaxT(roeU + roeA, uR + R.c);
 }
 
 // CompleteFromCons masked by `mask && rho > 0` (PerfectGas.cpp:126-144).
-template <class T>
-__device__ __forceinline__ void CompleteMasked(const GasT<T>& eq, C2T<T>& q, const T* u,
+template <class T, class M>
+__device__ __forceinline__ void CompleteMasked(const GasT<T, M>& eq, C2T<T>& q, const T* u,
                                                bool mask) {
   if (!(mask && u[0] > T(0))) {
     q.rho = T(0);
@@ -115,9 +148,10 @@ __device__ __forceinline__ void CompleteMasked(const GasT<T>& eq, C2T<T>& q, con
 }
 
 // Flux masked by `rho > 0` (PerfectGas.cpp:79-93, mask true).
-template <class T> __device__ __forceinline__ void FluxMasked(T* f, const C2T<T>& q, int dir) {
+template <class M, class T>
+__device__ __forceinline__ void FluxMasked(T* f, const C2T<T>& q, int dir) {
   const T rho = (q.rho > T(0)) ? q.rho : T(1);
-  const T velocity = q.m[dir] / rho;
+  const T velocity = M::Div(q.m[dir], rho);
   f[0] = q.m[dir];
   f[1] = velocity * q.m[0];
   f[2] = velocity * q.m[1];
@@ -126,31 +160,42 @@ template <class T> __device__ __forceinline__ void FluxMasked(T* f, const C2T<T>
 }
 
 // Masked Einfeldt speeds with mask true (EinfeldtSignalVelocities.hpp:99-142).
-template <class T>
-__device__ __forceinline__ void EinfeldtMasked(const GasT<T>& eq, const C2T<T>& L,
+template <class T, class M>
+__device__ __forceinline__ void EinfeldtMasked(const GasT<T, M>& eq, const C2T<T>& L,
                                                const C2T<T>& R, int dir, T& sL, T& sR) {
   const T rhoL = L.rho, rhoR = R.rho;
-  const T sqRhoL = sqrt(rhoL);
-  const T sqRhoR = sqrt(rhoR);
+  const T sqRhoL = M::Sqrt(rhoL);
+  const T sqRhoR = M::Sqrt(rhoR);
   const T sqRho = sqRhoL + sqRhoR;
-  const T uL = L.m[dir] / rhoL;
-  const T uR = R.m[dir] / rhoR;
-  const T wL = sqRhoL / sqRho;
-  const T wR = sqRhoR / sqRho;
+  T uL, uR, wL, wR, hL, hR;
+  if constexpr (M::kFast) {
+    const T irL = M::Rcp(rhoL), irR = M::Rcp(rhoR), iw = M::Rcp(sqRho);
+    uL = L.m[dir] * irL;
+    uR = R.m[dir] * irR;
+    wL = sqRhoL * iw;
+    wR = sqRhoR * iw;
+    hL = (L.E + L.p) * irL;
+    hR = (R.E + R.p) * irR;
+  } else {
+    uL = L.m[dir] / rhoL;
+    uR = R.m[dir] / rhoR;
+    wL = sqRhoL / sqRho;
+    wR = sqRhoR / sqRho;
+    hL = (L.E + L.p) / rhoL;
+    hR = (R.E + R.p) / rhoR;
+  }
   const T roeU = uL * wL + uR * wR;
-  const T hL = (L.E + L.p) / rhoL;
-  const T hR = (R.E + R.p) / rhoR;
   const T roeH = hL * wL + hR * wR;
   const T roeA2 = (eq.gamma - T(1)) * (roeH - T(0.5) * roeU * roeU);
-  const T roeA = sqrt(roeA2);
+  const T roeA = M::Sqrt(roeA2);
   sL = PMinT(uL - L.c, roeU - roeA);
   sR = PMaxT(roeU + roeA, uR + R.c);
 }
 
 // Masked MUSCL-Hancock predictor of one cell (both face states); the slope
 // is zeroed unless the three cells of its window have volume.
-template <class T>
-__device__ __forceinline__ void PredictMasked(const GasT<T>& eq, C2T<T>& recL, C2T<T>& recR,
+template <class T, class M>
+__device__ __forceinline__ void PredictMasked(const GasT<T, M>& eq, C2T<T>& recL, C2T<T>& recR,
                                               const T* q0, const T* q1, const T* q2, bool smask,
                                               int limiter, T lambda_half, int dir) {
   T uL[4], uR[4];
@@ -161,7 +206,7 @@ __device__ __forceinline__ void PredictMasked(const GasT<T>& eq, C2T<T>& recL, C
     T slope;
     if (limiter == exact::kVanLeer) {
       const T c = T(2) * sL * sR;
-      slope = (c > T(0)) ? c / (sL + sR) : T(0);
+      slope = (c > T(0)) ? M::Div(c, sL + sR) : T(0);
     } else if (limiter == exact::kMinMod) {
       slope = (sR > 0) ? PMaxT(T(0), PMinT(sL, sR)) : PMinT(T(0), PMaxT(sL, sR));
     } else {
@@ -174,8 +219,8 @@ __device__ __forceinline__ void PredictMasked(const GasT<T>& eq, C2T<T>& recL, C
   CompleteMasked(eq, qL, uL, true);
   CompleteMasked(eq, qR, uR, true);
   T fL[4], fR[4];
-  FluxMasked(fL, qL, dir);
-  FluxMasked(fR, qR, dir);
+  FluxMasked<M>(fL, qL, dir);
+  FluxMasked<M>(fR, qR, dir);
   T a[4], b[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
@@ -188,33 +233,39 @@ __device__ __forceinline__ void PredictMasked(const GasT<T>& eq, C2T<T>& recL, C
 }
 
 // Masked HLL flux of a face with beta > 0 (HllMethod.hpp:295-335).
-template <class T>
-__device__ __forceinline__ void HllMasked(const GasT<T>& eq, T* nf, const C2T<T>& L,
+template <class T, class M>
+__device__ __forceinline__ void HllMasked(const GasT<T, M>& eq, T* nf, const C2T<T>& L,
                                           const C2T<T>& R, int dir) {
   T s0, s1;
   EinfeldtMasked(eq, L, R, dir, s0, s1);
   T fL[4], fR[4];
-  FluxMasked(fL, L, dir);
-  FluxMasked(fR, R, dir);
+  FluxMasked<M>(fL, L, dir);
+  FluxMasked<M>(fR, R, dir);
   const T qL[4] = {L.rho, L.m[0], L.m[1], L.E};
   const T qR[4] = {R.rho, R.m[0], R.m[1], R.E};
   const T sL = PMinT(s0, T(0));
   const T sR = PMaxT(s1, T(0));
   const T sLsR = sL * sR;
   const T ds = sR - sL;
+  if constexpr (M::kFast) {
+    const T ids = M::Rcp(ds);
 #pragma unroll
-  for (int k = 0; k < 4; ++k) nf[k] = (sR * fL[k] - sL * fR[k] + sLsR * (qR[k] - qL[k])) / ds;
+    for (int k = 0; k < 4; ++k) nf[k] = (sR * fL[k] - sL * fR[k] + sLsR * (qR[k] - qL[k])) * ids;
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) nf[k] = (sR * fL[k] - sL * fR[k] + sLsR * (qR[k] - qL[k])) / ds;
+  }
 }
 
 // HllBase::SolveRiemannProblem (scalar, HllMethod.hpp:161-184), direction x.
-template <class T>
-__device__ __forceinline__ void HllRiemannState(const GasT<T>& eq, C2T<T>& sol,
+template <class T, class M>
+__device__ __forceinline__ void HllRiemannState(const GasT<T, M>& eq, C2T<T>& sol,
                                                 const C2T<T>& L, const C2T<T>& R) {
   T sL, sR;
   EinfeldtT(eq, L, R, 0, sL, sR);
   T fL[4], fR[4];
-  FluxT(fL, L, 0);
-  FluxT(fR, R, 0);
+  FluxT<M>(fL, L, 0);
+  FluxT<M>(fR, R, 0);
   const T qL[4] = {L.rho, L.m[0], L.m[1], L.E};
   const T qR[4] = {R.rho, R.m[0], R.m[1], R.E};
   const T ds = sL != sR ? sR - sL : T(1);
@@ -225,7 +276,7 @@ __device__ __forceinline__ void HllRiemannState(const GasT<T>& eq, C2T<T>& sol,
   } else {
     T u[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) u[k] = (sR * qR[k] - sL * qL[k] + fL[k] - fR[k]) / ds;
+    for (int k = 0; k < 4; ++k) u[k] = M::Div(sR * qR[k] - sL * qL[k] + fL[k] - fR[k], ds);
     CompleteT(eq, sol, u);
   }
 }
@@ -247,8 +298,8 @@ __device__ __forceinline__ void RotateMomentum(C2T<T>& q, T a0, T a1, T b0, T b1
 
 // Wall state: HLL solution of (reflected | state) in the frame of the
 // boundary normal, rotated back (KbnStabilisation.hpp:188-210, 229-238).
-template <class T>
-__device__ __forceinline__ C2T<T> WallSolution(const GasT<T>& eq, const C2T<T>& state, T n0,
+template <class T, class M>
+__device__ __forceinline__ C2T<T> WallSolution(const GasT<T, M>& eq, const C2T<T>& state, T n0,
                                                T n1) {
   C2T<T> rot = state;
   RotateMomentum(rot, n0, n1, T(1), T(0));
@@ -283,14 +334,14 @@ template <class T> __device__ __forceinline__ void Narrow(T* t, const double* u)
 }
 
 // KbnCutCellMethod::PreAdvanceHierarchy for the cut cells of [-1, n+1)^2.
-template <class T> __global__ void ReferenceStatesKernel(CcStateArgs a) {
+template <class T, class M> __global__ void ReferenceStatesKernel(CcStateArgs a) {
   const int w = a.g.nx + 2, h = a.g.ny + 2;
   const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (id >= int64_t(w) * h) return;
   const int i = static_cast<int>(id % w) - 1, j = static_cast<int>(id / w) - 1;
   const int64_t c = a.g.CellIndex(i, j);
   if (!a.g.cut[c]) return;
-  const GasT<T> eq = MakeGasT<T>(a.gamma);
+  const GasT<T, M> eq = MakeGasT<T, M>(a.gamma);
   double ud[4];
   LoadCons(a, i, j, ud);
   T u[4];
@@ -321,7 +372,7 @@ struct FaceData {
   double beta, us, sL, sR;
 };
 
-template <class T, int kMinBlocks>
+template <class T, class M, int kMinBlocks>
 __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a) {
   const CcGeom& g = a.s.g;
   const int dir = a.dir;
@@ -344,7 +395,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
   int status = 0;
   if (t64 < nt) {
     const int t = static_cast<int>(t64);
-    const GasT<T> eq = MakeGasT<T>(a.s.gamma);
+    const GasT<T, M> eq = MakeGasT<T, M>(a.s.gamma);
     const double dx = a.dx;
     const T lambda_half = NarrowTo<T>(0.5 * split_dt / dx);
     const double dt_dx = split_dt / dx;
@@ -393,7 +444,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
       C2T<T> q;
       CompleteMasked(eq, q, u, g.alpha[ci] > 0.0);
       T f[4];
-      FluxT(f, ref, dir);
+      FluxT<M>(f, ref, dir);
       const C2T<T> sol =
           WallSolution(eq, q, NarrowTo<T>(g.normal[ci]), NarrowTo<T>(g.normal[plane + ci]));
       f[1 + dir] += sol.p - ref.p;
@@ -526,7 +577,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
 
 // Masked stable dt over both directions: faces 0..n with beta > 0
 // (KbnStabilisation.hpp:275-345).
-template <class T>
+template <class T, class M>
 __global__ void KbnStableDtKernel(CcStateArgs a, unsigned long long* smax_out, Control* ctrl) {
   if (!BlockAll(!(ctrl && (ctrl->abort || ctrl->done)))) return;
   const CcGeom& g = a.g;
@@ -536,7 +587,7 @@ __global__ void KbnStableDtKernel(CcStateArgs a, unsigned long long* smax_out, C
   for (int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; id < int64_t(w) * h;
        id += int64_t(gridDim.x) * blockDim.x) {
     const int i = static_cast<int>(id % w), j = static_cast<int>(id / w);
-    const GasT<T> eq = MakeGasT<T>(a.gamma);
+    const GasT<T, M> eq = MakeGasT<T, M>(a.gamma);
     for (int d = 0; d < 2; ++d) {
       const int f = d == 0 ? i : j;
       const int t = d == 0 ? j : i;
@@ -564,14 +615,14 @@ __global__ void KbnStableDtKernel(CcStateArgs a, unsigned long long* smax_out, C
   BlockMaxAtomic<2>(smax_out, smd);
 }
 
-template <class T> cudaError_t LaunchKbnStates(const CcStateArgs& a, cudaStream_t s) {
+template <class T, class M> cudaError_t LaunchKbnStates(const CcStateArgs& a, cudaStream_t s) {
   const int64_t n = int64_t(a.g.nx + 2) * (a.g.ny + 2);
   const int block = 128;
-  ReferenceStatesKernel<T><<<unsigned((n + block - 1) / block), block, 0, s>>>(a);
+  ReferenceStatesKernel<T, M><<<unsigned((n + block - 1) / block), block, 0, s>>>(a);
   return cudaGetLastError();
 }
 
-template <class T> cudaError_t LaunchKbnSweep(const CcSweepArgs& a, cudaStream_t s) {
+template <class T, class M> cudaError_t LaunchKbnSweep(const CcSweepArgs& a, cudaStream_t s) {
   const int nd = a.dir == 0 ? a.s.g.nx : a.s.g.ny;
   const int nt = a.dir == 0 ? a.s.g.ny : a.s.g.nx;
   const int block = 128;
@@ -583,18 +634,18 @@ template <class T> cudaError_t LaunchKbnSweep(const CcSweepArgs& a, cudaStream_t
   // resident blocks per SM (spilling a little)
   constexpr int kMore = sizeof(T) == 4 ? 4 : 3;
   if (a.occupancy == kMore)
-    KbnSweepKernel<T, kMore><<<grid, block, 0, s>>>(b);
+    KbnSweepKernel<T, M, kMore><<<grid, block, 0, s>>>(b);
   else
-    KbnSweepKernel<T, 1><<<grid, block, 0, s>>>(b);
+    KbnSweepKernel<T, M, 1><<<grid, block, 0, s>>>(b);
   return cudaGetLastError();
 }
 
-template <class T>
+template <class T, class M>
 cudaError_t LaunchKbnStableDt(const CcStateArgs& a, unsigned long long* smax_out, Control* ctrl,
                               cudaStream_t s) {
   const int64_t n = int64_t(a.g.nx + 1) * (a.g.ny + 1);
   const int block = 128;
-  KbnStableDtKernel<T><<<GridStrideBlocks(n, block, 16), block, 0, s>>>(a, smax_out, ctrl);
+  KbnStableDtKernel<T, M><<<GridStrideBlocks(n, block, 16), block, 0, s>>>(a, smax_out, ctrl);
   return cudaGetLastError();
 }
 

@@ -165,16 +165,16 @@ cudaError_t LaunchCutCellGeometry(const CcGeomArgs& a, const CcGeom& g, cudaStre
 }
 
 cudaError_t LaunchCutCellReferenceStates(const CcStateArgs& a, cudaStream_t s) {
-  return cc::LaunchKbnStates<double>(a, s);
+  return cc::LaunchKbnStates<double, cc::CcIeee>(a, s);
 }
 
 cudaError_t LaunchCutCellSweep(const CcSweepArgs& a, cudaStream_t s) {
-  return cc::LaunchKbnSweep<double>(a, s);
+  return cc::LaunchKbnSweep<double, cc::CcIeee>(a, s);
 }
 
 cudaError_t LaunchCutCellStableDt(const CcStateArgs& a, unsigned long long* smax_out,
                                   Control* ctrl, cudaStream_t s) {
-  return cc::LaunchKbnStableDt<double>(a, smax_out, ctrl, s);
+  return cc::LaunchKbnStableDt<double, cc::CcIeee>(a, smax_out, ctrl, s);
 }
 
 namespace cc {

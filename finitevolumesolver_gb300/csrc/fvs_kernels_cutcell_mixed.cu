@@ -1,4 +1,5 @@
-// fvs_kernels_cutcell_mixed.cu -- the fast FP64 (FMA contraction) and the
+// fvs_kernels_cutcell_mixed.cu -- the fast FP64 (FMA contraction, refined
+// reciprocals and square roots: math policy CcFast) and the
 // mixed-precision (FP32 reconstruction, fluxes, wall states and CFL speeds;
 // FP64 state, fractions, h-box combination and update) instantiations of the
 // KBN cut-cell kernels (fvs_cutcell_kbn.cuh).
@@ -8,17 +9,19 @@
 namespace fvs {
 
 cudaError_t LaunchCutCellReferenceStatesT(int precision, const CcStateArgs& a, cudaStream_t s) {
-  return precision == 2 ? cc::LaunchKbnStates<float>(a, s) : cc::LaunchKbnStates<double>(a, s);
+  return precision == 2 ? cc::LaunchKbnStates<float, cc::CcIeee>(a, s)
+                        : cc::LaunchKbnStates<double, cc::CcFast>(a, s);
 }
 
 cudaError_t LaunchCutCellSweepT(int precision, const CcSweepArgs& a, cudaStream_t s) {
-  return precision == 2 ? cc::LaunchKbnSweep<float>(a, s) : cc::LaunchKbnSweep<double>(a, s);
+  return precision == 2 ? cc::LaunchKbnSweep<float, cc::CcIeee>(a, s)
+                        : cc::LaunchKbnSweep<double, cc::CcFast>(a, s);
 }
 
 cudaError_t LaunchCutCellStableDtT(int precision, const CcStateArgs& a,
                                    unsigned long long* smax_out, Control* ctrl, cudaStream_t s) {
-  return precision == 2 ? cc::LaunchKbnStableDt<float>(a, smax_out, ctrl, s)
-                        : cc::LaunchKbnStableDt<double>(a, smax_out, ctrl, s);
+  return precision == 2 ? cc::LaunchKbnStableDt<float, cc::CcIeee>(a, smax_out, ctrl, s)
+                        : cc::LaunchKbnStableDt<double, cc::CcFast>(a, smax_out, ctrl, s);
 }
 
 }  // namespace fvs

@@ -75,3 +75,33 @@ def test_method_defaults_match_reference(capi):
     assert m.max_iterations == 5000 and m.tolerance == 1e-7 and m.gamma == 1.4
     assert f.FluxMethod(f.PerfectGas(2)).GetStencilWidth() == 2
     assert f.FluxMethod(f.PerfectGas(2), "hlle").GetStencilWidth() == 1
+
+
+def test_no_template_shared_between_fma_and_no_fma_units(capi):
+    """A template instantiated with the same arguments in a -fmad=false unit
+    and in an FMA unit is one weak symbol: the linker keeps one copy, so one
+    flavour would silently run the other's kernels.  Every such template
+    carries a flavour argument; no weak symbol of the library's namespace is
+    defined by units compiled with different -fmad flags."""
+    import shutil
+    import subprocess
+
+    from finitevolumesolver_gb300 import build
+
+    nm = shutil.which("nm")
+    if nm is None:
+        pytest.skip("nm not available")
+    owners = {}
+    for src, flags in build.UNITS:
+        obj = build.BUILD_DIR / (src.rsplit(".", 1)[0] + ".o")
+        if not obj.exists():
+            pytest.skip(f"{obj.name} not built")
+        out = subprocess.run([nm, "-C", "--defined-only", str(obj)], capture_output=True,
+                             text=True, check=True).stdout
+        nofma = "-fmad=false" in flags
+        for line in out.splitlines():
+            parts = line.split(" ", 2)
+            if len(parts) == 3 and parts[1] in ("W", "V") and "fvs::" in parts[2]:
+                owners.setdefault(parts[2], set()).add(nofma)
+    clashes = sorted(sym for sym, kinds in owners.items() if len(kinds) > 1)
+    assert not clashes, clashes[:5]
