@@ -299,6 +299,7 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
     c.prev_check = prev_check;
     c.prev_dx = prev_dx;
     c.occupancy = s->occ_tuned[dir];
+    c.skip_cfl = skip_cfl ? 1 : 0;
     return s->m.precision == FVS_FP64_EXACT
                ? fvs::LaunchCutCellSweep(c, s->stream)
                : fvs::LaunchCutCellSweepT(s->m.precision, c, s->stream);
@@ -404,10 +405,11 @@ fvs::StepPlan MakePlan(const fvs_solver* s, int64_t cycle) {
   }
   for (int i = 0; i < p.nsweeps; ++i) p.dx[i] = s->g.dx[p.dir[i]];
   p.rank = D;
-  // HLL and HLLEM sweeps measure the same face speeds as the stable-dt pass
-  // when that pass takes every face (dt rule 0); cut cells, the exact Riemann
-  // solver's sweeps and the mixed flavour keep their own
-  p.skip0 = (!s->cc && s->g.dt_rule == 0 && !IsGodunov(s->m.flux_method) &&
+  // HLL and HLLEM sweeps (and the KBN cut-cell sweeps, faces of beta > 0)
+  // measure the same face speeds as the stable-dt pass when that pass takes
+  // every face (dt rule 0); the exact Riemann solver's sweeps and the mixed
+  // flavour keep their own
+  p.skip0 = (s->g.dt_rule == 0 && !IsGodunov(s->m.flux_method) &&
              s->m.precision != FVS_MIXED)
                 ? 1
                 : 0;

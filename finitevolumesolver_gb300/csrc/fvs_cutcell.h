@@ -76,6 +76,7 @@ struct CcSweepArgs {
   double prev_dx;
   int occupancy;  // 0, or resident 128-thread blocks per SM the kernel is compiled for
                   // (FP64: 3, FP32 reconstruction: 4)
+  int skip_cfl;   // FP64 flavours: no CFL speeds (a step's first sweep)
 };
 
 cudaError_t LaunchCutCellGeometry(const CcGeomArgs& a, const CcGeom& g, cudaStream_t s);

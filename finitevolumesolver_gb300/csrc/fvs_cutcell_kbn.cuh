@@ -393,6 +393,14 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
   if (!BlockAll(run)) return;
   T smax = T(0);
   int status = 0;
+  // CFL speeds: none in a step's first sweep (skip_cfl: the stable-dt pass
+  // measured the same faces of the same state); in FP64 flavours screened in
+  // FP32 as the uniform sweeps do (fvs_sweep.cuh, FilteredCfl), with the
+  // masked states and faces of beta > 0
+  constexpr bool kScreen = sizeof(T) == 8;
+  const bool skip_cfl = kScreen && a.skip_cfl != 0;
+  const bool screen = kScreen && a.s.gamma > 1.0 && a.s.gamma <= 2.0;
+  const unsigned amask = __ballot_sync(0xffffffffu, t64 < nt);
   if (t64 < nt) {
     const int t = static_cast<int>(t64);
     const GasT<T, M> eq = MakeGasT<T, M>(a.s.gamma);
@@ -465,6 +473,15 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
     double xb_prev = 0.0;
     C2T<T> q_prev;
     FaceData F_prev;
+    fast::Gas<float> g32;
+    g32.gamma = static_cast<float>(a.s.gamma);
+    g32.gm1 = static_cast<float>(a.s.gamma - 1.0);
+    fast::Wave<float> v_prev{};
+    bool ok_prev = false;
+    bool have_prev = false;  // q_prev holds the complete state of cell j-1
+    float thr = 0.0f;
+    if (kScreen && !skip_cfl && a.smax_out)
+      thr = CflFloatBelow(CflSync(a.smax_out, 0.0, amask));
     for (int j = j0 - 1; j <= j1; ++j) {
       load_cell(j + 1, up, ap);
       const bool smask = am > 0.0 && ac > 0.0 && ap > 0.0;
@@ -474,7 +491,19 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
       boundary_flux(j, uc, fb);
       const double xb = center_of(j);
       C2T<T> q;
-      CompleteMasked(eq, q, uc, true);  // uc is already masked by alpha
+      fast::Wave<float> v{};
+      bool ok = false;
+      if constexpr (kScreen) {
+        if (!skip_cfl) {
+          float c32[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) c32[k] = CflToF32(uc[k]);
+          v = fast::MakeWave<2, float>(g32, c32, dir);
+          ok = screen && CflInRange<2>(c32) && v.a > 0.0f;
+        }
+      } else {
+        CompleteMasked(eq, q, uc, true);  // uc is already masked by alpha
+      }
       if (j >= j0) {
         FaceData F;
         const int64_t fi = g.FaceIndex(dir, j, t);
@@ -485,15 +514,46 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
         const double us_rel = g.us_rel[dir][fi];
         const double sL_rel = g.sL_rel[dir][fi];
         const double sR_rel = g.sR_rel[dir][fi];
+        if constexpr (kScreen) {
+          if (!skip_cfl) {
+            bool need = false;
+            if (F.beta > 0.0) {
+              const float s32 = fast::FaceMaxSpeed<float>(g32, v_prev, v);
+              const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
+              need = !(ok && ok_prev && fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs)) < thr);
+            }
+            if (__any_sync(amask, need)) {
+              // the whole warp evaluates (the same instructions as some lanes)
+              if (!have_prev) CompleteMasked(eq, q_prev, um, true);
+              CompleteMasked(eq, q, uc, true);
+              if (F.beta > 0.0) {
+                T s0, s1;
+                EinfeldtMasked(eq, q_prev, q, dir, s0, s1);
+                const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
+                smax = mx > smax ? mx : smax;
+              }
+              thr = fmaxf(thr, CflFloatBelow(static_cast<double>(smax)));
+              q_prev = q;
+              have_prev = true;
+            } else {
+              have_prev = false;
+            }
+            if (a.smax_out && ((j - j0) % kCflSyncRows) == kCflSyncRows - 1)
+              thr = fmaxf(thr, CflFloatBelow(CflSync(a.smax_out, static_cast<double>(smax),
+                                                     amask)));
+          }
+        }
         if (F.beta > 0.0) {
           T f[4];
           HllMasked(eq, f, recR_prev, recL, dir);
 #pragma unroll
           for (int k = 0; k < 4; ++k) F.f[k] = Widen(f[k]);
-          T s0, s1;
-          EinfeldtMasked(eq, q_prev, q, dir, s0, s1);
-          const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
-          smax = mx > smax ? mx : smax;
+          if constexpr (!kScreen) {
+            T s0, s1;
+            EinfeldtMasked(eq, q_prev, q, dir, s0, s1);
+            const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
+            smax = mx > smax ? mx : smax;
+          }
         } else {
 #pragma unroll
           for (int k = 0; k < 4; ++k) F.f[k] = 0.0;
@@ -560,7 +620,9 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
 #pragma unroll
       for (int k = 0; k < 4; ++k) fb_prev[k] = fb[k];
       xb_prev = xb;
-      q_prev = q;
+      if constexpr (!kScreen) q_prev = q;
+      ok_prev = ok;
+      v_prev = v;
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         um[k] = uc[k];
