@@ -67,7 +67,7 @@ def parse():
                     help="profiling aid: run this many Strang steps of the --n workload in "
                          "--precision with the default launch shapes (no autotuner, no "
                          "timing) and exit; the first sweep launches are then the x, y, z "
-                         "sweeps of step 1")
+                         "sweeps of step 1 (with --report cutcell: the cut-cell workload)")
     return ap.parse_args()
 
 
@@ -504,6 +504,20 @@ def run_ours(args):
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     build.build()
+    if args.report == "cutcell" and args.profile_steps > 0:
+        # profiling aid: the cut-cell workload in --precision, default launch shapes
+        n = args.cutcell_n
+        circles, cons = workloads.shock_circles_2d(n, seed=5)
+        solver = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive",
+                            method=fvs.make_method(precision=args.precision))
+        solver.set_embedded_circles(circles)
+        solver.upload(cons)
+        st, _ = solver.run(cfl=0.5, t_end=1e9, max_steps=args.profile_steps)
+        solver.close()
+        if rank == 0:
+            print(json.dumps({"profile_steps": st.steps, "cutcell_n": n,
+                              "precision": args.precision}), flush=True)
+        return
     if args.report:
         peaks = load_peaks()
         if args.report == "sod":
