@@ -184,3 +184,30 @@ def test_amr_screened_speeds_bit_exact(fvs, orc, state):
     assert st.steps == 3 and st.restarts == rs
     np.testing.assert_array_equal(dts, ref_dts)
     np.testing.assert_array_equal(a.download(), ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64_exact", "fp64_fast"])
+@pytest.mark.parametrize("state", ["hypersonic", "hypersonic_mixed", "plateau", "cold"])
+def test_cutcell_screened_speeds(fvs, orc, state, prec):
+    # the KBN sweeps screen their CFL speeds over the faces with beta > 0; the
+    # stable-dt pass evaluates every such face: same number, bit for bit, and
+    # for the exact flavour the oracle's
+    n = 100
+    circles = [[0.35, 0.4, 0.12], [0.5, 0.45, 0.1], [0.7, 0.7, 0.15]]
+    rng = np.random.default_rng(zlib.crc32(f"cc{state}".encode()))
+    cons = STATES[state]((n, n), 2, rng).reshape(4, 1, n, n)
+    s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive",
+                   method=fvs.make_method(precision=prec))
+    s.set_embedded_circles(circles)
+    ref = orc.CutCellGeometry(n, n, circles)
+    for d in (0, 1):
+        s.upload(cons)
+        want = s.ComputeStableDt(d)
+        if prec == "fp64_exact":
+            assert want == ref.stable_dt(cons, d)
+        else:
+            assert want == pytest.approx(ref.stable_dt(cons, d), rel=1e-12)
+        s.upload(cons)
+        level = s.sweep(d, 1e-3 * want)
+        assert level == want, (d, level, want)
+    s.close()
