@@ -52,7 +52,8 @@ def parse():
     ap.add_argument("--no-reports", action="store_true",
                     help="skip the secondary workloads (learned start value, 2-D Godunov, "
                          "2-D cut cells)")
-    ap.add_argument("--report", choices=["sod", "learned", "godunov", "amr", "cutcell"],
+    ap.add_argument("--report", choices=["sod", "learned", "godunov", "amr", "cutcell",
+                                         "hllem"],
                     help="run only this secondary workload and print its JSON report")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000)
     ap.add_argument("--mlp-epochs", type=int, default=24)
@@ -62,6 +63,8 @@ def parse():
     ap.add_argument("--amr-steps", type=int, default=50)
     ap.add_argument("--amr-flavours", default="fp64_exact,fp64_fast,mixed")
     ap.add_argument("--cutcell-n", type=int, default=1024)
+    ap.add_argument("--hllem-n", type=int, default=192)
+    ap.add_argument("--hllem-steps", type=int, default=10)
     ap.add_argument("--cutcell-steps", type=int, default=400)
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling aid: run this many Strang steps of the --n workload in "
@@ -463,6 +466,56 @@ def report_cutcell(args, torch, fvs, workloads, peaks=None):
     return out
 
 
+def report_hllem(args, torch, fvs, workloads, peaks=None):
+    """HLLEM (Larrouturou) without reconstruction and with MUSCL-Hancock of the
+    conservative variables, and the perfect gas's characteristic and primitive
+    MUSCL-Hancock reconstructions with HLLEM (van Leer), exact FP64 (the only
+    flavour of this family), on the 3-D octants workload at --hllem-n; the
+    oracle's restatement timed on one Strang step of the same grid."""
+    n = args.hllem_n
+    cons = workloads.octants_3d(n)
+    out = {"workload": f"3D perfect gas {n}^3 periodic, Strang, CFL 0.8, seeded octants + "
+                       "Gaussian bumps, exact FP64", "methods": {}}
+    from oracle import build as obuild
+    obuild.build()
+    from oracle import oracle as orc
+    threads = orc.max_threads()
+    kinds = {"hllem": orc.HLLEM, "muscl_hllem": orc.MUSCL_HLLEM, "muscl_char": orc.MUSCL_CHAR,
+             "muscl_prim": orc.MUSCL_PRIM}
+    for name, kind in kinds.items():
+        s = fvs.Solver([n] * 3, [1.0 / n] * 3, "periodic",
+                       method=fvs.make_method(flux_method=name, precision="fp64_exact"))
+        stream = torch.cuda.ExternalStream(s.stream_handle())
+        s.upload(cons)
+        s.autotune()
+        s.run(cfl=0.8, t_end=1e9, max_steps=3)
+        s.upload(cons)
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        st, dts = s.run(cfl=0.8, t_end=1e9, max_steps=args.hllem_steps, log_len=1)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        rate = 6 * n ** 3 * st.steps / (ms / 1e3)
+        rec = {"steps": st.steps, "restarts": st.restarts, "ms_per_step": ms / max(st.steps, 1),
+               "cell_updates_per_s": rate}
+        if peaks:
+            rec["hbm_frac_algorithmic"] = rate * 80 / 1e9 / peaks["hbm_gbs"]
+        # CPU: the oracle's restatement, one Strang step with the GPU's first dt
+        g = orc.Grid(3, [n] * 3, [0, 0, 0], [1.0 / n] * 3)
+        t0 = time.perf_counter()
+        g.step(orc.method(kind=kind), cons, float(dts[0]), 0, nthreads=threads)
+        cpu_s = time.perf_counter() - t0
+        rec["cpu_baseline"] = {"value": 6 * n ** 3 / cpu_s, "unit": "cell-updates/s",
+                               "cores": threads, "kind": "port",
+                               "sample": "1 Strang step of the same grid"}
+        out["methods"][name] = rec
+        s.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -529,6 +582,8 @@ def run_ours(args):
             rep = report_godunov(args, torch, fvs, workloads, net, peaks)
         elif args.report == "amr":
             rep = report_amr(args, torch, fvs, workloads, peaks)
+        elif args.report == "hllem":
+            rep = report_hllem(args, torch, fvs, workloads, peaks)
         else:
             rep = report_cutcell(args, torch, fvs, workloads, peaks)
         if rank == 0:
@@ -669,7 +724,8 @@ def run_ours(args):
                                                               peaks)),
                         ("amr_2d", lambda: report_amr(args, torch, fvs, workloads, peaks)),
                         ("cutcell_2d", lambda: report_cutcell(args, torch, fvs, workloads,
-                                                              peaks))):
+                                                              peaks)),
+                        ("hllem_3d", lambda: report_hllem(args, torch, fvs, workloads, peaks))):
             try:
                 reports[key] = fn()
             except Exception as e:

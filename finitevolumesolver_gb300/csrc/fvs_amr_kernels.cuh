@@ -13,7 +13,7 @@
 // they live (Seg::halo): the same level's current buffer or the coarser
 // level, which is the ghost fill of those strips at sweep time.
 //
-// For FilteredCfl policies (exact and fast FP64) both kernels screen the CFL
+// For EinfeldtCfl policies (exact and fast FP64) both kernels screen the CFL
 // speeds in FP32 as the uniform sweeps do (fvs_sweep.cuh): a face's exact
 // speed is evaluated only when its FP32 speed plus error bound reaches the
 // thread's threshold.  The rows of a warp can differ in length, so the
@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
   R smax = R(0);
   int status = 0;
   typename P::Stats stats;
-  constexpr bool kFilter = FilteredCfl<P>::value && HasFluxOnly<P>::value;
+  constexpr bool kFilter = EinfeldtCfl<P>::value && HasFluxOnly<P>::value;
   const bool screen = kFilter && a.gamma > 1.0 && a.gamma <= 2.0;
   fast::Gas<float> g32;
   g32.gamma = static_cast<float>(a.gamma);
@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
   constexpr int K = kComp;
   const typename P::Gas eq = P::MakeGas(a.gamma);
   const int64_t N = a.ncells;
-  constexpr bool kFilter = FilteredCfl<P>::value;
+  constexpr bool kFilter = EinfeldtCfl<P>::value;
   const bool screen = kFilter && a.gamma > 1.0 && a.gamma <= 2.0;
   fast::Gas<float> g32;
   g32.gamma = static_cast<float>(a.gamma);

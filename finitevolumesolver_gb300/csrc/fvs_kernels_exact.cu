@@ -40,6 +40,7 @@ template <int D, int kRecon> struct HllemPolicyT {
   using Real = double;
   static constexpr bool kWarpX = false;
   static constexpr int kMinBlocks = 1;
+  static constexpr bool kHllemCfl = true;  // CFL speeds screened in FP32 (HllemScreen)
   using Gas = exact::Gas;
   using Rec = exact::Complete<D>;
   using Wave = HllemWave<D>;

@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(32 * kDtRows) StableDtMarch3Kernel(StableDtArg
   BlockMaxAtomic<3>(a.smax_out, smax);
 }
 
-// StableDtMarch3Kernel with the CFL speeds screened in FP32 (FilteredCfl
+// StableDtMarch3Kernel with the CFL speeds screened in FP32 (EinfeldtCfl
 // policies, 1 < gamma <= 2): the same blocks, marching and faces; the FP32
 // waves pass between lanes (x), warps (y, shared memory) and planes (z), and
 // a direction's exact speeds are evaluated only by warps holding a face of
@@ -362,7 +362,7 @@ cudaError_t LaunchStableDtT(const StableDtArgs& a, cudaStream_t s) {
         std::max<int64_t>(1, std::min<int64_t>(a.n[2], (want + tiles - 1) / tiles));
     const int seg = static_cast<int>((a.n[2] + zseg - 1) / zseg);
     const unsigned grid = static_cast<unsigned>(tiles * ((a.n[2] + seg - 1) / seg));
-    if constexpr (FilteredCfl<PT<3>>::value) {
+    if constexpr (EinfeldtCfl<PT<3>>::value) {
       if (a.gamma > 1.0 && a.gamma <= 2.0 && a.smax_out) {
         StableDtScreen3Kernel<PT><<<grid, 32 * kDtRows, 0, s>>>(a, seg);
         return cudaGetLastError();

@@ -187,9 +187,71 @@ __device__ __forceinline__ void SweepFluxOnly(const typename P::Gas& eq, F* flux
 // rows and read it back, so later blocks start with the maximum of earlier
 // ones.  The slot must start at zero (or at an evaluated speed of the same
 // sweep).
-template <class P, class = void> struct FilteredCfl : std::false_type {};
+template <class P, class = void> struct EinfeldtCfl : std::false_type {};
 template <class P>
-struct FilteredCfl<P, std::enable_if_t<P::kEinfeldtCfl>> : std::true_type {};
+struct EinfeldtCfl<P, std::enable_if_t<P::kEinfeldtCfl>> : std::true_type {};
+template <class P, class = void> struct HllemCfl : std::false_type {};
+template <class P> struct HllemCfl<P, std::enable_if_t<P::kHllemCfl>> : std::true_type {};
+template <class P>
+struct FilteredCfl : std::integral_constant<bool, EinfeldtCfl<P>::value || HllemCfl<P>::value> {};
+
+// The FP32 estimates: Einfeldt speeds (fast::MakeWave / fast::FaceMaxSpeed)
+// and the HLLEM stable-dt speed (Hllem<PerfectGas>: the Roe average over the
+// full velocity, max(c_L, c_R) for both outer waves, no zero in the max).
+// The HLLEM speed's errors have the same sources and form (roundings, and the
+// cancellations in p and in roeH - |roeU|^2 / 2 <= roeH), so the same bound
+// covers it.  V carries h and a for the bound and the range check.
+template <int D> struct EinfeldtScreen {
+  using V = fast::Wave<float>;
+  static __device__ __forceinline__ V Wave(const fast::Gas<float>& g, const float* c, int dir) {
+    return fast::MakeWave<D, float>(g, c, dir);
+  }
+  static __device__ __forceinline__ float Speed(const fast::Gas<float>& g, const V& l,
+                                                const V& r, int) {
+    return fast::FaceMaxSpeed<float>(g, l, r);
+  }
+};
+template <int D> struct HllemScreen {
+  struct V {
+    float sq, h, a;
+    float u[D];
+  };
+  static __device__ __forceinline__ V Wave(const fast::Gas<float>& g, const float* c, int) {
+    using M = fast::Math<float>;
+    V v;
+    const float rs = M::Rsqrt(c[0]);
+    const float ir = rs * rs;
+    v.sq = c[0] * rs;
+#pragma unroll
+    for (int i = 0; i < D; ++i) v.u[i] = c[1 + i] * ir;
+    const float ke = 0.5f * fast::SquaredNorm<D, float>(c + 1) * ir;
+    const float p = (c[1 + D] - ke) * g.gm1;
+    v.h = (c[1 + D] + p) * ir;
+    v.a = M::Sqrt(g.gamma * p * ir);
+    return v;
+  }
+  static __device__ __forceinline__ float Speed(const fast::Gas<float>& g, const V& l,
+                                                const V& r, int dir) {
+    using M = fast::Math<float>;
+    const float oo = M::Rcp(l.sq + r.sq);
+    const float wL = l.sq * oo, wR = r.sq * oo;
+    float roeU[D];
+    float sqN = 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      roeU[i] = fmaf(wL, l.u[i], wR * r.u[i]);
+      sqN = fmaf(roeU[i], roeU[i], sqN);
+    }
+    const float roeH = fmaf(wL, l.h, wR * r.h);
+    const float roeA = M::Sqrt(g.gm1 * fmaf(-0.5f, sqN, roeH));
+    const float maxA = fmaxf(l.a, r.a);
+    const float sL = fminf(l.u[dir] - maxA, roeU[dir] - roeA);
+    const float sR = fmaxf(roeU[dir] + roeA, r.u[dir] + maxA);
+    return fmaxf(fabsf(sL), fabsf(sR));
+  }
+};
+template <class P, int D>
+using CflScreen = std::conditional_t<HllemCfl<P>::value, HllemScreen<D>, EinfeldtScreen<D>>;
 
 constexpr float kCflRel = 1.0f + 1.0f / 1024.0f;
 constexpr float kCflScale = 1.0f / 64.0f;
@@ -346,7 +408,8 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
     fast::Gas<float> g32;
     g32.gamma = static_cast<float>(a.gamma);
     g32.gm1 = static_cast<float>(a.gamma - 1.0);
-    fast::Wave<float> v_prev{};
+    using S = CflScreen<P, D>;
+    typename S::V v_prev{};
     bool ok_prev = false;
     bool have_prev = false;  // w_prev holds the exact wave of cell j-1
     // skip threshold: a lower bound of an evaluated face's exact speed
@@ -360,10 +423,10 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
           float c32[K];
 #pragma unroll
           for (int c = 0; c < K; ++c) c32[c] = CflToF32(cc[c]);
-          const fast::Wave<float> v = fast::MakeWave<D, float>(g32, c32, DIR);
+          const typename S::V v = S::Wave(g32, c32, DIR);
           const bool ok = screen && CflInRange<D>(c32) && v.a > 0.0f;
           if (j >= j0) {
-            const float s32 = fast::FaceMaxSpeed<float>(g32, v_prev, v);
+            const float s32 = S::Speed(g32, v_prev, v, DIR);
             const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
             const float bound = fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs));
             const bool need = !(ok && ok_prev && bound < thr);

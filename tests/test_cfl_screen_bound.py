@@ -1,5 +1,6 @@
 """The error bound behind the FP32 screen of the CFL speeds (fvs_sweep.cuh,
-FilteredCfl), checked on the CPU.
+FilteredCfl: the Einfeldt speed and the HLLEM stable-dt speed), checked on
+the CPU.
 
 The sweeps skip a face's FP64 Einfeldt speed s when its FP32 estimate s32
 satisfies s32 / 1024 + sqrt(max(h_L, h_R)) / 64 + 2^-24 + s32 < threshold,
@@ -69,6 +70,61 @@ def speed32(L, R, g, rng):
     return np.maximum(np.maximum(F32(0), np.abs(sL)), np.abs(sR))
 
 
+def speed32_hllem(cL, cR, d, g, rng):
+    """HllemScreen::Speed (fvs_sweep.cuh) in emulated FP32, from the cells."""
+    def wave(c):
+        rho, m, E = c[0], c[1:-1], c[-1]
+        rs = approx(1.0 / np.sqrt(rho.astype(np.float64)), rng)
+        ir = r32(rs * rs)
+        sq = r32(rho * rs)
+        u = [r32(m[k] * ir) for k in range(m.shape[0])]
+        sn = r32(m[0] * m[0])
+        for k in range(1, m.shape[0]):
+            sn = fma32(m[k], m[k], sn)
+        ke = r32(r32(F32(0.5) * sn) * ir)
+        p = r32(r32(E - ke) * F32(g - 1.0))
+        h = r32(r32(E + p) * ir)
+        x = r32(r32(F32(g) * p) * ir)
+        xs = np.where(x > 0, x, F32(1))
+        a = np.where(x > 0, r32(x * approx(1.0 / np.sqrt(xs.astype(np.float64)), rng)), F32(0))
+        return sq, u, h, a
+    sqL, uL, hL, aL = wave(cL)
+    sqR, uR, hR, aR = wave(cR)
+    oo = approx(1.0 / (r32(sqL + sqR)).astype(np.float64), rng)
+    wL, wR = r32(sqL * oo), r32(sqR * oo)
+    roeU = [fma32(wL, uL[k], r32(wR * uR[k])) for k in range(len(uL))]
+    sqN = np.zeros_like(wL)
+    for k in range(len(roeU)):
+        sqN = fma32(roeU[k], roeU[k], sqN)
+    roeH = fma32(wL, hL, r32(wR * hR))
+    x = r32(F32(g - 1.0) * fma32(np.full_like(sqN, F32(-0.5)), sqN, roeH))
+    xs = np.where(x > 0, x, F32(1))
+    roeA = np.where(x > 0, r32(x * approx(1.0 / np.sqrt(xs.astype(np.float64)), rng)), F32(0))
+    maxA = np.maximum(aL, aR)
+    sL = np.minimum(r32(uL[d] - maxA), r32(roeU[d] - roeA))
+    sR = np.maximum(r32(roeU[d] + roeA), r32(uR[d] + maxA))
+    return np.maximum(np.abs(sL), np.abs(sR)), (aL > 0) & (aR > 0), np.maximum(hL, hR)
+
+
+def speed64_hllem(uL, uR, d, g):
+    """HllemMaxSpeed of the exact flavour (fvs_hllem.cuh)."""
+    def comp(u):
+        rho, m, E = u[0], u[1:-1], u[-1]
+        p = (E - 0.5 * (m * m).sum(axis=0) / rho) / (1.0 / (g - 1.0))
+        return rho, m / rho, (E + p) / rho, np.sqrt(g * p / rho)
+    rL, vL, hL, aL = comp(uL)
+    rR, vR, hR, aR = comp(uR)
+    sqL, sqR = np.sqrt(rL), np.sqrt(rR)
+    wL, wR = sqL / (sqL + sqR), sqR / (sqL + sqR)
+    roeU = wL * vL + wR * vR
+    roeH = wL * hL + wR * hR
+    roeA = np.sqrt((g - 1.0) * (roeH - 0.5 * (roeU * roeU).sum(axis=0)))
+    maxA = np.maximum(aL, aR)
+    sL = np.minimum(vL[d] - maxA, roeU[d] - roeA)
+    sR = np.maximum(roeU[d] + roeA, vR[d] + maxA)
+    return np.maximum(np.abs(sL), np.abs(sR))
+
+
 def speed64(uL, uR, d, g):
     """The exact flavour's Einfeldt face speed (fvs_physics_exact.cuh)."""
     def comp(u):
@@ -104,10 +160,11 @@ def states(rng, n, dim, g, kind):
     return np.concatenate([rho[None], rho * vel, E[None]])
 
 
+@pytest.mark.parametrize("speed", ["einfeldt", "hllem"])
 @pytest.mark.parametrize("gamma", [1.0 + 1e-3, 1.4, 5.0 / 3.0, 2.0])
 @pytest.mark.parametrize("kind", ["subsonic", "sonic", "hyper", "jump", "vacuum"])
-def test_screen_bound_holds(gamma, kind):
-    rng = np.random.default_rng(zlib.crc32(f"{gamma:.6f}{kind}".encode()))
+def test_screen_bound_holds(gamma, kind, speed):
+    rng = np.random.default_rng(zlib.crc32(f"{gamma:.6f}{kind}{speed}".encode()))
     n, dim = 200_000, 3
     uL = states(rng, n, dim, gamma, kind)
     uR = states(rng, n, dim, gamma, kind)
@@ -120,13 +177,20 @@ def test_screen_bound_holds(gamma, kind):
         for c in (cL, cR):
             ok &= (c[0] >= 2.0 ** -30) & (c[0] <= 2.0 ** 30) & (np.abs(c[-1]) <= 2.0 ** 40)
             ok &= (np.abs(c[1:-1]) <= 2.0 ** 30).all(axis=0)
-        wl = wave32(cL, d, gamma, rng)
-        wr = wave32(cR, d, gamma, rng)
-        ok &= (wl[3] > 0) & (wr[3] > 0)
         with np.errstate(all="ignore"):
-            s32 = speed32(wl, wr, gamma, rng).astype(np.float64)
-            s64 = speed64(uL, uR, d, gamma)
-        sh = np.sqrt(np.maximum(wl[2], wr[2]).astype(np.float64))
+            if speed == "einfeldt":
+                wl = wave32(cL, d, gamma, rng)
+                wr = wave32(cR, d, gamma, rng)
+                ok &= (wl[3] > 0) & (wr[3] > 0)
+                s32 = speed32(wl, wr, gamma, rng).astype(np.float64)
+                s64 = speed64(uL, uR, d, gamma)
+                hmax = np.maximum(wl[2], wr[2])
+            else:
+                s32, pos, hmax = speed32_hllem(cL, cR, d, gamma, rng)
+                ok &= pos
+                s32 = s32.astype(np.float64)
+                s64 = speed64_hllem(uL, uR, d, gamma)
+        sh = np.sqrt(hmax.astype(np.float64))
         bound = s32 / 1024.0 + sh / 64.0 + 2.0 ** -24
         sel = ok & np.isfinite(s64)
         assert sel.sum() > n // 20  # hypersonic states often leave the domain

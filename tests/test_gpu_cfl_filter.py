@@ -95,9 +95,13 @@ STATES = {"plateau": plateau, "hypersonic": hypersonic, "hypersonic_mixed": hype
 GRIDS = [(1, [1000]), (2, [150, 41]), (3, [40, 34, 37])]
 
 
-def check_sweeps(fvs, orc, rank, n, cons, prec, gamma=1.4, seg=0, oracle=True):
+ORACLE_KIND = {"muscl_hlle": 0, "hllem": 4, "muscl_hllem": 5, "muscl_char": 6, "muscl_prim": 7}
+
+
+def check_sweeps(fvs, orc, rank, n, cons, prec, gamma=1.4, seg=0, oracle=True,
+                 method="muscl_hlle"):
     dx = [0.1, 0.07, 0.05][:rank]
-    m = fvs.make_method(precision=prec, gamma=gamma)
+    m = fvs.make_method(flux_method=method, precision=prec, gamma=gamma)
     s = fvs.Solver(n, dx, "periodic", method=m)
     s.set_tiling(seg)
     g = orc.Grid(rank, n, [0] * rank, dx) if oracle else None
@@ -106,7 +110,7 @@ def check_sweeps(fvs, orc, rank, n, cons, prec, gamma=1.4, seg=0, oracle=True):
         ref = s.ComputeStableDt(d)
         assert np.isfinite(ref) and ref > 0
         if g is not None:
-            want = g.stable_dt(orc.method(), cons, d, 0)
+            want = g.stable_dt(orc.method(kind=ORACLE_KIND[method]), cons, d, 0)
             if prec == "fp64_exact":
                 assert ref == want
             else:
@@ -211,3 +215,14 @@ def test_cutcell_screened_speeds(fvs, orc, state, prec):
         level = s.sweep(d, 1e-3 * want)
         assert level == want, (d, level, want)
     s.close()
+
+
+@pytest.mark.parametrize("method", ["hllem", "muscl_hllem", "muscl_char", "muscl_prim"])
+@pytest.mark.parametrize("state", ["hypersonic", "hypersonic_mixed", "plateau", "cold", "scaled"])
+def test_hllem_screened_speeds(fvs, orc, method, state):
+    # the HLLEM sweeps screen their stable-dt speeds (Roe average over the full
+    # velocity, max(c_L, c_R)) with the same bound; exact FP64 only
+    rng = np.random.default_rng(zlib.crc32(f"hllem{state}".encode()))
+    n = [40, 34, 37]
+    cons = STATES[state](tuple(reversed(n)), 3, rng)
+    check_sweeps(fvs, orc, 3, n, cons, "fp64_exact", method=method)
