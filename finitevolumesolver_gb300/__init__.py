@@ -259,6 +259,19 @@ class Solver:
         out["ghost"] = G
         return out
 
+    def cutcell_shielded(self, dir: int):
+        """[us, sL, sR, us_rel, sL_rel, sR_rel] of direction `dir` over the
+        face array of the grown grid (the order of the oracle's
+        CutCellGeometry.shielded)."""
+        import numpy as np
+        G = lib().fvs_cutcell_ghost_layers()
+        NX, NY = self.n[0] + 2 * G, self.n[1] + 2 * G
+        shape = (NY, NX + 1) if dir == 0 else (NY + 1, NX)
+        outs = [np.zeros(shape) for _ in range(6)]
+        _capi.check(lib().fvs_solver_cutcell_shielded(self._h, int(dir),
+                                                       *[o.ctypes.data for o in outs]))
+        return outs
+
     def autotune(self):
         segs = (C.c_int * 3)()
         _capi.check(lib().fvs_solver_autotune(self._h, segs))

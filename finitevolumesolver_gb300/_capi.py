@@ -120,6 +120,7 @@ def load() -> C.CDLL:
     L.fvs_cutcell_ghost_layers.restype = C.c_int
     L.fvs_solver_set_embedded_circles.argtypes = [_VP, _VP, C.c_int, C.c_double, C.c_double]
     L.fvs_solver_cutcell_geometry.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
+    L.fvs_solver_cutcell_shielded.argtypes = [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP, _VP]
     L.fvs_solver_set_cycle.argtypes = [_VP, C.c_int64]
     L.fvs_solver_set_time.argtypes = [_VP, C.c_double]
     L.fvs_amr_create.argtypes = [P(AmrDesc), P(Method), P(_VP)]

@@ -35,16 +35,6 @@ int CudaFail(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return CudaFail(e_, #call);  \
   } while (0)
 
-int CheckDevice() {
-  int n = 0;
-  cudaError_t e = cudaGetDeviceCount(&n);
-  if (e != cudaSuccess || n == 0) {
-    cudaGetLastError();
-    return Fail(FVS_ERR_NO_DEVICE, "no CUDA device available");
-  }
-  return FVS_OK;
-}
-
 fvs::BoxDesc ToDesc(const fvs_box& b) {
   fvs::BoxDesc d;
   for (int i = 0; i < 3; ++i) {
@@ -68,24 +58,6 @@ bool Contains(const fvs_box& outer, const int* lo, const int* hi) {
 
 int64_t Volume(const fvs_box& b) {
   return int64_t(b.hi[0] - b.lo[0]) * (b.hi[1] - b.lo[1]) * (b.hi[2] - b.lo[2]);
-}
-
-int CheckMethod(const fvs_method* m, int rank) {
-  if (!m) return Fail(FVS_ERR_INVALID, "method is NULL");
-  if (rank < 1 || rank > 3) return Fail(FVS_ERR_INVALID, "rank must be 1, 2 or 3");
-  if (m->flux_method < 0 || m->flux_method > 7)
-    return Fail(FVS_ERR_INVALID, "unknown flux method");
-  if (m->limiter < 0 || m->limiter > 2) return Fail(FVS_ERR_INVALID, "unknown limiter");
-  // the characteristic method limits with VanLeer's two-slope functor only,
-  // the primitive one with its own fixed limiter
-  if ((m->flux_method == FVS_MUSCL_CHAR || m->flux_method == FVS_MUSCL_PRIM) &&
-      m->limiter != FVS_VAN_LEER)
-    return Fail(FVS_ERR_UNSUPPORTED, "the characteristic and primitive reconstructions "
-                                     "take no limiter choice (FVS_VAN_LEER)");
-  if (m->precision < 0 || m->precision > 3)
-    return Fail(FVS_ERR_INVALID, "unknown precision");
-  if (!(m->gamma > 1.0)) return Fail(FVS_ERR_INVALID, "gamma must exceed 1");
-  return FVS_OK;
 }
 
 bool IsGodunov(int method) { return method == FVS_GODUNOV || method == FVS_MUSCL_GODUNOV; }
@@ -125,6 +97,34 @@ double BitsToDouble(unsigned long long b) {
 namespace fvs {
 
 void SetLastError(const std::string& msg) { g_last_error = msg; }
+
+int CheckDevice() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return Fail(FVS_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  return FVS_OK;
+}
+
+int CheckMethod(const fvs_method* m, int rank) {
+  if (!m) return Fail(FVS_ERR_INVALID, "method is NULL");
+  if (rank < 1 || rank > 3) return Fail(FVS_ERR_INVALID, "rank must be 1, 2 or 3");
+  if (m->flux_method < 0 || m->flux_method > 7)
+    return Fail(FVS_ERR_INVALID, "unknown flux method");
+  if (m->limiter < 0 || m->limiter > 2) return Fail(FVS_ERR_INVALID, "unknown limiter");
+  // the characteristic method limits with VanLeer's two-slope functor only,
+  // the primitive one with its own fixed limiter
+  if ((m->flux_method == FVS_MUSCL_CHAR || m->flux_method == FVS_MUSCL_PRIM) &&
+      m->limiter != FVS_VAN_LEER)
+    return Fail(FVS_ERR_UNSUPPORTED, "the characteristic and primitive reconstructions "
+                                     "take no limiter choice (FVS_VAN_LEER)");
+  if (m->precision < 0 || m->precision > 3)
+    return Fail(FVS_ERR_INVALID, "unknown precision");
+  if (!(m->gamma > 1.0)) return Fail(FVS_ERR_INVALID, "gamma must exceed 1");
+  return FVS_OK;
+}
 
 __device__ __forceinline__ double BitsToDoubleDev(unsigned long long b) {
   return __longlong_as_double(static_cast<long long>(b));
@@ -202,6 +202,9 @@ __global__ void EndStepKernel(Control* c, StepPlan plan, int step_in_batch,
 }
 
 }  // namespace fvs
+
+using fvs::CheckDevice;
+using fvs::CheckMethod;
 
 // ---------------------------------------------------------------------------
 
@@ -967,6 +970,20 @@ int fvs_solver_cutcell_geometry(fvs_solver* s, double* alpha, double* betax, dou
   if (normal) FVS_CUDA(cudaMemcpy(normal, g.normal, 2 * cells * 8, cudaMemcpyDeviceToHost));
   if (center) FVS_CUDA(cudaMemcpy(center, g.center, 2 * cells * 8, cudaMemcpyDeviceToHost));
   if (cut_flags) FVS_CUDA(cudaMemcpy(cut_flags, g.cut, cells, cudaMemcpyDeviceToHost));
+  return FVS_OK;
+}
+
+int fvs_solver_cutcell_shielded(fvs_solver* s, int dir, double* us, double* sL, double* sR,
+                                double* us_rel, double* sL_rel, double* sR_rel) {
+  if (!s || !s->cc) return Fail(FVS_ERR_INVALID, "no embedded boundary");
+  if (dir < 0 || dir > 1) return Fail(FVS_ERR_INVALID, "direction out of range");
+  const fvs::CcGeom& g = s->ccg;
+  const size_t nf = dir == 0 ? size_t(g.NX() + 1) * g.NY() : size_t(g.NX()) * (g.NY() + 1);
+  double* dst[6] = {us, sL, sR, us_rel, sL_rel, sR_rel};
+  const double* src[6] = {g.us[dir], g.sL[dir], g.sR[dir], g.us_rel[dir], g.sL_rel[dir],
+                          g.sR_rel[dir]};
+  for (int k = 0; k < 6; ++k)
+    if (dst[k]) FVS_CUDA(cudaMemcpy(dst[k], src[k], nf * 8, cudaMemcpyDeviceToHost));
   return FVS_OK;
 }
 

@@ -7,6 +7,8 @@
 
 #include <cuda_runtime.h>
 
+struct fvs_method;  // include/fvs_gpu.h
+
 namespace fvs {
 
 // A box of an FArrayBox-layout array: lower corner and extents.
@@ -97,6 +99,12 @@ struct StableDtArgs {
 
 // Sets the message returned by fvs_last_error() (fvs_capi.cu).
 void SetLastError(const std::string& msg);
+// Argument checks shared by the C ABI's entry points (fvs_capi.cu): the
+// method's fields and rank (FVS_ERR_INVALID / FVS_ERR_UNSUPPORTED), and that
+// a CUDA device is present (FVS_ERR_NO_DEVICE, clearing the runtime's sticky
+// "no device" error).  Return FVS_OK or the status, with fvs_last_error() set.
+int CheckMethod(const ::fvs_method* m, int rank);
+int CheckDevice();
 
 // Exact FP64 kernels (fvs_kernels_exact.cu, compiled with -fmad=false).
 cudaError_t LaunchSweepExact(const SweepArgs& a, cudaStream_t s);

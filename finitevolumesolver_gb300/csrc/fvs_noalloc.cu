@@ -60,8 +60,11 @@ __device__ __forceinline__ fvs::exact::Complete<D> Load(const View& v, int i, in
   return q;
 }
 
+// Block max of non-negative speeds; a NaN speed counts as 0 (skipped), the
+// rule of the allocating entry point's reduction.
 __device__ __forceinline__ double BlockMax(double s) {
   __shared__ double warp_max[kThreads / 32];
+  s = s > 0.0 ? s : 0.0;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const double w = __shfl_xor_sync(0xffffffffu, s, o);
@@ -150,21 +153,23 @@ extern "C" int fvs_compute_stable_dt_noalloc(const fvs_method* m, int rank,
                                              const double* states_dev, fvs_box cell_box,
                                              double dx, int dir, int window_rule,
                                              double* dt_out, void* stream) {
-  if (!m) return Fail(FVS_ERR_INVALID, "method is NULL");
-  if (rank < 1 || rank > 3) return Fail(FVS_ERR_INVALID, "rank must be 1, 2 or 3");
-  if (!(m->gamma > 1.0)) return Fail(FVS_ERR_INVALID, "gamma must exceed 1");
-  if (m->flux_method != FVS_MUSCL_HLLE && m->flux_method != FVS_HLLE)
-    return Fail(FVS_ERR_UNSUPPORTED, "the allocation-free stable dt covers the HLLE methods");
+  // the allocating entry point's checks, in its order, so that both return
+  // the same status for the same arguments
+  if (int r = fvs::CheckMethod(m, rank)) return r;
   if (dir < 0 || dir >= rank) return Fail(FVS_ERR_INVALID, "direction out of range");
-  if (window_rule != 0 && window_rule != 1)
-    return Fail(FVS_ERR_INVALID, "window_rule must be 0 or 1");
-  if (!dt_out) return Fail(FVS_ERR_INVALID, "dt_out is NULL");
   fvs::BoxDesc cb;
   for (int d = 0; d < 3; ++d) {
     if (cell_box.hi[d] < cell_box.lo[d]) return Fail(FVS_ERR_INVALID, "invalid box");
     cb.lo[d] = cell_box.lo[d];
     cb.n[d] = cell_box.hi[d] - cell_box.lo[d];
   }
+  if (!dt_out) return Fail(FVS_ERR_INVALID, "dt_out is NULL");
+  if (window_rule != 0 && window_rule != 1)
+    return Fail(FVS_ERR_INVALID, "window_rule must be 0 or 1");
+  if (int r = fvs::CheckDevice()) return r;
+  if (m->flux_method != FVS_MUSCL_HLLE && m->flux_method != FVS_HLLE)
+    return Fail(FVS_ERR_UNSUPPORTED, "the allocation-free stable dt covers the HLLE methods "
+                                     "(FVS_MUSCL_HLLE, FVS_HLLE)");
   const int w = (m->flux_method == FVS_HLLE) ? 1 : 2;
   fvs::BoxDesc wbox = cb;
   wbox.n[dir] -= (window_rule == 0) ? 2 * w : 2 * w - 1;

@@ -45,7 +45,12 @@ __device__ __forceinline__ void AtomicMaxPositive(unsigned long long* word,
   atomicMax(word, static_cast<unsigned long long>(__double_as_longlong(v)));
 }
 
+// Max over a warp of non-negative face speeds.  A NaN speed (a state of
+// negative pressure) counts as 0, so it is skipped wherever it sits: without
+// the guard a NaN in lane 0 would survive the butterfly there (NaN > x and
+// x > NaN are both false) and discard the other 31 lanes' maxima.
 __device__ __forceinline__ double WarpMax(double v) {
+  v = v > 0.0 ? v : 0.0;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const double w = __shfl_xor_sync(0xffffffffu, v, o);

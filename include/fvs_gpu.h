@@ -153,7 +153,13 @@ int fvs_compute_stable_dt(const fvs_method* m, int rank,
  *    the limit -- split the patch or use fvs_compute_stable_dt.
  *  - The first call on each device looks up the array's device address
  *    (cudaGetSymbolAddress, with that device current); make that first call
- *    before any stream capture.
+ *    before any stream capture.  The address is kept for the life of the
+ *    process: after cudaDeviceReset on a device, do not call this entry
+ *    point on that device again (the kept address belongs to the context the
+ *    reset destroyed).
+ *  - Argument checks and status codes are those of fvs_compute_stable_dt
+ *    (FVS_ERR_NO_DEVICE without a GPU); other flux methods return
+ *    FVS_ERR_UNSUPPORTED.
  *  - All calls share the one array, and each call overwrites what the
  *    previous one left there (every slot it reads it has written first, so
  *    nothing needs clearing).  Calls that overlap on the GPU -- from several
@@ -317,6 +323,13 @@ int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int nc
  * [2][NY][NX], cut flags [NY][NX].  Any pointer may be NULL. */
 int fvs_solver_cutcell_geometry(fvs_solver* s, double* alpha, double* betax, double* betay,
                                 double* normal, double* center, int8_t* cut_flags);
+/* The shielded face fractions of direction dir (FillCutCellData,
+ * src/AMReX/cutcell/FillCutCellData.cpp:28-118): unshielded, left- and
+ * right-shielded fractions and the same divided by the face fraction, over
+ * the face array of the grown grid (betax's shape for dir 0, betay's for
+ * dir 1).  Any pointer may be NULL. */
+int fvs_solver_cutcell_shielded(fvs_solver* s, int dir, double* us, double* sL, double* sR,
+                                double* us_rel, double* sL_rel, double* sR_rel);
 /* Cycle counter used for the direction order of the next step. */
 int fvs_solver_set_cycle(fvs_solver* s, int64_t cycle);
 int fvs_solver_set_time(fvs_solver* s, double t);

@@ -221,7 +221,12 @@ double ComputeStableDt(const orc_method& m, const BoxView& states, double dx,
           st[s] = LoadComplete<D>(states, cell[0], cell[1], cell[2]);
         }
         const double dt = WindowDt<D>(eq, m, st, dx, dir);
-        min_dt = std::min(dt, min_dt);
+        // std::min(dt, min_dt) of the reference for every non-NaN dt.  A NaN
+        // window dt (a NaN face speed: negative pressure, outside the pinned
+        // domain) is skipped, the one NaN rule of the library's CFL maxima;
+        // the reference's std::min would instead forget every window before
+        // the NaN one.
+        if (dt < min_dt) min_dt = dt;
       }
     }
   }

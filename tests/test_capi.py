@@ -36,6 +36,12 @@ def test_no_gpu_reports_no_device(capi):
     assert L.fvs_solver_create(C.byref(g), C.byref(m), C.byref(h)) == capi.FVS_ERR_NO_DEVICE
     with pytest.raises(f.FvsError):
         f.Solver([8], [0.1], "transmissive")
+    # both stable-dt entry points report the missing device the same way
+    out = C.c_double(0.0)
+    b = f.box([0, 0], [8, 8])
+    for fn in (L.fvs_compute_stable_dt, L.fvs_compute_stable_dt_noalloc):
+        assert fn(C.byref(m), 2, 1, b, 0.1, 0, 0, C.byref(out), None) == \
+            capi.FVS_ERR_NO_DEVICE
 
 
 def test_argument_validation_before_device(capi):
@@ -60,6 +66,17 @@ def test_argument_validation_before_device(capi):
     r = L.fvs_update_conservatively(1, f.box([0], [4]), 1, f.box([0], [4]), 1, f.box([0], [4]),
                                     3, 0.1, 0.1, 0, None)
     assert r == capi.FVS_ERR_INVALID
+    # the allocation-free stable dt checks its arguments like the allocating one
+    for fn in (L.fvs_compute_stable_dt, L.fvs_compute_stable_dt_noalloc):
+        out = C.c_double(0.0)
+        assert fn(C.byref(m2), 1, 1, f.box([0], [8]), 0.1, 0, 0, C.byref(out), None) == \
+            capi.FVS_ERR_INVALID  # unknown limiter
+        m3 = f.make_method(precision="fp64_exact")
+        m3.precision = 9
+        assert fn(C.byref(m3), 1, 1, f.box([0], [8]), 0.1, 0, 0, C.byref(out), None) == \
+            capi.FVS_ERR_INVALID  # unknown precision
+        assert fn(C.byref(m), 1, 1, f.box([0], [8]), 0.1, 0, 2, C.byref(out), None) == \
+            capi.FVS_ERR_INVALID  # unknown window rule
     # bad grid
     g = capi.GridDesc()
     g.rank = 2

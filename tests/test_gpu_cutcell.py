@@ -31,6 +31,10 @@ def test_geometry_bit_exact(fvs, orc, n, circles):
         np.testing.assert_array_equal(g[key], getattr(ref, key), err_msg=key)
     G = ref.G
     np.testing.assert_array_equal(g["cut"][G:-G, G:-G].astype(np.int32), ref.cut_cells())
+    names = ("us", "sL", "sR", "us_rel", "sL_rel", "sR_rel")
+    for d in (0, 1):
+        for name, a, b in zip(names, s.cutcell_shielded(d), ref.shielded(d)):
+            np.testing.assert_array_equal(a, b, err_msg=f"{name} dir {d}")
     s.close()
 
 
