@@ -233,8 +233,15 @@ struct fvs_solver {
   fvs::CcGeom ccg{};
   double* cc_refs = nullptr;
   std::vector<void*> cc_allocs;
+  // the cut tiles of a KBN sweep run on `side`, forked from and joined back
+  // into `stream` by the two events
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   ~fvs_solver() {
     for (void* p : cc_allocs) cudaFree(p);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
     for (double* b : buf)
       if (b) cudaFree(b);
@@ -303,9 +310,24 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
     c.prev_dx = prev_dx;
     c.occupancy = s->occ_tuned[dir];
     c.skip_cfl = skip_cfl ? 1 : 0;
-    return s->m.precision == FVS_FP64_EXACT
-               ? fvs::LaunchCutCellSweep(c, s->stream)
-               : fvs::LaunchCutCellSweepT(s->m.precision, c, s->stream);
+    auto launch = [&](bool band, cudaStream_t st) {
+      return s->m.precision == FVS_FP64_EXACT
+                 ? fvs::LaunchCutCellSweep(c, band, st)
+                 : fvs::LaunchCutCellSweepT(s->m.precision, c, band, st);
+    };
+    // the cut tiles on the side stream, concurrent with the regular and
+    // covered tiles (disjoint output cells, one CFL maximum)
+    cudaError_t e = cudaSuccess;
+    const bool fork = s->ccg.nband[dir] > 0;
+    if (fork) {
+      e = cudaEventRecord(s->ev_fork, s->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s->side, s->ev_fork, 0);
+      if (e == cudaSuccess) e = launch(true, s->side);
+      if (e == cudaSuccess) e = cudaEventRecord(s->ev_join, s->side);
+    }
+    if (e == cudaSuccess) e = launch(false, s->stream);
+    if (fork && e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->ev_join, 0);
+    return e;
   }
   fvs::SweepArgs a{};
   a.in = in;
@@ -951,6 +973,35 @@ int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int nc
   ga.normal = g.normal;
   ga.center = g.center;
   FVS_CUDA(fvs::LaunchCutCellGeometry(ga, g, s->stream));
+  // tile classes of both sweep directions and the lists of cut tiles
+  for (int d = 0; d < 2; ++d) {
+    const size_t ntiles = size_t(g.NGroups(d)) * g.NTiles(d);
+    void* cls = nullptr;
+    FVS_CUDA(cudaMalloc(&cls, ntiles));
+    s->cc_allocs.push_back(cls);
+    g.tile_class[d] = static_cast<signed char*>(cls);
+    FVS_CUDA(fvs::LaunchCutCellTileClass(g, d, s->stream));
+    std::vector<signed char> h(ntiles);
+    FVS_CUDA(cudaMemcpyAsync(h.data(), cls, ntiles, cudaMemcpyDeviceToHost, s->stream));
+    FVS_CUDA(cudaStreamSynchronize(s->stream));
+    std::vector<int> band;
+    for (size_t k = 0; k < ntiles; ++k)
+      if (h[k] == fvs::kCcCut) band.push_back(static_cast<int>(k));
+    g.nband[d] = static_cast<int>(band.size());
+    g.band[d] = nullptr;
+    if (!band.empty()) {
+      void* b = nullptr;
+      FVS_CUDA(cudaMalloc(&b, band.size() * sizeof(int)));
+      s->cc_allocs.push_back(b);
+      g.band[d] = static_cast<int*>(b);
+      FVS_CUDA(cudaMemcpy(b, band.data(), band.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
+  }
+  if (!s->side) {
+    FVS_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+    FVS_CUDA(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+    FVS_CUDA(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+  }
   FVS_CUDA(cudaStreamSynchronize(s->stream));
   s->cc = true;
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);

@@ -363,14 +363,28 @@ template <class T, class M> __global__ void ReferenceStatesKernel(CcStateArgs a)
   a.refs[5 * plane + c] = Widen(r.c);
 }
 
-// The fused KBN sweep: one thread marches one grid line (segment) along
-// `dir`, evaluating per cell the masked predictor and the boundary flux, per
-// face the masked HLLE flux, the h-box stabilised fluxes and the CFL speed,
-// and per cell the cut-cell update.
+// The fused KBN sweep over the cut tiles (CcGeom::band): one warp per tile,
+// each thread marching the tile's cells of one grid line along `dir`,
+// evaluating per cell the masked predictor and the boundary flux, per face
+// the masked HLLE flux, the h-box stabilised fluxes and the CFL speed, and per
+// cell the cut-cell update.  Blocks are one warp.
 struct FaceData {
   double f[4], fs[4], fsL[4], fsR[4];
   double beta, us, sL, sR;
 };
+
+// False when the sweep must not run: the run was aborted or finished, or the
+// previous sweep's CFL check failed.
+__device__ __forceinline__ bool SweepGateCc(const CcSweepArgs& a, double split_dt) {
+  if (a.ctrl) {
+    if (a.ctrl->abort || a.ctrl->done) return false;
+    if (a.prev_check >= 0) {
+      const double smax = BitsToDouble(a.ctrl->smax_check[a.prev_check]);
+      if (a.prev_dx / smax < split_dt) return false;
+    }
+  }
+  return true;
+}
 
 template <class T, class M, int kMinBlocks>
 __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a) {
@@ -378,19 +392,16 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
   const int dir = a.dir;
   const int nd = dir == 0 ? g.nx : g.ny;
   const int nt = dir == 0 ? g.ny : g.nx;
-  const int64_t t64 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int j0 = blockIdx.y * a.seg_len;
-  const int j1 = min(nd, j0 + a.seg_len);
+  // the warp's tile; warps beyond the list only join the block reduction
+  const int slot = static_cast<int>(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
+  const bool has_tile = slot < g.nband[dir];
+  const int tile_id = has_tile ? g.band[dir][slot] : 0;
+  const int group = tile_id / g.NTiles(dir), tile = tile_id % g.NTiles(dir);
+  const int64_t t64 = has_tile ? int64_t(group) * 32 + (threadIdx.x & 31) : int64_t(nt);
+  const int j0 = tile * kCcTile;
+  const int j1 = min(nd, j0 + kCcTile);
   const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
-  bool run = true;
-  if (a.ctrl) {
-    if (a.ctrl->abort || a.ctrl->done) run = false;
-    if (a.prev_check >= 0) {
-      const double smax = BitsToDouble(a.ctrl->smax_check[a.prev_check]);
-      if (a.prev_dx / smax < split_dt) run = false;
-    }
-  }
-  if (!BlockAll(run)) return;
+  if (!BlockAll(SweepGateCc(a, split_dt))) return;
   T smax = T(0);
   int status = 0;
   // CFL speeds: none in a step's first sweep (skip_cfl: the stable-dt pass
@@ -637,6 +648,185 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
   if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
 }
 
+// The regular and covered tiles of a KBN sweep (CcTileClass).  On a regular
+// tile the KBN arithmetic reduces, bit for bit, to the masked MUSCL-Hancock
+// predictor and masked HLL flux with every mask true, the stabilised flux
+// us_rel f + sL_rel fsL + sR_rel fsR = 1 f + 0 fsL + 0 fsR = f + 0 (for every
+// finite f; the + 0 turns a -0 into +0 as the zero terms do), and the update
+// U + dt/dx (fs_L - fs_R) of cells with equal face fractions
+// (src/AMReX/cutcell/TimeIntegrator.cpp:65-221): the kernel evaluates exactly
+// that, from the same inline functions, and reads no geometry.  A covered
+// tile's cells are 0 and its faces (beta 0) add no CFL speed.  Each thread
+// marches the runs of consecutive regular tiles of its segment of one grid
+// line; the tile class is the warp's, so the control flow is warp-uniform.
+template <class T, class M, int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweepArgs a) {
+  const CcGeom& g = a.s.g;
+  const int dir = a.dir;
+  const int nd = dir == 0 ? g.nx : g.ny;
+  const int nt = dir == 0 ? g.ny : g.nx;
+  const int64_t t64 = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int group = static_cast<int>(t64 >> 5);
+  const int s0 = blockIdx.y * a.seg_len;  // a multiple of kCcTile
+  const int s1 = min(nd, s0 + a.seg_len);
+  const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
+  if (!BlockAll(SweepGateCc(a, split_dt))) return;
+  T smax = T(0);
+  int status = 0;
+  constexpr bool kScreen = sizeof(T) == 8;
+  const bool skip_cfl = kScreen && a.skip_cfl != 0;
+  const bool screen = kScreen && a.s.gamma > 1.0 && a.s.gamma <= 2.0;
+  const unsigned amask = __ballot_sync(0xffffffffu, t64 < nt);
+  if (t64 < nt) {
+    const int t = static_cast<int>(t64);
+    const GasT<T, M> eq = MakeGasT<T, M>(a.s.gamma);
+    const T lambda_half = NarrowTo<T>(0.5 * split_dt / a.dx);
+    const double dt_dx = split_dt / a.dx;
+    const int64_t cs = int64_t(g.nx) * g.ny;
+    const int ntl = g.NTiles(dir);
+    const signed char* cls = g.tile_class[dir] + int64_t(group) * ntl;
+    auto offset = [&](int c) {
+      return dir == 0 ? int64_t(t) * g.nx + c : int64_t(c) * g.nx + t;
+    };
+    // masked state of cell c (alpha 1: zeroed only where rho <= 0)
+    auto load_cell = [&](int c, T* u) {
+      double vd[4];
+      if (dir == 0)
+        LoadCons(a.s, c, t, vd);
+      else
+        LoadCons(a.s, t, c, vd);
+      T v[4];
+      Narrow(v, vd);
+      C2T<T> q;
+      CompleteMasked(eq, q, v, true);
+      u[0] = q.rho;
+      u[1] = q.m[0];
+      u[2] = q.m[1];
+      u[3] = q.E;
+    };
+    fast::Gas<float> g32;
+    g32.gamma = static_cast<float>(a.s.gamma);
+    g32.gm1 = static_cast<float>(a.s.gamma - 1.0);
+    float thr = 0.0f;
+    if (kScreen && !skip_cfl && a.smax_out)
+      thr = CflFloatBelow(CflSync(a.smax_out, 0.0, amask));
+    int rows = 0;  // faces since the last publication of the warp's maximum
+    const int tile_end = (s1 + kCcTile - 1) / kCcTile;
+    int tile = s0 / kCcTile;
+    while (tile < tile_end) {
+      const int k = cls[tile];
+      if (k == kCcCut) {
+        ++tile;
+        continue;
+      }
+      if (k == kCcCovered) {
+        const int c1 = min(nd, (tile + 1) * kCcTile);
+        for (int c = tile * kCcTile; c < c1; ++c) {
+          const int64_t o = offset(c);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) a.out[q * cs + o] = 0.0;
+        }
+        ++tile;
+        continue;
+      }
+      int r1 = tile + 1;
+      while (r1 < tile_end && cls[r1] == kCcRegular) ++r1;
+      const int j0 = tile * kCcTile, j1 = min(nd, r1 * kCcTile);
+      tile = r1;
+      // march the run [j0, j1): faces j0 .. j1, cells j0 .. j1-1
+      T um[4], uc[4], up[4];
+      load_cell(j0 - 2, um);
+      load_cell(j0 - 1, uc);
+      C2T<T> recR_prev, q_prev;
+      double fs_prev[4];
+      fast::Wave<float> v_prev{};
+      bool ok_prev = false;
+      bool have_prev = false;
+      for (int j = j0 - 1; j <= j1; ++j) {
+        load_cell(j + 1, up);
+        C2T<T> recL, recR;
+        PredictMasked(eq, recL, recR, um, uc, up, true, a.limiter, lambda_half, dir);
+        C2T<T> q;
+        fast::Wave<float> v{};
+        bool ok = false;
+        if constexpr (kScreen) {
+          if (!skip_cfl) {
+            float c32[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) c32[c] = CflToF32(uc[c]);
+            v = fast::MakeWave<2, float>(g32, c32, dir);
+            ok = screen && CflInRange<2>(c32) && v.a > 0.0f;
+          }
+        } else {
+          CompleteMasked(eq, q, uc, true);
+        }
+        if (j >= j0) {
+          if constexpr (kScreen) {
+            if (!skip_cfl) {
+              const float s32 = fast::FaceMaxSpeed<float>(g32, v_prev, v);
+              const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
+              const bool need =
+                  !(ok && ok_prev && fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs)) < thr);
+              if (__any_sync(amask, need)) {
+                if (!have_prev) CompleteMasked(eq, q_prev, um, true);
+                CompleteMasked(eq, q, uc, true);
+                T s0w, s1w;
+                EinfeldtMasked(eq, q_prev, q, dir, s0w, s1w);
+                const T mx = PMaxT(PMaxT(T(0), fabs(s0w)), fabs(s1w));
+                smax = mx > smax ? mx : smax;
+                thr = fmaxf(thr, CflFloatBelow(static_cast<double>(smax)));
+                q_prev = q;
+                have_prev = true;
+              } else {
+                have_prev = false;
+              }
+              if (a.smax_out && ++rows == kCflSyncRows) {
+                rows = 0;
+                thr = fmaxf(thr, CflFloatBelow(CflSync(a.smax_out, static_cast<double>(smax),
+                                                       amask)));
+              }
+            }
+          }
+          T f[4];
+          HllMasked(eq, f, recR_prev, recL, dir);
+          double fs[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) fs[c] = Widen(f[c]) + 0.0;
+          if constexpr (!kScreen) {
+            T s0w, s1w;
+            EinfeldtMasked(eq, q_prev, q, dir, s0w, s1w);
+            const T mx = PMaxT(PMaxT(T(0), fabs(s0w)), fabs(s1w));
+            smax = mx > smax ? mx : smax;
+          }
+          if (j > j0) {
+            const int64_t o = offset(j - 1);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              const double prev = __ldg(a.s.in + c * cs + o);
+              a.out[c * cs + o] = prev + dt_dx * (fs_prev[c] - fs[c]);
+            }
+            if (__double_as_longlong(a.out[o]) <= 0) status |= kStatusNonPositiveDensity;
+          }
+#pragma unroll
+          for (int c = 0; c < 4; ++c) fs_prev[c] = fs[c];
+        }
+        recR_prev = recR;
+        if constexpr (!kScreen) q_prev = q;
+        ok_prev = ok;
+        v_prev = v;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          um[c] = uc[c];
+          uc[c] = up[c];
+        }
+      }
+    }
+  }
+  const double smax_d = static_cast<double>(smax);
+  BlockMaxAtomic<1>(a.smax_out, &smax_d);
+  if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
+}
+
 // Masked stable dt over both directions: faces 0..n with beta > 0
 // (KbnStabilisation.hpp:275-345).
 template <class T, class M>
@@ -684,21 +874,30 @@ template <class T, class M> cudaError_t LaunchKbnStates(const CcStateArgs& a, cu
   return cudaGetLastError();
 }
 
-template <class T, class M> cudaError_t LaunchKbnSweep(const CcSweepArgs& a, cudaStream_t s) {
+template <class T, class M>
+cudaError_t LaunchKbnSweep(const CcSweepArgs& a, bool band, cudaStream_t s) {
   const int nd = a.dir == 0 ? a.s.g.nx : a.s.g.ny;
   const int nt = a.dir == 0 ? a.s.g.ny : a.s.g.nx;
+  if (band) {
+    // cut tiles: one warp each; register/occupancy variant: the default, or
+    // compiled for 3 (FP64) / 4 (FP32) resident 128-thread blocks per SM
+    // (spilling a little)
+    const int n = a.s.g.nband[a.dir];
+    if (n == 0) return cudaSuccess;
+    constexpr int kMore = sizeof(T) == 4 ? 4 : 3;
+    if (a.occupancy == kMore)
+      KbnSweepKernel<T, M, kMore><<<unsigned(n), 32, 0, s>>>(a);
+    else
+      KbnSweepKernel<T, M, 1><<<unsigned(n), 32, 0, s>>>(a);
+    return cudaGetLastError();
+  }
   const int block = 128;
-  const int seg = a.seg_len > 0 ? a.seg_len : nd;
+  int seg = a.seg_len > 0 ? a.seg_len : nd;
+  seg = (seg + kCcTile - 1) / kCcTile * kCcTile;
   CcSweepArgs b = a;
   b.seg_len = seg;
   dim3 grid(unsigned((nt + block - 1) / block), unsigned((nd + seg - 1) / seg));
-  // register/occupancy variant: the default, or compiled for 3 (FP64) / 4 (FP32)
-  // resident blocks per SM (spilling a little)
-  constexpr int kMore = sizeof(T) == 4 ? 4 : 3;
-  if (a.occupancy == kMore)
-    KbnSweepKernel<T, M, kMore><<<grid, block, 0, s>>>(b);
-  else
-    KbnSweepKernel<T, M, 1><<<grid, block, 0, s>>>(b);
+  KbnRegularSweepKernel<T, M, sizeof(T) == 4 ? 4 : 3><<<grid, block, 0, s>>>(b);
   return cudaGetLastError();
 }
 

@@ -141,10 +141,50 @@ __global__ void CutFlagKernel(CcGeom g) {
   g.cut[id] = static_cast<signed char>(cut);
 }
 
+// Class of the tile (group, tile) of direction d (CcTileClass): one block of
+// 32 threads, one per line of the group; lines beyond the grid agree with
+// every class.
+__global__ void TileClassKernel(CcGeom g, int d) {
+  const int ntl = g.NTiles(d);
+  const int group = blockIdx.x / ntl, tile = blockIdx.x % ntl;
+  const int nd = d == 0 ? g.nx : g.ny;
+  const int nt = d == 0 ? g.ny : g.nx;
+  const int t = group * 32 + static_cast<int>(threadIdx.x);
+  const int c0 = tile * kCcTile, c1 = min(nd, c0 + kCcTile);
+  bool regular = true, covered = true;
+  if (t < nt) {
+    auto cell = [&](int c) { return d == 0 ? g.CellIndex(c, t) : g.CellIndex(t, c); };
+    for (int c = c0 - 2; c <= c1 + 1; ++c) {
+      const int64_t ci = cell(c);
+      const double a = g.alpha[ci];
+      regular = regular && a == 1.0;
+      if (c >= c0 - 1 && c <= c1) regular = regular && g.cut[ci] == 0;
+      if (c >= c0 && c < c1) covered = covered && a == 0.0;
+    }
+    for (int f = c0; f <= c1; ++f) {
+      const int64_t fi = g.FaceIndex(d, f, t);
+      const double b = g.beta[d][fi];
+      regular = regular && b == 1.0 && g.us_rel[d][fi] == 1.0 && g.sL_rel[d][fi] == 0.0 &&
+                g.sR_rel[d][fi] == 0.0;
+      covered = covered && !(b > 0.0);
+    }
+  }
+  regular = __all_sync(0xffffffffu, regular);
+  covered = __all_sync(0xffffffffu, covered);
+  if (threadIdx.x == 0)
+    g.tile_class[d][blockIdx.x] = regular ? kCcRegular : (covered ? kCcCovered : kCcCut);
+}
+
 }  // namespace cc
 
 // ---------------------------------------------------------------------------
 // Launchers
+
+cudaError_t LaunchCutCellTileClass(const CcGeom& g, int d, cudaStream_t s) {
+  const int64_t n = int64_t(g.NGroups(d)) * g.NTiles(d);
+  if (n > 0) cc::TileClassKernel<<<unsigned(n), 32, 0, s>>>(g, d);
+  return cudaGetLastError();
+}
 
 cudaError_t LaunchCutCellGeometry(const CcGeomArgs& a, const CcGeom& g, cudaStream_t s) {
   const int NX = a.nx + 2 * kCcGhost, NY = a.ny + 2 * kCcGhost;
@@ -168,8 +208,8 @@ cudaError_t LaunchCutCellReferenceStates(const CcStateArgs& a, cudaStream_t s) {
   return cc::LaunchKbnStates<double, cc::CcIeee>(a, s);
 }
 
-cudaError_t LaunchCutCellSweep(const CcSweepArgs& a, cudaStream_t s) {
-  return cc::LaunchKbnSweep<double, cc::CcIeee>(a, s);
+cudaError_t LaunchCutCellSweep(const CcSweepArgs& a, bool band, cudaStream_t s) {
+  return cc::LaunchKbnSweep<double, cc::CcIeee>(a, band, s);
 }
 
 cudaError_t LaunchCutCellStableDt(const CcStateArgs& a, unsigned long long* smax_out,

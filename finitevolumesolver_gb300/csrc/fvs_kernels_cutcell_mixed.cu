@@ -13,9 +13,9 @@ cudaError_t LaunchCutCellReferenceStatesT(int precision, const CcStateArgs& a, c
                         : cc::LaunchKbnStates<double, cc::CcFast>(a, s);
 }
 
-cudaError_t LaunchCutCellSweepT(int precision, const CcSweepArgs& a, cudaStream_t s) {
-  return precision == 2 ? cc::LaunchKbnSweep<float, cc::CcIeee>(a, s)
-                        : cc::LaunchKbnSweep<double, cc::CcFast>(a, s);
+cudaError_t LaunchCutCellSweepT(int precision, const CcSweepArgs& a, bool band, cudaStream_t s) {
+  return precision == 2 ? cc::LaunchKbnSweep<float, cc::CcIeee>(a, band, s)
+                        : cc::LaunchKbnSweep<double, cc::CcFast>(a, band, s);
 }
 
 cudaError_t LaunchCutCellStableDtT(int precision, const CcStateArgs& a,
