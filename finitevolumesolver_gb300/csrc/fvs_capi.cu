@@ -812,7 +812,7 @@ int fvs_solver_set_launch(fvs_solver* s, int dir, int seg_len, int variant) {
     ok = variant == 0 || variant == 4 || variant == 5 ||
          (dir == 0 && (variant == 10 || variant == 14 || variant == 15));
   if (s->m.precision == FVS_FP64_DF && plain_hlle) ok = variant == 0 || variant == 3;
-  if (s->cc) ok = variant == 0 || variant == (s->m.precision == FVS_MIXED ? 4 : 3);
+  if (s->cc) ok = variant == 0;
   if (!ok) return Fail(FVS_ERR_INVALID, "no such launch variant for this method");
   s->seg_tuned[dir] = seg_len;
   s->occ_tuned[dir] = variant;
@@ -836,10 +836,9 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   const int occs_mixed[] = {0, 4, 5};
   const int occs_df[] = {0, 3};
   const int occs_plain[] = {0};
-  // cut cells: the KBN sweep in its default and its higher-occupancy build
-  const int occs_cc64[] = {0, 3};
-  const int occs_cc32[] = {0, 4};
-  const bool cc32 = s->cc && s->m.precision == FVS_MIXED;
+  // cut cells: segment lengths of the FP64 flavours' regular-cell sweep (the
+  // mixed flavour's cut-cell kernels have no launch parameter to tune)
+  const bool cc_cell = s->cc && s->m.precision == FVS_MIXED;
   const int saved = s->seg_len;
   cudaEvent_t e0, e1;
   FVS_CUDA(cudaEventCreate(&e0));
@@ -855,9 +854,8 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   if (s->cc) FVS_CUDA(CcReferenceStates(s, s->buf[s->cur]));
   for (int d = 0; d < s->g.rank; ++d) {
     const int nd = s->g.n[d];
-    const int* occs = mixed ? (d == 0 ? occs_mixed_x : occs_mixed)
-                            : (df ? occs_df : (s->cc ? (cc32 ? occs_cc32 : occs_cc64) : occs_plain));
-    const int nocc = mixed ? (d == 0 ? 6 : 3) : ((df || s->cc) ? 2 : 1);
+    const int* occs = mixed ? (d == 0 ? occs_mixed_x : occs_mixed) : (df ? occs_df : occs_plain);
+    const int nocc = mixed ? (d == 0 ? 6 : 3) : (df ? 2 : 1);
     float best = 1e30f;
     int best_seg = 0, best_occ = 0;
     for (int oi = 0; oi < nocc; ++oi) {
@@ -866,7 +864,7 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
       const bool warp_x = mixed && d == 0 && occs[oi] < 10;
       for (int c : cands) {
         if (c > 2 * nd && c != cands[0]) break;
-        if (warp_x && c != cands[0]) break;
+        if ((warp_x || cc_cell) && c != cands[0]) break;
         s->seg_len = c;
         float ms_sum = 0.f;
         for (int rep = 0; rep < 3; ++rep) {
@@ -973,20 +971,26 @@ int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int nc
   ga.normal = g.normal;
   ga.center = g.center;
   FVS_CUDA(fvs::LaunchCutCellGeometry(ga, g, s->stream));
-  // tile classes of both sweep directions and the lists of cut tiles
+  // cell classes of both sweep directions, the tiles with regular cells and
+  // the lists of band cells
   for (int d = 0; d < 2; ++d) {
+    const size_t ncell = size_t(g.nx) * g.ny;
     const size_t ntiles = size_t(g.NGroups(d)) * g.NTiles(d);
     void* cls = nullptr;
-    FVS_CUDA(cudaMalloc(&cls, ntiles));
+    void* treg = nullptr;
+    FVS_CUDA(cudaMalloc(&cls, ncell));
     s->cc_allocs.push_back(cls);
-    g.tile_class[d] = static_cast<signed char*>(cls);
-    FVS_CUDA(fvs::LaunchCutCellTileClass(g, d, s->stream));
-    std::vector<signed char> h(ntiles);
-    FVS_CUDA(cudaMemcpyAsync(h.data(), cls, ntiles, cudaMemcpyDeviceToHost, s->stream));
+    FVS_CUDA(cudaMalloc(&treg, ntiles));
+    s->cc_allocs.push_back(treg);
+    g.cell_class[d] = static_cast<signed char*>(cls);
+    g.tile_regular[d] = static_cast<signed char*>(treg);
+    FVS_CUDA(fvs::LaunchCutCellClasses(g, d, s->stream));
+    std::vector<signed char> h(ncell);
+    FVS_CUDA(cudaMemcpyAsync(h.data(), cls, ncell, cudaMemcpyDeviceToHost, s->stream));
     FVS_CUDA(cudaStreamSynchronize(s->stream));
     std::vector<int> band;
-    for (size_t k = 0; k < ntiles; ++k)
-      if (h[k] == fvs::kCcCut) band.push_back(static_cast<int>(k));
+    for (size_t k = 0; k < ncell; ++k)
+      if (h[k] == fvs::kCcBand) band.push_back(static_cast<int>(k));
     g.nband[d] = static_cast<int>(band.size());
     g.band[d] = nullptr;
     if (!band.empty()) {

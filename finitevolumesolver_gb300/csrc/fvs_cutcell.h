@@ -12,18 +12,19 @@ namespace fvs {
 // sweep (MUSCL stencil of 2 plus the neighbour faces of the shielding).
 constexpr int kCcGhost = 3;
 
-// Tiles of a KBN sweep in direction d: a group of 32 consecutive grid lines
-// along d (one warp) times kCcTile consecutive cells along d.  A tile is
-//   regular: every cell of its stencil reach [c0-2, c1+1] has alpha 1, no
-//     cell of [c0-1, c1] is cut, and every face of [c0, c1] has beta 1,
+// Cells of a KBN sweep in direction d fall into three classes:
+//   regular: every cell of its stencil reach j-2 .. j+2 along d has alpha 1,
+//     none of j-1 .. j+1 is cut, and its faces j and j+1 have beta 1,
 //     unshielded fraction 1 and shielded fractions 0 -- there the KBN update
-//     is masked MUSCL-Hancock + HLL and U + dt/dx (f_L - f_R), with no
-//     geometry to read;
-//   covered: its cells have alpha 0 and its faces beta 0 (the cells stay 0
-//     and add no CFL speed);
-//   cut: everything else, the full KBN arithmetic.
+//     is masked MUSCL-Hancock + HLL with every mask true and
+//     U + dt/dx (f_L - f_R), with no geometry to read;
+//   covered: alpha 0 (the cell stays 0; its faces have beta 0);
+//   band: everything else, the full KBN arithmetic.
+// Tiles group 32 consecutive grid lines (one warp) x kCcTile consecutive
+// cells along d; a tile is marched by the regular kernels when it holds a
+// regular cell.
 constexpr int kCcTile = 8;
-enum CcTileClass : signed char { kCcRegular = 0, kCcCovered = 1, kCcCut = 2 };
+enum CcCellClass : signed char { kCcRegular = 0, kCcCovered = 1, kCcBand = 2 };
 
 // Geometry over the grid grown by kCcGhost layers (component-major, x
 // fastest).  Cells: [NY][NX]; x faces: [NY][NX+1]; y faces: [NY+1][NX].
@@ -40,9 +41,11 @@ struct CcGeom {
   double* sL_rel[2];
   double* sR_rel[2];
   signed char* cut;  // IsCutCell
-  // per direction: class of every tile, [NGroups(d)][NTiles(d)], and the
-  // ids (group * NTiles(d) + tile) of the cut tiles
-  signed char* tile_class[2];
+  // per direction: the class of every interior cell ([ny][nx], CcCellClass),
+  // whether a tile holds a regular cell ([NGroups(d)][NTiles(d)], 0 or 1),
+  // and the list of band cells (indices j * nx + i)
+  signed char* cell_class[2];
+  signed char* tile_regular[2];
   int* band[2];
   int nband[2];
   __host__ __device__ int NTiles(int d) const { return ((d == 0 ? nx : ny) + kCcTile - 1) / kCcTile; }
@@ -100,8 +103,9 @@ struct CcSweepArgs {
 };
 
 cudaError_t LaunchCutCellGeometry(const CcGeomArgs& a, const CcGeom& g, cudaStream_t s);
-// Classifies the tiles of direction d into g.tile_class[d] (CcTileClass).
-cudaError_t LaunchCutCellTileClass(const CcGeom& g, int d, cudaStream_t s);
+// Classifies the cells of direction d into g.cell_class[d] (CcCellClass)
+// and marks the tiles with a regular cell in g.tile_regular[d].
+cudaError_t LaunchCutCellClasses(const CcGeom& g, int d, cudaStream_t s);
 cudaError_t LaunchCutCellReferenceStates(const CcStateArgs& a, cudaStream_t s);
 // Plotfile components of rows [j0, j0 + rows): masked Complete (6),
 // Boundary_X, Boundary_Y, vfrac; [9][rows][nx].
@@ -109,9 +113,10 @@ cudaError_t LaunchCutCellPlotData(const CcGeom& g, const double* cons, double ga
                                   int rows, double* out, cudaStream_t s);
 // Fast FP64 (precision 1) and mixed (precision 2) flavours of the KBN kernels.
 // A KBN sweep is two launches that write disjoint cells of `out` and feed the
-// same CFL maximum: the regular and covered tiles (band = false; threads
-// march segments of a.seg_len cells, a multiple of kCcTile) and the cut tiles
-// (band = true; one warp per tile of g.band[dir]).  They may run concurrently.
+// same CFL maximum: the regular and covered cells (band = false; tiles with a
+// regular cell are marched, the FP64 flavours' threads over segments of
+// a.seg_len cells, a multiple of kCcTile) and the band cells (band = true;
+// one thread per cell of g.band[dir]).  They may run concurrently.
 cudaError_t LaunchCutCellReferenceStatesT(int precision, const CcStateArgs& a, cudaStream_t s);
 cudaError_t LaunchCutCellSweepT(int precision, const CcSweepArgs& a, bool band, cudaStream_t s);
 cudaError_t LaunchCutCellStableDtT(int precision, const CcStateArgs& a,

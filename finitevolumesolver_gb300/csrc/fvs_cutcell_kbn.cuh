@@ -54,6 +54,17 @@ struct CcFast {
   static __device__ __forceinline__ double Sqrt(double a) { return fast::Math<double>::Sqrt(a); }
 };
 
+// The mixed flavour's FP32 arithmetic: quotients as __fdividef, square roots
+// as a times rsqrtf(a) (0 for a <= 0), as the uniform grid's mixed sweeps
+// compute them (fvs_physics_fast.cuh, Math<float>); the FP32 rounding of the
+// reconstruction dominates either way.
+struct CcFast32 {
+  static constexpr bool kFast = true;
+  static __device__ __forceinline__ float Div(float a, float b) { return __fdividef(a, b); }
+  static __device__ __forceinline__ float Rcp(float a) { return __fdividef(1.0f, a); }
+  static __device__ __forceinline__ float Sqrt(float a) { return a > 0.0f ? a * rsqrtf(a) : 0.0f; }
+};
+
 template <class T, class M = CcIeee> struct GasT {
   T gamma;
   T gamma_minus_1_inv;
@@ -67,6 +78,19 @@ template <class T> struct C2T {
   T p;
   T c;
 };
+
+// Component d of a 2-vector and f[1 + d] += x, for a run-time direction d:
+// selects instead of indexing, so the arrays stay in registers (an indexed
+// local array would live in local memory).
+template <class T> __device__ __forceinline__ T Sel(const T (&m)[2], int d) {
+  return d == 0 ? m[0] : m[1];
+}
+template <class T> __device__ __forceinline__ void AddMomentum(T* f, int d, T x) {
+  if (d == 0)
+    f[1] += x;
+  else
+    f[2] += x;
+}
 
 template <class T> __device__ __forceinline__ T PMinT(T a, T b) { return a < b ? a : b; }
 template <class T> __device__ __forceinline__ T PMaxT(T a, T b) { return a > b ? a : b; }
@@ -102,11 +126,11 @@ __device__ __forceinline__ void CompleteT(const GasT<T, M>& eq, C2T<T>& q, const
 
 // PerfectGas<2>::Flux (PerfectGas.cpp:52-64).
 template <class M, class T> __device__ __forceinline__ void FluxT(T* f, const C2T<T>& q, int dir) {
-  const T velocity = M::Div(q.m[dir], q.rho);
-  f[0] = q.m[dir];
+  const T velocity = M::Div(Sel(q.m, dir), q.rho);
+  f[0] = Sel(q.m, dir);
   f[1] = velocity * q.m[0];
   f[2] = velocity * q.m[1];
-  f[1 + dir] += q.p;
+  AddMomentum(f, dir, q.p);
   f[3] = velocity * (q.E + q.p);
 }
 
@@ -119,8 +143,8 @@ __device__ __forceinline__ void EinfeldtT(const GasT<T, M>& eq, const C2T<T>& L,
   const T sqRhoL = M::Sqrt(rhoL);
   const T sqRhoR = M::Sqrt(rhoR);
   const T oosqRhoSum = M::Div(T(1), sqRhoL + sqRhoR);
-  const T uL = M::Div(L.m[dir], rhoL);
-  const T uR = M::Div(R.m[dir], rhoR);
+  const T uL = M::Div(Sel(L.m, dir), rhoL);
+  const T uR = M::Div(Sel(R.m, dir), rhoR);
   const T roeU = (uL * sqRhoL + uR * sqRhoR) * oosqRhoSum;
   const T hL = M::Div(L.E + L.p, rhoL);
   const T hR = M::Div(R.E + R.p, rhoR);
@@ -151,11 +175,11 @@ __device__ __forceinline__ void CompleteMasked(const GasT<T, M>& eq, C2T<T>& q, 
 template <class M, class T>
 __device__ __forceinline__ void FluxMasked(T* f, const C2T<T>& q, int dir) {
   const T rho = (q.rho > T(0)) ? q.rho : T(1);
-  const T velocity = M::Div(q.m[dir], rho);
-  f[0] = q.m[dir];
+  const T velocity = M::Div(Sel(q.m, dir), rho);
+  f[0] = Sel(q.m, dir);
   f[1] = velocity * q.m[0];
   f[2] = velocity * q.m[1];
-  f[1 + dir] += q.p;
+  AddMomentum(f, dir, q.p);
   f[3] = velocity * (q.E + q.p);
 }
 
@@ -170,15 +194,15 @@ __device__ __forceinline__ void EinfeldtMasked(const GasT<T, M>& eq, const C2T<T
   T uL, uR, wL, wR, hL, hR;
   if constexpr (M::kFast) {
     const T irL = M::Rcp(rhoL), irR = M::Rcp(rhoR), iw = M::Rcp(sqRho);
-    uL = L.m[dir] * irL;
-    uR = R.m[dir] * irR;
+    uL = Sel(L.m, dir) * irL;
+    uR = Sel(R.m, dir) * irR;
     wL = sqRhoL * iw;
     wR = sqRhoR * iw;
     hL = (L.E + L.p) * irL;
     hR = (R.E + R.p) * irR;
   } else {
-    uL = L.m[dir] / rhoL;
-    uR = R.m[dir] / rhoR;
+    uL = Sel(L.m, dir) / rhoL;
+    uR = Sel(R.m, dir) / rhoR;
     wL = sqRhoL / sqRho;
     wR = sqRhoR / sqRho;
     hL = (L.E + L.p) / rhoL;
@@ -363,11 +387,6 @@ template <class T, class M> __global__ void ReferenceStatesKernel(CcStateArgs a)
   a.refs[5 * plane + c] = Widen(r.c);
 }
 
-// The fused KBN sweep over the cut tiles (CcGeom::band): one warp per tile,
-// each thread marching the tile's cells of one grid line along `dir`,
-// evaluating per cell the masked predictor and the boundary flux, per face
-// the masked HLLE flux, the h-box stabilised fluxes and the CFL speed, and per
-// cell the cut-cell update.  Blocks are one warp.
 struct FaceData {
   double f[4], fs[4], fsL[4], fsR[4];
   double beta, us, sL, sR;
@@ -386,261 +405,392 @@ __device__ __forceinline__ bool SweepGateCc(const CcSweepArgs& a, double split_d
   return true;
 }
 
-template <class T, class M, int kMinBlocks>
-__global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a) {
+// The per-sweep constants (dt / dx, the half-step factor, the gas) involve
+// FP64 divisions, which cost tens of cycles of the narrow FP64 pipe; one
+// thread of the block evaluates them and the sweep's gate, the others read
+// them from shared memory after a barrier (`run` is block-uniform).
+template <class T, class M> struct KbnConst {
+  GasT<T, M> eq;
+  T lambda_half;
+  double dt_dx;
+  int run;
+};
+
+template <class T, class M>
+__device__ __forceinline__ const KbnConst<T, M>& KbnBlockConst(const CcSweepArgs& a) {
+  __shared__ KbnConst<T, M> kc;
+  if (threadIdx.x == 0) {
+    const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
+    kc.run = SweepGateCc(a, split_dt) ? 1 : 0;
+    kc.eq = MakeGasT<T, M>(a.s.gamma);
+    kc.lambda_half = NarrowTo<T>(0.5 * split_dt / a.dx);
+    kc.dt_dx = split_dt / a.dx;
+  }
+  __syncthreads();
+  return kc;
+}
+
+// One cell of a KBN sweep, evaluated on its own: cell j of grid line t gets
+// the masked states of cells j-2 .. j+2, the masked MUSCL-Hancock predictors
+// of cells j-1, j, j+1, the boundary fluxes and centroids of those three
+// cells, the masked HLLE fluxes and h-box stabilised fluxes of its faces j and
+// j+1, and the cut-cell update (KbnStabilisation.hpp:347-429,
+// KbnStabilisation.cpp:55-105, TimeIntegrator.cpp:65-221).  Every quantity
+// comes from the same inline functions on the same operands as in a sweep
+// that marches the line, so the result is the same to the bit; a face is
+// evaluated by both of its cells.  The CFL speed of face j (and of face j+1
+// when `right_face`) is folded into smax unless `cfl` is false.
+template <class T, class M>
+__device__ __forceinline__ void KbnCell(const CcSweepArgs& a, int t, int j, bool right_face,
+                                        bool cfl, const KbnConst<T, M>& kc, T& smax,
+                                        int& status) {
+  const CcGeom& g = a.s.g;
+  const int dir = a.dir;
+  const GasT<T, M> eq = kc.eq;
+  const T lambda_half = kc.lambda_half;
+  const double dt_dx = kc.dt_dx;
+  const int64_t plane = int64_t(g.NX()) * g.NY();
+  auto gcell = [&](int c) { return dir == 0 ? g.CellIndex(c, t) : g.CellIndex(t, c); };
+  // masked states (alpha > 0 and rho > 0) of cells j-2 .. j+2
+  T u[5][4];
+  double al[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int c = j - 2 + k;
+    double vd[4];
+    if (dir == 0)
+      LoadCons(a.s, c, t, vd);
+    else
+      LoadCons(a.s, t, c, vd);
+    T v[4];
+    Narrow(v, vd);
+    al[k] = g.alpha[gcell(c)];
+    C2T<T> q;
+    CompleteMasked(eq, q, v, al[k] > 0.0);
+    u[k][0] = q.rho;
+    u[k][1] = q.m[0];
+    u[k][2] = q.m[1];
+    u[k][3] = q.E;
+  }
+  // predictors of cells j-1 (its right state), j (both), j+1 (its left state)
+  C2T<T> recLm, recRm, recL0, recR0, recLp, recRp;
+  PredictMasked(eq, recLm, recRm, u[0], u[1], u[2], al[0] > 0.0 && al[1] > 0.0 && al[2] > 0.0,
+                a.limiter, lambda_half, dir);
+  PredictMasked(eq, recL0, recR0, u[1], u[2], u[3], al[1] > 0.0 && al[2] > 0.0 && al[3] > 0.0,
+                a.limiter, lambda_half, dir);
+  PredictMasked(eq, recLp, recRp, u[2], u[3], u[4], al[2] > 0.0 && al[3] > 0.0 && al[4] > 0.0,
+                a.limiter, lambda_half, dir);
+  // CFL speeds of faces j and j+1 from the masked states
+  if (cfl) {
+    C2T<T> qm, q0;
+    CompleteMasked(eq, qm, u[1], true);
+    CompleteMasked(eq, q0, u[2], true);
+    if (g.beta[dir][g.FaceIndex(dir, j, t)] > 0.0) {
+      T s0, s1;
+      EinfeldtMasked(eq, qm, q0, dir, s0, s1);
+      const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
+      smax = mx > smax ? mx : smax;
+    }
+    if (right_face && g.beta[dir][g.FaceIndex(dir, j + 1, t)] > 0.0) {
+      C2T<T> qp;
+      CompleteMasked(eq, qp, u[3], true);
+      T s0, s1;
+      EinfeldtMasked(eq, q0, qp, dir, s0, s1);
+      const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
+      smax = mx > smax ? mx : smax;
+    }
+  }
+  const int64_t cs = int64_t(g.nx) * g.ny;
+  const int64_t out = dir == 0 ? int64_t(t) * g.nx + j : int64_t(j) * g.nx + t;
+  // boundary flux of cell c (0 unless it is a cut cell), from its masked state
+  auto boundary_flux = [&](int c, const T* uc, double* fb) {
+    const int64_t ci = gcell(c);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) fb[k] = 0.0;
+    if (!g.cut[ci]) return;
+    C2T<T> ref;
+    ref.rho = NarrowTo<T>(a.s.refs[ci]);
+    ref.m[0] = NarrowTo<T>(a.s.refs[plane + ci]);
+    ref.m[1] = NarrowTo<T>(a.s.refs[2 * plane + ci]);
+    ref.E = NarrowTo<T>(a.s.refs[3 * plane + ci]);
+    ref.p = NarrowTo<T>(a.s.refs[4 * plane + ci]);
+    ref.c = NarrowTo<T>(a.s.refs[5 * plane + ci]);
+    C2T<T> q;
+    CompleteMasked(eq, q, uc, g.alpha[ci] > 0.0);
+    T f[4];
+    FluxT<M>(f, ref, dir);
+    const C2T<T> sol =
+        WallSolution(eq, q, NarrowTo<T>(g.normal[ci]), NarrowTo<T>(g.normal[plane + ci]));
+    AddMomentum(f, dir, sol.p - ref.p);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) fb[k] = Widen(f[k]);
+  };
+  double fbm[4], fb0[4], fbp[4];
+  boundary_flux(j - 1, u[1], fbm);
+  boundary_flux(j, u[2], fb0);
+  boundary_flux(j + 1, u[3], fbp);
+  const double xbm = g.center[int64_t(dir) * plane + gcell(j - 1)];
+  const double xb0 = g.center[int64_t(dir) * plane + gcell(j)];
+  const double xbp = g.center[int64_t(dir) * plane + gcell(j + 1)];
+  // face data of face f between cells with boundary fluxes fbL, fbR and
+  // centroids xbL, xbR (ComputeStableFluxComponents)
+  auto face = [&](FaceData& F, int f, const C2T<T>& L, const C2T<T>& R, const double* fbL,
+                  const double* fbR, double xbL, double xbR) {
+    const int64_t fi = g.FaceIndex(dir, f, t);
+    F.beta = g.beta[dir][fi];
+    F.us = g.us[dir][fi];
+    F.sL = g.sL[dir][fi];
+    F.sR = g.sR[dir][fi];
+    const double us_rel = g.us_rel[dir][fi];
+    const double sL_rel = g.sL_rel[dir][fi];
+    const double sR_rel = g.sR_rel[dir][fi];
+    if (F.beta > 0.0) {
+      T fl[4];
+      HllMasked(eq, fl, L, R, dir);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) F.f[k] = Widen(fl[k]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) F.f[k] = 0.0;
+    }
+    const double dL = Clamp01(0.5 - xbL);
+    const double dR = Clamp01(0.5 + xbR);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const double fk = F.f[k];
+      const double sLk = dL * fk + (1.0 - dL) * fbL[k];
+      const double sRk = dR * fk + (1.0 - dR) * fbR[k];
+      F.fsL[k] = sLk;
+      F.fsR[k] = sRk;
+      F.fs[k] = us_rel * fk + sL_rel * sLk + sR_rel * sRk;
+    }
+  };
+  FaceData Fl, Fr;
+  face(Fl, j, recRm, recL0, fbm, fb0, xbm, xb0);
+  face(Fr, j + 1, recR0, recLp, fb0, fbp, xb0, xbp);
+  // UpdateConservatively_Row for cell j (faces j and j+1)
+  const double alpha = al[2];
+  const double betaL = Fl.beta, betaR = Fr.beta;
+  const double center = xb0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    double next;
+    if (alpha == 0.0) {
+      next = 0.0;
+    } else {
+      const double prev = __ldg(a.s.in + k * cs + out);
+      const double fLs = Fl.fs[k], fRs = Fr.fs[k];
+      const double fLu = Fl.f[k], fRu = Fr.f[k];
+      if (betaL == betaR) {
+        next = prev + dt_dx * (fLs - fRs);
+      } else if (betaL > betaR) {
+        const double bus = Fl.us / alpha;
+        const double bsL = Fl.sL / alpha;
+        const double dist = 0.5 + center;
+        const double dBeta = Clamp01((Fl.sR * dist) / alpha);
+        const double dF_us = fLu - fRs;
+        const double dF_sL = Fl.fsL[k] - fRs;
+        const double dB = fLu - fb0[k];
+        next = prev + dt_dx * bus * dF_us + dt_dx * bsL * dF_sL + dt_dx * dBeta * dB;
+      } else {
+        const double bus = Fr.us / alpha;
+        const double bsR = Fr.sR / alpha;
+        const double dist = 0.5 - center;
+        const double dBeta = Clamp01((Fr.sL * dist) / alpha);
+        const double dF_us = fLs - fRu;
+        const double dF_sR = fLs - Fr.fsR[k];
+        const double dB = fb0[k] - fRu;
+        next = prev + dt_dx * bus * dF_us + dt_dx * bsR * dF_sR + dt_dx * dBeta * dB;
+      }
+    }
+    a.out[k * cs + out] = next;
+  }
+  if (alpha > 0.0 && __double_as_longlong(a.out[out]) <= 0) status |= kStatusNonPositiveDensity;
+}
+
+// The band cells of a KBN sweep (CcGeom::band), one thread per cell
+// (KbnCell, the full KBN arithmetic) with both of its faces' CFL speeds.  The
+// FP64 flavours evaluate every CFL speed of the band (their screened sweeps
+// give the same maximum), none in a step's first sweep.
+template <class T, class M>
+__global__ void __launch_bounds__(64, 1) KbnBandKernel(CcSweepArgs a) {
+  const CcGeom& g = a.s.g;
+  const int dir = a.dir;
+  const KbnConst<T, M>& kc = KbnBlockConst<T, M>(a);
+  if (!kc.run) return;  // block-uniform
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool cfl = !(sizeof(T) == 8 && a.skip_cfl != 0) && a.smax_out;
+  T smax = T(0);
+  int status = 0;
+  if (k < g.nband[dir]) {
+    const int id = g.band[dir][k];
+    const int i = id % g.nx, jj = id / g.nx;
+    KbnCell<T, M>(a, dir == 0 ? jj : i, dir == 0 ? i : jj, true, cfl, kc, smax, status);
+  }
+  const double smax_d = static_cast<double>(smax);
+  BlockMaxAtomic<1>(a.smax_out, &smax_d);
+  if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
+}
+
+// Class of cell c of grid line t for sweeps in direction dir (CcCellClass);
+// cells outside the interior count as band (neither written nor regular).
+__device__ __forceinline__ int CellClassAt(const CcGeom& g, int dir, int t, int c) {
+  const int nd = dir == 0 ? g.nx : g.ny;
+  if (c < 0 || c >= nd) return kCcBand;
+  const int64_t id = dir == 0 ? int64_t(t) * g.nx + c : int64_t(c) * g.nx + t;
+  return g.cell_class[dir][id];
+}
+
+// The regular and covered cells of a mixed-precision KBN sweep, staged in
+// shared memory.  A block takes 32 grid lines (one tile group) x 64 cells (8
+// tiles) along the sweep direction: it loads the masked FP32 states of the
+// cells and their 2-cell halos once (coalesced, one conversion per value;
+// the x sweep's lanes run along x) into shared memory, then each warp marches
+// one tile that holds a regular cell -- its lanes the 32 lines, each thread
+// 8 cells -- from shared memory: masked MUSCL-Hancock + HLL with every mask
+// true, f + 0 and U + dt/dx (fs_L - fs_R), the FP64 state re-read for the
+// update.  On a regular cell the KBN arithmetic is exactly this (the
+// stabilised flux us_rel f + sL_rel fsL + sR_rel fsR = 1 f + 0 fsL + 0 fsR is
+// f + 0 for every finite f; the + 0 turns a -0 into +0 as the zero terms
+// do), and its stencil (cells j-2 .. j+2) holds only regular-valued data, so
+// computing every cell of the tile this way and writing the regular ones is
+// exact.  Covered cells are written as 0; band cells are the band kernel's.
+// A face's CFL speed is counted here when one of its cells is regular.
+template <class T, class M>
+__global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
+  constexpr int kL = 32;                 // lines of a tile group
+  constexpr int kNSeg = 8;               // tiles per block
+  constexpr int kC = kCcTile * kNSeg;    // cells per block along dir
+  constexpr int kH = kC + 4;             // with the 2-cell halos
+  constexpr int kP = kL + 1;             // padded line stride (no bank conflicts)
+  __shared__ T su[4][kH][kP];
   const CcGeom& g = a.s.g;
   const int dir = a.dir;
   const int nd = dir == 0 ? g.nx : g.ny;
   const int nt = dir == 0 ? g.ny : g.nx;
-  // the warp's tile; warps beyond the list only join the block reduction
-  const int slot = static_cast<int>(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5));
-  const bool has_tile = slot < g.nband[dir];
-  const int tile_id = has_tile ? g.band[dir][slot] : 0;
-  const int group = tile_id / g.NTiles(dir), tile = tile_id % g.NTiles(dir);
-  const int64_t t64 = has_tile ? int64_t(group) * 32 + (threadIdx.x & 31) : int64_t(nt);
-  const int j0 = tile * kCcTile;
-  const int j1 = min(nd, j0 + kCcTile);
-  const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
-  if (!BlockAll(SweepGateCc(a, split_dt))) return;
+  const int ntl = g.NTiles(dir);
+  const int nsup = (ntl + kNSeg - 1) / kNSeg;
+  const int group = blockIdx.x / nsup, sup = blockIdx.x % nsup;
+  const int C0 = sup * kC;
+  const signed char* treg = g.tile_regular[dir] + int64_t(group) * ntl;
+  bool any_regular = false;  // block-uniform
+#pragma unroll
+  for (int k = 0; k < kNSeg; ++k) {
+    const int tl = sup * kNSeg + k;
+    any_regular = any_regular || (tl < ntl && treg[tl] != 0);
+  }
+  const KbnConst<T, M>& kc = KbnBlockConst<T, M>(a);
+  if (!kc.run) return;  // block-uniform
+  const GasT<T, M> eq = kc.eq;
+  if (any_regular) {
+    for (int idx = threadIdx.x; idx < kH * kL; idx += blockDim.x) {
+      int line, cell;
+      if (dir == 0) {
+        cell = idx % kH;
+        line = idx / kH;
+      } else {
+        line = idx % kL;
+        cell = idx / kL;
+      }
+      const int t = group * kL + line, c = C0 - 2 + cell;
+      T v[4] = {T(0), T(0), T(0), T(0)};
+      if (t < nt && c <= nd + 1) {
+        double vd[4];
+        if (dir == 0)
+          LoadCons(a.s, c, t, vd);
+        else
+          LoadCons(a.s, t, c, vd);
+        T w[4];
+        Narrow(w, vd);
+        C2T<T> q;
+        CompleteMasked(eq, q, w, true);
+        v[0] = q.rho;
+        v[1] = q.m[0];
+        v[2] = q.m[1];
+        v[3] = q.E;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) su[k][cell][line] = v[k];
+    }
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int tile = sup * kNSeg + warp;
+  const int t = group * kL + lane;
+  const int c0 = tile * kCcTile, c1 = min(nd, c0 + kCcTile);
+  const int64_t cs = int64_t(g.nx) * g.ny;
+  auto offset = [&](int c) {
+    return dir == 0 ? int64_t(t) * g.nx + c : int64_t(c) * g.nx + t;
+  };
   T smax = T(0);
   int status = 0;
-  // CFL speeds: none in a step's first sweep (skip_cfl: the stable-dt pass
-  // measured the same faces of the same state); in FP64 flavours screened in
-  // FP32 as the uniform sweeps do (fvs_sweep.cuh, FilteredCfl), with the
-  // masked states and faces of beta > 0
-  constexpr bool kScreen = sizeof(T) == 8;
-  const bool skip_cfl = kScreen && a.skip_cfl != 0;
-  const bool screen = kScreen && a.s.gamma > 1.0 && a.s.gamma <= 2.0;
-  const unsigned amask = __ballot_sync(0xffffffffu, t64 < nt);
-  if (t64 < nt) {
-    const int t = static_cast<int>(t64);
-    const GasT<T, M> eq = MakeGasT<T, M>(a.s.gamma);
-    const double dx = a.dx;
-    const T lambda_half = NarrowTo<T>(0.5 * split_dt / dx);
-    const double dt_dx = split_dt / dx;
-    const int64_t plane = int64_t(g.NX()) * g.NY();
-    const int64_t cs = int64_t(g.nx) * g.ny;
-    auto cell_ij = [&](int c, int& i, int& j) {
-      if (dir == 0) {
-        i = c;
-        j = t;
-      } else {
-        i = t;
-        j = c;
-      }
-    };
-    // masked complete state (alpha > 0 and rho > 0) of cell c
-    auto load_cell = [&](int c, T* u, double& alpha) {
-      int i, j;
-      cell_ij(c, i, j);
-      double vd[4];
-      LoadCons(a.s, i, j, vd);
-      T v[4];
-      Narrow(v, vd);
-      alpha = g.alpha[g.CellIndex(i, j)];
-      C2T<T> q;
-      CompleteMasked(eq, q, v, alpha > 0.0);
-      u[0] = q.rho;
-      u[1] = q.m[0];
-      u[2] = q.m[1];
-      u[3] = q.E;
-    };
-    // boundary flux of cell c (0 unless it is a cut cell)
-    auto boundary_flux = [&](int c, const T* u, double* fb) {
-      int i, j;
-      cell_ij(c, i, j);
-      const int64_t ci = g.CellIndex(i, j);
+  if (tile < ntl && t < nt) {
+    if (treg[tile] == 0) {
+      for (int c = c0; c < c1; ++c)
+        if (CellClassAt(g, dir, t, c) == kCcCovered) {
+          const int64_t o = offset(c);
 #pragma unroll
-      for (int k = 0; k < 4; ++k) fb[k] = 0.0;
-      if (!g.cut[ci]) return;
-      C2T<T> ref;
-      ref.rho = NarrowTo<T>(a.s.refs[ci]);
-      ref.m[0] = NarrowTo<T>(a.s.refs[plane + ci]);
-      ref.m[1] = NarrowTo<T>(a.s.refs[2 * plane + ci]);
-      ref.E = NarrowTo<T>(a.s.refs[3 * plane + ci]);
-      ref.p = NarrowTo<T>(a.s.refs[4 * plane + ci]);
-      ref.c = NarrowTo<T>(a.s.refs[5 * plane + ci]);
-      C2T<T> q;
-      CompleteMasked(eq, q, u, g.alpha[ci] > 0.0);
-      T f[4];
-      FluxT<M>(f, ref, dir);
-      const C2T<T> sol =
-          WallSolution(eq, q, NarrowTo<T>(g.normal[ci]), NarrowTo<T>(g.normal[plane + ci]));
-      f[1 + dir] += sol.p - ref.p;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) fb[k] = Widen(f[k]);
-    };
-    auto center_of = [&](int c) {
-      int i, j;
-      cell_ij(c, i, j);
-      return g.center[int64_t(dir) * plane + g.CellIndex(i, j)];
-    };
-    T um[4], uc[4], up[4];
-    double am, ac, ap;
-    load_cell(j0 - 2, um, am);
-    load_cell(j0 - 1, uc, ac);
-    C2T<T> recR_prev;
-    double fb_prev[4];
-    double xb_prev = 0.0;
-    C2T<T> q_prev;
-    FaceData F_prev;
-    fast::Gas<float> g32;
-    g32.gamma = static_cast<float>(a.s.gamma);
-    g32.gm1 = static_cast<float>(a.s.gamma - 1.0);
-    fast::Wave<float> v_prev{};
-    bool ok_prev = false;
-    bool have_prev = false;  // q_prev holds the complete state of cell j-1
-    float thr = 0.0f;
-    if (kScreen && !skip_cfl && a.smax_out)
-      thr = CflFloatBelow(CflSync(a.smax_out, 0.0, amask));
-    for (int j = j0 - 1; j <= j1; ++j) {
-      load_cell(j + 1, up, ap);
-      const bool smask = am > 0.0 && ac > 0.0 && ap > 0.0;
-      C2T<T> recL, recR;
-      PredictMasked(eq, recL, recR, um, uc, up, smask, a.limiter, lambda_half, dir);
-      double fb[4];
-      boundary_flux(j, uc, fb);
-      const double xb = center_of(j);
-      C2T<T> q;
-      fast::Wave<float> v{};
-      bool ok = false;
-      if constexpr (kScreen) {
-        if (!skip_cfl) {
-          float c32[4];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) c32[k] = CflToF32(uc[k]);
-          v = fast::MakeWave<2, float>(g32, c32, dir);
-          ok = screen && CflInRange<2>(c32) && v.a > 0.0f;
+          for (int k = 0; k < 4; ++k) a.out[k * cs + o] = 0.0;
         }
-      } else {
-        CompleteMasked(eq, q, uc, true);  // uc is already masked by alpha
-      }
-      if (j >= j0) {
-        FaceData F;
-        const int64_t fi = g.FaceIndex(dir, j, t);
-        F.beta = g.beta[dir][fi];
-        F.us = g.us[dir][fi];
-        F.sL = g.sL[dir][fi];
-        F.sR = g.sR[dir][fi];
-        const double us_rel = g.us_rel[dir][fi];
-        const double sL_rel = g.sL_rel[dir][fi];
-        const double sR_rel = g.sR_rel[dir][fi];
-        if constexpr (kScreen) {
-          if (!skip_cfl) {
-            bool need = false;
-            if (F.beta > 0.0) {
-              const float s32 = fast::FaceMaxSpeed<float>(g32, v_prev, v);
-              const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
-              need = !(ok && ok_prev && fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs)) < thr);
-            }
-            if (__any_sync(amask, need)) {
-              // the whole warp evaluates (the same instructions as some lanes)
-              if (!have_prev) CompleteMasked(eq, q_prev, um, true);
-              CompleteMasked(eq, q, uc, true);
-              if (F.beta > 0.0) {
-                T s0, s1;
-                EinfeldtMasked(eq, q_prev, q, dir, s0, s1);
-                const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
-                smax = mx > smax ? mx : smax;
-              }
-              thr = fmaxf(thr, CflFloatBelow(static_cast<double>(smax)));
-              q_prev = q;
-              have_prev = true;
-            } else {
-              have_prev = false;
-            }
-            if (a.smax_out && ((j - j0) % kCflSyncRows) == kCflSyncRows - 1)
-              thr = fmaxf(thr, CflFloatBelow(CflSync(a.smax_out, static_cast<double>(smax),
-                                                     amask)));
-          }
-        }
-        if (F.beta > 0.0) {
+    } else {
+      const T lambda_half = kc.lambda_half;
+      const double dt_dx = kc.dt_dx;
+      auto fetch = [&](int c, T* u) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) u[k] = su[k][c - C0 + 2][lane];
+      };
+      T um[4], uc[4], up[4];
+      fetch(c0 - 2, um);
+      fetch(c0 - 1, uc);
+      C2T<T> recR_prev, q_prev;
+      double fs_prev[4];
+      int cls_prev = CellClassAt(g, dir, t, c0 - 1);
+      for (int j = c0 - 1; j <= c1; ++j) {
+        fetch(j + 1, up);
+        C2T<T> recL, recR;
+        PredictMasked(eq, recL, recR, um, uc, up, true, a.limiter, lambda_half, dir);
+        C2T<T> q;
+        CompleteMasked(eq, q, uc, true);
+        if (j >= c0) {
+          const int cls = CellClassAt(g, dir, t, j);
           T f[4];
           HllMasked(eq, f, recR_prev, recL, dir);
-#pragma unroll
-          for (int k = 0; k < 4; ++k) F.f[k] = Widen(f[k]);
-          if constexpr (!kScreen) {
-            T s0, s1;
-            EinfeldtMasked(eq, q_prev, q, dir, s0, s1);
-            const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
+          if (cls == kCcRegular || cls_prev == kCcRegular) {
+            T s0w, s1w;
+            EinfeldtMasked(eq, q_prev, q, dir, s0w, s1w);
+            const T mx = PMaxT(PMaxT(T(0), fabs(s0w)), fabs(s1w));
             smax = mx > smax ? mx : smax;
           }
-        } else {
+          double fs[4];
 #pragma unroll
-          for (int k = 0; k < 4; ++k) F.f[k] = 0.0;
+          for (int k = 0; k < 4; ++k) fs[k] = Widen(f[k] + T(0));
+          if (j > c0 && cls_prev != kCcBand) {
+            // cell j-1: regular, or covered (0)
+            const int64_t o = offset(j - 1);
+            if (cls_prev == kCcRegular) {
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                const double prev = __ldg(a.s.in + k * cs + o);
+                a.out[k * cs + o] = prev + dt_dx * (fs_prev[k] - fs[k]);
+              }
+              if (__double_as_longlong(a.out[o]) <= 0) status |= kStatusNonPositiveDensity;
+            } else {
+#pragma unroll
+              for (int k = 0; k < 4; ++k) a.out[k * cs + o] = 0.0;
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 4; ++k) fs_prev[k] = fs[k];
+          cls_prev = cls;
         }
-        const double dL = Clamp01(0.5 - xb_prev);
-        const double dR = Clamp01(0.5 + xb);
+        recR_prev = recR;
+        q_prev = q;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-          const double fk = F.f[k];
-          const double sLk = dL * fk + (1.0 - dL) * fb_prev[k];
-          const double sRk = dR * fk + (1.0 - dR) * fb[k];
-          F.fsL[k] = sLk;
-          F.fsR[k] = sRk;
-          F.fs[k] = us_rel * fk + sL_rel * sLk + sR_rel * sRk;
+          um[k] = uc[k];
+          uc[k] = up[k];
         }
-        if (j > j0) {
-          // cut-cell update of cell j-1 (faces j-1 and j)
-          const int c = j - 1;
-          int i, jj;
-          cell_ij(c, i, jj);
-          const int64_t out = int64_t(jj) * g.nx + i;
-          const double alpha = am;  // alpha of cell j-1
-          const double betaL = F_prev.beta, betaR = F.beta;
-          const double center = xb_prev;
-#pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            double next;
-            if (alpha == 0.0) {
-              next = 0.0;
-            } else {
-              const double prev = __ldg(a.s.in + k * cs + out);
-              const double fLs = F_prev.fs[k], fRs = F.fs[k];
-              const double fLu = F_prev.f[k], fRu = F.f[k];
-              if (betaL == betaR) {
-                next = prev + dt_dx * (fLs - fRs);
-              } else if (betaL > betaR) {
-                const double bus = F_prev.us / alpha;
-                const double bsL = F_prev.sL / alpha;
-                const double dist = 0.5 + center;
-                const double dBeta = Clamp01((F_prev.sR * dist) / alpha);
-                const double dF_us = fLu - fRs;
-                const double dF_sL = F_prev.fsL[k] - fRs;
-                const double dB = fLu - fb_prev[k];
-                next = prev + dt_dx * bus * dF_us + dt_dx * bsL * dF_sL + dt_dx * dBeta * dB;
-              } else {
-                const double bus = F.us / alpha;
-                const double bsR = F.sR / alpha;
-                const double dist = 0.5 - center;
-                const double dBeta = Clamp01((F.sL * dist) / alpha);
-                const double dF_us = fLs - fRu;
-                const double dF_sR = fLs - F.fsR[k];
-                const double dB = fb_prev[k] - fRu;
-                next = prev + dt_dx * bus * dF_us + dt_dx * bsR * dF_sR + dt_dx * dBeta * dB;
-              }
-            }
-            a.out[k * cs + out] = next;
-          }
-          if (alpha > 0.0 && __double_as_longlong(a.out[out]) <= 0)
-            status |= kStatusNonPositiveDensity;
-        }
-        F_prev = F;
       }
-      recR_prev = recR;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) fb_prev[k] = fb[k];
-      xb_prev = xb;
-      if constexpr (!kScreen) q_prev = q;
-      ok_prev = ok;
-      v_prev = v;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        um[k] = uc[k];
-        uc[k] = up[k];
-      }
-      am = ac;
-      ac = ap;
     }
   }
   const double smax_d = static_cast<double>(smax);
@@ -648,17 +798,14 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnSweepKernel(CcSweepArgs a)
   if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
 }
 
-// The regular and covered tiles of a KBN sweep (CcTileClass).  On a regular
-// tile the KBN arithmetic reduces, bit for bit, to the masked MUSCL-Hancock
-// predictor and masked HLL flux with every mask true, the stabilised flux
-// us_rel f + sL_rel fsL + sR_rel fsR = 1 f + 0 fsL + 0 fsR = f + 0 (for every
-// finite f; the + 0 turns a -0 into +0 as the zero terms do), and the update
-// U + dt/dx (fs_L - fs_R) of cells with equal face fractions
-// (src/AMReX/cutcell/TimeIntegrator.cpp:65-221): the kernel evaluates exactly
-// that, from the same inline functions, and reads no geometry.  A covered
-// tile's cells are 0 and its faces (beta 0) add no CFL speed.  Each thread
-// marches the runs of consecutive regular tiles of its segment of one grid
-// line; the tile class is the warp's, so the control flow is warp-uniform.
+// The regular and covered cells of a KBN sweep in the FP64 flavours (bound by
+// the FP64 pipe): each thread marches the runs of consecutive tiles with a
+// regular cell in its segment of one grid line, one predictor per cell, with
+// the arithmetic and the regular-cell argument of KbnRegularTileKernel; the
+// CFL speeds are screened in FP32 as in the uniform sweeps (FilteredCfl,
+// fvs_sweep.cuh), none in a step's first sweep.  Tiles without a regular
+// cell only write their covered cells (0).  The tile flag is the warp's, so
+// the control flow is warp-uniform.
 template <class T, class M, int kMinBlocks>
 __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweepArgs a) {
   const CcGeom& g = a.s.g;
@@ -669,8 +816,8 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
   const int group = static_cast<int>(t64 >> 5);
   const int s0 = blockIdx.y * a.seg_len;  // a multiple of kCcTile
   const int s1 = min(nd, s0 + a.seg_len);
-  const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
-  if (!BlockAll(SweepGateCc(a, split_dt))) return;
+  const KbnConst<T, M>& kc = KbnBlockConst<T, M>(a);
+  if (!kc.run) return;  // block-uniform
   T smax = T(0);
   int status = 0;
   constexpr bool kScreen = sizeof(T) == 8;
@@ -679,16 +826,17 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
   const unsigned amask = __ballot_sync(0xffffffffu, t64 < nt);
   if (t64 < nt) {
     const int t = static_cast<int>(t64);
-    const GasT<T, M> eq = MakeGasT<T, M>(a.s.gamma);
-    const T lambda_half = NarrowTo<T>(0.5 * split_dt / a.dx);
-    const double dt_dx = split_dt / a.dx;
+    const GasT<T, M> eq = kc.eq;
+    const T lambda_half = kc.lambda_half;
+    const double dt_dx = kc.dt_dx;
     const int64_t cs = int64_t(g.nx) * g.ny;
     const int ntl = g.NTiles(dir);
-    const signed char* cls = g.tile_class[dir] + int64_t(group) * ntl;
+    const signed char* treg = g.tile_regular[dir] + int64_t(group) * ntl;
     auto offset = [&](int c) {
       return dir == 0 ? int64_t(t) * g.nx + c : int64_t(c) * g.nx + t;
     };
-    // masked state of cell c (alpha 1: zeroed only where rho <= 0)
+    // state of cell c masked as on a regular cell (alpha 1: zeroed only where
+    // rho <= 0)
     auto load_cell = [&](int c, T* u) {
       double vd[4];
       if (dir == 0)
@@ -714,23 +862,19 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
     const int tile_end = (s1 + kCcTile - 1) / kCcTile;
     int tile = s0 / kCcTile;
     while (tile < tile_end) {
-      const int k = cls[tile];
-      if (k == kCcCut) {
-        ++tile;
-        continue;
-      }
-      if (k == kCcCovered) {
+      if (treg[tile] == 0) {
         const int c1 = min(nd, (tile + 1) * kCcTile);
-        for (int c = tile * kCcTile; c < c1; ++c) {
-          const int64_t o = offset(c);
+        for (int c = tile * kCcTile; c < c1; ++c)
+          if (CellClassAt(g, dir, t, c) == kCcCovered) {
+            const int64_t o = offset(c);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) a.out[q * cs + o] = 0.0;
-        }
+            for (int q = 0; q < 4; ++q) a.out[q * cs + o] = 0.0;
+          }
         ++tile;
         continue;
       }
       int r1 = tile + 1;
-      while (r1 < tile_end && cls[r1] == kCcRegular) ++r1;
+      while (r1 < tile_end && treg[r1] != 0) ++r1;
       const int j0 = tile * kCcTile, j1 = min(nd, r1 * kCcTile);
       tile = r1;
       // march the run [j0, j1): faces j0 .. j1, cells j0 .. j1-1
@@ -742,6 +886,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
       fast::Wave<float> v_prev{};
       bool ok_prev = false;
       bool have_prev = false;
+      int cls_prev = CellClassAt(g, dir, t, j0 - 1);
       for (int j = j0 - 1; j <= j1; ++j) {
         load_cell(j + 1, up);
         C2T<T> recL, recR;
@@ -761,19 +906,26 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
           CompleteMasked(eq, q, uc, true);
         }
         if (j >= j0) {
+          const int cls = CellClassAt(g, dir, t, j);
+          const bool count = cls == kCcRegular || cls_prev == kCcRegular;
           if constexpr (kScreen) {
             if (!skip_cfl) {
-              const float s32 = fast::FaceMaxSpeed<float>(g32, v_prev, v);
-              const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
-              const bool need =
-                  !(ok && ok_prev && fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs)) < thr);
+              bool need = false;
+              if (count) {
+                const float s32 = fast::FaceMaxSpeed<float>(g32, v_prev, v);
+                const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
+                need = !(ok && ok_prev &&
+                         fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs)) < thr);
+              }
               if (__any_sync(amask, need)) {
                 if (!have_prev) CompleteMasked(eq, q_prev, um, true);
                 CompleteMasked(eq, q, uc, true);
-                T s0w, s1w;
-                EinfeldtMasked(eq, q_prev, q, dir, s0w, s1w);
-                const T mx = PMaxT(PMaxT(T(0), fabs(s0w)), fabs(s1w));
-                smax = mx > smax ? mx : smax;
+                if (count) {
+                  T s0w, s1w;
+                  EinfeldtMasked(eq, q_prev, q, dir, s0w, s1w);
+                  const T mx = PMaxT(PMaxT(T(0), fabs(s0w)), fabs(s1w));
+                  smax = mx > smax ? mx : smax;
+                }
                 thr = fmaxf(thr, CflFloatBelow(static_cast<double>(smax)));
                 q_prev = q;
                 have_prev = true;
@@ -791,24 +943,32 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
           HllMasked(eq, f, recR_prev, recL, dir);
           double fs[4];
 #pragma unroll
-          for (int c = 0; c < 4; ++c) fs[c] = Widen(f[c]) + 0.0;
+          for (int c = 0; c < 4; ++c) fs[c] = Widen(f[c] + T(0));
           if constexpr (!kScreen) {
-            T s0w, s1w;
-            EinfeldtMasked(eq, q_prev, q, dir, s0w, s1w);
-            const T mx = PMaxT(PMaxT(T(0), fabs(s0w)), fabs(s1w));
-            smax = mx > smax ? mx : smax;
-          }
-          if (j > j0) {
-            const int64_t o = offset(j - 1);
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              const double prev = __ldg(a.s.in + c * cs + o);
-              a.out[c * cs + o] = prev + dt_dx * (fs_prev[c] - fs[c]);
+            if (count) {
+              T s0w, s1w;
+              EinfeldtMasked(eq, q_prev, q, dir, s0w, s1w);
+              const T mx = PMaxT(PMaxT(T(0), fabs(s0w)), fabs(s1w));
+              smax = mx > smax ? mx : smax;
             }
-            if (__double_as_longlong(a.out[o]) <= 0) status |= kStatusNonPositiveDensity;
+          }
+          if (j > j0 && cls_prev != kCcBand) {
+            const int64_t o = offset(j - 1);
+            if (cls_prev == kCcRegular) {
+#pragma unroll
+              for (int c = 0; c < 4; ++c) {
+                const double prev = __ldg(a.s.in + c * cs + o);
+                a.out[c * cs + o] = prev + dt_dx * (fs_prev[c] - fs[c]);
+              }
+              if (__double_as_longlong(a.out[o]) <= 0) status |= kStatusNonPositiveDensity;
+            } else {
+#pragma unroll
+              for (int c = 0; c < 4; ++c) a.out[c * cs + o] = 0.0;
+            }
           }
 #pragma unroll
           for (int c = 0; c < 4; ++c) fs_prev[c] = fs[c];
+          cls_prev = cls;
         }
         recR_prev = recR;
         if constexpr (!kScreen) q_prev = q;
@@ -835,11 +995,12 @@ __global__ void KbnStableDtKernel(CcStateArgs a, unsigned long long* smax_out, C
   const CcGeom& g = a.g;
   const int w = g.nx + 1, h = g.ny + 1;
   T sm[2] = {T(0), T(0)};
+  const GasT<T, M> eq = MakeGasT<T, M>(a.gamma);
   // grid-stride over faces; one atomic per block and direction at the end
   for (int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; id < int64_t(w) * h;
        id += int64_t(gridDim.x) * blockDim.x) {
     const int i = static_cast<int>(id % w), j = static_cast<int>(id / w);
-    const GasT<T, M> eq = MakeGasT<T, M>(a.gamma);
+#pragma unroll
     for (int d = 0; d < 2; ++d) {
       const int f = d == 0 ? i : j;
       const int t = d == 0 ? j : i;
@@ -879,25 +1040,25 @@ cudaError_t LaunchKbnSweep(const CcSweepArgs& a, bool band, cudaStream_t s) {
   const int nd = a.dir == 0 ? a.s.g.nx : a.s.g.ny;
   const int nt = a.dir == 0 ? a.s.g.ny : a.s.g.nx;
   if (band) {
-    // cut tiles: one warp each; register/occupancy variant: the default, or
-    // compiled for 3 (FP64) / 4 (FP32) resident 128-thread blocks per SM
-    // (spilling a little)
     const int n = a.s.g.nband[a.dir];
-    if (n == 0) return cudaSuccess;
-    constexpr int kMore = sizeof(T) == 4 ? 4 : 3;
-    if (a.occupancy == kMore)
-      KbnSweepKernel<T, M, kMore><<<unsigned(n), 32, 0, s>>>(a);
-    else
-      KbnSweepKernel<T, M, 1><<<unsigned(n), 32, 0, s>>>(a);
+    if (n > 0) KbnBandKernel<T, M><<<unsigned((n + 63) / 64), 64, 0, s>>>(a);
     return cudaGetLastError();
   }
-  const int block = 128;
-  int seg = a.seg_len > 0 ? a.seg_len : nd;
-  seg = (seg + kCcTile - 1) / kCcTile * kCcTile;
-  CcSweepArgs b = a;
-  b.seg_len = seg;
-  dim3 grid(unsigned((nt + block - 1) / block), unsigned((nd + seg - 1) / seg));
-  KbnRegularSweepKernel<T, M, sizeof(T) == 4 ? 4 : 3><<<grid, block, 0, s>>>(b);
+  if constexpr (sizeof(T) == 4) {
+    // mixed: tiles staged in shared memory, 32 lines x 64 cells per block
+    const int64_t blocks = int64_t(a.s.g.NGroups(a.dir)) * ((a.s.g.NTiles(a.dir) + 7) / 8);
+    if (blocks > 0) KbnRegularTileKernel<T, M><<<unsigned(blocks), 256, 0, s>>>(a);
+  } else {
+    // FP64 flavours (bound by the FP64 pipe): threads march runs of tiles,
+    // one predictor per cell
+    const int block = 128;
+    int seg = a.seg_len > 0 ? a.seg_len : nd;
+    seg = (seg + kCcTile - 1) / kCcTile * kCcTile;
+    CcSweepArgs b = a;
+    b.seg_len = seg;
+    dim3 grid(unsigned((nt + block - 1) / block), unsigned((nd + seg - 1) / seg));
+    KbnRegularSweepKernel<T, M, 3><<<grid, block, 0, s>>>(b);
+  }
   return cudaGetLastError();
 }
 

@@ -141,38 +141,50 @@ __global__ void CutFlagKernel(CcGeom g) {
   g.cut[id] = static_cast<signed char>(cut);
 }
 
-// Class of the tile (group, tile) of direction d (CcTileClass): one block of
-// 32 threads, one per line of the group; lines beyond the grid agree with
-// every class.
-__global__ void TileClassKernel(CcGeom g, int d) {
+// Class of interior cell (i, j) for sweeps in direction d (CcCellClass).
+__global__ void CellClassKernel(CcGeom g, int d) {
+  const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (id >= int64_t(g.nx) * g.ny) return;
+  const int i = static_cast<int>(id % g.nx), jj = static_cast<int>(id / g.nx);
+  const int t = d == 0 ? jj : i;  // grid line
+  const int j = d == 0 ? i : jj;  // cell along d
+  auto cell = [&](int c) { return d == 0 ? g.CellIndex(c, t) : g.CellIndex(t, c); };
+  signed char k;
+  if (g.alpha[cell(j)] == 0.0) {
+    k = kCcCovered;
+  } else {
+    bool regular = true;
+    for (int c = j - 2; c <= j + 2; ++c) {
+      regular = regular && g.alpha[cell(c)] == 1.0;
+      if (c >= j - 1 && c <= j + 1) regular = regular && g.cut[cell(c)] == 0;
+    }
+    for (int f = j; f <= j + 1; ++f) {
+      const int64_t fi = g.FaceIndex(d, f, t);
+      regular = regular && g.beta[d][fi] == 1.0 && g.us_rel[d][fi] == 1.0 &&
+                g.sL_rel[d][fi] == 0.0 && g.sR_rel[d][fi] == 0.0;
+    }
+    k = regular ? kCcRegular : kCcBand;
+  }
+  g.cell_class[d][id] = k;
+}
+
+// Whether the tile (group, tile) of direction d holds a regular cell: one
+// block of 32 threads, one per line of the group.
+__global__ void TileRegularKernel(CcGeom g, int d) {
   const int ntl = g.NTiles(d);
   const int group = blockIdx.x / ntl, tile = blockIdx.x % ntl;
   const int nd = d == 0 ? g.nx : g.ny;
   const int nt = d == 0 ? g.ny : g.nx;
   const int t = group * 32 + static_cast<int>(threadIdx.x);
   const int c0 = tile * kCcTile, c1 = min(nd, c0 + kCcTile);
-  bool regular = true, covered = true;
-  if (t < nt) {
-    auto cell = [&](int c) { return d == 0 ? g.CellIndex(c, t) : g.CellIndex(t, c); };
-    for (int c = c0 - 2; c <= c1 + 1; ++c) {
-      const int64_t ci = cell(c);
-      const double a = g.alpha[ci];
-      regular = regular && a == 1.0;
-      if (c >= c0 - 1 && c <= c1) regular = regular && g.cut[ci] == 0;
-      if (c >= c0 && c < c1) covered = covered && a == 0.0;
+  bool any = false;
+  if (t < nt)
+    for (int c = c0; c < c1; ++c) {
+      const int64_t id = d == 0 ? int64_t(t) * g.nx + c : int64_t(c) * g.nx + t;
+      any = any || g.cell_class[d][id] == kCcRegular;
     }
-    for (int f = c0; f <= c1; ++f) {
-      const int64_t fi = g.FaceIndex(d, f, t);
-      const double b = g.beta[d][fi];
-      regular = regular && b == 1.0 && g.us_rel[d][fi] == 1.0 && g.sL_rel[d][fi] == 0.0 &&
-                g.sR_rel[d][fi] == 0.0;
-      covered = covered && !(b > 0.0);
-    }
-  }
-  regular = __all_sync(0xffffffffu, regular);
-  covered = __all_sync(0xffffffffu, covered);
-  if (threadIdx.x == 0)
-    g.tile_class[d][blockIdx.x] = regular ? kCcRegular : (covered ? kCcCovered : kCcCut);
+  any = __any_sync(0xffffffffu, any);
+  if (threadIdx.x == 0) g.tile_regular[d][blockIdx.x] = any ? 1 : 0;
 }
 
 }  // namespace cc
@@ -180,9 +192,11 @@ __global__ void TileClassKernel(CcGeom g, int d) {
 // ---------------------------------------------------------------------------
 // Launchers
 
-cudaError_t LaunchCutCellTileClass(const CcGeom& g, int d, cudaStream_t s) {
+cudaError_t LaunchCutCellClasses(const CcGeom& g, int d, cudaStream_t s) {
+  const int64_t cells = int64_t(g.nx) * g.ny;
+  if (cells > 0) cc::CellClassKernel<<<unsigned((cells + 127) / 128), 128, 0, s>>>(g, d);
   const int64_t n = int64_t(g.NGroups(d)) * g.NTiles(d);
-  if (n > 0) cc::TileClassKernel<<<unsigned(n), 32, 0, s>>>(g, d);
+  if (n > 0) cc::TileRegularKernel<<<unsigned(n), 32, 0, s>>>(g, d);
   return cudaGetLastError();
 }
 

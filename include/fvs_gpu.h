@@ -263,11 +263,10 @@ int fvs_solver_set_tiling(fvs_solver* s, int seg_len);
  * seg_out (may be NULL) receives rank values.  Does not change the state. */
 int fvs_solver_autotune(fvs_solver* s, int* seg_out);
 /* The tuned segment lengths and occupancy variants per direction: 0 =
- * registers as needed, 3 (double-float; cut cells in FP64), 4 or 5 (mixed;
- * 4 for cut cells in mixed precision) = compiled for that many resident
- * 128-thread blocks per SM; for mixed x sweeps 10 + v = variant v with the
- * marching kernel instead of the lanes-along-x kernel.  Either pointer may be
- * NULL. */
+ * registers as needed, 3 (double-float), 4 or 5 (mixed) = compiled for that
+ * many resident 128-thread blocks per SM; for mixed x sweeps 10 + v = variant
+ * v with the marching kernel instead of the lanes-along-x kernel.  Grids with
+ * cut cells have variant 0 only.  Either pointer may be NULL. */
 int fvs_solver_tuning(fvs_solver* s, int32_t* seg, int32_t* occupancy);
 /* Forces the launch shape of direction dir, as fvs_solver_autotune would set
  * it: segment length (0 = automatic) and variant (the occupancy codes above;

@@ -64,7 +64,7 @@ def test_sweeps_bit_exact(fvs, orc, n, circles):
     s.close()
 
 
-@pytest.mark.parametrize("launch", ["default", "tuned", "occupancy3"])
+@pytest.mark.parametrize("launch", ["default", "tuned", "seg32"])
 def test_shock_over_circles_run_bit_exact(fvs, orc, launch):
     n = 96
     circles, cons = workloads.shock_circles_2d(n, seed=5)
@@ -73,9 +73,11 @@ def test_shock_over_circles_run_bit_exact(fvs, orc, launch):
     s.upload(cons)
     if launch == "tuned":  # timed on the live state, which it leaves unchanged
         s.autotune()
-    elif launch == "occupancy3":  # the KBN sweep built for 3 blocks per SM
-        s.set_launch(0, 16, 3)
-        s.set_launch(1, 32, 3)
+    elif launch == "seg32":  # regular-cell segments of 32 cells (FP64 flavours)
+        s.set_launch(0, 32, 0)
+        s.set_launch(1, 32, 0)
+        with pytest.raises(fvs.FvsError):
+            s.set_launch(1, 32, 3)  # cut-cell grids have no occupancy variants
     st, dts = s.run(cfl=0.5, t_end=10.0, max_steps=6, log_len=8)
     out, ref_dts, rs = ref.run(cons, 0.5, 10.0, max_steps=6)
     assert st.steps == 6 and st.restarts == rs
@@ -95,7 +97,9 @@ def test_flavours_track_exact_and_conserve(fvs, orc, prec, variant):
     FP32 reconstruction error.  Periodic in x and y with the body inside the
     domain: the volume-weighted mass and energy change only through the FP64
     round-off of the cut-cell update (the wall flux carries no mass or
-    energy); 1e-11 relative over 10 steps of 16k cells."""
+    energy); 1e-11 relative over 10 steps of 16k cells.  variant: segments of
+    24 cells (rounded up to whole tiles of 8) for the FP64 flavours'
+    regular-cell sweep."""
     n = 128
     circles = np.array([[0.5, 0.5, 0.15], [0.3, 0.7, 0.08]])
     cons = workloads.random_state((n, n), 2, seed=9).reshape(4, 1, n, n)
@@ -109,9 +113,9 @@ def test_flavours_track_exact_and_conserve(fvs, orc, prec, variant):
     st_e, dts_e = ex.run(cfl=0.5, t_end=10.0, max_steps=10, log_len=10)
     s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "periodic", method=fvs.make_method(precision=prec))
     s.set_embedded_circles(circles)
-    if variant:  # the KBN sweep's higher-occupancy build
+    if variant:
         for d in (0, 1):
-            s.set_launch(d, 32, 4 if prec == "mixed" else 3)
+            s.set_launch(d, 24, 0)
     s.upload(cons)
     st, dts = s.run(cfl=0.5, t_end=10.0, max_steps=10, log_len=10)
     out, ref = s.download(), ex.download()
