@@ -33,10 +33,10 @@ __all__ = ["PerfectGas", "FluxMethod", "HyperbolicPatchIntegrator", "CompleteFro
 
 FLUX_METHODS = {"muscl_hlle": 0, "hlle": 1, "godunov": 2, "muscl_godunov": 3, "hllem": 4,
                 "muscl_hllem": 5, "muscl_char": 6, "muscl_prim": 7}
-LIMITERS = {"van_leer": 0, "minmod": 1, "none": 2}
+LIMITERS = {"van_leer": 0, "minmod": 1, "none": 2, "no_limiter": 2, "no_gradient": 3}
 PRECISIONS = {"fp64_exact": 0, "fp64_fast": 1, "mixed": 2, "fp64_df": 3}
 GUESSES = {"mean": 0, "pvrs_tr": 1, "mlp": 2}
-BCS = {"periodic": 0, "transmissive": 1}
+BCS = {"periodic": 0, "transmissive": 1, "reflective": 2}
 
 
 def lib() -> C.CDLL:

@@ -131,8 +131,11 @@ struct fvs_amr {
     const PatchHost& P = patches[size_t(p)];
     return P.block_start + (j - P.lo[1] + kGhost) * P.pitch + (i - P.lo[0] + kGhost);
   }
+  // level coordinate x of a direction of n cells mapped into the domain:
+  // periodic wrap, transmissive clamp, reflective mirror (ReflectIndex)
   int MapCoord(int x, int n, int d) const {
     if (bc[d] == 0) return ((x % n) + n) % n;
+    if (bc[d] == 2) return x < 0 ? -1 - x : (x >= n ? 2 * n - 1 - x : x);
     return x < 0 ? 0 : (x >= n ? n - 1 : x);
   }
 };
@@ -251,9 +254,12 @@ int Build(fvs_amr* a) {
         for (int t = 0; t < nt; ++t) {
           Row& r = rows_h[d][size_t(l)][size_t(P.row_offset[d] + t)];
           const int pos[4] = {-2, -1, nd, nd + 1};
+          r.flip = 0;
           for (int h = 0; h < 4; ++h) {
             const int li = d == 0 ? pos[h] : t, lj = d == 0 ? t : pos[h];
             if (int e = src_of(li, lj, r.halo[h])) return e;
+            const int g = P.lo[d] + pos[h];
+            if (a->bc[d] == FVS_BC_REFLECTIVE && (g < 0 || g >= L.n[d])) r.flip |= 1 << h;
           }
         }
       }
@@ -286,7 +292,7 @@ int Build(fvs_amr* a) {
             const int gj = P.lo[1] + (d == 0 ? t : x_in);
             int oi = gi + (d == 0 ? step : 0), oj = gj + (d == 0 ? 0 : step);
             const int on = d == 0 ? oi : oj;
-            if (a->bc[d] == 1 && (on < 0 || on >= F.n[d])) continue;
+            if (a->bc[d] != FVS_BC_PERIODIC && (on < 0 || on >= F.n[d])) continue;
             oi = a->MapCoord(oi, F.n[0], 0);
             oj = a->MapCoord(oj, F.n[1], 1);
             if (F.Owner(oi, oj) >= 0) continue;
@@ -395,6 +401,7 @@ int Build(fvs_amr* a) {
             sg.stride = R[r].stride;
             sg.n = nn;
             for (int h = 0; h < 4; ++h) sg.halo[h] = R[r].halo[h];
+            sg.flip = R[r].flip;
             sg.j0 = int32_t(int64_t(k) * nn / parts);
             sg.j1 = int32_t(int64_t(k + 1) * nn / parts);
             sg.cap_begin = c;
@@ -609,9 +616,13 @@ int fvs_amr_create(const fvs_amr_desc* d, const fvs_method* m, fvs_amr** out) {
     return Fail(FVS_ERR_INVALID, "1 to 4 levels");
   if (d->n0[0] < 1 || d->n0[1] < 1 || !(d->dx0 > 0.0) || d->npatches < 1)
     return Fail(FVS_ERR_INVALID, "bad level-0 size, dx or patch count");
-  for (int k = 0; k < 2; ++k)
-    if (d->bc[k] != FVS_BC_PERIODIC && d->bc[k] != FVS_BC_TRANSMISSIVE)
+  for (int k = 0; k < 2; ++k) {
+    if (d->bc[k] != FVS_BC_PERIODIC && d->bc[k] != FVS_BC_TRANSMISSIVE &&
+        d->bc[k] != FVS_BC_REFLECTIVE)
       return Fail(FVS_ERR_INVALID, "bad boundary condition");
+    if (d->bc[k] == FVS_BC_REFLECTIVE && d->n0[k] < 2)
+      return Fail(FVS_ERR_INVALID, "a reflective direction needs at least 2 cells");
+  }
   fvs_method mm;
   if (m) {
     mm = *m;

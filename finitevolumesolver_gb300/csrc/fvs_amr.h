@@ -33,6 +33,8 @@ struct Row {
   int32_t n;        // interior cells
   int32_t cap_end;  // captures of this row: [previous row's cap_end, cap_end)
   int32_t halo[4];  // sources of the halo cells -2, -1, n, n+1
+  int32_t flip;     // bit h: halo cell h is a reflective boundary's image (its
+                    // momentum along the row is negated)
 };
 
 // A segment [j0, j1) of a row, the work item of a sweep thread: it computes
@@ -47,6 +49,7 @@ struct Seg {
   int32_t cap_begin, cap_end;
   int32_t n;        // the row's interior cells
   int32_t halo[4];  // the row's halo sources (Row::halo)
+  int32_t flip;     // Row::flip
 };
 
 constexpr int kSplits = 4;  // rows are offered split into 1, 2, 4 or 8 segments

@@ -67,10 +67,12 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
     auto load = [&](double* u, int j) {
       const double* src = in;
       int64_t off, cs = N;
+      bool flip = false;
       if (j >= 0 && j < w.n) {
         off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
       } else {  // halo cell: its source in this level or the coarser one
-        const int32_t g = w.halo[j < 0 ? j + 2 : j - w.n + 2];
+        const int h = j < 0 ? j + 2 : j - w.n + 2;
+        const int32_t g = w.halo[h];
         if (g >= 0) {
           off = g;
         } else {
@@ -78,9 +80,11 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
           src = a.coarse;
           cs = a.coarse_ncells;
         }
+        flip = (w.flip >> h) & 1;
       }
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(src + c * cs + off);
+      if (flip) u[1 + DIR] = -u[1 + DIR];  // a reflective boundary's image
     };
     // the update re-reads the FP64 state of cell j-1 (an L1 hit) instead of
     // carrying a window of FP64 states in registers
@@ -200,10 +204,12 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
     auto cell = [&](int j, R* v) {
       const double* src = a.in;
       int64_t off, cs = N;
+      bool flip = false;
       if (j >= 0 && j < w.n) {
         off = int64_t(w.base) + int64_t(j + kGhost) * w.stride;
       } else {  // halo cell (j = -1 or n)
-        const int32_t g = w.halo[j < 0 ? j + 2 : j - w.n + 2];
+        const int h = j < 0 ? j + 2 : j - w.n + 2;
+        const int32_t g = w.halo[h];
         if (g >= 0) {
           off = g;
         } else {
@@ -211,10 +217,12 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
           src = a.coarse;
           cs = a.coarse_ncells;
         }
+        flip = (w.flip >> h) & 1;
       }
       double u[K];
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(src + c * cs + off);
+      if (flip) u[1 + DIR] = -u[1 + DIR];  // a reflective boundary's image
       P::ToCell(v, u);
     };
     if constexpr (kFilter) {

@@ -113,7 +113,7 @@ int CheckMethod(const fvs_method* m, int rank) {
   if (rank < 1 || rank > 3) return Fail(FVS_ERR_INVALID, "rank must be 1, 2 or 3");
   if (m->flux_method < 0 || m->flux_method > 7)
     return Fail(FVS_ERR_INVALID, "unknown flux method");
-  if (m->limiter < 0 || m->limiter > 2) return Fail(FVS_ERR_INVALID, "unknown limiter");
+  if (m->limiter < 0 || m->limiter > 3) return Fail(FVS_ERR_INVALID, "unknown limiter");
   // the characteristic method limits with VanLeer's two-slope functor only,
   // the primitive one with its own fixed limiter
   if ((m->flux_method == FVS_MUSCL_CHAR || m->flux_method == FVS_MUSCL_PRIM) &&
@@ -654,8 +654,11 @@ int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
     if (used && grid->n[d] < 1) return Fail(FVS_ERR_INVALID, "extent must be >= 1");
     if (!used && grid->n[d] != 1)
       return Fail(FVS_ERR_INVALID, "unused directions must have extent 1");
-    if (used && grid->bc[d] != FVS_BC_PERIODIC && grid->bc[d] != FVS_BC_TRANSMISSIVE)
+    if (used && grid->bc[d] != FVS_BC_PERIODIC && grid->bc[d] != FVS_BC_TRANSMISSIVE &&
+        grid->bc[d] != FVS_BC_REFLECTIVE)
       return Fail(FVS_ERR_INVALID, "unknown boundary condition");
+    if (used && grid->bc[d] == FVS_BC_REFLECTIVE && grid->n[d] < 2)
+      return Fail(FVS_ERR_INVALID, "a reflective direction needs at least 2 cells");
     if (used && !(grid->dx[d] > 0.0)) return Fail(FVS_ERR_INVALID, "dx must be positive");
   }
   if (grid->dt_rule != 0 && grid->dt_rule != 1)

@@ -233,6 +233,8 @@ __device__ __forceinline__ void PredictMasked(const GasT<T, M>& eq, C2T<T>& recL
       slope = (c > T(0)) ? M::Div(c, sL + sR) : T(0);
     } else if (limiter == exact::kMinMod) {
       slope = (sR > 0) ? PMaxT(T(0), PMinT(sL, sR)) : PMinT(T(0), PMaxT(sL, sR));
+    } else if (limiter == exact::kNoLimiter) {
+      slope = T(0.5) * (sL + sR);
     } else {
       slope = T(0);
     }
@@ -343,6 +345,9 @@ __device__ __forceinline__ double Clamp01(double x) {
   return 1.0 < x ? 1.0 : x;
 }
 
+// Conservative state of cell (i, j), ghost cells (one direction at a time)
+// the boundary condition's images: reflective ghosts carry the reflected
+// momentum of their direction.
 __device__ __forceinline__ void LoadCons(const CcStateArgs& a, int i, int j, double* u) {
   const int si = BcIndex(i, a.g.nx, a.bc[0]);
   const int sj = BcIndex(j, a.g.ny, a.bc[1]);
@@ -350,6 +355,8 @@ __device__ __forceinline__ void LoadCons(const CcStateArgs& a, int i, int j, dou
   const int64_t off = int64_t(sj) * a.g.nx + si;
 #pragma unroll
   for (int k = 0; k < 4; ++k) u[k] = __ldg(a.in + k * cs + off);
+  if (BcFlip(i, a.g.nx, a.bc[0])) u[1] = -u[1];
+  if (BcFlip(j, a.g.ny, a.bc[1])) u[2] = -u[2];
 }
 
 template <class T> __device__ __forceinline__ void Narrow(T* t, const double* u) {

@@ -190,7 +190,8 @@ __global__ void __launch_bounds__(256) StableDtKernel(StableDtArgs a) {
         const int f = idx[d] + fi;
         if (a.rule == 1 && d > 0 && !ReferenceTileFace(f, nd, a.width)) continue;
         if (fi == 1 && a.bc[d] == 0) continue;  // periodic: face n == face 0
-        const int other = BcIndex(fi == 0 ? f - 1 : f, nd, a.bc[d]);
+        const int og = fi == 0 ? f - 1 : f;
+        const int other = BcIndex(og, nd, a.bc[d]);
         int oidx[3] = {i, j, k};
         oidx[d] = other;
         const int64_t ocell =
@@ -198,6 +199,7 @@ __global__ void __launch_bounds__(256) StableDtKernel(StableDtArgs a) {
         double v[K];
 #pragma unroll
         for (int c = 0; c < K; ++c) v[c] = __ldg(a.in + c * cs + ocell);
+        if (BcFlip(og, nd, a.bc[d])) v[1 + d] = -v[1 + d];
         const exact::CellWave wo = exact::MakeCellWave<D>(eq, v, d);
         const double s = (fi == 0) ? exact::FaceMaxSpeed(eq, wo, w)
                                    : exact::FaceMaxSpeed(eq, w, wo);

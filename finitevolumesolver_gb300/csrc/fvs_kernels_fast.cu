@@ -39,10 +39,13 @@ template <template <int> class PT> cudaError_t LaunchSweepMixedT(const SweepArgs
 // occupancy: 0, 4, 5 = register/occupancy variant (x sweeps with lanes along
 // x); 10, 14, 15 = the same variants with the marching kernel in x.
 cudaError_t LaunchSweepMixed(const SweepArgs& a, cudaStream_t s) {
-  if (a.dir == 0 && a.occupancy >= 10) {
+  // reflective rows: the marching kernel (its loads reflect ghost states)
+  if (a.dir == 0 && (a.occupancy >= 10 || a.bc == 2)) {
     switch (a.occupancy) {
+    case 4:
     case 14:
       return LaunchSweepMixedT<Mixed32PolicyMarchXOcc4>(a, s);
+    case 5:
     case 15:
       return LaunchSweepMixedT<Mixed32PolicyMarchXOcc5>(a, s);
     default:

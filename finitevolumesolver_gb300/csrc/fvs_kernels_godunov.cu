@@ -127,11 +127,13 @@ __global__ void __launch_bounds__(256) GodunovStableDtKernel(StableDtArgs a, int
         if (a.rule == 1 && d > 0 && !ReferenceTileFaceT(f, nd, a.width)) continue;
         if (fi == 1 && a.bc[d] == 0) continue;
         int oidx[3] = {idx[0], idx[1], idx[2]};
-        oidx[d] = BcIndex(fi == 0 ? f - 1 : f, nd, a.bc[d]);
+        const int og = fi == 0 ? f - 1 : f;
+        oidx[d] = BcIndex(og, nd, a.bc[d]);
         const int64_t ocell = (int64_t(oidx[2]) * ny + oidx[1]) * int64_t(nx) + oidx[0];
         double v[K];
 #pragma unroll
         for (int c = 0; c < K; ++c) v[c] = __ldg(a.in + c * cs + ocell);
+        if (BcFlip(og, nd, a.bc[d])) v[1 + d] = -v[1 + d];
         exact::Complete<D> o;
         exact::CompleteFromCons<D>(g.eq, o, v);
         const exact::Complete<D>& L = (fi == 0) ? o : q;

@@ -160,7 +160,9 @@ __device__ __forceinline__ double FaceMaxSpeed(const Gas& eq, const CellWave& L,
   return PMax(PMax(0.0, fabs(sL)), fabs(sR));
 }
 
-enum Limiter : int { kVanLeer = 0, kMinMod = 1, kNoLimiter = 2 };
+// VanLeer, MinMod, NoLimiter (the central slope, unlimited) and NoGradient
+// (slope 0) -- include/fub/flux_method/MusclHancockMethod.hpp:31-187.
+enum Limiter : int { kVanLeer = 0, kMinMod = 1, kNoLimiter = 2, kNoGradient = 3 };
 
 __device__ __forceinline__ double LimitedSlope(int limiter, double qL, double qM,
                                                double qR) {
@@ -173,6 +175,7 @@ __device__ __forceinline__ double LimitedSlope(int limiter, double qL, double qM
   if (limiter == kMinMod) {
     return (sR > 0) ? PMax(0.0, PMin(sL, sR)) : PMin(0.0, PMax(sL, sR));
   }
+  if (limiter == kNoLimiter) return 0.5 * (sL + sR);
   return 0.0;
 }
 

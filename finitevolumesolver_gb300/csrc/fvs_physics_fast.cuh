@@ -207,7 +207,8 @@ __device__ __forceinline__ T HalfSlope(int limiter, T qL, T qM, T qR) {
   if (limiter == 1) {  // MinMod
     return T(0.5) * ((sR > T(0)) ? Max(T(0), Min(sL, sR)) : Min(T(0), Max(sL, sR)));
   }
-  return T(0);
+  if (limiter == 2) return T(0.25) * (sL + sR);  // NoLimiter: half of 0.5 (sL + sR)
+  return T(0);  // NoGradient
 }
 
 // MUSCL-Hancock predictor of one cell: its left-face and right-face states.

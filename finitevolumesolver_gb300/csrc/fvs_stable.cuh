@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(256) StableDtKernelT(StableDtArgs a) {
         const int f = idx[d] + fi;
         if (a.rule == 1 && d > 0 && !ReferenceTileFaceT(f, nd, a.width)) continue;
         if (fi == 1 && a.bc[d] == 0) continue;  // periodic: face n == face 0
-        const int other = BcIndex(fi == 0 ? f - 1 : f, nd, a.bc[d]);
+        const int og = fi == 0 ? f - 1 : f;
+        const int other = BcIndex(og, nd, a.bc[d]);
         int oidx[3] = {i, j, k};
         oidx[d] = other;
         const int64_t ocell = (int64_t(oidx[2]) * ny + oidx[1]) * int64_t(nx) + oidx[0];
@@ -75,6 +76,7 @@ __global__ void __launch_bounds__(256) StableDtKernelT(StableDtArgs a) {
         R v[K];
 #pragma unroll
         for (int c = 0; c < K; ++c) vd[c] = __ldg(a.in + c * cs + ocell);
+        if (BcFlip(og, nd, a.bc[d])) vd[1 + d] = -vd[1 + d];
         P::ToCell(v, vd);
         const typename P::Wave wo = P::MakeWave(eq, v, d);
         const R s = (fi == 0) ? P::FaceMaxSpeed(eq, wo, w) : P::FaceMaxSpeed(eq, w, wo);
@@ -353,7 +355,8 @@ template <template <int> class PT>
 cudaError_t LaunchStableDtT(const StableDtArgs& a, cudaStream_t s) {
   const int64_t cells = int64_t(a.n[0]) * a.n[1] * a.n[2];
   const int block = 256;
-  if (a.rank == 3) {
+  const bool reflective = a.bc[0] == 2 || a.bc[1] == 2 || a.bc[2] == 2;
+  if (a.rank == 3 && !reflective) {
     // blocks of kDtRows x rows; enough blocks for about two waves of the GPU,
     // the planes split accordingly; every block full (see the kernel)
     const int64_t tiles = int64_t((a.n[0] + 30) / 31) * ((a.n[1] + kDtRows - 1) / kDtRows);
@@ -371,11 +374,15 @@ cudaError_t LaunchStableDtT(const StableDtArgs& a, cudaStream_t s) {
     StableDtMarch3Kernel<PT><<<grid, 32 * kDtRows, 0, s>>>(a, seg);
     return cudaGetLastError();
   }
+  // ranks 1 and 2, and 3-D grids with a reflective direction (the cell-wise
+  // kernel reflects the ghost states of the boundary faces)
   const unsigned grid = GridStrideBlocks(cells, block, 8);
   if (a.rank == 1)
     StableDtKernelT<1, PT><<<grid, block, 0, s>>>(a);
-  else
+  else if (a.rank == 2)
     StableDtKernelT<2, PT><<<grid, block, 0, s>>>(a);
+  else
+    StableDtKernelT<3, PT><<<grid, block, 0, s>>>(a);
   return cudaGetLastError();
 }
 

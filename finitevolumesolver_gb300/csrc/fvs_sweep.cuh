@@ -30,13 +30,28 @@
 
 namespace fvs {
 
+// The interior cell whose state ghost cell j of a grid line of n cells
+// images under boundary condition bc (FVS_BC_*): periodic -- the periodic
+// image; transmissive -- the boundary cell (TransmissiveBoundary.cpp:31-42);
+// reflective -- the mirror cell (ReflectIndex,
+// src/boundary_condition/ReflectiveBoundary.cpp:24-36; needs n >= 2 for the
+// two ghost layers), whose momentum along the line is reflected (BcFlip).
 __device__ __forceinline__ int BcIndex(int j, int n, int bc) {
   if (j >= 0 && j < n) return j;
   if (bc == 0) {
     int r = j % n;
     return r < 0 ? r + n : r;
   }
+  if (bc == 2) return j < 0 ? -1 - j : 2 * n - 1 - j;
   return j < 0 ? 0 : n - 1;
+}
+
+// Whether ghost cell j's state is the reflected image of BcIndex(j, n, bc):
+// Reflect (src/equations/PerfectGas.cpp:266-300) with the unit normal of the
+// line, m - 2 (m . e) e, negates the momentum along the line and keeps the
+// other components.
+__device__ __forceinline__ bool BcFlip(int j, int n, int bc) {
+  return bc == 2 && (j < 0 || j >= n);
 }
 
 __device__ __forceinline__ void AtomicMaxPositive(unsigned long long* word,
@@ -394,6 +409,7 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
       const int64_t off = base + int64_t(BcIndex(j, nd, a.bc)) * stride;
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * cs + off);
+      if (BcFlip(j, nd, a.bc)) u[1 + DIR] = -u[1 + DIR];
     };
     // compute-precision window of three cells; the FP64 loads run one cell
     // ahead of the arithmetic (dn is the next "up").  The update of cell j-1
@@ -748,6 +764,8 @@ cudaError_t LaunchSweepT(const SweepArgs& a, cudaStream_t s) {
   switch (a.dir) {
   case 0:
     if constexpr (P<D>::kWarpX) {
+      // (x sweeps of reflective rows take the marching kernel: the caller
+      // routes them to a policy without kWarpX)
       const int64_t rows = int64_t(a.n[1]) * a.n[2];
       const unsigned xgrid = static_cast<unsigned>((rows * 32 + block - 1) / block);
       SweepXWarpKernel<D, P><<<xgrid, block, 0, s>>>(b);

@@ -59,10 +59,13 @@ typedef enum fvs_flux_method {
                            src/equations/perfect_gas/MusclHancockPrimMethod.hpp */
 } fvs_flux_method;
 
+/* Slope limiters of MusclHancock (include/fub/flux_method/
+ * MusclHancockMethod.hpp:31-187). */
 typedef enum fvs_limiter {
   FVS_VAN_LEER = 0,
   FVS_MINMOD = 1,
-  FVS_NO_LIMITER = 2
+  FVS_NO_LIMITER = 2,   /* NoLimiter: the central slope 0.5 (sL + sR), unlimited */
+  FVS_NO_GRADIENT = 3   /* NoGradient: slope 0 (first order in space) */
 } fvs_limiter;
 
 typedef enum fvs_precision {
@@ -81,9 +84,19 @@ typedef enum fvs_guess {
   FVS_GUESS_MLP = 2      /* learned guess, PVRS/TR fallback */
 } fvs_guess;
 
+/* Boundary conditions, per direction (both sides):
+ *  periodic;
+ *  transmissive: ghost cells copy the boundary cell
+ *    (src/AMReX/boundary_condition/TransmissiveBoundary.cpp:31-93);
+ *  reflective: ghost cells are the mirror cells' states reflected at the wall,
+ *    the momentum normal to it negated (include/fub/AMReX/boundary_condition/
+ *    ReflectiveBoundary.hpp:34-64, src/boundary_condition/
+ *    ReflectiveBoundary.cpp:24-36, Reflect src/equations/PerfectGas.cpp:266-300);
+ *    needs at least 2 cells in that direction. */
 typedef enum fvs_bc {
   FVS_BC_PERIODIC = 0,
-  FVS_BC_TRANSMISSIVE = 1
+  FVS_BC_TRANSMISSIVE = 1,
+  FVS_BC_REFLECTIVE = 2
 } fvs_bc;
 
 typedef struct fvs_box {

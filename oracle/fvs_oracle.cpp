@@ -263,7 +263,7 @@ void UpdateConservatively(const BoxView& next, const BoxView& prev,
 struct Grid {
   int D;
   int n[3];
-  int bc[3];  // 0 periodic, 1 transmissive
+  int bc[3];  // 0 periodic, 1 transmissive, 2 reflective
   double dx[3];
   int64_t cells() const { return int64_t(n[0]) * n[1] * n[2]; }
 };
@@ -280,11 +280,15 @@ Grid MakeGrid(int rank, const int32_t* n, const int32_t* bc, const double* dx) {
 }
 
 // Index of the cell supplying the value of (possibly ghost) index i in a
-// direction of extent n: periodic image or the boundary cell (transmissive,
-// TransmissiveBoundary.cpp:31-42 copies the boundary cell, no mirroring).
+// direction of extent n: periodic image, the boundary cell (transmissive,
+// TransmissiveBoundary.cpp:31-42 copies the boundary cell, no mirroring) or
+// the mirror cell (reflective, ReflectIndex of
+// src/boundary_condition/ReflectiveBoundary.cpp:24-36 with the ghost strip as
+// the fill box: lower side i -> -1 - i, upper side i -> 2n - 1 - i).
 inline int SourceIndex(int i, int n, int bc) {
   if (i >= 0 && i < n) return i;
   if (bc == 0) return ((i % n) + n) % n;
+  if (bc == 2) return i < 0 ? -1 - i : 2 * n - 1 - i;
   return i < 0 ? 0 : n - 1;
 }
 
@@ -315,6 +319,10 @@ std::vector<double> BuildScratch(const Grid& g, const double* cons, int dir,
         LoadCons<D>(u, cv, src[0], src[1], src[2]);
         Complete<D> q;
         CompleteFromCons<D>(eq, q, u);
+        // ReflectiveBoundary::FillBoundary: the ghost is Reflect of the mirror
+        // cell's complete state (ReflectiveBoundary.hpp:61-75)
+        const int at[3] = {i, j, k};
+        if (g.bc[dir] == 2 && (at[dir] < 0 || at[dir] >= g.n[dir])) ReflectMomentum<D>(q.m, dir);
         sv(0, i, j, k) = q.rho;
         for (int d = 0; d < D; ++d) sv(1 + d, i, j, k) = q.m[d];
         sv(1 + D, i, j, k) = q.E;

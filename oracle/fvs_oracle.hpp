@@ -253,8 +253,21 @@ inline void HllRiemannState(const Gas& eq, Complete<D>& sol,
   }
 }
 
-// Slope limiters  include/fub/flux_method/MusclHancockMethod.hpp:92-187.
-enum Limiter : int { kVanLeer = 0, kMinMod = 1, kNoLimiter = 2 };
+// Reflect (src/equations/PerfectGas.cpp:266-300) of the momentum m[D] about
+// the unit normal of direction dir: m - 2 (m . e) e, the dot product summed in
+// component order (the other state components are unchanged).
+template <int D> inline void ReflectMomentum(double* m, int dir) {
+  double e[D];
+  for (int d = 0; d < D; ++d) e[d] = d == dir ? 1.0 : 0.0;
+  double dot = m[0] * e[0];
+  for (int d = 1; d < D; ++d) dot += m[d] * e[d];
+  for (int d = 0; d < D; ++d) m[d] = m[d] - 2 * (dot * e[d]);
+}
+
+// Slope limiters  include/fub/flux_method/MusclHancockMethod.hpp:31-187:
+// VanLeer, MinMod, NoLimiter (:31-69, the central slope 0.5 (sL + sR)) and
+// NoGradient (:71-90, slope 0).
+enum Limiter : int { kVanLeer = 0, kMinMod = 1, kNoLimiter = 2, kNoGradient = 3 };
 
 inline double VanLeer(double sL, double sR) {
   const double c = 2.0 * sL * sR;
@@ -273,6 +286,8 @@ inline double LimitedSlope(int limiter, double qL, double qM, double qR) {
   case kMinMod:
     return MinMod(sL, sR);
   case kNoLimiter:
+    return 0.5 * (sL + sR);
+  case kNoGradient:
     return 0.0;
   default:
     return VanLeer(sL, sR);

@@ -107,8 +107,11 @@ struct Hier {
   Gas eq;
   int limiter = 0;  // van Leer
 
+  // periodic wrap, transmissive clamp, reflective mirror (ReflectIndex,
+  // src/boundary_condition/ReflectiveBoundary.cpp:24-36)
   int MapCoord(int x, int n, int d) const {
     if (bc[d] == 0) return ((x % n) + n) % n;
+    if (bc[d] == 2) return x < 0 ? -1 - x : (x >= n ? 2 * n - 1 - x : x);
     return x < 0 ? 0 : (x >= n ? n - 1 : x);
   }
 
@@ -130,10 +133,14 @@ struct Hier {
     for (int q = 0; q < np; ++q) {
       Patch& P = patches[size_t(L.patches[size_t(q)])];
       auto fill = [&](int li, int lj) {
-        const int si = MapCoord(P.lo[0] + li, L.n[0], 0);
-        const int sj = MapCoord(P.lo[1] + lj, L.n[1], 1);
+        const int gi = P.lo[0] + li, gj = P.lo[1] + lj;
+        const int si = MapCoord(gi, L.n[0], 0);
+        const int sj = MapCoord(gj, L.n[1], 1);
         double v[kK];
         Value(l, si, sj, v);
+        // a reflective wall's ghost: Reflect of the mirror cell's state
+        if (bc[0] == 2 && (gi < 0 || gi >= L.n[0])) ReflectMomentum<2>(v + 1, 0);
+        if (bc[1] == 2 && (gj < 0 || gj >= L.n[1])) ReflectMomentum<2>(v + 1, 1);
         for (int c = 0; c < kK; ++c) P.At(c, li, lj) = v[c];
       };
       for (int lj = 0; lj < P.n[1]; ++lj)
@@ -269,7 +276,7 @@ struct Hier {
               int oi = gi + (d == 0 ? step : 0);
               int oj = gj + (d == 0 ? 0 : step);
               const int on = d == 0 ? oi : oj;
-              if (bc[d] == 1 && (on < 0 || on >= L.n[d])) continue;  // physical boundary
+              if (bc[d] != 0 && (on < 0 || on >= L.n[d])) continue;  // physical boundary
               oi = MapCoord(oi, L.n[0], 0);
               oj = MapCoord(oj, L.n[1], 1);
               if (L.Owner(oi, oj) >= 0) continue;  // same-level neighbour

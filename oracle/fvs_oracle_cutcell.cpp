@@ -339,10 +339,12 @@ namespace {
 
 constexpr int kG = 3;  // ghost layers of the geometry and state scratch
 
-// Periodic image or transmissive boundary cell of index i (extent n).
+// Periodic image, transmissive boundary cell or reflective mirror cell of
+// index i (extent n); see SourceIndex of the uniform grid.
 inline int SourceIndexCc(int i, int n, int bc) {
   if (i >= 0 && i < n) return i;
   if (bc == 0) return ((i % n) + n) % n;
+  if (bc == 2) return i < 0 ? -1 - i : 2 * n - 1 - i;
   return i < 0 ? 0 : n - 1;
 }
 
@@ -467,6 +469,8 @@ void MaskedMusclFlux(const Gas& eq, double* nf, const C2* st, const double* alph
       if (limiter == kMinMod) {
         slope = MinMod(sL, sR);
       } else if (limiter == kNoLimiter) {
+        slope = 0.5 * (sL + sR);  // NoLimiter, masked form (MusclHancockMethod.hpp:56-68)
+      } else if (limiter == kNoGradient) {
         slope = 0.0;
       } else {
         slope = VanLeer(sL, sR);
@@ -518,6 +522,9 @@ std::vector<C2> CcScratch(const CcGrid& g, const double* cons) {
       for (int c = 0; c < 4; ++c) u[c] = cons[c * n + int64_t(sj) * g.nx + si];
       C2 q;
       CompleteFromConsMasked<2>(eq, q, u, g.Alpha(ii, jj) > 0.0);
+      // reflective walls: Reflect of the mirror cell's state, x then y
+      if (g.bc[0] == 2 && (ii < 0 || ii >= g.nx)) ReflectMomentum<2>(q.m, 0);
+      if (g.bc[1] == 2 && (jj < 0 || jj >= g.ny)) ReflectMomentum<2>(q.m, 1);
       sc[size_t(g.C(ii, jj))] = q;
     }
   }

@@ -16,7 +16,7 @@ from . import build as _build
 
 MUSCL_HLLE, HLLE, GODUNOV, MUSCL_GODUNOV, HLLEM, MUSCL_HLLEM = 0, 1, 2, 3, 4, 5
 MUSCL_CHAR, MUSCL_PRIM = 6, 7
-VAN_LEER, MINMOD, NO_LIMITER = 0, 1, 2
+VAN_LEER, MINMOD, NO_LIMITER, NO_GRADIENT = 0, 1, 2, 3
 GUESS_MEAN, GUESS_PVRS_TR, GUESS_GIVEN = 0, 1, 2
 
 
