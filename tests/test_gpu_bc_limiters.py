@@ -72,11 +72,15 @@ def test_fast_flavours_reflective(fvs, orc, rank, n, bc, prec):
 
 @pytest.mark.parametrize("xvariant", [0, 4, 10])
 def test_mixed_closed_box(fvs, orc, xvariant):
-    """Walls on every side, mixed precision: the mass and energy fluxes
-    through a wall vanish, so their totals only change by FP64 round-off;
-    the state tracks the FP64 oracle to the FP32 reconstruction error.  The
-    lanes-along-x variants (0, 4) run their x sweeps with the marching kernel
-    on reflective rows."""
+    """Walls on every side, mixed precision: the state tracks the FP64
+    oracle to the FP32 reconstruction error, and the interior fluxes cancel
+    exactly in the FP64 update, so mass and energy change only through the
+    walls.  There the flux of a state and its mirror image is an FP32
+    expression (with FMA contraction) whose mass and energy parts cancel to
+    FP32 round-off rather than to zero (exactly zero in the exact flavour):
+    5e-12 relative after 10 steps, bounded here by 1e-10.  The lanes-along-x
+    variants (0, 4) run their x sweeps with the marching kernel on reflective
+    rows."""
     n = 48
     cons = workloads.octants_3d(n, seed=9)
     dx = [1.0 / n] * 3
@@ -93,7 +97,7 @@ def test_mixed_closed_box(fvs, orc, xvariant):
     s.run(cfl=0.8, t_end=10.0, max_steps=10)
     out = s.download()
     for c in (0, 4):
-        assert abs(out[c].sum() - cons[c].sum()) <= 1e-13 * abs(cons[c]).sum()
+        assert abs(out[c].sum() - cons[c].sum()) <= 1e-10 * abs(cons[c]).sum()
     s.close()
 
 
