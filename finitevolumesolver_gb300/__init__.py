@@ -167,6 +167,59 @@ def CompleteFromCons(equation: PerfectGas, complete, complete_box, cons, cons_bo
         _as_box(cons_box), _as_box(region), _stream(stream)))
 
 
+class HostPatchContext:
+    """The patch-level calls for patch arrays in host memory (NumPy arrays,
+    C-contiguous float64, FArrayBox layout): FluxMethod.ComputeNumericFluxes,
+    ComputeStableDt, HyperbolicPatchIntegrator.UpdateConservatively and
+    CompleteFromCons as a CPU build of the reference calls them.  The
+    context stages the boxes through device buffers on its own stream."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        _capi.check(lib().fvs_patch_ctx_create(C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().fvs_patch_ctx_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    @staticmethod
+    def _np(a):
+        import numpy as np
+        if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+            raise TypeError("host patch arrays are C-contiguous float64 NumPy arrays")
+        return a.ctypes.data
+
+    def ComputeNumericFluxes(self, fm: "FluxMethod", fluxes, face_box, states, cell_box, dt,
+                             dx, dir) -> None:
+        _capi.check(lib().fvs_compute_numeric_fluxes_host(
+            self._h, C.byref(fm.method), fm.equation.rank, self._np(fluxes), _as_box(face_box),
+            self._np(states), _as_box(cell_box), float(dt), float(dx), int(dir)))
+
+    def ComputeStableDt(self, fm: "FluxMethod", states, cell_box, dx, dir,
+                        window_rule=1) -> float:
+        out = C.c_double(0.0)
+        _capi.check(lib().fvs_compute_stable_dt_host(
+            self._h, C.byref(fm.method), fm.equation.rank, self._np(states), _as_box(cell_box),
+            float(dx), int(dir), int(window_rule), C.byref(out)))
+        return out.value
+
+    def UpdateConservatively(self, next, next_box, prev, prev_box, fluxes, face_box, ncomp, dt,
+                             dx, dir) -> None:
+        _capi.check(lib().fvs_update_conservatively_host(
+            self._h, self._np(next), _as_box(next_box), self._np(prev), _as_box(prev_box),
+            self._np(fluxes), _as_box(face_box), int(ncomp), float(dt), float(dx), int(dir)))
+
+    def CompleteFromCons(self, equation: PerfectGas, complete, complete_box, cons, cons_box,
+                         region) -> None:
+        _capi.check(lib().fvs_complete_from_cons_host(
+            self._h, equation.rank, equation.gamma, self._np(complete), _as_box(complete_box),
+            self._np(cons), _as_box(cons_box), _as_box(region)))
+
+
 class Solver:
     """A uniform single-level grid advanced by the reference's split step
     sequence, with the time step kept on the device."""

@@ -97,6 +97,15 @@ def load() -> C.CDLL:
     L.fvs_update_conservatively_region.argtypes = [_VP, Box, Box, _VP, Box, _VP, Box, C.c_int,
                                                    C.c_double, C.c_double, C.c_int, _VP]
     L.fvs_complete_from_cons.argtypes = [C.c_int, C.c_double, _VP, Box, _VP, Box, Box, _VP]
+    L.fvs_patch_ctx_create.argtypes = [P(_VP)]
+    L.fvs_patch_ctx_destroy.argtypes = [_VP]
+    L.fvs_compute_numeric_fluxes_host.argtypes = [_VP, P(Method), C.c_int, _VP, Box, _VP, Box,
+                                                  C.c_double, C.c_double, C.c_int]
+    L.fvs_compute_stable_dt_host.argtypes = [_VP, P(Method), C.c_int, _VP, Box, C.c_double,
+                                             C.c_int, C.c_int, P(C.c_double)]
+    L.fvs_update_conservatively_host.argtypes = [_VP, _VP, Box, _VP, Box, _VP, Box, C.c_int,
+                                                 C.c_double, C.c_double, C.c_int]
+    L.fvs_complete_from_cons_host.argtypes = [_VP, C.c_int, C.c_double, _VP, Box, _VP, Box, Box]
     L.fvs_solver_create.argtypes = [P(GridDesc), P(Method), P(_VP)]
     L.fvs_solver_destroy.argtypes = [_VP]
     L.fvs_solver_upload.argtypes = [_VP, _VP]

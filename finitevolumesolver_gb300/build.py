@@ -33,6 +33,7 @@ UNITS = [
     ("fvs_kernels_cutcell_mixed.cu", []),
     ("fvs_capi.cu", []),
     ("fvs_noalloc.cu", ["-fmad=false"]),
+    ("fvs_host_patch.cu", []),
     ("fvs_mlp_train.cu", []),
     ("fvs_amr.cu", []),
     ("fvs_amr_exact.cu", ["-fmad=false"]),

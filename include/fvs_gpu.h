@@ -213,6 +213,38 @@ int fvs_complete_from_cons(int rank, double gamma, double* complete_dev,
                            fvs_box complete_box, const double* cons_dev,
                            fvs_box cons_box, fvs_box region, void* stream);
 
+/* ---- Patch level with host-resident patches ---------------------------- */
+/* The four patch calls above for patch arrays in host memory, the way a CPU
+ * build of the reference hands FluxMethodAdapter its FArrayBoxes
+ * (include/fub/AMReX/FluxMethodAdapter.hpp:120-150; HyperbolicMethod's
+ * time integrator and reconstruction likewise).  A patch context owns a
+ * CUDA stream and device staging buffers that grow to the largest patch it
+ * has seen (the only allocations; a context reused for same-sized patches
+ * allocates nothing more).  Each call copies its input boxes to the device
+ * (one cudaMemcpyAsync per array), runs the device entry point on them,
+ * copies its output box back and synchronises the context's stream, so the
+ * host arrays are complete on return.  Results equal the device-pointer
+ * calls' bit for bit.  Arguments, layouts and status codes as above; pinned
+ * host memory copies fastest.  A context serves one host thread at a time. */
+typedef struct fvs_patch_ctx fvs_patch_ctx;
+int fvs_patch_ctx_create(fvs_patch_ctx** out);
+int fvs_patch_ctx_destroy(fvs_patch_ctx* c);
+int fvs_compute_numeric_fluxes_host(fvs_patch_ctx* c, const fvs_method* m, int rank,
+                                    double* fluxes_host, fvs_box face_box,
+                                    const double* states_host, fvs_box cell_box, double dt,
+                                    double dx, int dir);
+int fvs_compute_stable_dt_host(fvs_patch_ctx* c, const fvs_method* m, int rank,
+                               const double* states_host, fvs_box cell_box, double dx, int dir,
+                               int window_rule, double* dt_out);
+int fvs_update_conservatively_host(fvs_patch_ctx* c, double* next_host, fvs_box next_box,
+                                   const double* prev_host, fvs_box prev_box,
+                                   const double* fluxes_host, fvs_box face_box, int ncomp,
+                                   double dt, double dx, int dir);
+/* Cells of complete_box outside `region` keep the values complete_host holds. */
+int fvs_complete_from_cons_host(fvs_patch_ctx* c, int rank, double gamma, double* complete_host,
+                                fvs_box complete_box, const double* cons_host, fvs_box cons_box,
+                                fvs_box region);
+
 /* ExactRiemannSolver<PerfectGas<1>>::ComputeMiddleState for n independent
  * problems given by primitive states (device arrays of length n)
  * (src/equations/perfect_gas/ExactRiemannSolver.hpp:34-97,

@@ -36,6 +36,8 @@ def test_no_gpu_reports_no_device(capi):
     assert L.fvs_solver_create(C.byref(g), C.byref(m), C.byref(h)) == capi.FVS_ERR_NO_DEVICE
     with pytest.raises(f.FvsError):
         f.Solver([8], [0.1], "transmissive")
+    h2 = C.c_void_p()
+    assert L.fvs_patch_ctx_create(C.byref(h2)) == capi.FVS_ERR_NO_DEVICE
     # both stable-dt entry points report the missing device the same way
     out = C.c_double(0.0)
     b = f.box([0, 0], [8, 8])
