@@ -90,6 +90,8 @@ def load() -> C.CDLL:
                                              C.c_double, C.c_int, _VP]
     L.fvs_compute_stable_dt.argtypes = [P(Method), C.c_int, _VP, Box, C.c_double, C.c_int,
                                         C.c_int, _DP, _VP]
+    L.fvs_compute_max_speed.argtypes = [P(Method), C.c_int, _VP, Box, C.c_int, C.c_int, _VP,
+                                         _VP]
     L.fvs_compute_stable_dt_noalloc.argtypes = [P(Method), C.c_int, _VP, Box, C.c_double,
                                                 C.c_int, C.c_int, _DP, _VP]
     L.fvs_update_conservatively.argtypes = [_VP, Box, _VP, Box, _VP, Box, C.c_int, C.c_double,

@@ -584,6 +584,35 @@ int fvs_compute_stable_dt(const fvs_method* m, int rank, const double* states_de
   return FVS_OK;
 }
 
+int fvs_compute_max_speed(const fvs_method* m, int rank, const double* states_dev,
+                          fvs_box cell_box, int dir, int window_rule,
+                          unsigned long long* smax_bits_dev, void* stream) {
+  if (int r = CheckMethod(m, rank)) return r;
+  if (dir < 0 || dir >= rank) return Fail(FVS_ERR_INVALID, "direction out of range");
+  if (!ValidBox(cell_box)) return Fail(FVS_ERR_INVALID, "invalid box");
+  if (!smax_bits_dev) return Fail(FVS_ERR_INVALID, "smax_bits_dev is NULL");
+  if (window_rule != 0 && window_rule != 1)
+    return Fail(FVS_ERR_INVALID, "window_rule must be 0 or 1");
+  if (IsGodunov(m->flux_method) && m->guess == FVS_GUESS_MLP && !m->mlp_params)
+    return Fail(FVS_ERR_INVALID, "FVS_GUESS_MLP needs mlp_params");
+  if (int r = CheckDevice()) return r;
+  if (Volume(cell_box) == 0) return FVS_OK;
+  if (!states_dev) return Fail(FVS_ERR_INVALID, "NULL data pointer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (IsGodunov(m->flux_method)) {
+    e = fvs::LaunchPatchGodunovStableDt(m->flux_method == FVS_MUSCL_GODUNOV, rank, m->gamma,
+                                        m->guess, m->max_iterations, m->tolerance,
+                                        m->mlp_params, states_dev, ToDesc(cell_box),
+                                        window_rule, dir, smax_bits_dev, st);
+  } else {
+    e = fvs::LaunchPatchStableDtExact(m->flux_method, rank, m->gamma, states_dev,
+                                      ToDesc(cell_box), window_rule, dir, smax_bits_dev, st);
+  }
+  if (e != cudaSuccess) return CudaFail(e, "fvs_compute_max_speed");
+  return FVS_OK;
+}
+
 int fvs_update_conservatively_region(double* next_dev, fvs_box next_box, fvs_box region,
                                      const double* prev_dev, fvs_box prev_box,
                                      const double* fluxes_dev, fvs_box face_box, int ncomp,

@@ -149,6 +149,19 @@ int fvs_compute_stable_dt(const fvs_method* m, int rank,
                           double dx, int dir, int window_rule, double* dt_out,
                           void* stream);
 
+/* The reduction of fvs_compute_stable_dt without its synchronisation: folds
+ * the patch's maximum face speed max(0, |sL|, |sR|) into *smax_bits_dev
+ * (device, 8 bytes) by an atomic maximum on the bit pattern of the double
+ * (non-negative doubles order like their bits; the caller zeroes the word
+ * first).  Enqueued on `stream`; allocates nothing.  After the launches of
+ * every patch of a level, dx / (the word as a double) is the level's stable
+ * dt in `dir` -- the same number as the minimum of the patches'
+ * fvs_compute_stable_dt -- with one synchronisation instead of one per patch
+ * (FluxMethodAdapter.hpp:69-114 reduces the patches' dts). */
+int fvs_compute_max_speed(const fvs_method* m, int rank, const double* states_dev,
+                          fvs_box cell_box, int dir, int window_rule,
+                          unsigned long long* smax_bits_dev, void* stream);
+
 /* Allocation-free variant of fvs_compute_stable_dt, for callers that cannot
  * let a library allocate device memory -- for example an integrator that
  * hands out every byte of device memory through its own arena, where a

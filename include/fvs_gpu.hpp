@@ -35,11 +35,16 @@
 // way of reporting failures (NewtonIteration.hpp:44-50).
 #pragma once
 
+#include <cuda_runtime_api.h>
+
 #include <algorithm>
 #include <chrono>
+#include <cstring>
 #include <limits>
+#include <memory>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "fvs_gpu.h"
 
@@ -59,6 +64,10 @@ class Error : public std::runtime_error {
 
 inline void Check(int code) {
   if (code != FVS_OK) throw Error(code, fvs_last_error());
+}
+
+inline void CheckCuda(cudaError_t e) {
+  if (e != cudaSuccess) throw Error(FVS_ERR_CUDA, cudaGetErrorString(e));
 }
 
 // One patch (tile) of a level, device pointers.
@@ -102,19 +111,41 @@ template <class Adapter> class FluxMethod {
   }
 
   // min over the level's patches of FluxMethod::ComputeStableDt (simd window
-  // rule, the reference's default OpenMpSimdTag).
+  // rule, the reference's default OpenMpSimdTag): every patch folds its
+  // maximum face speed into one device word (fvs_compute_max_speed), the
+  // level synchronises once, dt = dx / max speed (the minimum of the
+  // patches' dts: division by a positive number is monotonic).  Patches on
+  // other streams wait for the word's reset and are waited for.
   template <class Context, class Direction>
   Duration ComputeStableDt(Context& ctx, int level, Direction dir) {
     const int d = static_cast<int>(dir);
     const double dx = adapter_.CellSize(ctx, level, d);
-    double dt = std::numeric_limits<double>::max();
+    if (fvs_device_count() == 0) throw Error(FVS_ERR_NO_DEVICE, "no CUDA device available");
+    std::vector<cudaStream_t> streams;
     adapter_.ForEachPatch(ctx, level, d, [&](const Patch& p) {
-      double local = 0.0;
-      Check(fvs_compute_stable_dt(&m_, adapter_.Rank(), p.scratch, p.scratch_box, dx, d, 1,
-                                  &local, p.stream));
-      dt = std::min(dt, local);
+      const cudaStream_t s = static_cast<cudaStream_t>(p.stream);
+      if (std::find(streams.begin(), streams.end(), s) == streams.end()) streams.push_back(s);
     });
-    return Duration(dt);
+    if (streams.empty()) return Duration(std::numeric_limits<double>::max());
+    Reduction& r = reduction();
+    const cudaStream_t s0 = streams.front();
+    CheckCuda(cudaMemsetAsync(r.word, 0, sizeof(unsigned long long), s0));
+    CheckCuda(cudaEventRecord(r.ready, s0));
+    for (size_t k = 1; k < streams.size(); ++k) CheckCuda(cudaStreamWaitEvent(streams[k], r.ready, 0));
+    adapter_.ForEachPatch(ctx, level, d, [&](const Patch& p) {
+      Check(fvs_compute_max_speed(&m_, adapter_.Rank(), p.scratch, p.scratch_box, d, 1, r.word,
+                                  p.stream));
+    });
+    for (size_t k = 1; k < streams.size(); ++k) {
+      CheckCuda(cudaEventRecord(r.done, streams[k]));
+      CheckCuda(cudaStreamWaitEvent(s0, r.done, 0));
+    }
+    unsigned long long bits = 0;
+    CheckCuda(cudaMemcpyAsync(&bits, r.word, sizeof bits, cudaMemcpyDeviceToHost, s0));
+    CheckCuda(cudaStreamSynchronize(s0));
+    double smax;
+    std::memcpy(&smax, &bits, sizeof smax);
+    return Duration(smax > 0.0 ? dx / smax : std::numeric_limits<double>::infinity());
   }
 
   // Fluxes on every face of the patch's flux array (its box must leave the
@@ -133,8 +164,31 @@ template <class Adapter> class FluxMethod {
   fvs_method& method() { return m_; }
 
  private:
+  // the level reduction's device word and events, made on first use and
+  // shared by copies of the flux method (the reference copies methods)
+  struct Reduction {
+    unsigned long long* word = nullptr;
+    cudaEvent_t ready = nullptr, done = nullptr;
+    ~Reduction() {
+      if (word) cudaFree(word);
+      if (ready) cudaEventDestroy(ready);
+      if (done) cudaEventDestroy(done);
+    }
+  };
+  Reduction& reduction() {
+    if (!reduction_) {
+      auto r = std::make_shared<Reduction>();
+      CheckCuda(cudaMalloc(reinterpret_cast<void**>(&r->word), sizeof(unsigned long long)));
+      CheckCuda(cudaEventCreateWithFlags(&r->ready, cudaEventDisableTiming));
+      CheckCuda(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming));
+      reduction_ = std::move(r);
+    }
+    return *reduction_;
+  }
+
   fvs_method m_{};
   Adapter adapter_;
+  std::shared_ptr<Reduction> reduction_;
 };
 
 template <class Adapter> class TimeIntegrator {

@@ -4,7 +4,13 @@
 //                with FVS_ERR_NO_DEVICE;
 //   "gpu":       a uniform 2-D state on one 16x8 patch: the stable dt is
 //                dx / (|u| + c), the fluxes are the physical flux, and the
-//                update and CompleteFromCons leave the state unchanged.
+//                update and CompleteFromCons leave the state unchanged;
+//   "patches IN OUT": a level of several patches read from file IN (doubles:
+//                nx, ny, ghosts, npatch, dx, then each patch's Complete
+//                scratch, 6 x (ny + 2g) x (nx + 2g)), each on its own CUDA
+//                stream: the level's stable dt in x, the x fluxes with half
+//                of it, the update and CompleteFromCons; writes to OUT the dt,
+//                then each patch's fluxes and its scratch.
 #include <cuda_runtime_api.h>
 
 #include <cmath>
@@ -29,6 +35,76 @@ struct OnePatchAdapter {
   double CellSize(FakeContext& c, int, int) { return c.dx; }
   template <class F> void ForEachPatch(FakeContext& c, int, int, F&& f) { f(c.patch); }
 };
+
+struct LevelContext {
+  std::vector<fvs_gpu::Patch> patches;
+  double dx = 0.0;
+};
+
+struct LevelAdapter {
+  int Rank() const { return 2; }
+  double Gamma() const { return 1.4; }
+  double CellSize(LevelContext& c, int, int) { return c.dx; }
+  template <class F> void ForEachPatch(LevelContext& c, int, int, F&& f) {
+    for (const fvs_gpu::Patch& p : c.patches) f(p);
+  }
+};
+
+int Patches(const char* in_path, const char* out_path) {
+  std::FILE* in = std::fopen(in_path, "rb");
+  if (!in) return 3;
+  double head[5];
+  if (std::fread(head, sizeof(double), 5, in) != 5) return 3;
+  const int nx = int(head[0]), ny = int(head[1]), g = int(head[2]), np = int(head[3]);
+  const int NX = nx + 2 * g, NY = ny + 2 * g;
+  const size_t nscr = size_t(6) * NX * NY, nflux = size_t(4) * (nx + 1) * ny;
+  LevelContext ctx;
+  ctx.dx = head[4];
+  std::vector<double*> dev_s(np), dev_f(np);
+  std::vector<cudaStream_t> streams(np);
+  std::vector<double> h(nscr);
+  for (int p = 0; p < np; ++p) {
+    if (std::fread(h.data(), sizeof(double), nscr, in) != nscr) return 3;
+    if (cudaStreamCreate(&streams[p]) != cudaSuccess ||
+        cudaMalloc(reinterpret_cast<void**>(&dev_s[p]), nscr * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(reinterpret_cast<void**>(&dev_f[p]), nflux * sizeof(double)) != cudaSuccess)
+      return 2;
+    cudaMemcpy(dev_s[p], h.data(), nscr * sizeof(double), cudaMemcpyHostToDevice);
+    fvs_gpu::Patch pt{};
+    pt.scratch = dev_s[p];
+    pt.scratch_box = {{-g, -g, 0}, {nx + g, ny + g, 1}};
+    pt.valid_box = {{0, 0, 0}, {nx, ny, 1}};
+    pt.fluxes = dev_f[p];
+    pt.flux_box = {{0, 0, 0}, {nx + 1, ny, 1}};
+    pt.stream = streams[p];
+    ctx.patches.push_back(pt);
+  }
+  std::fclose(in);
+  fvs_gpu::FluxMethod<LevelAdapter> fm;
+  fvs_gpu::TimeIntegrator<LevelAdapter> ti;
+  fvs_gpu::Reconstruction<LevelAdapter> rc;
+  const double dt = fm.ComputeStableDt(ctx, 0, Direction::X).count();
+  fm.ComputeNumericFluxes(ctx, 0, fvs_gpu::Duration(0.5 * dt), Direction::X);
+  ti.UpdateConservatively(ctx, 0, fvs_gpu::Duration(0.5 * dt), Direction::X);
+  rc.CompleteFromCons(ctx, 0, fvs_gpu::Duration(0.5 * dt));
+  if (cudaDeviceSynchronize() != cudaSuccess) return 2;
+  std::FILE* out = std::fopen(out_path, "wb");
+  if (!out) return 3;
+  std::fwrite(&dt, sizeof(double), 1, out);
+  std::vector<double> f(nflux);
+  for (int p = 0; p < np; ++p) {
+    cudaMemcpy(f.data(), dev_f[p], nflux * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(h.data(), dev_s[p], nscr * sizeof(double), cudaMemcpyDeviceToHost);
+    std::fwrite(f.data(), sizeof(double), nflux, out);
+    std::fwrite(h.data(), sizeof(double), nscr, out);
+    cudaFree(dev_s[p]);
+    cudaFree(dev_f[p]);
+    cudaStreamDestroy(streams[p]);
+  }
+  std::fclose(out);
+  std::printf("patches %d dt %.17g\n", np, dt);
+  return 0;
+}
 
 int NoDevice() {
   FakeContext ctx{};
@@ -110,5 +186,6 @@ int WithGpu() {
 
 int main(int argc, char** argv) {
   if (argc > 1 && std::strcmp(argv[1], "gpu") == 0) return WithGpu();
+  if (argc > 3 && std::strcmp(argv[1], "patches") == 0) return Patches(argv[2], argv[3]);
   return NoDevice();
 }
