@@ -165,18 +165,31 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
   } else {
     const double pv = PvrsTrGuess(g, L.rho, uL, L.p, L.a, R.rho, uR, R.p, R.a);
     x0 = pv;
-    // The learned start is used only where the PVRS/TR start is poor: its
-    // residual |f(p_pvrs)| exceeds kLearnedGate (aL + aR), i.e. roughly a
-    // relative error of more than a few per cent in p*.  Weak waves (most
-    // faces of a real flow), where PVRS/TR is accurate to second order in
-    // the wave strength and Newton needs zero or one step from it, keep
-    // their start and never pay for the network.
-    constexpr double kLearnedGate = 0.05;
+    // Cost-aware use of the learned start: the network costs less than one
+    // Newton step (its 5-64-64-1 FP32 multiply-adds against two FP64 pow
+    // evaluations per step), so it is used only where it is expected to
+    // save at least one step.  Newton converges quadratically, so from a
+    // start whose relative residual is r = |f(p0)| / (aL + aR) it needs
+    // about k(r) = ceil(log2(log(tol') / log(r))) steps to reach
+    // |f| <= tol, tol' = tol / (aL + aR).  The PVRS/TR start's r is known
+    // from its residual; the learned start's is taken as kLearnedRelErr,
+    // the network's typical relative error in p*.  Weak waves (most faces of
+    // a real flow), where PVRS/TR is accurate to second order in the wave
+    // strength, keep their start and never pay for the network.
+    constexpr float kLearnedRelErr = 0.01f;
     double f_pv = 0.0;
     bool screened = false;
     if (opt.guess == kGuessMlp) {
       f_pv = FSide(R, gm1, exponent, pv) + FSide(L, gm1, exponent, pv) + du;
-      screened = !(fabs(f_pv) > kLearnedGate * (L.a + R.a));
+      const float scale = static_cast<float>(L.a + R.a);
+      const float lt = __log2f(static_cast<float>(opt.tol) / scale);  // < 0 for tol < scale
+      auto steps = [&](float r) -> float {
+        if (!(r > exp2f(lt))) return 0.0f;   // already within the tolerance
+        if (!(r < 0.5f)) return 1e30f;       // outside the quadratic regime
+        return ceilf(__log2f(lt / __log2f(r)));
+      };
+      const float r_pv = static_cast<float>(fabs(f_pv)) / scale;
+      screened = !(steps(r_pv) >= steps(kLearnedRelErr) + 1.0f);
       if (screened || !opt.mlp) {
         // PVRS/TR start, reusing the residual just evaluated
         NewtonFrom(L, R, du, gm1, exponent, d_exponent, pv, f_pv, opt.tol, opt.max_iterations,

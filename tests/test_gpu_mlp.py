@@ -163,6 +163,9 @@ def test_training_cuts_newton_iterations(fvs, torch_cuda):
     summary = {k: v[:3] for k, v in stats.items()}
     print("newton iterations / fallback rate / failures:", summary)
     assert mlp_it < 0.75 * mean_it, summary
+    # the gain over PVRS/TR, the start value the solver would use without
+    # the network: fewer Newton steps per problem at this tolerance
+    assert mlp_it < 0.95 * pvrs_it, summary
     assert stats["mlp"][2] <= stats["mean"][2]
     conv = (stats["mlp"][4] != 0) & (stats["mean"][4] != 0)
     # same root from either start value; near-vacuum p* (down to 1e-28 here)
