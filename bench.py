@@ -484,10 +484,16 @@ def report_cutcell(args, torch, fvs, workloads, peaks=None):
         s.close()
         # drift: the same flow in a closed box (reflective walls on the domain
         # boundary), where nothing enters or leaves, so the volume-weighted
-        # mass and energy totals may change only by round-off
+        # mass and energy totals may change only by round-off.  Bodies that
+        # cross a wall are left out: behind a reflective wall the reference
+        # reflects the states but keeps the bodies' real geometry
+        # (cutcell::ReflectiveBoundary), which exchanges mass with the ghost
+        # layers where a body straddles the wall.
+        inside = circles[(circles[:, 0] - circles[:, 2] > 0) & (circles[:, 0] + circles[:, 2] < 1) &
+                         (circles[:, 1] - circles[:, 2] > 0) & (circles[:, 1] + circles[:, 2] < 1)]
         s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "reflective",
                        method=fvs.make_method(precision=prec))
-        s.set_embedded_circles(circles)
+        s.set_embedded_circles(inside)
         s.upload(cons)
         st, _ = s.run(cfl=0.5, t_end=1e9, max_steps=args.cutcell_steps)
         closed = s.download()
@@ -498,7 +504,8 @@ def report_cutcell(args, torch, fvs, workloads, peaks=None):
         t1 = (closed * w).reshape(4, -1).sum(axis=1)
         scale = (np.abs(cons) * w).reshape(4, -1).sum(axis=1)
         out["flavours"][prec]["closed_box_drift_rel"] = {
-            "steps": st.steps, "mass": float(abs(t1[0] - t0[0]) / scale[0]),
+            "steps": st.steps, "circles": int(len(inside)),
+            "mass": float(abs(t1[0] - t0[0]) / scale[0]),
             "energy": float(abs(t1[3] - t0[3]) / scale[3])}
         s.close()
     ref = finals["fp64_exact"]

@@ -345,9 +345,12 @@ __device__ __forceinline__ double Clamp01(double x) {
   return 1.0 < x ? 1.0 : x;
 }
 
-// Conservative state of cell (i, j), ghost cells (one direction at a time)
-// the boundary condition's images: reflective ghosts carry the reflected
-// momentum of their direction.
+// Conservative state of cell (i, j), ghost cells the boundary condition's
+// images.  A reflective ghost is the mirror cell's state with the momentum of
+// its direction reflected, or zero where the mirror cell has no volume
+// (cutcell::ReflectiveBoundary, include/fub/AMReX/cutcell/boundary_condition/
+// ReflectiveBoundary.hpp:72-122; where the ghost cell itself has no volume
+// the masked loads zero it).
 __device__ __forceinline__ void LoadCons(const CcStateArgs& a, int i, int j, double* u) {
   const int si = BcIndex(i, a.g.nx, a.bc[0]);
   const int sj = BcIndex(j, a.g.ny, a.bc[1]);
@@ -355,8 +358,13 @@ __device__ __forceinline__ void LoadCons(const CcStateArgs& a, int i, int j, dou
   const int64_t off = int64_t(sj) * a.g.nx + si;
 #pragma unroll
   for (int k = 0; k < 4; ++k) u[k] = __ldg(a.in + k * cs + off);
-  if (BcFlip(i, a.g.nx, a.bc[0])) u[1] = -u[1];
-  if (BcFlip(j, a.g.ny, a.bc[1])) u[2] = -u[2];
+  const bool fx = BcFlip(i, a.g.nx, a.bc[0]), fy = BcFlip(j, a.g.ny, a.bc[1]);
+  if (fx) u[1] = -u[1];
+  if (fy) u[2] = -u[2];
+  if ((fx || fy) && !(a.g.alpha[a.g.CellIndex(si, sj)] > 0.0)) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) u[k] = 0.0;
+  }
 }
 
 template <class T> __device__ __forceinline__ void Narrow(T* t, const double* u) {

@@ -522,9 +522,14 @@ std::vector<C2> CcScratch(const CcGrid& g, const double* cons) {
       for (int c = 0; c < 4; ++c) u[c] = cons[c * n + int64_t(sj) * g.nx + si];
       C2 q;
       CompleteFromConsMasked<2>(eq, q, u, g.Alpha(ii, jj) > 0.0);
-      // reflective walls: Reflect of the mirror cell's state, x then y
-      if (g.bc[0] == 2 && (ii < 0 || ii >= g.nx)) ReflectMomentum<2>(q.m, 0);
-      if (g.bc[1] == 2 && (jj < 0 || jj >= g.ny)) ReflectMomentum<2>(q.m, 1);
+      // reflective walls (cutcell::ReflectiveBoundary, ReflectiveBoundary.hpp:
+      // 72-122): Reflect of the mirror cell's state, x then y, or zeros where
+      // the mirror cell has no volume (the ghost's own alpha masks above)
+      const bool rx = g.bc[0] == 2 && (ii < 0 || ii >= g.nx);
+      const bool ry = g.bc[1] == 2 && (jj < 0 || jj >= g.ny);
+      if (rx) ReflectMomentum<2>(q.m, 0);
+      if (ry) ReflectMomentum<2>(q.m, 1);
+      if ((rx || ry) && !(g.Alpha(si, sj) > 0.0)) q = C2{};
       sc[size_t(g.C(ii, jj))] = q;
     }
   }
