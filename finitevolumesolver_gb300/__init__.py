@@ -298,6 +298,31 @@ class Solver:
         _capi.check(lib().fvs_solver_set_embedded_circles(self._h, c.ctypes.data, len(c),
                                                           float(x0), float(y0)))
 
+    def set_embedded_geometry(self, shapes, x0=0.0, y0=0.0) -> None:
+        """Union of shapes as the embedded body (the KBN cut-cell update):
+        dicts {"kind": "circle", "p": (cx, cy, r)}, {"kind": "halfspace",
+        "p": (nx, ny, offset)} (inside n . x - offset > 0), {"kind":
+        "polygon", "xy": [(x, y), ...]} (closed), each with an optional
+        "inverted": True (the body is the shape's outside)."""
+        import numpy as np
+        kinds = {"circle": 0, "halfspace": 1, "polygon": 2}
+        arr = (_capi.Shape * len(shapes))()
+        keep = []
+        for k, sh in enumerate(shapes):
+            arr[k].kind = kinds[sh["kind"]]
+            arr[k].inverted = 1 if sh.get("inverted") else 0
+            if sh["kind"] == "polygon":
+                xy = np.ascontiguousarray(sh["xy"], dtype=np.float64).reshape(-1, 2)
+                keep.append(xy)
+                arr[k].nvertices = len(xy)
+                arr[k].xy = xy.ctypes.data_as(C.POINTER(C.c_double))
+            else:
+                for i in range(3):
+                    arr[k].p[i] = float(sh["p"][i])
+        self._shapes = (arr, keep)
+        _capi.check(lib().fvs_solver_set_embedded_geometry(self._h, arr, len(shapes), float(x0),
+                                                           float(y0)))
+
     def cutcell_geometry(self):
         import numpy as np
         G = lib().fvs_cutcell_ghost_layers()

@@ -26,6 +26,12 @@ STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "DT_TOO_LARGE", 4: "UNSUPPO
                 5: "NO_DEVICE", 6: "STATE"}
 
 
+class Shape(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("inverted", C.c_int32), ("p", C.c_double * 3),
+                ("nvertices", C.c_int32), ("reserved", C.c_int32),
+                ("xy", C.POINTER(C.c_double))]
+
+
 class Box(C.Structure):
     _fields_ = [("lo", C.c_int32 * 3), ("hi", C.c_int32 * 3)]
 
@@ -131,6 +137,8 @@ def load() -> C.CDLL:
     L.fvs_cutcell_ghost_layers.restype = C.c_int
     L.fvs_solver_set_embedded_circles.argtypes = [_VP, _VP, C.c_int, C.c_double, C.c_double]
     L.fvs_solver_cutcell_geometry.argtypes = [_VP, _VP, _VP, _VP, _VP, _VP, _VP]
+    L.fvs_solver_set_embedded_geometry.argtypes = [_VP, P(Shape), C.c_int, C.c_double,
+                                                   C.c_double]
     L.fvs_solver_cutcell_shielded.argtypes = [_VP, C.c_int, _VP, _VP, _VP, _VP, _VP, _VP]
     L.fvs_solver_set_cycle.argtypes = [_VP, C.c_int64]
     L.fvs_solver_set_time.argtypes = [_VP, C.c_double]

@@ -941,17 +941,19 @@ int fvs_solver_tuning(fvs_solver* s, int32_t* seg, int32_t* occupancy) {
 
 int fvs_cutcell_ghost_layers(void) { return fvs::kCcGhost; }
 
-int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int ncircles,
-                                    double x0, double y0) {
-  if (!s || !circles) return Fail(FVS_ERR_INVALID, "NULL argument");
+}  // extern "C"
+
+namespace {
+
+// Embeds the body given by shape records (fvs_cutcell_geometry.cuh) into a
+// rank-2 MUSCL-HLLE solver: geometry, shielded fractions, cut flags, cell
+// classes and band lists on the device.
+int EmbedShapes(fvs_solver* s, const std::vector<double>& words, double x0, double y0) {
   if (s->g.rank != 2) return Fail(FVS_ERR_UNSUPPORTED, "cut cells need a rank-2 grid");
   if (s->m.flux_method != FVS_MUSCL_HLLE)
     return Fail(FVS_ERR_UNSUPPORTED, "cut cells run MUSCL-Hancock + HLLE");
   if (s->m.precision == FVS_FP64_DF)
     return Fail(FVS_ERR_UNSUPPORTED, "cut cells run in exact FP64, fast FP64 or mixed precision");
-  if (ncircles < 1 || ncircles > 16) return Fail(FVS_ERR_INVALID, "1 to 16 circles");
-  for (int k = 0; k < ncircles; ++k)
-    if (!(circles[3 * k + 2] > 0.0)) return Fail(FVS_ERR_INVALID, "circle radius must be > 0");
   if (s->cc) return Fail(FVS_ERR_INVALID, "embedded boundary already set");
   fvs::CcGeom& g = s->ccg;
   g.nx = s->g.n[0];
@@ -985,9 +987,10 @@ int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int nc
   FVS_CUDA(cudaMalloc(&cut, cells));
   s->cc_allocs.push_back(cut);
   g.cut = static_cast<signed char*>(cut);
-  double* dcirc = nullptr;
-  FVS_CUDA(alloc(&dcirc, size_t(3) * ncircles));
-  FVS_CUDA(cudaMemcpy(dcirc, circles, sizeof(double) * 3 * ncircles, cudaMemcpyHostToDevice));
+  double* dshape = nullptr;
+  FVS_CUDA(alloc(&dshape, words.size()));
+  FVS_CUDA(cudaMemcpy(dshape, words.data(), sizeof(double) * words.size(),
+                      cudaMemcpyHostToDevice));
   fvs::CcGeomArgs ga{};
   ga.nx = g.nx;
   ga.ny = g.ny;
@@ -995,8 +998,8 @@ int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int nc
   ga.y0 = y0;
   ga.dx = s->g.dx[0];
   ga.dy = s->g.dx[1];
-  ga.ncirc = ncircles;
-  ga.circles = dcirc;
+  ga.nwords = static_cast<int>(words.size());
+  ga.shapes = dshape;
   ga.alpha = g.alpha;
   ga.betax = g.beta[0];
   ga.betay = g.beta[1];
@@ -1043,6 +1046,78 @@ int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int nc
   for (auto& kv : s->graphs) cudaGraphExecDestroy(kv.second);
   s->graphs.clear();
   return FVS_OK;
+}
+
+// Crossings of the grid lines x = x0 + i dx and y = y0 + j dy (the grown
+// grid's cell edges) with a polygon's edges, at most per line.
+int MaxCrossings(const double* xy, int nv, int n, double origin, double h, bool vertical) {
+  int worst = 0;
+  for (int i = -fvs::kCcGhost; i <= n + fvs::kCcGhost; ++i) {
+    const double c = origin + double(i) * h;
+    int m = 0;
+    for (int e = 0; e + 1 < nv; ++e) {
+      const double vf = vertical ? xy[2 * e] : xy[2 * e + 1];
+      const double wf = vertical ? xy[2 * e + 2] : xy[2 * e + 3];
+      if ((vf < c && c <= wf) || (wf < c && c <= vf)) ++m;
+    }
+    worst = std::max(worst, m);
+  }
+  return worst;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int ncircles,
+                                    double x0, double y0) {
+  if (!s || !circles) return Fail(FVS_ERR_INVALID, "NULL argument");
+  if (ncircles < 1 || ncircles > 16) return Fail(FVS_ERR_INVALID, "1 to 16 circles");
+  std::vector<double> words;
+  for (int k = 0; k < ncircles; ++k) {
+    if (!(circles[3 * k + 2] > 0.0)) return Fail(FVS_ERR_INVALID, "circle radius must be > 0");
+    const double rec[5] = {0.0, 0.0, circles[3 * k], circles[3 * k + 1], circles[3 * k + 2]};
+    words.insert(words.end(), rec, rec + 5);
+  }
+  return EmbedShapes(s, words, x0, y0);
+}
+
+int fvs_solver_set_embedded_geometry(fvs_solver* s, const fvs_shape* shapes, int nshapes,
+                                     double x0, double y0) {
+  if (!s || !shapes) return Fail(FVS_ERR_INVALID, "NULL argument");
+  if (nshapes < 1 || nshapes > 256) return Fail(FVS_ERR_INVALID, "1 to 256 shapes");
+  std::vector<double> words;
+  for (int k = 0; k < nshapes; ++k) {
+    const fvs_shape& sh = shapes[k];
+    const double inv = sh.inverted ? 1.0 : 0.0;
+    if (sh.kind == FVS_SHAPE_CIRCLE) {
+      if (!(sh.p[2] > 0.0)) return Fail(FVS_ERR_INVALID, "circle radius must be > 0");
+      const double rec[5] = {0.0, inv, sh.p[0], sh.p[1], sh.p[2]};
+      words.insert(words.end(), rec, rec + 5);
+    } else if (sh.kind == FVS_SHAPE_HALFSPACE) {
+      // the normal made a unit vector (Halfspace's constructor normalises)
+      const double nn = std::sqrt(sh.p[0] * sh.p[0] + sh.p[1] * sh.p[1]);
+      if (!(nn > 0.0)) return Fail(FVS_ERR_INVALID, "half-space normal must be nonzero");
+      const double rec[5] = {1.0, inv, sh.p[0] / nn, sh.p[1] / nn, sh.p[2]};
+      words.insert(words.end(), rec, rec + 5);
+    } else if (sh.kind == FVS_SHAPE_POLYGON) {
+      const int nv = sh.nvertices;
+      if (nv < 4 || !sh.xy) return Fail(FVS_ERR_INVALID, "a polygon needs >= 4 vertices");
+      if (sh.xy[0] != sh.xy[2 * (nv - 1)] || sh.xy[1] != sh.xy[2 * (nv - 1) + 1])
+        return Fail(FVS_ERR_INVALID, "polygon not closed: first and last vertex must agree");
+      const int cx = MaxCrossings(sh.xy, nv, s->g.n[0], x0, s->g.dx[0], true);
+      const int cy = MaxCrossings(sh.xy, nv, s->g.n[1], y0, s->g.dx[1], false);
+      if (std::max(cx, cy) > 64)
+        return Fail(FVS_ERR_UNSUPPORTED, "a grid line crosses the polygon more than 64 times");
+      words.push_back(2.0);
+      words.push_back(inv);
+      words.push_back(double(nv));
+      words.insert(words.end(), sh.xy, sh.xy + 2 * nv);
+    } else {
+      return Fail(FVS_ERR_INVALID, "unknown shape kind");
+    }
+  }
+  return EmbedShapes(s, words, x0, y0);
 }
 
 int fvs_solver_cutcell_geometry(fvs_solver* s, double* alpha, double* betax, double* betay,

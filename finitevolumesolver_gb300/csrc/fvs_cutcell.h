@@ -66,8 +66,8 @@ struct CcGeom {
 struct CcGeomArgs {
   int nx, ny;
   double x0, y0, dx, dy;
-  int ncirc;
-  const double* circles;  // device, [ncirc][3]
+  int nwords;
+  const double* shapes;   // device, shape records (fvs_cutcell_geometry.cuh)
   double* alpha;
   double* betax;
   double* betay;

@@ -1,14 +1,25 @@
-// fvs_cutcell_geometry.cuh -- FP64 cut-cell geometry of a union of circles
-// (the embedded body is the inside of the circles), one cell or face per
+// fvs_cutcell_geometry.cuh -- FP64 cut-cell geometry of a union of shapes
+// (the embedded body is the union of their insides), one cell or face per
 // thread.
 //
-// AMReX's EB2 geometry generator, which the reference reads its cut-cell
-// data from (src/AMReX/cutcell/PatchHierarchy.cpp:507-547), is not part of
-// the reference tree; this is the library's own generator:
+// Shape records (flat doubles; the forms of the reference's
+// include/fub/geometry/*: Ball, Halfspace, Polygon, Invert, PolymorphicUnion):
+//   circle     [0, inverted, cx, cy, r]     inside: |x - c| < r
+//   halfspace  [1, inverted, nx, ny, o]     inside: n . x - o > 0, n a unit vector
+//                                           (src/geometry/Halfspace.cpp)
+//   polygon    [2, inverted, nv, x_0, y_0, ..., x_{nv-1}, y_{nv-1}]
+//              closed (last vertex = first), inside by the even-odd rule
+//              (src/geometry/Polygon.cpp)
+// inverted != 0: the shape's outside (Invert).
+//
+// AMReX's EB2 geometry generator, which the reference feeds these shapes to
+// and reads its cut-cell data from (src/AMReX/cutcell/PatchHierarchy.cpp:
+// 507-547), is not part of the reference tree; this is the library's own
+// generator:
 //  - face fraction beta: fluid length of the face / face length, from the
-//    exact intervals the circles cover on the face;
+//    exact intervals the shapes cover on the face;
 //  - volume fraction alpha: area of the polygon formed by the fluid parts of
-//    the cell's perimeter with every covered perimeter arc replaced by the
+//    the cell's perimeter with every covered perimeter piece replaced by the
 //    straight chord joining its ends (shoelace formula, cell units);
 //  - boundary normal: sum of the chords' left normals (pointing into the
 //    fluid, the sign convention of fub's GetBoundaryNormal,
@@ -24,32 +35,131 @@
 namespace fvs {
 namespace ccgeom {
 
-constexpr int kMaxCircles = 64;
+constexpr int kMaxIntervals = 64;  // intervals per segment, crossings per line
 
 struct Iv {
   double lo, hi;
 };
 
-// Merged covered intervals of the segment {fixed = c, free in [a, b]}.
-__device__ __forceinline__ int Covered(double c, double a, double b, bool vertical, int ncirc,
-                                       const double* __restrict__ circ, Iv* out) {
-  Iv iv[16];
+__device__ __forceinline__ int ShapeWords(const double* s) {
+  return s[0] == 2.0 ? 3 + 2 * int(s[2]) : 5;
+}
+
+// Intervals of [a, b] (sorted, disjoint) inside one shape on the segment
+// {fixed = c, free in [a, b]}; `vertical`: x = c.
+__device__ inline int ShapeIntervals(const double* __restrict__ s, double c, double a, double b,
+                                     bool vertical, Iv* out) {
   int n = 0;
-  for (int k = 0; k < ncirc && n < 16; ++k) {
-    const double cx = circ[3 * k], cy = circ[3 * k + 1], r = circ[3 * k + 2];
+  const int kind = int(s[0]);
+  if (kind == 0) {
+    const double cx = s[2], cy = s[3], r = s[4];
     const double d = vertical ? (c - cx) : (c - cy);
     if (fabs(d) < r) {
-      const double s = sqrt(r * r - d * d);
+      const double h = sqrt(r * r - d * d);
       const double m = vertical ? cy : cx;
-      double lo = m - s, hi = m + s;
+      double lo = m - h, hi = m + h;
       lo = lo > a ? lo : a;
       hi = hi < b ? hi : b;
       if (lo < hi) {
-        iv[n].lo = lo;
-        iv[n].hi = hi;
+        out[n].lo = lo;
+        out[n].hi = hi;
         ++n;
       }
     }
+  } else if (kind == 1) {
+    // phi(free) = k1 * free + k0 > 0 inside
+    const double nx = s[2], ny = s[3], o = s[4];
+    const double k1 = vertical ? ny : nx;
+    const double k0 = (vertical ? nx : ny) * c - o;
+    if (k1 == 0.0) {
+      if (k0 > 0.0) {
+        out[n].lo = a;
+        out[n].hi = b;
+        ++n;
+      }
+    } else {
+      const double root = -k0 / k1;
+      double lo = a, hi = b;
+      if (k1 > 0.0)
+        lo = root > a ? root : a;
+      else
+        hi = root < b ? root : b;
+      if (lo < hi) {
+        out[n].lo = lo;
+        out[n].hi = hi;
+        ++n;
+      }
+    }
+  } else {
+    // crossings of the polygon's edges with the line fixed = c (half-open
+    // rule on the fixed coordinate), sorted along the line
+    const int nv = int(s[2]);
+    const double* xy = s + 3;
+    double cr[kMaxIntervals];
+    int m = 0;
+    for (int e = 0; e + 1 < nv && m < kMaxIntervals; ++e) {
+      const double vf = vertical ? xy[2 * e] : xy[2 * e + 1];
+      const double wf = vertical ? xy[2 * e + 2] : xy[2 * e + 3];
+      const double vs = vertical ? xy[2 * e + 1] : xy[2 * e];
+      const double ws = vertical ? xy[2 * e + 3] : xy[2 * e + 2];
+      if ((vf < c && c <= wf) || (wf < c && c <= vf)) {
+        const double t = (c - vf) / (wf - vf);
+        cr[m++] = (1.0 - t) * vs + t * ws;
+      }
+    }
+    for (int i = 1; i < m; ++i) {
+      const double t = cr[i];
+      int j = i - 1;
+      while (j >= 0 && cr[j] > t) {
+        cr[j + 1] = cr[j];
+        --j;
+      }
+      cr[j + 1] = t;
+    }
+    for (int i = 0; i + 1 < m && n < kMaxIntervals; i += 2) {
+      const double lo = cr[i] > a ? cr[i] : a;
+      const double hi = cr[i + 1] < b ? cr[i + 1] : b;
+      if (lo < hi) {
+        out[n].lo = lo;
+        out[n].hi = hi;
+        ++n;
+      }
+    }
+  }
+  if (s[1] != 0.0) {
+    // complement within [a, b]
+    Iv inv[kMaxIntervals];
+    int k = 0;
+    double pos = a;
+    for (int i = 0; i < n && k < kMaxIntervals; ++i) {
+      if (out[i].lo > pos) {
+        inv[k].lo = pos;
+        inv[k].hi = out[i].lo;
+        ++k;
+      }
+      pos = out[i].hi;
+    }
+    if (pos < b && k < kMaxIntervals) {
+      inv[k].lo = pos;
+      inv[k].hi = b;
+      ++k;
+    }
+    for (int i = 0; i < k; ++i) out[i] = inv[i];
+    n = k;
+  }
+  return n;
+}
+
+// Merged covered intervals of the segment {fixed = c, free in [a, b]} by the
+// union of the shapes (nwords doubles of records).
+__device__ inline int Covered(double c, double a, double b, bool vertical, int nwords,
+                              const double* __restrict__ shapes, Iv* out) {
+  Iv iv[kMaxIntervals];
+  int n = 0;
+  for (int w = 0; w < nwords && n < kMaxIntervals; w += ShapeWords(shapes + w)) {
+    Iv part[kMaxIntervals];
+    const int k = ShapeIntervals(shapes + w, c, a, b, vertical, part);
+    for (int i = 0; i < k && n < kMaxIntervals; ++i) iv[n++] = part[i];
   }
   for (int i = 1; i < n; ++i) {
     const Iv t = iv[i];
@@ -120,36 +230,52 @@ __device__ __forceinline__ void UV(const PP& p, double& u, double& v) {
   }
 }
 
+// Position of v on a cell edge [a, b] of length h as a fraction of the edge,
+// walked from a (EdgeFrac) or from b (EdgeFracRev): the ends exactly 0 and 1
+// -- an interval clamped to an edge end stops there, and the perimeter walk
+// must see it meet the next edge's interval (a - b + h need not round to 0)
+// -- else (v - a) / h or (b - v) / h.
+__device__ __forceinline__ double EdgeFrac(double v, double a, double b, double h) {
+  if (v == a) return 0.0;
+  if (v == b) return 1.0;
+  return (v - a) / h;
+}
+__device__ __forceinline__ double EdgeFracRev(double v, double a, double b, double h) {
+  if (v == b) return 0.0;
+  if (v == a) return 1.0;
+  return (b - v) / h;
+}
+
 struct Cell {
   double alpha, nx, ny, cx, cy;
 };
 
-__device__ __forceinline__ Cell CellGeometry(double xa, double ya, double dx, double dy,
-                                             int ncirc, const double* __restrict__ circ) {
+__device__ inline Cell CellGeometry(double xa, double ya, double dx, double dy, int nwords,
+                                    const double* __restrict__ shapes) {
   const double xb = xa + dx, yb = ya + dy;
-  constexpr int kArcs = 64;
+  constexpr int kArcs = 4 * kMaxIntervals;
   PP lo[kArcs], hi[kArcs];
   int nc = 0;
-  Iv iv[16];
-  int n = Covered(ya, xa, xb, false, ncirc, circ, iv);
+  Iv iv[kMaxIntervals];
+  int n = Covered(ya, xa, xb, false, nwords, shapes, iv);
   for (int i = 0; i < n && nc < kArcs; ++i, ++nc) {
-    lo[nc] = Pt(0, (iv[i].lo - xa) / dx);
-    hi[nc] = Pt(0, (iv[i].hi - xa) / dx);
+    lo[nc] = Pt(0, EdgeFrac(iv[i].lo, xa, xb, dx));
+    hi[nc] = Pt(0, EdgeFrac(iv[i].hi, xa, xb, dx));
   }
-  n = Covered(xb, ya, yb, true, ncirc, circ, iv);
+  n = Covered(xb, ya, yb, true, nwords, shapes, iv);
   for (int i = 0; i < n && nc < kArcs; ++i, ++nc) {
-    lo[nc] = Pt(1, (iv[i].lo - ya) / dy);
-    hi[nc] = Pt(1, (iv[i].hi - ya) / dy);
+    lo[nc] = Pt(1, EdgeFrac(iv[i].lo, ya, yb, dy));
+    hi[nc] = Pt(1, EdgeFrac(iv[i].hi, ya, yb, dy));
   }
-  n = Covered(yb, xa, xb, false, ncirc, circ, iv);
+  n = Covered(yb, xa, xb, false, nwords, shapes, iv);
   for (int i = n - 1; i >= 0 && nc < kArcs; --i, ++nc) {
-    lo[nc] = Pt(2, (xb - iv[i].hi) / dx);
-    hi[nc] = Pt(2, (xb - iv[i].lo) / dx);
+    lo[nc] = Pt(2, EdgeFracRev(iv[i].hi, xa, xb, dx));
+    hi[nc] = Pt(2, EdgeFracRev(iv[i].lo, xa, xb, dx));
   }
-  n = Covered(xa, ya, yb, true, ncirc, circ, iv);
+  n = Covered(xa, ya, yb, true, nwords, shapes, iv);
   for (int i = n - 1; i >= 0 && nc < kArcs; --i, ++nc) {
-    lo[nc] = Pt(3, (yb - iv[i].hi) / dy);
-    hi[nc] = Pt(3, (yb - iv[i].lo) / dy);
+    lo[nc] = Pt(3, EdgeFracRev(iv[i].hi, ya, yb, dy));
+    hi[nc] = Pt(3, EdgeFracRev(iv[i].lo, ya, yb, dy));
   }
   Cell g{1.0, 0.0, 0.0, 0.0, 0.0};
   if (nc == 0) return g;

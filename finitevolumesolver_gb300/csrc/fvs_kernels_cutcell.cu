@@ -37,7 +37,7 @@ __global__ void GeometryCellKernel(CcGeomArgs a) {
   const int ii = static_cast<int>(id % NX), jj = static_cast<int>(id / NX);
   const double xa = a.x0 + double(ii - kCcGhost) * a.dx;
   const double ya = a.y0 + double(jj - kCcGhost) * a.dy;
-  const ccgeom::Cell g = ccgeom::CellGeometry(xa, ya, a.dx, a.dy, a.ncirc, a.circles);
+  const ccgeom::Cell g = ccgeom::CellGeometry(xa, ya, a.dx, a.dy, a.nwords, a.shapes);
   const int64_t plane = int64_t(NX) * NY;
   a.alpha[id] = g.alpha;
   a.normal[id] = g.nx;
@@ -51,19 +51,19 @@ __global__ void GeometryFaceKernel(CcGeomArgs a) {
   const int64_t nxf = int64_t(NX + 1) * NY;
   const int64_t nyf = int64_t(NX) * (NY + 1);
   const int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  ccgeom::Iv iv[16];
+  ccgeom::Iv iv[ccgeom::kMaxIntervals];
   if (id < nxf) {
     const int ii = static_cast<int>(id % (NX + 1)), jj = static_cast<int>(id / (NX + 1));
     const double xf = a.x0 + double(ii - kCcGhost) * a.dx;
     const double ya = a.y0 + double(jj - kCcGhost) * a.dy;
-    const int n = ccgeom::Covered(xf, ya, ya + a.dy, true, a.ncirc, a.circles, iv);
+    const int n = ccgeom::Covered(xf, ya, ya + a.dy, true, a.nwords, a.shapes, iv);
     a.betax[id] = ccgeom::FaceFraction(iv, n, ya, ya + a.dy);
   } else if (id < nxf + nyf) {
     const int64_t k = id - nxf;
     const int ii = static_cast<int>(k % NX), jj = static_cast<int>(k / NX);
     const double yf = a.y0 + double(jj - kCcGhost) * a.dy;
     const double xa = a.x0 + double(ii - kCcGhost) * a.dx;
-    const int n = ccgeom::Covered(yf, xa, xa + a.dx, false, a.ncirc, a.circles, iv);
+    const int n = ccgeom::Covered(yf, xa, xa + a.dx, false, a.nwords, a.shapes, iv);
     a.betay[k] = ccgeom::FaceFraction(iv, n, xa, xa + a.dx);
   }
 }

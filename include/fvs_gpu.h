@@ -374,6 +374,39 @@ int fvs_cutcell_ghost_layers(void);
  * states (PreAdvanceHierarchy). */
 int fvs_solver_set_embedded_circles(fvs_solver* s, const double* circles, int ncircles,
                                     double x0, double y0);
+/* Shapes of an embedded body, the forms of the reference's geometry
+ * (include/fub/geometry/Ball.hpp, Halfspace.hpp, Polygon.hpp, Invert.hpp;
+ * a list of shapes is their PolymorphicUnion):
+ *  circle:    p = (cx, cy, r), inside |x - c| < r;
+ *  halfspace: p = (nx, ny, offset), inside n . x - offset > 0 with n
+ *             normalised (src/geometry/Halfspace.cpp);
+ *  polygon:   nvertices (x, y) pairs in xy (host), closed (the last vertex
+ *             equals the first, as the reference requires), inside by the
+ *             even-odd rule (src/geometry/Polygon.cpp); a grid line may cross
+ *             it at most 64 times;
+ *  inverted != 0: the body is the shape's outside (Invert). */
+typedef enum fvs_shape_kind {
+  FVS_SHAPE_CIRCLE = 0,
+  FVS_SHAPE_HALFSPACE = 1,
+  FVS_SHAPE_POLYGON = 2
+} fvs_shape_kind;
+
+typedef struct fvs_shape {
+  int32_t kind;      /* fvs_shape_kind */
+  int32_t inverted;
+  double p[3];
+  int32_t nvertices; /* polygon */
+  int32_t reserved;
+  const double* xy;  /* polygon: host array [nvertices][2] */
+} fvs_shape;
+
+/* Embeds the union of `nshapes` (1..256) shapes as the body of a rank-2
+ * MUSCL-HLLE solver, exactly as fvs_solver_set_embedded_circles does for
+ * circles (which is this call with circle shapes): the library's FP64
+ * cut-cell geometry of the shapes (the reference hands them to AMReX's EB2,
+ * src/AMReX/cutcell/PatchHierarchy.cpp:507-547), computed on the device. */
+int fvs_solver_set_embedded_geometry(fvs_solver* s, const fvs_shape* shapes, int nshapes,
+                                     double x0, double y0);
 /* Copies the geometry to host arrays over the grid grown by
  * fvs_cutcell_ghost_layers() = G layers (NX = nx + 2G, NY = ny + 2G):
  * alpha [NY][NX], betax [NY][NX+1], betay [NY+1][NX], normal and center

@@ -19,8 +19,9 @@
 // KbnCutCellMethod(MusclHancock, HllMethod) in examples/AMReX/EB/2D/Schardin.cpp:58-61).
 //
 // Geometry: AMReX EB2 is not part of the reference, so this oracle computes
-// its own FP64 cut-cell geometry for a union of circles (the body is the
-// inside of the circles): face fractions from the exact covered intervals of
+// its own FP64 cut-cell geometry for a union of shapes -- circles,
+// half-spaces and polygons, each possibly inverted (the body is the union of
+// their insides): face fractions from the exact covered intervals of
 // each cell face, volume fractions as the area of the polygon formed by the
 // fluid parts of the cell boundary joined by straight chords, boundary normal
 // (into the fluid) and centroid (cell units, relative to the cell centre)
@@ -48,24 +49,112 @@ struct Interval {
   double lo, hi;
 };
 
-// Covered intervals of the segment {fixed coordinate = c, free coordinate in
-// [a, b]} by the union of circles, merged and sorted (free-coordinate units).
-// `vertical`: the segment is x = c (free coordinate y); else y = c.
-int CoveredIntervals(double c, double a, double b, bool vertical, int ncirc,
-                     const double* circ, Interval* out) {
-  Interval iv[64];
+// Shape records of the embedded body, the union of the shapes, as a flat
+// array of doubles (the forms of include/fub/geometry/*: Ball, Halfspace,
+// Polygon, Invert, PolymorphicUnion):
+//   circle     [0, inverted, cx, cy, r]     inside: |x - c| < r
+//   halfspace  [1, inverted, nx, ny, o]     inside: n . x - o > 0, n a unit vector
+//                                           (Halfspace::operator(), src/geometry/Halfspace.cpp)
+//   polygon    [2, inverted, nv, x_0, y_0, ..., x_{nv-1}, y_{nv-1}]
+//              closed (last vertex = first), inside by the even-odd rule
+//              (Polygon::ComputeDistanceTo, src/geometry/Polygon.cpp)
+// `inverted` != 0: the shape's outside (Invert).
+constexpr int kMaxIntervals = 64;
+
+int ShapeWords(const double* s) { return s[0] == 2.0 ? 3 + 2 * int(s[2]) : 5; }
+
+// Intervals of [a, b] (sorted, disjoint) inside one shape on the segment
+// {fixed coordinate = c, free coordinate in [a, b]}; `vertical`: x = c.
+int ShapeIntervals(const double* s, double c, double a, double b, bool vertical, Interval* out) {
   int n = 0;
-  for (int k = 0; k < ncirc && n < 64; ++k) {
-    const double cx = circ[3 * k], cy = circ[3 * k + 1], r = circ[3 * k + 2];
+  const int kind = int(s[0]);
+  if (kind == 0) {
+    const double cx = s[2], cy = s[3], r = s[4];
     const double d = vertical ? (c - cx) : (c - cy);
     if (std::fabs(d) < r) {
-      const double s = std::sqrt(r * r - d * d);
+      const double h = std::sqrt(r * r - d * d);
       const double m = vertical ? cy : cx;
-      double lo = m - s, hi = m + s;
+      double lo = m - h, hi = m + h;
       lo = lo > a ? lo : a;
       hi = hi < b ? hi : b;
-      if (lo < hi) iv[n++] = Interval{lo, hi};
+      if (lo < hi) out[n++] = Interval{lo, hi};
     }
+  } else if (kind == 1) {
+    // phi(free) = k1 * free + k0 > 0 inside
+    const double nx = s[2], ny = s[3], o = s[4];
+    const double k1 = vertical ? ny : nx;
+    const double k0 = (vertical ? nx : ny) * c - o;
+    if (k1 == 0.0) {
+      if (k0 > 0.0) out[n++] = Interval{a, b};
+    } else {
+      const double root = -k0 / k1;
+      double lo = a, hi = b;
+      if (k1 > 0.0)
+        lo = root > a ? root : a;
+      else
+        hi = root < b ? root : b;
+      if (lo < hi) out[n++] = Interval{lo, hi};
+    }
+  } else {
+    // crossings of the polygon's edges with the line fixed = c (half-open
+    // rule on the fixed coordinate, as CountCrossedLines_), sorted along it
+    const int nv = int(s[2]);
+    const double* xy = s + 3;
+    double cr[kMaxIntervals];
+    int m = 0;
+    for (int e = 0; e + 1 < nv && m < kMaxIntervals; ++e) {
+      const double vf = vertical ? xy[2 * e] : xy[2 * e + 1];
+      const double wf = vertical ? xy[2 * e + 2] : xy[2 * e + 3];
+      const double vs = vertical ? xy[2 * e + 1] : xy[2 * e];
+      const double ws = vertical ? xy[2 * e + 3] : xy[2 * e + 2];
+      if ((vf < c && c <= wf) || (wf < c && c <= vf)) {
+        const double t = (c - vf) / (wf - vf);
+        cr[m++] = (1.0 - t) * vs + t * ws;
+      }
+    }
+    for (int i = 1; i < m; ++i) {
+      const double t = cr[i];
+      int j = i - 1;
+      while (j >= 0 && cr[j] > t) {
+        cr[j + 1] = cr[j];
+        --j;
+      }
+      cr[j + 1] = t;
+    }
+    for (int i = 0; i + 1 < m && n < kMaxIntervals; i += 2) {
+      double lo = cr[i] > a ? cr[i] : a;
+      double hi = cr[i + 1] < b ? cr[i + 1] : b;
+      if (lo < hi) out[n++] = Interval{lo, hi};
+    }
+  }
+  if (s[1] != 0.0) {
+    // complement within [a, b]
+    Interval inv[kMaxIntervals];
+    int k = 0;
+    double pos = a;
+    for (int i = 0; i < n && k < kMaxIntervals; ++i) {
+      if (out[i].lo > pos) inv[k++] = Interval{pos, out[i].lo};
+      pos = out[i].hi;
+    }
+    if (pos < b && k < kMaxIntervals) inv[k++] = Interval{pos, b};
+    for (int i = 0; i < k; ++i) out[i] = inv[i];
+    n = k;
+  }
+  return n;
+}
+
+// Covered intervals of the segment {fixed coordinate = c, free coordinate in
+// [a, b]} by the union of the shapes (nwords doubles of records), merged and
+// sorted (free-coordinate units).  `vertical`: the segment is x = c (free
+// coordinate y); else y = c.
+int CoveredIntervals(double c, double a, double b, bool vertical, int nwords,
+                     const double* shapes, Interval* out) {
+  Interval iv[kMaxIntervals];
+  int n = 0;
+  for (int w = 0; w < nwords && n < kMaxIntervals; w += ShapeWords(shapes + w)) {
+    Interval part[kMaxIntervals];
+    const int k = ShapeIntervals(shapes + w, c, a, b, vertical, part);
+    for (int i = 0; i < k && n < kMaxIntervals; ++i) iv[n++] = part[i];
   }
   // insertion sort by lower end (stable)
   for (int i = 1; i < n; ++i) {
@@ -145,41 +234,57 @@ struct CellGeom {
   double cx, cy;  // boundary centroid, cell units relative to the centre
 };
 
+// Position of v on a cell edge [a, b] of length h as a fraction of the edge,
+// walked from a (EdgeFrac) or from b (EdgeFracRev): the ends exactly 0 and 1
+// -- an interval clamped to an edge end stops there, and the perimeter walk
+// must see it meet the next edge's interval (a - b + h need not round to 0)
+// -- else (v - a) / h or (b - v) / h.
+inline double EdgeFrac(double v, double a, double b, double h) {
+  if (v == a) return 0.0;
+  if (v == b) return 1.0;
+  return (v - a) / h;
+}
+inline double EdgeFracRev(double v, double a, double b, double h) {
+  if (v == b) return 0.0;
+  if (v == a) return 1.0;
+  return (b - v) / h;
+}
+
 // Volume fraction, normal and centroid of the cell [xa, xa+dx] x [ya, ya+dy].
 // Covered arcs of the perimeter are joined by straight chords; the fluid
 // region is the polygon made of the fluid perimeter arcs and the chords.
-CellGeom ComputeCell(double xa, double ya, double dx, double dy, int ncirc,
-                     const double* circ) {
+CellGeom ComputeCell(double xa, double ya, double dx, double dy, int nwords,
+                     const double* shapes) {
   const double xb = xa + dx, yb = ya + dy;
   PerimPoint lo[256], hi[256];
   int nc = 0;
   Interval iv[64];
   // bottom: y = ya, walked with x increasing
-  int n = CoveredIntervals(ya, xa, xb, false, ncirc, circ, iv);
+  int n = CoveredIntervals(ya, xa, xb, false, nwords, shapes, iv);
   for (int i = 0; i < n; ++i) {
-    lo[nc] = MakePoint(0, (iv[i].lo - xa) / dx);
-    hi[nc] = MakePoint(0, (iv[i].hi - xa) / dx);
+    lo[nc] = MakePoint(0, EdgeFrac(iv[i].lo, xa, xb, dx));
+    hi[nc] = MakePoint(0, EdgeFrac(iv[i].hi, xa, xb, dx));
     ++nc;
   }
   // right: x = xb, y increasing
-  n = CoveredIntervals(xb, ya, yb, true, ncirc, circ, iv);
+  n = CoveredIntervals(xb, ya, yb, true, nwords, shapes, iv);
   for (int i = 0; i < n; ++i) {
-    lo[nc] = MakePoint(1, (iv[i].lo - ya) / dy);
-    hi[nc] = MakePoint(1, (iv[i].hi - ya) / dy);
+    lo[nc] = MakePoint(1, EdgeFrac(iv[i].lo, ya, yb, dy));
+    hi[nc] = MakePoint(1, EdgeFrac(iv[i].hi, ya, yb, dy));
     ++nc;
   }
   // top: y = yb, x decreasing
-  n = CoveredIntervals(yb, xa, xb, false, ncirc, circ, iv);
+  n = CoveredIntervals(yb, xa, xb, false, nwords, shapes, iv);
   for (int i = n - 1; i >= 0; --i) {
-    lo[nc] = MakePoint(2, (xb - iv[i].hi) / dx);
-    hi[nc] = MakePoint(2, (xb - iv[i].lo) / dx);
+    lo[nc] = MakePoint(2, EdgeFracRev(iv[i].hi, xa, xb, dx));
+    hi[nc] = MakePoint(2, EdgeFracRev(iv[i].lo, xa, xb, dx));
     ++nc;
   }
   // left: x = xa, y decreasing
-  n = CoveredIntervals(xa, ya, yb, true, ncirc, circ, iv);
+  n = CoveredIntervals(xa, ya, yb, true, nwords, shapes, iv);
   for (int i = n - 1; i >= 0; --i) {
-    lo[nc] = MakePoint(3, (yb - iv[i].hi) / dy);
-    hi[nc] = MakePoint(3, (yb - iv[i].lo) / dy);
+    lo[nc] = MakePoint(3, EdgeFracRev(iv[i].hi, ya, yb, dy));
+    hi[nc] = MakePoint(3, EdgeFracRev(iv[i].lo, ya, yb, dy));
     ++nc;
   }
   CellGeom g{1.0, 0.0, 0.0, 0.0, 0.0};
@@ -271,15 +376,15 @@ CellGeom ComputeCell(double xa, double ya, double dx, double dy, int ncirc,
 
 extern "C" {
 
-// Geometry of the union of circles on an nx x ny grid of cells
-// [x0 + i dx, x0 + (i+1) dx] x [y0 + j dy, ...] grown by G ghost layers.
-// Outputs (component-major, x fastest, over the grown boxes):
-//   alpha [ny+2G][nx+2G]; betax [ny+2G][nx+2G+1] (face i between cells i-1
-//   and i); betay [ny+2G+1][nx+2G]; normal [2][ny+2G][nx+2G] (into the
-//   fluid); center [2][ny+2G][nx+2G] (cell units).
-void orc_cc_geometry(int nx, int ny, double x0, double y0, double dx, double dy, int G,
-                     int ncirc, const double* circ, double* alpha, double* betax,
-                     double* betay, double* normal, double* center) {
+// Geometry of the union of shapes (nwords doubles of shape records) on an
+// nx x ny grid of cells [x0 + i dx, x0 + (i+1) dx] x [y0 + j dy, ...] grown
+// by G ghost layers.  Outputs (component-major, x fastest, over the grown
+// boxes): alpha [ny+2G][nx+2G]; betax [ny+2G][nx+2G+1] (face i between
+// cells i-1 and i); betay [ny+2G+1][nx+2G]; normal [2][ny+2G][nx+2G] (into
+// the fluid); center [2][ny+2G][nx+2G] (cell units).
+void orc_cc_geometry_shapes(int nx, int ny, double x0, double y0, double dx, double dy, int G,
+                            int nwords, const double* shapes, double* alpha, double* betax,
+                            double* betay, double* normal, double* center) {
   const int NX = nx + 2 * G, NY = ny + 2 * G;
   const int64_t cells = int64_t(NX) * NY;
 #pragma omp parallel for schedule(dynamic, 16)
@@ -288,7 +393,7 @@ void orc_cc_geometry(int nx, int ny, double x0, double y0, double dx, double dy,
     for (int ii = 0; ii < NX; ++ii) {
       const double xa = x0 + double(ii - G) * dx;
       const double ya = y0 + double(jj - G) * dy;
-      const CellGeom g = ComputeCell(xa, ya, dx, dy, ncirc, circ);
+      const CellGeom g = ComputeCell(xa, ya, dx, dy, nwords, shapes);
       const int64_t c = int64_t(jj) * NX + ii;
       alpha[c] = g.alpha;
       normal[c] = g.nx;
@@ -299,7 +404,7 @@ void orc_cc_geometry(int nx, int ny, double x0, double y0, double dx, double dy,
     for (int ii = 0; ii <= NX; ++ii) {
       const double xf = x0 + double(ii - G) * dx;
       const double ya = y0 + double(jj - G) * dy;
-      const int n = CoveredIntervals(xf, ya, ya + dy, true, ncirc, circ, iv);
+      const int n = CoveredIntervals(xf, ya, ya + dy, true, nwords, shapes, iv);
       betax[int64_t(jj) * (NX + 1) + ii] = FaceFraction(iv, n, ya, ya + dy);
     }
   }
@@ -309,7 +414,7 @@ void orc_cc_geometry(int nx, int ny, double x0, double y0, double dx, double dy,
     for (int ii = 0; ii < NX; ++ii) {
       const double yf = y0 + double(jj - G) * dy;
       const double xa = x0 + double(ii - G) * dx;
-      const int n = CoveredIntervals(yf, xa, xa + dx, false, ncirc, circ, iv);
+      const int n = CoveredIntervals(yf, xa, xa + dx, false, nwords, shapes, iv);
       betay[int64_t(jj) * NX + ii] = FaceFraction(iv, n, xa, xa + dx);
     }
   }
@@ -328,6 +433,19 @@ void orc_cc_geometry(int nx, int ny, double x0, double y0, double dx, double dy,
         betay[int64_t(jj) * NX + ii] = 0.0;
     }
   }
+}
+
+// The same for a union of ncirc circles (cx, cy, r triples).
+void orc_cc_geometry(int nx, int ny, double x0, double y0, double dx, double dy, int G,
+                     int ncirc, const double* circ, double* alpha, double* betax,
+                     double* betay, double* normal, double* center) {
+  std::vector<double> words;
+  for (int k = 0; k < ncirc; ++k) {
+    const double rec[5] = {0.0, 0.0, circ[3 * k], circ[3 * k + 1], circ[3 * k + 2]};
+    words.insert(words.end(), rec, rec + 5);
+  }
+  orc_cc_geometry_shapes(nx, ny, x0, y0, dx, dy, G, int(words.size()), words.data(), alpha,
+                         betax, betay, normal, center);
 }
 
 }  // extern "C"

@@ -207,6 +207,8 @@ def _cc_lib():
         L.orc_cc_ghost_layers.restype = C.c_int
         L.orc_cc_geometry.argtypes = [I, I, C.c_double, C.c_double, C.c_double, C.c_double, I, I,
                                       _P, _P, _P, _P, _P, _P]
+        L.orc_cc_geometry_shapes.argtypes = [I, I, C.c_double, C.c_double, C.c_double,
+                                             C.c_double, I, I, _P, _P, _P, _P, _P, _P]
         L.orc_cc_shielded.argtypes = [I, I, I, _P, _P, _P, _P, _P, _P, _P, _P]
         L.orc_cc_cutcells.argtypes = [_I32, _P, _P, _P, _I32]
         L.orc_cc_reference_states.argtypes = [_I32, _I32, _P, _P, _P, _P, _P, _P, _P, _P]
@@ -221,12 +223,35 @@ def _cc_lib():
     return L
 
 
-class CutCellGeometry:
-    """FP64 geometry of a union of circles (solid inside) on an nx x ny grid
-    grown by `ghost` layers: alpha [NY][NX], betax [NY][NX+1],
-    betay [NY+1][NX], normal/center [2][NY][NX]."""
+def shape_words(shapes):
+    """Shape records (the oracle's and the library's flat form) of a list of
+    shapes given as dicts: {"kind": "circle", "p": (cx, cy, r)},
+    {"kind": "halfspace", "p": (nx, ny, offset)} (the normal is normalised
+    here, as Halfspace's constructor does), {"kind": "polygon", "xy":
+    [(x, y), ...]} (closed); optional "inverted": True."""
+    import math
+    words = []
+    for s in shapes:
+        inv = 1.0 if s.get("inverted") else 0.0
+        if s["kind"] == "circle":
+            words += [0.0, inv] + [float(v) for v in s["p"]]
+        elif s["kind"] == "halfspace":
+            nx, ny, o = (float(v) for v in s["p"])
+            nn = math.sqrt(nx * nx + ny * ny)
+            words += [1.0, inv, nx / nn, ny / nn, o]
+        else:
+            xy = [(float(x), float(y)) for x, y in s["xy"]]
+            words += [2.0, inv, float(len(xy))] + [v for pt in xy for v in pt]
+    return np.array(words, dtype=np.float64)
 
-    def __init__(self, nx, ny, circles, x0=0.0, y0=0.0, dx=None, dy=None):
+
+class CutCellGeometry:
+    """FP64 geometry of a union of circles (solid inside) -- or, with
+    `shapes`, of a union of shapes (shape_words) -- on an nx x ny grid grown
+    by `ghost` layers: alpha [NY][NX], betax [NY][NX+1], betay [NY+1][NX],
+    normal/center [2][NY][NX]."""
+
+    def __init__(self, nx, ny, circles=None, x0=0.0, y0=0.0, dx=None, dy=None, shapes=None):
         L = _cc_lib()
         self.G = int(L.orc_cc_ghost_layers())
         self.nx, self.ny = nx, ny
@@ -238,6 +263,12 @@ class CutCellGeometry:
         self.betay = np.zeros((NY + 1, NX))
         self.normal = np.zeros((2, NY, NX))
         self.center = np.zeros((2, NY, NX))
+        if shapes is not None:
+            words = shape_words(shapes)
+            L.orc_cc_geometry_shapes(nx, ny, x0, y0, self.dx, self.dy, self.G, len(words),
+                                     _d(words), _d(self.alpha), _d(self.betax), _d(self.betay),
+                                     _d(self.normal), _d(self.center))
+            return
         circ = np.ascontiguousarray(circles, dtype=np.float64).reshape(-1, 3)
         self.circles = circ
         L.orc_cc_geometry(nx, ny, x0, y0, self.dx, self.dy, self.G, len(circ), _d(circ.ravel()),

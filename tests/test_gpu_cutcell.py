@@ -127,3 +127,57 @@ def test_flavours_track_exact_and_conserve(fvs, orc, prec, variant):
     scale = (np.abs(cons) * w).reshape(4, -1).sum(axis=1)
     drift = np.abs(t1 - t0) / scale
     assert drift[0] < 1e-11 and drift[3] < 1e-11, drift
+
+
+def _star_polygon(cx, cy, r0, r1, n=5, phase=0.3):
+    import math
+    pts = []
+    for k in range(2 * n):
+        r = r0 if k % 2 == 0 else r1
+        t = phase + math.pi * k / n
+        pts.append((cx + r * math.cos(t), cy + r * math.sin(t)))
+    return pts + [pts[0]]
+
+
+SHAPE_CASES = {
+    "ramp": [{"kind": "halfspace", "p": (0.5, -1.0, -0.35)}],  # body below y = 0.35 + x/2
+    "star": [{"kind": "polygon", "xy": _star_polygon(0.5, 0.5, 0.3, 0.18)}],
+    "channel": [{"kind": "polygon", "inverted": True,
+                 "xy": [(-0.1, 0.2), (1.1, 0.3), (1.1, 0.8), (-0.1, 0.7), (-0.1, 0.2)]}],
+    "union": [{"kind": "halfspace", "p": (-0.2, 1.0, 0.85)},
+              {"kind": "circle", "p": (0.55, 0.4, 0.15)},
+              {"kind": "polygon", "xy": [(0.1, 0.1), (0.3, 0.1), (0.2, 0.3), (0.1, 0.1)]}],
+}
+
+
+@pytest.mark.parametrize("case", list(SHAPE_CASES))
+def test_general_geometry_bit_exact(fvs, orc, case):
+    n = 100
+    shapes = SHAPE_CASES[case]
+    s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive")
+    s.set_embedded_geometry(shapes)
+    g = s.cutcell_geometry()
+    ref = orc.CutCellGeometry(n, n, shapes=shapes)
+    for key in ("alpha", "betax", "betay", "normal", "center"):
+        np.testing.assert_array_equal(g[key], getattr(ref, key), err_msg=key)
+    G = ref.G
+    np.testing.assert_array_equal(g["cut"][G:-G, G:-G].astype(np.int32), ref.cut_cells())
+    assert ref.cut_cells().sum() > 0
+    s.close()
+
+
+@pytest.mark.parametrize("case", ["ramp", "union"])
+def test_shock_over_general_geometry_run_bit_exact(fvs, orc, case):
+    n = 96
+    shapes = SHAPE_CASES[case]
+    _, cons = workloads.shock_circles_2d(n, seed=5)
+    ref = orc.CutCellGeometry(n, n, shapes=shapes)
+    s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive")
+    s.set_embedded_geometry(shapes)
+    s.upload(cons)
+    st, dts = s.run(cfl=0.5, t_end=10.0, max_steps=6, log_len=8)
+    out, ref_dts, rs = ref.run(cons, 0.5, 10.0, max_steps=6)
+    assert st.steps == 6 and st.restarts == rs
+    np.testing.assert_array_equal(dts, ref_dts)
+    np.testing.assert_array_equal(s.download(), out)
+    s.close()
