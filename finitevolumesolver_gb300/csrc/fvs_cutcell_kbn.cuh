@@ -758,7 +758,10 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
       fetch(c0 - 2, um);
       fetch(c0 - 1, uc);
       C2T<T> recR_prev, q_prev;
-      double fs_prev[4];
+      // the previous face's flux (FP32 in the mixed flavour: the FP64
+      // difference is formed by DiffToDouble, one FP64 operation per
+      // component in the update)
+      T f_prev[4];
       int cls_prev = CellClassAt(g, dir, t, c0 - 1);
       for (int j = c0 - 1; j <= c1; ++j) {
         fetch(j + 1, up);
@@ -776,9 +779,6 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
             const T mx = PMaxT(PMaxT(T(0), fabs(s0w)), fabs(s1w));
             smax = mx > smax ? mx : smax;
           }
-          double fs[4];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) fs[k] = Widen(f[k] + T(0));
           if (j > c0 && cls_prev != kCcBand) {
             // cell j-1: regular, or covered (0)
             const int64_t o = offset(j - 1);
@@ -786,7 +786,12 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
 #pragma unroll
               for (int k = 0; k < 4; ++k) {
                 const double prev = __ldg(a.s.in + k * cs + o);
-                a.out[k * cs + o] = prev + dt_dx * (fs_prev[k] - fs[k]);
+                double d;
+                if constexpr (sizeof(T) == 4)
+                  d = DiffToDouble(f_prev[k], f[k]);
+                else
+                  d = Widen(f_prev[k] + T(0)) - Widen(f[k] + T(0));
+                a.out[k * cs + o] = prev + dt_dx * d;
               }
               if (__double_as_longlong(a.out[o]) <= 0) status |= kStatusNonPositiveDensity;
             } else {
@@ -795,7 +800,7 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
             }
           }
 #pragma unroll
-          for (int k = 0; k < 4; ++k) fs_prev[k] = fs[k];
+          for (int k = 0; k < 4; ++k) f_prev[k] = f[k];
           cls_prev = cls;
         }
         recR_prev = recR;

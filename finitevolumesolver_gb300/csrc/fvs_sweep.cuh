@@ -317,12 +317,12 @@ __device__ __forceinline__ double CflSync(unsigned long long* slot, double mine,
   return __longlong_as_double(static_cast<long long>(g > w ? g : w));
 }
 
-// F_L - F_R in FP64 for the conservative update: FP32 fluxes are widened
-// (exactly, on the integer pipe) and subtracted in FP64.
+// F_L - F_R in FP64 for the conservative update.  FP32 fluxes: the FP64
+// difference formed on the FP32 and integer pipes (DiffToDouble: exact
+// wherever the FP64 subtraction of the widened fluxes is exact), so the
+// update costs one FP64 operation per component, the FMA with dt/dx.
 __device__ __forceinline__ double FluxDiff(double a, double b) { return a - b; }
-__device__ __forceinline__ double FluxDiff(float a, float b) {
-  return FloatToDoubleBits(a) - FloatToDoubleBits(b);
-}
+__device__ __forceinline__ double FluxDiff(float a, float b) { return DiffToDouble(a, b); }
 __device__ __forceinline__ double FluxWiden(double a) { return a; }
 __device__ __forceinline__ double FluxWiden(float a) { return FloatToDoubleBits(a); }
 
