@@ -72,6 +72,11 @@ def parse():
     ap.add_argument("--hllem-n", type=int, default=192)
     ap.add_argument("--hllem-steps", type=int, default=10)
     ap.add_argument("--cutcell-steps", type=int, default=400)
+    ap.add_argument("--launch", action="append", default=[], metavar="DIR:SEG:VARIANT",
+                    help="with --profile-steps: force a direction's segment length and launch "
+                         "variant (fvs_solver_set_launch), e.g. 1:32:25 for the TMA-staged y "
+                         "sweep; with --report amr: LEVEL:DIR:BLOCK:GRID:THREADS_PER_ROW "
+                         "(fvs_amr_set_launch)")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiling aid: run this many Strang steps of the --n workload in "
                          "--precision with the default launch shapes (no autotuner, no "
@@ -386,6 +391,17 @@ def report_amr(args, torch, fvs, workloads, peaks):
     h, cons = workloads.amr_blast_2d(args.amr_n0, 3, seed=7, target=4096)
     cells = h.cells()
     upd_per_step = int(4 * sum(int(cells[l]) << l for l in range(h.nlevels)))
+    if args.profile_steps > 0:
+        # profiling aid: the first flavour, launch shapes from --launch
+        # (LEVEL:DIR:BLOCK:GRID:THREADS_PER_ROW) or the defaults, no autotuner
+        a = fvs.AmrSolver(h, fvs.make_method(precision=args.amr_flavours.split(",")[0]))
+        for spec in args.launch:
+            lv, d, block, grid, tpr = (int(v) for v in spec.split(":"))
+            a.set_launch(lv, d, block, grid, tpr)
+        a.upload(cons)
+        st, _ = a.run(cfl=0.8, t_end=1e9, max_steps=args.profile_steps)
+        a.close()
+        return {"profile_steps": st.steps}
     out = {"workload": f"2D blast on {h.npatches} patches, 3 levels (level 0 {args.amr_n0}^2), "
                        "ratio 2, extents from {8,16,32,64}, MUSCL-Hancock/VanLeer + HLLE, "
                        "subcycled Strang coarse steps, CFL 0.8, transmissive",
@@ -663,6 +679,9 @@ def run_ours(args):
     if args.profile_steps > 0:
         solver = fvs.Solver([n] * 3, [1.0 / n] * 3, "periodic",
                             method=fvs.make_method(precision=args.precision))
+        for spec in args.launch:
+            d, seg, var = (int(v) for v in spec.split(":"))
+            solver.set_launch(d, seg, var)
         solver.upload(cons)
         st, _ = solver.run(cfl=0.8, t_end=1e9, max_steps=args.profile_steps)
         solver.close()

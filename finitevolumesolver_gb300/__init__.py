@@ -576,6 +576,9 @@ class AmrSolver:
         return st, log[:min(log_len, st.steps)].copy()
 
     def set_launch(self, level, dir, block, grid, threads_per_row=1) -> None:
+        """Launch shape of a level's sweeps in direction dir: threads per
+        block, blocks, threads per patch row (1, 2, 4, 8; 32 for the mixed x
+        sweep with the lanes of a warp along x)."""
         _capi.check(lib().fvs_amr_set_launch(self._h, int(level), int(dir), int(block),
                                              int(grid), int(threads_per_row)))
 

@@ -57,7 +57,11 @@ struct LevelHost {
   int32_t nrows[2] = {0, 0};
   Seg* segs[2][kSplits] = {};
   int32_t nsegs[2][kSplits] = {};
-  int split[2] = {0, 0};  // index into kSplitOf
+  int split[2] = {0, 0};  // index into kSplitOf; kSplits: x rows with lanes along x
+  // slots of the x sweep with lanes along x (PatchSweepArgs::slot_row)
+  int32_t* slot_row = nullptr;
+  int32_t* row_slot0 = nullptr;
+  int64_t nslots = 0;
   Cap* caps[2] = {nullptr, nullptr};
   RefluxCell* reflux = nullptr;
   int32_t nreflux = 0;
@@ -417,6 +421,17 @@ int Build(fvs_amr* a) {
         Lv.nsegs[d][si] = int32_t(segs.size());
         AMR_CUDA(a->Upload(&Lv.segs[d][si], segs));
       }
+      if (d == 0) {
+        // x rows end to end as slots, cells -1..n of each
+        std::vector<int32_t> slot_row, row_slot0(R.size());
+        for (size_t r = 0; r < R.size(); ++r) {
+          row_slot0[r] = int32_t(slot_row.size());
+          slot_row.insert(slot_row.end(), size_t(R[r].n) + 2, int32_t(r));
+        }
+        Lv.nslots = int64_t(slot_row.size());
+        AMR_CUDA(a->Upload(&Lv.slot_row, slot_row));
+        AMR_CUDA(a->Upload(&Lv.row_slot0, row_slot0));
+      }
     }
     AMR_CUDA(a->Upload(&Lv.reflux, reflux_h[size_t(l)]));
     Lv.nreflux = int32_t(reflux_h[size_t(l)].size());
@@ -467,8 +482,17 @@ cudaError_t LaunchSweep(fvs_amr* a, int l, int d, const double* in, double* out,
     s.coarse = a->L[size_t(l - 1)].A;
     s.coarse_ncells = int32_t(a->L[size_t(l - 1)].ncells);
   }
-  s.segs = Lv.segs[d][split];
-  s.nsegs = Lv.nsegs[d][split];
+  if (split == kSplits) {  // x rows with the lanes of a warp along x
+    s.segs = Lv.segs[d][0];
+    s.nsegs = Lv.nsegs[d][0];
+    s.slot_row = Lv.slot_row;
+    s.row_slot0 = Lv.row_slot0;
+    s.nslots = Lv.nslots;
+    occ += 10;
+  } else {
+    s.segs = Lv.segs[d][split];
+    s.nsegs = Lv.nsegs[d][split];
+  }
   s.caps = Lv.caps[d];
   s.reg = a->reg;
   s.gamma = a->m.gamma;
@@ -900,7 +924,10 @@ int fvs_amr_set_launch(fvs_amr* a, int level, int dir, int block, int grid,
   int si = -1;
   for (int k = 0; k < kSplits; ++k)
     if (kSplitOf[k] == threads_per_row) si = k;
-  if (si < 0) return Fail(FVS_ERR_INVALID, "threads per row must be 1, 2, 4 or 8");
+  if (threads_per_row == 32 && dir == 0 && a->m.precision == FVS_MIXED) si = kSplits;
+  if (si < 0)
+    return Fail(FVS_ERR_INVALID,
+                "threads per row must be 1, 2, 4 or 8 (or 32: x rows with lanes along x, mixed)");
   a->L[size_t(level)].block[dir] = block;
   a->L[size_t(level)].grid[dir] = grid;
   a->L[size_t(level)].split[dir] = si;
@@ -934,12 +961,20 @@ int fvs_amr_autotune(fvs_amr* a, int32_t* configs) {
       float best = 1e30f;
       Tuned bt{128, Lv.grid[d], 0, 0};
       const bool mixed = a->m.precision == FVS_MIXED;
-      for (int si = 0; si < kSplits; ++si) {
-        if (si > 0 && Lv.nsegs[d][si] == Lv.nsegs[d][si - 1]) continue;  // rows too short
+      // splits of the marching kernel, and (mixed x sweeps) the kernel with
+      // the lanes of a warp along x
+      for (int si = 0; si <= kSplits; ++si) {
+        if (si == kSplits && !(mixed && d == 0)) continue;
+        if (si > 0 && si < kSplits && Lv.nsegs[d][si] == Lv.nsegs[d][si - 1])
+          continue;  // rows too short
+        const int64_t threads =
+            si == kSplits
+                ? 32 * std::max<int64_t>(1, (Lv.nslots - 1 + kRowWarpStep - 1) / kRowWarpStep)
+                : int64_t(Lv.nsegs[d][si]);
         for (int occ : {0, 5}) {
           if (occ && !mixed) continue;
           for (int block : {64, 128}) {
-            const int full = std::max(1, (Lv.nsegs[d][si] + block - 1) / block);
+            const int full = int(std::max<int64_t>(1, (threads + block - 1) / block));
             for (int bps : {1, 2, 4, 8, 16, 64}) {
               const int grid = std::min(full, a->sms * bps);
               float sum = 0.f;
@@ -980,7 +1015,8 @@ int fvs_amr_autotune(fvs_amr* a, int32_t* configs) {
       for (int d = 0; d < 2; ++d) {
         configs[(l * 2 + d) * 3] = a->L[size_t(l)].block[d];
         configs[(l * 2 + d) * 3 + 1] = a->L[size_t(l)].grid[d];
-        configs[(l * 2 + d) * 3 + 2] = kSplitOf[a->L[size_t(l)].split[d]];
+        configs[(l * 2 + d) * 3 + 2] =
+            a->L[size_t(l)].split[d] == kSplits ? 32 : kSplitOf[a->L[size_t(l)].split[d]];
       }
   DropGraphs(a);
   return FVS_OK;

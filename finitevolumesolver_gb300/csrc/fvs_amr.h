@@ -119,7 +119,18 @@ struct PatchSweepArgs {
   double dt_scale;       // split dt = dt_scale * (*dt_ptr)
   unsigned long long* smax_out;  // this sweep's max signal speed (bits)
   AmrControl* ctrl;
+  // x sweeps with the lanes of a warp along x (PatchRowWarpKernel): the
+  // level's rows (segs, one segment per row) laid end to end as slots,
+  // n + 2 per row (cells -1..n); slot_row[s] is slot s's row, row_slot0[r]
+  // row r's first slot
+  const int32_t* slot_row;
+  const int32_t* row_slot0;
+  int64_t nslots;
 };
+
+// Slots of a row-warp sweep: warp w takes slots kRowWarpStep * w ..
+// kRowWarpStep * w + 31 and owns (updates, captures, CFL) the middle 30.
+constexpr int kRowWarpStep = 30;
 
 struct MaxSpeedArgs {
   const double* in;

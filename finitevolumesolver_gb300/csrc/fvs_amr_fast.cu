@@ -12,8 +12,14 @@ cudaError_t LaunchPatchSweepFast(int dir, const PatchSweepArgs& a, int grid, int
   return LaunchPatchSweepT<Fast64Policy>(dir, a, grid, block, s);
 }
 
+// occupancy 0 or 5: register/occupancy variant; + 10 for the x sweep with
+// the lanes of a warp along x (PatchRowWarpKernel)
 cudaError_t LaunchPatchSweepMixed(int dir, const PatchSweepArgs& a, int grid, int block,
                                   int occupancy, cudaStream_t s) {
+  if (dir == 0 && occupancy >= 10) {
+    if (occupancy == 15) return LaunchPatchRowWarpT<Mixed32PolicyOcc5>(a, grid, block, s);
+    return LaunchPatchRowWarpT<Mixed32Policy>(a, grid, block, s);
+  }
   if (occupancy == 5) return LaunchPatchSweepT<Mixed32PolicyOcc5>(dir, a, grid, block, s);
   return LaunchPatchSweepT<Mixed32Policy>(dir, a, grid, block, s);
 }

@@ -179,6 +179,145 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
   if (status) atomicOr(&a.ctrl->step_status, status);
 }
 
+// PatchRowWarpKernel: the x sweeps of the mixed flavour with the lanes of a
+// warp along x.  The level's x rows are laid end to end as slots, n + 2 per
+// row (cells -1..n); warp w takes slots 30w .. 30w + 31 (grid-stride).  Lane
+// l holds the cell of slot 30w + l in the compute precision and gets its
+// neighbours by shuffles, or loads them where the neighbour lies in another
+// row (the halo cells -2 and n + 1) or outside the warp; it evaluates that
+// cell's MUSCL predictor once, and lanes 1..31 the flux of the face on the
+// cell's left.  Lanes 1..30 own their slots: they update interior cells
+// (0 <= c < n) with the faces on both sides (the right one from the next
+// lane), accumulate captured faces into the flux registers and fold their
+// faces' signal speeds into the sweep's maximum.  Every predictor is
+// evaluated once per row (plus those of cells -1 and n, which faces 0 and n
+// need), where PatchSweepKernel's segments repeat two per segment and load
+// four halo cells each, and a warp's loads of a row are consecutive.  The
+// arithmetic per cell and face is PatchSweepKernel's: the results are the
+// same, bit for bit.  Policies whose CFL speeds are FP32-screened (the FP64
+// flavours) keep PatchSweepKernel.
+template <template <int> class PT>
+__global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchRowWarpKernel(PatchSweepArgs a) {
+  using P = PT<2>;
+  using R = typename P::Real;
+  constexpr int K = kComp;
+  static_assert(!(EinfeldtCfl<P>::value && HasFluxOnly<P>::value),
+                "screened-CFL policies use PatchSweepKernel");
+  using Cell = CellArr<R, K>;
+  using FluxT = typename FluxOf<P>::type;
+  using Flx = CellArr<FluxT, K>;
+  const double split_dt = a.dt_scale * (*a.dt_ptr);
+  const typename P::Gas eq = P::MakeGas(a.gamma);
+  const double lambda_half = 0.5 * split_dt / a.dx;
+  const double dt_dx = split_dt / a.dx;
+  const int64_t N = a.ncells;
+  const double* __restrict__ in = a.in;
+  double* __restrict__ out = a.out;
+  const int lane = threadIdx.x & 31;
+  R smax = R(0);
+  int status = 0;
+  typename P::Stats stats;
+  const int64_t nwarps = a.nslots > 1 ? (a.nslots - 1 + kRowWarpStep - 1) / kRowWarpStep : 0;
+  const int64_t wstride = (int64_t(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w < nwarps;
+       w += wstride) {
+    const int64_t s = w * kRowWarpStep + lane;
+    const bool valid = s < a.nslots;
+    Seg row{};
+    int c = 0;
+    if (valid) {
+      const int32_t r = a.slot_row[s];
+      row = a.segs[r];
+      c = static_cast<int>(s - a.row_slot0[r]) - 1;
+    }
+    // cell x (-2..n+1) of the slot's row: interior, or a halo cell where it
+    // lives (this level or the coarser one, a reflective image flipped)
+    auto load = [&](double* u, int x) {
+      const double* src = in;
+      int64_t off, cs = N;
+      bool flip = false;
+      if (x >= 0 && x < row.n) {
+        off = int64_t(row.base) + x + kGhost;
+      } else {
+        const int h = x < 0 ? x + 2 : x - row.n + 2;
+        const int32_t g = row.halo[h];
+        if (g >= 0) {
+          off = g;
+        } else {
+          off = -int64_t(g) - 1;
+          src = a.coarse;
+          cs = a.coarse_ncells;
+        }
+        flip = (row.flip >> h) & 1;
+      }
+#pragma unroll
+      for (int k = 0; k < K; ++k) u[k] = __ldg(src + k * cs + off);
+      if (flip) u[1] = -u[1];
+    };
+    Cell C{}, Cm{}, Cp{};
+    double u[K];
+    if (valid) {
+      load(u, c);
+      P::ToCell(C.v, u);
+    }
+    const Cell up = ShflUp(C, 1), down = ShflDown(C, 1);
+    if (valid) {
+      if (c == -1 || lane == 0) {
+        load(u, c - 1);
+        P::ToCell(Cm.v, u);
+      } else {
+        Cm = up;
+      }
+      if (c == row.n || lane == 31) {
+        load(u, c + 1);
+        P::ToCell(Cp.v, u);
+      } else {
+        Cp = down;
+      }
+    }
+    typename P::Rec recL, recR;
+    P::Predict(eq, recL, recR, Cm.v, C.v, Cp.v, a.limiter, lambda_half, 0);
+    const typename P::Wave W = P::MakeWave(eq, C.v, 0);
+    const typename P::Rec recRm = ShflUp(recR, 1);
+    const typename P::Wave Wm = ShflUp(W, 1);
+    // face c (cells c-1 and c)
+    Flx F{};
+    R sp = R(0);
+    if (valid && lane >= 1 && c >= 0) sp = SweepFace<P>(eq, F.v, recRm, recL, Wm, W, 0, stats);
+    const Flx Fr = ShflDown(F, 1);  // face c + 1
+    const bool own = valid && lane >= 1 && lane <= kRowWarpStep && c >= 0;
+    if (own) {
+      smax = sp > smax ? sp : smax;
+      for (int q = row.cap_begin; q < row.cap_end; ++q) {
+        const Cap cp = a.caps[q];
+        if (cp.face != c) continue;
+        double* dst = a.reg + int64_t(cp.dst) * K;
+#pragma unroll
+        for (int k = 0; k < K; ++k) dst[k] = dst[k] + split_dt * FluxWiden(F.v[k]);
+      }
+      if (c < row.n) {
+        const int64_t off = int64_t(row.base) + c + kGhost;
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const double v = __ldg(in + k * N + off) + dt_dx * FluxDiff(F.v[k], Fr.v[k]);
+          out[k * N + off] = v;
+          if (k == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
+        }
+      }
+    }
+  }
+  const double smax_d = static_cast<double>(smax);
+  BlockMaxAtomic<1>(a.smax_out, &smax_d);
+  if (status) atomicOr(&a.ctrl->step_status, status);
+}
+
+template <template <int> class PT>
+cudaError_t LaunchPatchRowWarpT(const PatchSweepArgs& a, int grid, int block, cudaStream_t s) {
+  if (a.nslots == 0) return cudaSuccess;
+  PatchRowWarpKernel<PT><<<grid, block, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 // Max signal speed over the faces 0..n of every row (the stable dt of the
 // level in that direction is dx / max): a segment [j0, j1) of a row takes
 // the faces j0..j1 (neighbouring segments share a face; the max does not

@@ -5,6 +5,7 @@
 #include "fvs_cutcell.h"
 #include "fvs_internal.h"
 #include "fvs_plotfile.h"
+#include "fvs_tma.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -237,6 +238,10 @@ struct fvs_solver {
   // into `stream` by the two events
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // tensor maps of the three state buffers for the TMA-staged y and z
+  // sweeps of the mixed flavour ([buffer][dir - 1]); built on first use
+  alignas(64) CUtensorMap tmap[3][2];
+  int tmap_state = 0;  // 0 not tried, 1 built, -1 not available
   ~fvs_solver() {
     for (void* p : cc_allocs) cudaFree(p);
     if (ev_fork) cudaEventDestroy(ev_fork);
@@ -255,6 +260,58 @@ struct fvs_solver {
 };
 
 namespace {
+
+// The tensor maps of the TMA-staged sweep: each state buffer as
+// [K][nz][ny][nx] (rank 3) or [K][ny][nx] (rank 2) FP64 with boxes of
+// 32 x-cells by kTmaRows cells along y or z by all K components.  Available
+// for the mixed flavour's MUSCL-HLLE / HLLE sweeps of grids of rank >= 2
+// with an even nx (TMA's row pitch must be a multiple of 16 bytes).
+bool TmaMapsReady(fvs_solver* s) {
+  if (s->tmap_state != 0) return s->tmap_state > 0;
+  s->tmap_state = -1;
+  const int rank = s->g.rank;
+  if (s->cc || s->m.precision != FVS_MIXED || s->m.flux_method > FVS_HLLE || rank < 2 ||
+      (s->g.n[0] % 2) != 0)
+    return false;
+  const fvs::tma::EncodeTiledFn fn = fvs::tma::EncodeTiled();
+  if (!fn) return false;
+  const int K = rank + 2;
+  const cuuint64_t nx = cuuint64_t(s->g.n[0]), ny = cuuint64_t(s->g.n[1]),
+                   nz = cuuint64_t(rank == 3 ? s->g.n[2] : 1);
+  for (int b = 0; b < 3; ++b) {
+    for (int d = 1; d < rank; ++d) {
+      CUresult r;
+      const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
+      if (rank == 3) {
+        const cuuint64_t dims[4] = {nx, ny, nz, cuuint64_t(K)};
+        const cuuint64_t strides[3] = {nx * 8, nx * ny * 8, nx * ny * nz * 8};
+        const cuuint32_t box[4] = {32u, d == 1 ? cuuint32_t(fvs::kTmaRows) : 1u,
+                                   d == 2 ? cuuint32_t(fvs::kTmaRows) : 1u, cuuint32_t(K)};
+        r = fn(&s->tmap[b][d - 1], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, s->buf[b], dims,
+               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      } else {
+        const cuuint64_t dims[3] = {nx, ny, cuuint64_t(K)};
+        const cuuint64_t strides[2] = {nx * 8, nx * ny * 8};
+        const cuuint32_t box[3] = {32u, cuuint32_t(fvs::kTmaRows), cuuint32_t(K)};
+        r = fn(&s->tmap[b][d - 1], CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, s->buf[b], dims,
+               strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      }
+      if (r != CUDA_SUCCESS) return false;
+    }
+  }
+  s->tmap_state = 1;
+  return true;
+}
+
+// The tensor map of `in` (one of the state buffers) for a sweep in `dir`.
+const void* TmaMapOf(const fvs_solver* s, const double* in, int dir) {
+  if (s->tmap_state <= 0 || dir < 1) return nullptr;
+  for (int b = 0; b < 3; ++b)
+    if (s->buf[b] == in) return &s->tmap[b][dir - 1];
+  return nullptr;
+}
 
 int SegLen(const fvs_solver* s, int dir) {
   if (s->seg_len > 0) return s->seg_len;
@@ -354,6 +411,7 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
   a.mlp = s->m.mlp_params;
   a.stats_out = ctrl ? ctrl->newton : s->newton_words;
   a.skip_cfl = skip_cfl ? 1 : 0;
+  a.tmap = a.occupancy >= 20 ? TmaMapOf(s, in, dir) : nullptr;
   if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
     return fvs::LaunchSweepGodunov(a, s->m.flux_method == FVS_MUSCL_GODUNOV, s->stream);
   if (HllemRecon(s->m.flux_method) >= 0)
@@ -842,7 +900,8 @@ int fvs_solver_set_launch(fvs_solver* s, int dir, int seg_len, int variant) {
   bool ok = variant == 0;
   if (s->m.precision == FVS_MIXED && plain_hlle)
     ok = variant == 0 || variant == 4 || variant == 5 ||
-         (dir == 0 && (variant == 10 || variant == 14 || variant == 15));
+         (dir == 0 && (variant == 10 || variant == 14 || variant == 15)) ||
+         (dir >= 1 && (variant == 20 || variant == 24 || variant == 25) && TmaMapsReady(s));
   if (s->m.precision == FVS_FP64_DF && plain_hlle) ok = variant == 0 || variant == 3;
   if (s->cc) ok = variant == 0;
   if (!ok) return Fail(FVS_ERR_INVALID, "no such launch variant for this method");
@@ -863,9 +922,11 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   const bool plain_hlle = s->m.flux_method <= FVS_HLLE && !s->cc;
   const bool mixed = s->m.precision == FVS_MIXED && plain_hlle;
   const bool df = s->m.precision == FVS_FP64_DF && plain_hlle;
-  // mixed x sweeps: lanes-along-x kernel (0, 4, 5) or marching kernel (10, 14, 15)
+  // mixed x sweeps: lanes-along-x kernel (0, 4, 5) or marching kernel (10, 14, 15);
+  // mixed y/z sweeps: marching kernel (0, 4, 5) or TMA-staged kernel (20, 24, 25)
   const int occs_mixed_x[] = {0, 4, 5, 10, 14, 15};
-  const int occs_mixed[] = {0, 4, 5};
+  const int occs_mixed[] = {0, 4, 5, 20, 24, 25};
+  const bool tma = mixed && TmaMapsReady(s);
   const int occs_df[] = {0, 3};
   const int occs_plain[] = {0};
   // cut cells: segment lengths of the FP64 flavours' regular-cell sweep (the
@@ -887,7 +948,7 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   for (int d = 0; d < s->g.rank; ++d) {
     const int nd = s->g.n[d];
     const int* occs = mixed ? (d == 0 ? occs_mixed_x : occs_mixed) : (df ? occs_df : occs_plain);
-    const int nocc = mixed ? (d == 0 ? 6 : 3) : (df ? 2 : 1);
+    const int nocc = mixed ? (d == 0 || tma ? 6 : 3) : (df ? 2 : 1);
     float best = 1e30f;
     int best_seg = 0, best_occ = 0;
     for (int oi = 0; oi < nocc; ++oi) {
@@ -1370,6 +1431,8 @@ int fvs_solver_run(fvs_solver* s, double cfl, double t_end, int max_steps,
     stats->status = h.status;
     stats->last_dt = h.dt;
   }
+  if (h.status & fvs::kStatusCopyTimeout)
+    return Fail(FVS_ERR_CUDA, "a staged copy of a sweep did not land in time");
   if (h.status) return Fail(FVS_ERR_STATE, "non-positive density encountered");
   return FVS_OK;
 }

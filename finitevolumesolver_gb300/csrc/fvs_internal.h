@@ -45,7 +45,14 @@ enum StatusBits : int {
   kStatusNonPositiveDensity = 1,
   kStatusNonFinite = 2,
   kStatusNewtonNotConverged = 4,
+  kStatusCopyTimeout = 8,  // a staged (TMA) copy did not land in time
 };
+
+// The TMA-staged y/z sweep (mixed flavour): each warp stages its 32 lines
+// in a ring of kTmaStages buffers of kTmaRows cells; blocks of kTmaWarps.
+constexpr int kTmaRows = 2;
+constexpr int kTmaStages = 4;
+constexpr int kTmaWarps = 4;
 
 // One directional sweep of a uniform grid: fluxes, conservative update and
 // the CFL reduction of the input state, in one pass.
@@ -81,7 +88,9 @@ struct SweepArgs {
   int skip_cfl;
   int occupancy;        // 0 (registers as needed) or the resident blocks per SM a
                         // variant is compiled for (mixed: 4, 5; double-float: 3);
-                        // mixed x sweeps: + 10 for the marching kernel in x
+                        // mixed x sweeps: + 10 for the marching kernel in x;
+                        // mixed y/z sweeps: + 20 for the TMA-staged kernel
+  const void* tmap;     // host: CUtensorMap of `in` for the TMA-staged kernel, or NULL
 };
 
 // Stable-dt pass over all directions (max face speed per direction).

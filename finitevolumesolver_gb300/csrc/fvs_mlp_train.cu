@@ -148,29 +148,8 @@ __global__ void __launch_bounds__(tc::kThreads)
   if (warp == 0) tc::TmemDealloc(tmem, kCols);
 }
 
-using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-// cuTensorMapEncodeTiled from the driver, found through the runtime (no
-// link-time dependency on libcuda).
-EncodeTiledFn EncodeTiled() {
-  static EncodeTiledFn fn = nullptr;
-  static bool looked = false;
-  if (!looked) {
-    looked = true;
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-    else
-      cudaGetLastError();
-  }
-  return fn;
-}
+using tma::EncodeTiled;
+using tma::EncodeTiledFn;
 
 // Tensor map of a row-major bf16 matrix [rows][inner] with row pitch `ld`
 // elements; boxes of 8 elements x box_rows rows.

@@ -25,6 +25,7 @@
 #include "fvs_convert.cuh"
 #include "fvs_internal.h"
 #include "fvs_physics_fast.cuh"
+#include "fvs_tma.cuh"
 
 #include <cstring>
 
@@ -352,166 +353,377 @@ struct NewtonStats {
   }
 };
 
+// The cells of one grid line of a marching sweep, read from global memory:
+// Load gives cell j's conservative state (FP64; a ghost cell is the
+// boundary condition's image), CellRef an interior cell's components for
+// the update, Advance is called at the start of every iteration (nothing to
+// do here).
+template <int K, int DIR> struct GlobalLine {
+  const double* __restrict__ in;
+  int64_t base, stride, cs;  // stride: cells between neighbours (1 in x)
+  int nd, bc;
+  __device__ __forceinline__ int64_t Stride() const { return DIR == 0 ? 1 : stride; }
+  __device__ __forceinline__ void Load(double* u, int j) const {
+    const int64_t off = base + int64_t(BcIndex(j, nd, bc)) * Stride();
+#pragma unroll
+    for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * cs + off);
+    if (BcFlip(j, nd, bc)) u[1 + DIR] = -u[1 + DIR];
+  }
+  // interior cell j's components for the update (an L1 hit: loaded two
+  // iterations earlier)
+  struct Ref {
+    const double* p;
+    int64_t cs;
+    __device__ __forceinline__ double operator[](int c) const { return __ldg(p + c * cs); }
+  };
+  __device__ __forceinline__ Ref CellRef(int j) const {
+    return Ref{in + base + int64_t(j) * Stride(), cs};
+  }
+  __device__ __forceinline__ void Advance(int) {}
+};
+
 // Policy P = PT<D> provides: Real (compute precision), Gas, Rec (face
 // state), Wave (cell wave data), Stats, MakeGas(), ToCell() (double ->
 // Real), Predict(), MakeWave(), and Face(): the numeric flux of the face
 // between recR of the left cell and recL of the right cell (as double) and
 // the face's max signal speed of the input state (the CFL check).
+//
+// MarchSegment: one thread's segment [j0, j1) of its grid line `line`:
+// computes the faces j0..j1, writes the updated cells j0..j1-1 and folds the
+// input's face speeds into smax.  Lanes of `amask` march together (the CFL
+// screen's votes).
+template <int D, int DIR, class P, class Line>
+__device__ __forceinline__ void MarchSegment(const SweepArgs& a, Line& line, int j0, int j1,
+                                             unsigned amask, double split_dt,
+                                             typename P::Real& smax, int& status,
+                                             typename P::Stats& stats) {
+  constexpr int K = D + 2;
+  const bool skip_cfl = HasFluxOnly<P>::value && a.skip_cfl != 0;
+  constexpr bool kFilter = FilteredCfl<P>::value && HasFluxOnly<P>::value;
+  // the FP32 screen's error bound is stated for 1 < gamma <= 2
+  const bool screen = kFilter && !skip_cfl && a.gamma > 1.0 && a.gamma <= 2.0;
+  const typename P::Gas eq = P::MakeGasFor(a);
+  const double lambda_half = 0.5 * split_dt / a.dx;
+  const double dt_dx = split_dt / a.dx;
+  using R = typename P::Real;
+  double* __restrict__ out = a.out;
+  const int64_t cs = line.cs;
+  // compute-precision window of three cells; the FP64 loads run one cell
+  // ahead of the arithmetic (dn is the next "up").  The update of cell j-1
+  // re-reads its FP64 state (Line::Cell) instead of carrying a window of
+  // FP64 states in registers.
+  double dn[K];
+  R cm[K], cc[K], cp[K];
+  line.Load(dn, j0 - 2);
+  P::ToCell(cm, dn);
+  line.Load(dn, j0 - 1);
+  P::ToCell(cc, dn);
+  line.Load(dn, j0);
+  using FluxT = typename FluxOf<P>::type;
+  typename P::Rec recR_prev;
+  typename P::Wave w_prev;
+  FluxT F_prev[K];
+  fast::Gas<float> g32;
+  g32.gamma = static_cast<float>(a.gamma);
+  g32.gm1 = static_cast<float>(a.gamma - 1.0);
+  using S = CflScreen<P, D>;
+  typename S::V v_prev{};
+  bool ok_prev = false;
+  bool have_prev = false;  // w_prev holds the exact wave of cell j-1
+  // skip threshold: a lower bound of an evaluated face's exact speed
+  float thr = 0.0f;
+  if (kFilter && !skip_cfl && a.smax_out) thr = CflFloatBelow(CflSync(a.smax_out, 0.0, amask));
+  for (int j = j0 - 1; j <= j1; ++j) {
+    line.Advance(j);
+    if constexpr (kFilter) {
+      // the CFL speed of face j (cells j-1, j), before the reconstruction
+      // so that its registers are free
+      if (!skip_cfl) {
+        float c32[K];
+#pragma unroll
+        for (int c = 0; c < K; ++c) c32[c] = CflToF32(cc[c]);
+        const typename S::V v = S::Wave(g32, c32, DIR);
+        const bool ok = screen && CflInRange<D>(c32) && v.a > 0.0f;
+        if (j >= j0) {
+          const float s32 = S::Speed(g32, v_prev, v, DIR);
+          const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
+          const float bound = fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs));
+          const bool need = !(ok && ok_prev && bound < thr);
+          if (__any_sync(amask, need)) {
+            // the whole warp evaluates (the same instructions as some lanes)
+            const typename P::Wave wl = have_prev ? w_prev : P::MakeWave(eq, cm, DIR);
+            w_prev = P::MakeWave(eq, cc, DIR);
+            const R s = P::FaceMaxSpeed(eq, wl, w_prev);
+            smax = s > smax ? s : smax;
+            thr = fmaxf(thr, CflFloatBelow(static_cast<double>(smax)));
+            have_prev = true;
+          } else {
+            have_prev = false;
+          }
+          if (a.smax_out && ((j - j0) % kCflSyncRows) == kCflSyncRows - 1)
+            thr = fmaxf(thr, CflFloatBelow(CflSync(a.smax_out, static_cast<double>(smax), amask)));
+        }
+        ok_prev = ok;
+        v_prev = v;
+      }
+    }
+    P::ToCell(cp, dn);
+    if (j + 2 <= j1 + 1) line.Load(dn, j + 2);
+    typename P::Rec recL, recR;
+    P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
+    typename P::Wave w{};
+    if (!kFilter && !skip_cfl) w = P::MakeWave(eq, cc, DIR);
+    if (j >= j0) {
+      FluxT F[K];
+      if constexpr (kFilter) {
+        SweepFluxOnly<P>(eq, F, recR_prev, recL, DIR);
+      } else if constexpr (HasFluxOnly<P>::value) {
+        if (skip_cfl) {
+          SweepFluxOnly<P>(eq, F, recR_prev, recL, DIR);
+        } else {
+          const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
+          smax = s > smax ? s : smax;
+        }
+      } else {
+        const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
+        smax = s > smax ? s : smax;
+      }
+      if (j > j0) {
+        // cell j-1 (inside [0, nd)): U' = U + dt/dx (F_{j-1} - F_j)
+        const int64_t off = line.base + int64_t(j - 1) * line.Stride();
+        const auto cell = line.CellRef(j - 1);
+#pragma unroll
+        for (int c = 0; c < K; ++c) {
+          const double v = cell[c] + dt_dx * FluxDiff(F_prev[c], F[c]);
+          out[c * cs + off] = v;
+          // non-positive density: sign bit set or zero (integer test)
+          if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < K; ++c) F_prev[c] = F[c];
+    }
+    recR_prev = recR;
+    if constexpr (!kFilter) w_prev = w;
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+      cm[c] = cc[c];
+      cc[c] = cp[c];
+    }
+  }
+}
+
 template <int D, int DIR, template <int> class PT>
 __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(SweepArgs a) {
   using P = PT<D>;
   constexpr int K = D + 2;
   const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
-  const int nd = a.n[DIR];
-  const int64_t cs = int64_t(nx) * ny * nz;  // component stride
   int64_t ntrans;
   if (DIR == 0) ntrans = int64_t(ny) * nz;
   else if (DIR == 1) ntrans = int64_t(nx) * nz;
   else ntrans = int64_t(nx) * ny;
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int j0 = blockIdx.y * a.seg_len;
-  const int j1 = min(nd, j0 + a.seg_len);
+  const int j1 = min(a.n[DIR], j0 + a.seg_len);
 
   const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
   if (!BlockAll(SweepGate(a, split_dt))) return;
   const bool active = t < ntrans;
-  const bool skip_cfl = HasFluxOnly<P>::value && a.skip_cfl != 0;
-  constexpr bool kFilter = FilteredCfl<P>::value && HasFluxOnly<P>::value;
   const unsigned amask = __ballot_sync(0xffffffffu, active);
-  // the FP32 screen's error bound is stated for 1 < gamma <= 2
-  const bool screen = kFilter && !skip_cfl && a.gamma > 1.0 && a.gamma <= 2.0;
 
-  int64_t base, stride;
+  GlobalLine<K, DIR> line;
+  line.in = a.in;
+  line.cs = int64_t(nx) * ny * nz;
+  line.nd = a.n[DIR];
+  line.bc = a.bc;
   if (DIR == 0) {
-    base = t * nx;
-    stride = 1;
+    line.base = t * nx;
+    line.stride = 1;
   } else if (DIR == 1) {
     const int64_t i = t % nx, k = t / nx;
-    base = k * int64_t(nx) * ny + i;
-    stride = nx;
+    line.base = k * int64_t(nx) * ny + i;
+    line.stride = nx;
   } else {
-    base = t;
-    stride = int64_t(nx) * ny;
+    line.base = t;
+    line.stride = int64_t(nx) * ny;
   }
+  using R = typename P::Real;
+  R smax = R(0);
+  int status = 0;
+  typename P::Stats stats;
+  if (active) MarchSegment<D, DIR, P>(a, line, j0, j1, amask, split_dt, smax, status, stats);
+  stats.Flush(a.stats_out);
+  const double smax_d = static_cast<double>(smax);
+  BlockMaxAtomic<1>(a.smax_out, &smax_d);
+  if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
+}
 
-  const typename P::Gas eq = P::MakeGasFor(a);
-  const double lambda_half = 0.5 * split_dt / a.dx;
-  const double dt_dx = split_dt / a.dx;
+// The cells of a warp's 32 x-neighbouring grid lines of a y or z sweep,
+// staged into shared memory by TMA.  The warp owns a ring of kStages
+// buffers, each holding kRows cells of its 32 lines with all K components
+// ([K][kRows][32] doubles, one cp.async.bulk.tensor box of this GPU's own
+// state buffer: 32 x-cells by kRows cells along the sweep by K components);
+// lane 0 issues a buffer's copy, which completes on the buffer's mbarrier,
+// and every lane waits for it before its first read.  A buffer is refilled
+// with the rows kStages buffers further on once the march has left its last
+// row behind (the update's re-read of cell j-1 is its last use): the lanes
+// meet at __syncwarp, and lane 0 orders their reads before the copy
+// (fence.proxy.async).  Ghost cells outside the grid come from global memory
+// as in GlobalLine (the box's rows there are zero-filled and unused).  Every
+// wait is bounded: a timeout clears `ok`, the march goes on without waiting
+// and the sweep reports kStatusCopyTimeout; Finish waits (bounded) for the
+// copies the march did not consume before the warp leaves.
+constexpr uint32_t kTmaPolls = 1u << 22;
+
+template <int K, int DIR, int kRows, int kStages> struct TmaLine : GlobalLine<K, DIR> {
+  static constexpr int kBox = K * kRows * 32;  // doubles per buffer
+  double* ring;     // [kStages][kBox]
+  uint64_t* bars;   // [kStages]
+  const void* map;  // CUtensorMap (kernel parameter space)
+  int lane, x0, tr;     // box origin: x, the other transverse coordinate
+  int first, nstages;   // row of buffer 0's first cell; buffers of the segment
+  int ready, released;  // buffers waited for; buffers released
+  unsigned amask;
+  bool ok;
+
+  __device__ __forceinline__ void Issue(int q) {  // lane 0
+    const int slot = q % kStages;
+    tma::MbarArriveExpectTx(&bars[slot], kBox * 8);
+    double* dst = ring + slot * kBox;
+    const int row = first + q * kRows;
+    if constexpr (K == 5) {
+      if (DIR == 1)
+        tma::TmaLoad4D(dst, map, x0, row, tr, 0, &bars[slot]);
+      else
+        tma::TmaLoad4D(dst, map, x0, tr, row, 0, &bars[slot]);
+    } else {
+      tma::TmaLoad3D(dst, map, x0, row, 0, &bars[slot]);
+    }
+  }
+  __device__ __forceinline__ void Start(int j0, int j1) {
+    first = j0 - 2;
+    nstages = (j1 - j0 + 4 + kRows - 1) / kRows;
+    ready = 0;
+    released = 0;
+    ok = true;
+    if (lane == 0)
+      for (int q = 0; q < kStages && q < nstages; ++q) Issue(q);
+  }
+  __device__ __forceinline__ void WaitUpTo(int q) {
+    for (; ready <= q; ++ready)
+      if (ok && !tma::MbarWait(&bars[ready % kStages], (ready / kStages) & 1, kTmaPolls))
+        ok = false;
+  }
+  __device__ __forceinline__ const double* At(int j) {  // interior cell j
+    const unsigned rel = static_cast<unsigned>(j - first);
+    const int q = static_cast<int>(rel / kRows);
+    WaitUpTo(q);
+    return ring + (q % kStages) * kBox + (rel % kRows) * 32 + lane;
+  }
+  __device__ __forceinline__ void Load(double* u, int j) {
+    if (j < 0 || j >= this->nd) {
+      GlobalLine<K, DIR>::Load(u, j);
+      return;
+    }
+    const double* p = At(j);
+#pragma unroll
+    for (int c = 0; c < K; ++c) u[c] = p[c * kRows * 32];
+  }
+  struct Ref {
+    const double* p;
+    __device__ __forceinline__ double operator[](int c) const { return p[c * kRows * 32]; }
+  };
+  __device__ __forceinline__ Ref CellRef(int j) { return Ref{At(j)}; }
+  __device__ __forceinline__ void Advance(int j) {
+    while (released < nstages && first + (released + 1) * kRows <= j - 1) {
+      WaitUpTo(released);  // the buffer's copy has landed before it is refilled
+      __syncwarp(amask);
+      if (lane == 0 && ok && released + kStages < nstages) {
+        tma::FenceProxyAsync();
+        Issue(released + kStages);
+      }
+      ++released;
+    }
+  }
+  // Lane 0: waits for the issued copies nobody waited for.
+  __device__ __forceinline__ void Finish() {
+    if (lane != 0) return;
+    const int issued = min(nstages, released + kStages);
+    for (; ready < issued; ++ready)
+      if (!tma::MbarWait(&bars[ready % kStages], (ready / kStages) & 1, kTmaPolls)) ok = false;
+  }
+};
+
+template <int K> constexpr size_t TmaSweepSmemBytes() {
+  return size_t(kTmaWarps) * kTmaStages * (K * kTmaRows * 32 * 8 + 8);
+}
+
+// A y or z sweep with the cells staged by TMA (TmaLine): warp w of the grid
+// owns x-chunk w % ceil(nx / 32) of the lines at transverse index w / that
+// (z for y sweeps, y for z sweeps), segment blockIdx.y.  `map` describes this
+// GPU's own input state buffer as [K][nz][ny][nx] doubles (3-D) or
+// [K][ny][nx] (2-D) with boxes of 32 x kTmaRows cells along DIR.
+template <int D, int DIR, template <int> class PT>
+__global__ void __launch_bounds__(128, PT<D>::kMinBlocks)
+    SweepTmaKernel(SweepArgs a, const __grid_constant__ CUtensorMap map) {
+  static_assert(DIR >= 1 && DIR < D, "y or z sweeps");
+  using P = PT<D>;
+  constexpr int K = D + 2;
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nx = a.n[0], ny = a.n[1], nz = a.n[2];
+  const int nchunks = (nx + 31) / 32;
+  const int ntr = DIR == 1 ? nz : ny;
+  const int64_t gw = int64_t(blockIdx.x) * kTmaWarps + warp;
+  const bool has_work = gw < int64_t(nchunks) * ntr;  // warp-uniform
+  const int xc = has_work ? static_cast<int>(gw % nchunks) : 0;
+  const int tr = has_work ? static_cast<int>(gw / nchunks) : 0;
+  const int i = xc * 32 + lane;
+  const int j0 = blockIdx.y * a.seg_len;
+  const int j1 = min(a.n[DIR], j0 + a.seg_len);
+
+  const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
+  if (!BlockAll(SweepGate(a, split_dt))) return;
+  const bool active = has_work && i < nx;
+  const unsigned amask = __ballot_sync(0xffffffffu, active);
+
+  using Line = TmaLine<K, DIR, kTmaRows, kTmaStages>;
+  Line line;
+  line.in = a.in;
+  line.cs = int64_t(nx) * ny * nz;
+  line.nd = a.n[DIR];
+  line.bc = a.bc;
+  if (DIR == 1) {
+    line.base = int64_t(tr) * nx * ny + i;
+    line.stride = nx;
+  } else {
+    line.base = int64_t(tr) * nx + i;
+    line.stride = int64_t(nx) * ny;
+  }
+  line.ring = reinterpret_cast<double*>(tma_smem) + size_t(warp) * kTmaStages * Line::kBox;
+  line.bars = reinterpret_cast<uint64_t*>(tma_smem + size_t(kTmaWarps) * kTmaStages *
+                                                        Line::kBox * 8) +
+              warp * kTmaStages;
+  line.map = &map;
+  line.lane = lane;
+  line.x0 = xc * 32;
+  line.tr = tr;
+  line.amask = amask;
 
   using R = typename P::Real;
   R smax = R(0);
   int status = 0;
   typename P::Stats stats;
-  if (active) {
-    const double* __restrict__ in = a.in;
-    double* __restrict__ out = a.out;
-    auto load = [&](double* u, int j) {
-      const int64_t off = base + int64_t(BcIndex(j, nd, a.bc)) * stride;
-#pragma unroll
-      for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * cs + off);
-      if (BcFlip(j, nd, a.bc)) u[1 + DIR] = -u[1 + DIR];
-    };
-    // compute-precision window of three cells; the FP64 loads run one cell
-    // ahead of the arithmetic (dn is the next "up").  The update of cell j-1
-    // re-reads its FP64 state (loaded two iterations earlier, an L1 hit)
-    // instead of carrying a window of FP64 states in registers.
-    double dn[K];
-    R cm[K], cc[K], cp[K];
-    load(dn, j0 - 2);
-    P::ToCell(cm, dn);
-    load(dn, j0 - 1);
-    P::ToCell(cc, dn);
-    load(dn, j0);
-    using FluxT = typename FluxOf<P>::type;
-    typename P::Rec recR_prev;
-    typename P::Wave w_prev;
-    FluxT F_prev[K];
-    fast::Gas<float> g32;
-    g32.gamma = static_cast<float>(a.gamma);
-    g32.gm1 = static_cast<float>(a.gamma - 1.0);
-    using S = CflScreen<P, D>;
-    typename S::V v_prev{};
-    bool ok_prev = false;
-    bool have_prev = false;  // w_prev holds the exact wave of cell j-1
-    // skip threshold: a lower bound of an evaluated face's exact speed
-    float thr = 0.0f;
-    if (kFilter && !skip_cfl && a.smax_out) thr = CflFloatBelow(CflSync(a.smax_out, 0.0, amask));
-    for (int j = j0 - 1; j <= j1; ++j) {
-      if constexpr (kFilter) {
-        // the CFL speed of face j (cells j-1, j), before the reconstruction
-        // so that its registers are free
-        if (!skip_cfl) {
-          float c32[K];
-#pragma unroll
-          for (int c = 0; c < K; ++c) c32[c] = CflToF32(cc[c]);
-          const typename S::V v = S::Wave(g32, c32, DIR);
-          const bool ok = screen && CflInRange<D>(c32) && v.a > 0.0f;
-          if (j >= j0) {
-            const float s32 = S::Speed(g32, v_prev, v, DIR);
-            const float sh = fast::Math<float>::Sqrt(fmaxf(v_prev.h, v.h));
-            const float bound = fmaf(s32, kCflRel, fmaf(kCflScale, sh, kCflAbs));
-            const bool need = !(ok && ok_prev && bound < thr);
-            if (__any_sync(amask, need)) {
-              // the whole warp evaluates (the same instructions as some lanes)
-              const typename P::Wave wl = have_prev ? w_prev : P::MakeWave(eq, cm, DIR);
-              w_prev = P::MakeWave(eq, cc, DIR);
-              const R s = P::FaceMaxSpeed(eq, wl, w_prev);
-              smax = s > smax ? s : smax;
-              thr = fmaxf(thr, CflFloatBelow(static_cast<double>(smax)));
-              have_prev = true;
-            } else {
-              have_prev = false;
-            }
-            if (a.smax_out && ((j - j0) % kCflSyncRows) == kCflSyncRows - 1)
-              thr = fmaxf(thr, CflFloatBelow(CflSync(a.smax_out, static_cast<double>(smax), amask)));
-          }
-          ok_prev = ok;
-          v_prev = v;
-        }
-      }
-      P::ToCell(cp, dn);
-      if (j + 2 <= j1 + 1) load(dn, j + 2);
-      typename P::Rec recL, recR;
-      P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
-      typename P::Wave w{};
-      if (!kFilter && !skip_cfl) w = P::MakeWave(eq, cc, DIR);
-      if (j >= j0) {
-        FluxT F[K];
-        if constexpr (kFilter) {
-          SweepFluxOnly<P>(eq, F, recR_prev, recL, DIR);
-        } else if constexpr (HasFluxOnly<P>::value) {
-          if (skip_cfl) {
-            SweepFluxOnly<P>(eq, F, recR_prev, recL, DIR);
-          } else {
-            const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
-            smax = s > smax ? s : smax;
-          }
-        } else {
-          const R s = SweepFace<P>(eq, F, recR_prev, recL, w_prev, w, DIR, stats);
-          smax = s > smax ? s : smax;
-        }
-        if (j > j0) {
-          // cell j-1 (inside [0, nd)): U' = U + dt/dx (F_{j-1} - F_j)
-          const int64_t off = base + int64_t(j - 1) * stride;
-#pragma unroll
-          for (int c = 0; c < K; ++c) {
-            const double v = __ldg(in + c * cs + off) + dt_dx * FluxDiff(F_prev[c], F[c]);
-            out[c * cs + off] = v;
-            // non-positive density: sign bit set or zero (integer test)
-            if (c == 0 && __double_as_longlong(v) <= 0) status |= kStatusNonPositiveDensity;
-          }
-        }
-#pragma unroll
-        for (int c = 0; c < K; ++c) F_prev[c] = F[c];
-      }
-      recR_prev = recR;
-      if constexpr (!kFilter) w_prev = w;
-#pragma unroll
-      for (int c = 0; c < K; ++c) {
-        cm[c] = cc[c];
-        cc[c] = cp[c];
-      }
+  if (has_work) {
+    if (lane == 0) {
+      for (int q = 0; q < kTmaStages; ++q) tma::MbarInit(&line.bars[q], 1);
+      tma::FenceMbarInit();
     }
+    __syncwarp();
+    line.Start(j0, j1);
+    if (active) MarchSegment<D, DIR, P>(a, line, j0, j1, amask, split_dt, smax, status, stats);
+    line.Finish();
+    if (!line.ok) status |= kStatusCopyTimeout;
   }
   stats.Flush(a.stats_out);
   const double smax_d = static_cast<double>(smax);
@@ -749,6 +961,33 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(Sweep
   if (status && a.ctrl) atomicOr(&a.ctrl->step_status, status);
 }
 
+// The TMA-staged y/z sweep (a.tmap: the host's tensor map of a.in), built
+// for the mixed flavour's policies with lanes-along-x x sweeps.
+template <class P, class = void> struct TmaStaged : std::false_type {};
+template <class P>
+struct TmaStaged<P, std::enable_if_t<P::kFloatFlux && P::kWarpX>> : std::true_type {};
+template <class P> constexpr bool kTmaStaged = TmaStaged<P>::value;
+
+// The TMA-staged y/z sweep (a.tmap: the host's tensor map of a.in).
+template <int D, int DIR, template <int> class P>
+cudaError_t LaunchSweepTma(const SweepArgs& a, cudaStream_t s) {
+  constexpr size_t smem = TmaSweepSmemBytes<D + 2>();
+  static bool attr_set = false;
+  if (!attr_set) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        SweepTmaKernel<D, DIR, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  const int64_t warps = int64_t((a.n[0] + 31) / 32) * (DIR == 1 ? a.n[2] : a.n[1]);
+  const int seg = a.seg_len > 0 ? a.seg_len : a.n[DIR];
+  dim3 grid(static_cast<unsigned>((warps + kTmaWarps - 1) / kTmaWarps),
+            static_cast<unsigned>((a.n[DIR] + seg - 1) / seg));
+  SweepTmaKernel<D, DIR, P><<<grid, 32 * kTmaWarps, smem, s>>>(
+      a, *static_cast<const CUtensorMap*>(a.tmap));
+  return cudaGetLastError();
+}
+
 template <int D, template <int> class P>
 cudaError_t LaunchSweepT(const SweepArgs& a, cudaStream_t s) {
   const int nd = a.n[a.dir];
@@ -774,10 +1013,18 @@ cudaError_t LaunchSweepT(const SweepArgs& a, cudaStream_t s) {
     }
     break;
   case 1:
-    if constexpr (D >= 2) SweepMarchKernel<D, 1, P><<<grid, block, 0, s>>>(b);
+    if constexpr (D >= 2) {
+      if constexpr (kTmaStaged<P<D>>)
+        if (a.occupancy >= 20 && a.tmap) return LaunchSweepTma<D, 1, P>(b, s);
+      SweepMarchKernel<D, 1, P><<<grid, block, 0, s>>>(b);
+    }
     break;
   default:
-    if constexpr (D >= 3) SweepMarchKernel<D, 2, P><<<grid, block, 0, s>>>(b);
+    if constexpr (D >= 3) {
+      if constexpr (kTmaStaged<P<D>>)
+        if (a.occupancy >= 20 && a.tmap) return LaunchSweepTma<D, 2, P>(b, s);
+      SweepMarchKernel<D, 2, P><<<grid, block, 0, s>>>(b);
+    }
     break;
   }
   return cudaGetLastError();

@@ -22,16 +22,21 @@
 #include <cstdint>
 #include <cuda_bf16.h>
 
+#include "fvs_tma.cuh"
+
 namespace fvs {
 namespace tc {
+
+using tma::FenceProxyAsync;
+using tma::MbarArriveExpectTx;
+using tma::MbarInit;
+using tma::MbarWait;
+using tma::SmemAddr;
+using tma::TmaLoad2D;
 
 constexpr int kTileM = 128;
 constexpr int kChunkK = 64;
 constexpr int kThreads = 128;
-
-__device__ __forceinline__ uint32_t SmemAddr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
 
 // Shared-memory matrix descriptor (tcgen05): start address, leading- and
 // stride-dimension byte offsets (all >> 4), descriptor version 1 at bits
@@ -50,26 +55,6 @@ __device__ __forceinline__ uint64_t SmemDesc(uint32_t addr, uint32_t lbo, uint32
 // bits 24-28.
 __host__ __device__ constexpr uint32_t InstrDescBf16(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
-}
-
-__device__ __forceinline__ void MbarInit(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(SmemAddr(bar)), "r"(count));
-}
-
-// Bounded wait for the mbarrier phase `parity`; returns false on timeout.
-__device__ __forceinline__ bool MbarWait(uint64_t* bar, uint32_t parity, uint32_t max_polls) {
-  uint32_t done = 0;
-  for (uint32_t i = 0; i < max_polls; ++i) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(SmemAddr(bar)), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
 }
 
 __device__ __forceinline__ void TmemAlloc(uint32_t* dst_smem, uint32_t ncols) {
@@ -108,30 +93,6 @@ __device__ __forceinline__ void FenceBeforeSync() {
 __device__ __forceinline__ void FenceAfterSync() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-__device__ __forceinline__ void FenceProxyAsync() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-
-// The next phase of `bar` completes once `bytes` of asynchronous copies
-// have landed (plus this one arrival).
-__device__ __forceinline__ void MbarArriveExpectTx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(SmemAddr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-// TMA: box of a 2-D tensor map at element coordinates (x, y) into shared
-// memory, completing on `bar`.  x * element size must be a multiple of 16
-// bytes; rows outside the tensor are filled with zeros.
-__device__ __forceinline__ void TmaLoad2D(void* smem_dst, const void* tensor_map, int x, int y,
-                                          uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes "
-      "[%0], [%1, {%2, %3}], [%4];" ::"r"(SmemAddr(smem_dst)),
-      "l"(reinterpret_cast<uint64_t>(tensor_map)), "r"(x), "r"(y), "r"(SmemAddr(bar))
-      : "memory");
-}
-
 // 16 fp32 columns of this thread's TMEM lane starting at column `col`.
 __device__ __forceinline__ void TmemLoad16(uint32_t taddr, float* v) {
   uint32_t r[16];

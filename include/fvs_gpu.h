@@ -484,7 +484,8 @@ int fvs_amr_run(fvs_amr* a, double cfl, double t_end, int max_steps, double* dt_
                 int log_len, fvs_run_stats* stats);
 /* Persistent launch shape of a level's sweeps in direction dir: threads per
  * block, blocks, and threads per patch row (1, 2, 4 or 8: each row split into
- * that many segments). */
+ * that many segments; 32, mixed flavour x sweeps only: the rows laid end to
+ * end with the lanes of a warp along x). */
 int fvs_amr_set_launch(fvs_amr* a, int level, int dir, int block, int grid, int threads_per_row);
 /* Times the sweeps of every level and direction for a set of launch shapes
  * (threads per row, threads per block, blocks, and for the mixed flavour a

@@ -79,6 +79,31 @@ def test_launch_shape_and_autotune_do_not_change_results(fvs, orc):
     np.testing.assert_array_equal(b.download(), ref)
 
 
+@pytest.mark.parametrize("bc", [(1, 1), (0, 0), (2, 2)])
+def test_mixed_row_warp_x_sweep_matches_marching(fvs, bc):
+    """The mixed x sweep with the lanes of a warp along x (rows laid end to
+    end as slots, threads_per_row 32) gives the marching kernel's results bit
+    for bit: halo cells from the same level and the coarser one, reflective
+    images, flux-register captures and patch widths 8 to 32."""
+    h, cons = workloads.amr_blast_2d(96, 3, target=150, sizes=(8, 16, 32))
+    h = workloads.AmrHierarchy(h.nlevels, h.n0, bc, h.dx0, h.levels, h.boxes)
+    outs = []
+    for tpr, block, grid in ((1, 128, 64), (32, 128, 64), (32, 64, 3)):
+        a = fvs.AmrSolver(h, fvs.make_method(precision="mixed"))
+        for l in range(3):
+            a.set_launch(l, 0, block, grid, tpr)
+        a.upload(cons)
+        st, _ = a.run(cfl=0.8, t_end=10.0, max_steps=4)
+        assert st.steps == 4
+        outs.append(a.download())
+        if tpr == 32:
+            with pytest.raises(fvs.FvsError):
+                a.set_launch(0, 1, 128, 64, 32)  # y rows have no lanes-along-x kernel
+        a.close()
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[0], outs[2])
+
+
 def test_uniform_state_stays_uniform(fvs):
     h, _ = workloads.amr_blast_2d(64, 3, target=80, sizes=(8, 16))
     cons = h.cons_from(lambda X, Y: workloads.cons_from_prim(

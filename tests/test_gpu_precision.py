@@ -172,3 +172,45 @@ def test_mixed_launch_variants(fvs, orc, xvariant):
     with pytest.raises(fvs.FvsError):
         s.set_launch(1, 16, 10)  # the marching-x variants exist for x only
     s.close()
+
+
+@pytest.mark.parametrize("rank,nx,bc,seg", [
+    (3, 50, "periodic", 16), (3, 64, "transmissive", 0), (3, 34, "reflective", 7),
+    (2, 98, "periodic", 0), (2, 66, "reflective", 24)])
+@pytest.mark.parametrize("variant", [20, 24, 25])
+def test_mixed_tma_sweeps_match_marching(fvs, rank, nx, bc, seg, variant):
+    """The TMA-staged y/z sweep (cells staged into shared memory by
+    cp.async.bulk.tensor) runs the marching sweep's arithmetic on the same
+    cells: its Strang steps equal the marching kernel's bit for bit, for x
+    extents that are not multiples of the 32-cell box, ragged segments and
+    every boundary kind."""
+    shape = [nx, 28, 20][:rank]
+    dx = [1.0 / 64] * rank
+    cons = (workloads.octants_3d(64, seed=31)[:, :shape[2], :shape[1], :shape[0]]
+            if rank == 3 else workloads.random_state((shape[1], shape[0]), 2, seed=31, v=0.6))
+    cons = np.ascontiguousarray(cons.reshape(rank + 2, *shape[::-1]))
+    outs = []
+    for v in (variant % 10, variant):
+        s = fvs.Solver(shape, dx, bc, method=fvs.make_method(precision="mixed"))
+        for d in range(1, rank):
+            s.set_launch(d, seg, v)
+        s.upload(cons)
+        st, _ = s.run(cfl=0.8, t_end=10.0, max_steps=4)
+        assert st.steps == 4
+        outs.append(s.download())
+        s.close()
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
+def test_mixed_tma_variant_needs_even_nx(fvs):
+    """TMA rows must start on 16-byte boundaries: an odd x extent has no
+    TMA-staged variant, and x sweeps never have one."""
+    s = fvs.Solver([33, 16, 8], [0.1] * 3, "periodic", method=fvs.make_method(precision="mixed"))
+    with pytest.raises(fvs.FvsError):
+        s.set_launch(1, 16, 20)
+    s.close()
+    s = fvs.Solver([32, 16, 8], [0.1] * 3, "periodic", method=fvs.make_method(precision="mixed"))
+    s.set_launch(1, 16, 20)
+    with pytest.raises(fvs.FvsError):
+        s.set_launch(0, 16, 20)
+    s.close()
