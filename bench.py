@@ -57,7 +57,7 @@ def parse():
                     help="skip the secondary workloads (learned start value, 2-D Godunov, "
                          "2-D cut cells)")
     ap.add_argument("--report", choices=["sod", "learned", "godunov", "amr", "cutcell",
-                                         "hllem"],
+                                         "hllem", "sweep_variants"],
                     help="run only this secondary workload and print its JSON report")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000)
     ap.add_argument("--mlp-epochs", type=int, default=24)
@@ -383,6 +383,57 @@ def report_godunov(args, torch, fvs, workloads, net, peaks=None):
                         "Strang, CFL 0.8, transmissive", "by_tolerance": by_tol}
 
 
+def report_sweep_variants(args, torch, fvs, workloads, peaks):
+    """Single sweeps of the --n^3 octants workload in --precision, timed with
+    CUDA events on the solver's stream, for every launch variant and segment
+    length the autotuner tries (mixed: x lanes-along-x 0/4/5 or marching
+    10/14/15; y/z marching 0/4/5 or TMA-staged 20/24/25); the best segment
+    length per variant, 80 B per cell-update."""
+    n = args.n
+    cons = workloads.octants_3d(n)
+    s = fvs.Solver([n] * 3, [1.0 / n] * 3, "periodic",
+                   method=fvs.make_method(precision=args.precision))
+    s.upload(cons)
+    stream = torch.cuda.ExternalStream(s.stream_handle())
+    dt = 0.4 * s.ComputeStableDt(-1)
+    mixed = args.precision == "mixed"
+    out = {"workload": f"single sweeps of the 3D {n}^3 octants state, {args.precision}",
+           "sweeps": {}}
+    for d in range(3):
+        if mixed:
+            variants = [0, 4, 5, 10, 14, 15] if d == 0 else [0, 4, 5, 20, 24, 25]
+        else:
+            variants = [0]
+        for v in variants:
+            best = None
+            segs = [16] if (mixed and d == 0 and v < 10) else [16, 32, 64, 128, 256]
+            for seg in segs:
+                try:
+                    s.set_launch(d, seg, v)
+                except fvs.FvsError:
+                    break  # a variant this grid does not have (odd nx: no TMA)
+                ts = []
+                for rep in range(6):
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    s.sweep(d, dt)
+                    b.record(stream)
+                    torch.cuda.synchronize()
+                    if rep >= 2:
+                        ts.append(a.elapsed_time(b))
+                ms = float(np.mean(ts))
+                if best is None or ms < best[0]:
+                    best = (ms, seg)
+            if best is not None:
+                gbs = 80 * n ** 3 / (best[0] / 1e3) / 1e9
+                out["sweeps"][f"dir{d}_variant{v}"] = {
+                    "ms": best[0], "segment_cells": best[1], "GB_per_s": gbs,
+                    "hbm_frac": gbs / peaks["hbm_gbs"]}
+    s.close()
+    return out
+
+
 def report_amr(args, torch, fvs, workloads, peaks):
     """Batched AMR patch set: 2-D blast (p 10 inside r < 0.1 about a seeded
     centre), 3 levels, ratio 2, 4096 patches with extents from {8, 16, 32,
@@ -666,6 +717,8 @@ def run_ours(args):
             rep = report_godunov(args, torch, fvs, workloads, net, peaks)
         elif args.report == "amr":
             rep = report_amr(args, torch, fvs, workloads, peaks)
+        elif args.report == "sweep_variants":
+            rep = report_sweep_variants(args, torch, fvs, workloads, peaks)
         elif args.report == "hllem":
             rep = report_hllem(args, torch, fvs, workloads, peaks)
         else:
