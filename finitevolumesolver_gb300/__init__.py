@@ -392,6 +392,25 @@ class Solver:
     def step(self, dt: float, cycle: int) -> None:
         _capi.check(lib().fvs_solver_step(self._h, float(dt), int(cycle)))
 
+    def step_host(self, cons_host, cfl=0.8, t_end=1e300):
+        """One split step of a host-resident state, in place (fvs_solver_step_host):
+        cons_host is a C-contiguous float64 array or tensor in host memory
+        (page-locked for overlapped copies) holding the conservative state."""
+        import numpy as np
+        if hasattr(cons_host, "data_ptr"):
+            if getattr(cons_host, "is_cuda", False):
+                raise ValueError("cons_host must live in host memory")
+            assert cons_host.numel() == int(np.prod(self.shape()))
+            ptr = cons_host.data_ptr()
+        else:
+            assert cons_host.flags["C_CONTIGUOUS"] and cons_host.dtype == np.float64
+            assert cons_host.size == int(np.prod(self.shape()))
+            ptr = cons_host.ctypes.data
+        st = RunStats()
+        _capi.check(lib().fvs_solver_step_host(self._h, C.c_void_p(ptr), float(cfl),
+                                               float(t_end), C.byref(st)))
+        return st
+
     def run(self, cfl=0.8, t_end=1.0, max_steps=-1, log_len=0):
         import numpy as np
         log = np.zeros(max(log_len, 1))

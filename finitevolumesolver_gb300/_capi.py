@@ -117,6 +117,7 @@ def load() -> C.CDLL:
     L.fvs_solver_create.argtypes = [P(GridDesc), P(Method), P(_VP)]
     L.fvs_solver_destroy.argtypes = [_VP]
     L.fvs_solver_upload.argtypes = [_VP, _VP]
+    L.fvs_solver_step_host.argtypes = [_VP, _VP, C.c_double, C.c_double, P(RunStats)]
     L.fvs_solver_download.argtypes = [_VP, _VP]
     L.fvs_solver_write_plotfile.argtypes = [_VP, C.c_char_p]
     L.fvs_solver_state_device.argtypes = [_VP, P(_VP)]

@@ -242,7 +242,17 @@ struct fvs_solver {
   // sweeps of the mixed flavour ([buffer][dir - 1]); built on first use
   alignas(64) CUtensorMap tmap[3][2];
   int tmap_state = 0;  // 0 not tried, 1 built, -1 not available
+  // host-resident steps (fvs_solver_step_host): the copies of the last
+  // sweep's slabs run on `copy`, each after its slab's event
+  cudaStream_t copy = nullptr, slab = nullptr;
+  cudaEvent_t slab_ev[fvs::kHostSlabs + 1] = {};
+  cudaEvent_t slab_fork = nullptr;
   ~fvs_solver() {
+    for (cudaEvent_t e : slab_ev)
+      if (e) cudaEventDestroy(e);
+    if (slab_fork) cudaEventDestroy(slab_fork);
+    if (copy) cudaStreamDestroy(copy);
+    if (slab) cudaStreamDestroy(slab);
     for (void* p : cc_allocs) cudaFree(p);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
@@ -349,7 +359,8 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
                         int dir, const double* dt_ptr, double dt_scale,
                         double dt_value, unsigned long long* smax_out,
                         fvs::Control* ctrl, int prev_check, double prev_dx,
-                        bool skip_cfl = false) {
+                        bool skip_cfl = false, int64_t t_lo = 0, int64_t t_hi = 0,
+                        cudaStream_t stream = nullptr) {
   if (s->cc) {
     fvs::CcSweepArgs c{};
     c.s = MakeCcState(s, in);
@@ -412,24 +423,30 @@ cudaError_t LaunchSweep(const fvs_solver* s, const double* in, double* out,
   a.stats_out = ctrl ? ctrl->newton : s->newton_words;
   a.skip_cfl = skip_cfl ? 1 : 0;
   a.tmap = a.occupancy >= 20 ? TmaMapOf(s, in, dir) : nullptr;
+  a.t_lo = t_lo;
+  a.t_hi = t_hi;
+  cudaStream_t st = stream ? stream : s->stream;
   if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
-    return fvs::LaunchSweepGodunov(a, s->m.flux_method == FVS_MUSCL_GODUNOV, s->stream);
+    return fvs::LaunchSweepGodunov(a, s->m.flux_method == FVS_MUSCL_GODUNOV, st);
   if (HllemRecon(s->m.flux_method) >= 0)
-    return fvs::LaunchSweepHllem(a, HllemRecon(s->m.flux_method), s->stream);
+    return fvs::LaunchSweepHllem(a, HllemRecon(s->m.flux_method), st);
   switch (s->m.precision) {
   case FVS_FP64_EXACT:
-    return fvs::LaunchSweepExact(a, s->stream);
+    return fvs::LaunchSweepExact(a, st);
   case FVS_FP64_FAST:
-    return fvs::LaunchSweepFast(a, s->stream);
+    return fvs::LaunchSweepFast(a, st);
   case FVS_FP64_DF:
-    return fvs::LaunchSweepDf64(a, s->stream);
+    return fvs::LaunchSweepDf64(a, st);
   default:
-    return fvs::LaunchSweepMixed(a, s->stream);
+    return fvs::LaunchSweepMixed(a, st);
   }
 }
 
+// k_hi > 0: the faces of planes [k_lo, k_hi) only (3-D HLLE methods without
+// a reflective direction: StablePlanesOk).
 cudaError_t LaunchStable(const fvs_solver* s, const double* in,
-                         unsigned long long* smax_out, fvs::Control* ctrl) {
+                         unsigned long long* smax_out, fvs::Control* ctrl, int k_lo = 0,
+                         int k_hi = 0) {
   if (s->cc)
     return s->m.precision == FVS_FP64_EXACT
                ? fvs::LaunchCutCellStableDt(MakeCcState(s, in), smax_out, ctrl, s->stream)
@@ -447,6 +464,9 @@ cudaError_t LaunchStable(const fvs_solver* s, const double* in,
   a.gamma = s->m.gamma;
   a.smax_out = smax_out;
   a.ctrl = ctrl;
+  a.k_lo = k_lo;
+  a.k_hi = k_hi;
+  if (k_hi > 0 && (s->m.flux_method > FVS_HLLE || s->g.rank != 3)) return cudaErrorNotSupported;
   if (s->m.flux_method == FVS_GODUNOV || s->m.flux_method == FVS_MUSCL_GODUNOV)
     return fvs::LaunchStableDtGodunov(a, s->m.guess, s->m.max_iterations, s->m.tolerance,
                                       s->m.mlp_params, s->stream);
@@ -502,8 +522,79 @@ fvs::StepPlan MakePlan(const fvs_solver* s, int64_t cycle) {
 
 int NextBuffer(int start, int nsweeps) { return (start + (nsweeps % 2 ? 1 : 2)) % 3; }
 
-// Enqueue one device-driven split step starting in buffer `start`.
-cudaError_t EnqueueStep(fvs_solver* s, int start, int64_t cycle, int step_in_batch) {
+// The lines of the last sweep of a step split into fvs::kHostSlabs slabs
+// along the slowest transverse direction, and the host copies of a slab's
+// cells: per component one contiguous run or one 2-D copy (pitch, width,
+// rows) in doubles.
+struct SlabCopy {
+  int64_t t_lo, t_hi;      // the sweep's lines
+  int64_t offset;          // first cell of the slab within a component
+  int64_t width, pitch, rows;  // rows of `width` cells, `pitch` apart
+};
+
+int HostSlabs(const fvs_solver* s, int dir, SlabCopy* out) {
+  const int64_t nx = s->g.n[0], ny = s->g.n[1], nz = s->g.n[2];
+  // the line index t of a sweep in `dir` and its slowest transverse extent
+  int64_t outer, inner;  // t = a + inner * b, b in [0, outer)
+  if (dir == 0) {
+    inner = ny;
+    outer = nz;
+  } else if (dir == 1) {
+    inner = nx;
+    outer = nz;
+  } else {
+    inner = nx;
+    outer = ny;
+  }
+  if (s->g.rank == 2 && dir == 0) {  // rows j: slabs of rows
+    inner = 1;
+    outer = ny;
+  }
+  if (s->g.rank == 2 && dir == 1) {  // columns i: slabs of columns
+    inner = 1;
+    outer = nx;
+  }
+  const int n = static_cast<int>(std::min<int64_t>(fvs::kHostSlabs, std::max<int64_t>(1, outer)));
+  if (s->g.rank == 1) {
+    out[0] = {0, 1, 0, nx, nx, 1};
+    return 1;
+  }
+  for (int k = 0; k < n; ++k) {
+    const int64_t b0 = outer * k / n, b1 = outer * (k + 1) / n;
+    SlabCopy& c = out[k];
+    c.t_lo = b0 * inner;
+    c.t_hi = b1 * inner;
+    if (s->g.rank == 3 && dir <= 1) {  // z-planes [b0, b1): contiguous
+      c.offset = b0 * nx * ny;
+      c.width = (b1 - b0) * nx * ny;
+      c.pitch = c.width;
+      c.rows = 1;
+    } else if (s->g.rank == 3) {  // y-rows [b0, b1) of every z-plane
+      c.offset = b0 * nx;
+      c.width = (b1 - b0) * nx;
+      c.pitch = nx * ny;
+      c.rows = nz;
+    } else if (dir == 0) {  // 2-D rows [b0, b1): contiguous
+      c.offset = b0 * nx;
+      c.width = (b1 - b0) * nx;
+      c.pitch = c.width;
+      c.rows = 1;
+    } else {  // 2-D columns [b0, b1) of every row
+      c.offset = b0;
+      c.width = b1 - b0;
+      c.pitch = nx;
+      c.rows = ny;
+    }
+  }
+  return n;
+}
+
+// Enqueue one device-driven split step starting in buffer `start`.  With
+// `host_out`, the step's last sweep runs slab by slab and each slab's cells
+// are copied to host_out on the copy stream as soon as the slab is done
+// (the stream joins back into the solver's stream at the end).
+cudaError_t EnqueueStep(fvs_solver* s, int start, int64_t cycle, int step_in_batch,
+                        double* host_out = nullptr, bool stable_enqueued = false) {
   const fvs::StepPlan plan = MakePlan(s, cycle);
   cudaError_t e = cudaSuccess;
   if (s->cc) {
@@ -511,19 +602,55 @@ cudaError_t EnqueueStep(fvs_solver* s, int start, int64_t cycle, int step_in_bat
     e = CcReferenceStates(s, s->buf[start]);
     if (e != cudaSuccess) return e;
   }
-  // the pass's max slots start at zero (its screened speeds need it)
-  e = cudaMemsetAsync(s->ctrl->smax_stable, 0, sizeof(s->ctrl->smax_stable), s->stream);
-  if (e != cudaSuccess) return e;
-  e = LaunchStable(s, s->buf[start], s->ctrl->smax_stable, s->ctrl);
-  if (e != cudaSuccess) return e;
+  if (!stable_enqueued) {
+    // the pass's max slots start at zero (its screened speeds need it)
+    e = cudaMemsetAsync(s->ctrl->smax_stable, 0, sizeof(s->ctrl->smax_stable), s->stream);
+    if (e != cudaSuccess) return e;
+    e = LaunchStable(s, s->buf[start], s->ctrl->smax_stable, s->ctrl);
+    if (e != cudaSuccess) return e;
+  }
   fvs::BeginStepKernel<<<1, 1, 0, s->stream>>>(s->ctrl, plan);
   const int X = (start + 1) % 3, Y = (start + 2) % 3;
   int src = start, dst = X;
   for (int q = 0; q < plan.nsweeps; ++q) {
     const bool skip = q == 0 && plan.skip0;
-    e = LaunchSweep(s, s->buf[src], s->buf[dst], plan.dir[q], &s->ctrl->dt,
-                    plan.frac, 0.0, skip ? nullptr : &s->ctrl->smax_check[q], s->ctrl,
-                    q > 0 ? q - 1 : -1, q > 0 ? plan.dx[q - 1] : 0.0, skip);
+    if (host_out && q == plan.nsweeps - 1) {
+      // the slabs alternate between the solver's stream and `slab` (forked
+      // here, joined below) so that one slab's tail overlaps the next slab
+      SlabCopy slabs[fvs::kHostSlabs];
+      const int n = HostSlabs(s, plan.dir[q], slabs);
+      const size_t cs = size_t(s->cells);
+      e = cudaEventRecord(s->slab_fork, s->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s->slab, s->slab_fork, 0);
+      for (int k = 0; k < n && e == cudaSuccess; ++k) {
+        cudaStream_t st = (k % 2) ? s->slab : s->stream;
+        e = LaunchSweep(s, s->buf[src], s->buf[dst], plan.dir[q], &s->ctrl->dt, plan.frac, 0.0,
+                        skip ? nullptr : &s->ctrl->smax_check[q], s->ctrl,
+                        q > 0 ? q - 1 : -1, q > 0 ? plan.dx[q - 1] : 0.0, skip, slabs[k].t_lo,
+                        slabs[k].t_hi, st);
+        if (e == cudaSuccess) e = cudaEventRecord(s->slab_ev[k], st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s->copy, s->slab_ev[k], 0);
+        for (int c = 0; c < s->ncons && e == cudaSuccess; ++c) {
+          const SlabCopy& sc = slabs[k];
+          double* dsth = host_out + c * cs + sc.offset;
+          const double* srcd = s->buf[dst] + c * cs + sc.offset;
+          e = sc.rows == 1
+                  ? cudaMemcpyAsync(dsth, srcd, size_t(sc.width) * 8, cudaMemcpyDeviceToHost,
+                                    s->copy)
+                  : cudaMemcpy2DAsync(dsth, size_t(sc.pitch) * 8, srcd, size_t(sc.pitch) * 8,
+                                      size_t(sc.width) * 8, size_t(sc.rows),
+                                      cudaMemcpyDeviceToHost, s->copy);
+        }
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(s->slab_fork, s->slab);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->slab_fork, 0);
+      if (e == cudaSuccess) e = cudaEventRecord(s->slab_ev[fvs::kHostSlabs], s->copy);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s->stream, s->slab_ev[fvs::kHostSlabs], 0);
+    } else {
+      e = LaunchSweep(s, s->buf[src], s->buf[dst], plan.dir[q], &s->ctrl->dt,
+                      plan.frac, 0.0, skip ? nullptr : &s->ctrl->smax_check[q], s->ctrl,
+                      q > 0 ? q - 1 : -1, q > 0 ? plan.dx[q - 1] : 0.0, skip);
+    }
     if (e != cudaSuccess) return e;
     src = dst;
     dst = (dst == X) ? Y : X;
@@ -1335,6 +1462,97 @@ int fvs_exact_riemann_star(const fvs_method* m, int64_t n, const double* rhoL_de
 int fvs_solver_stream(fvs_solver* s, void** stream) {
   if (!s || !stream) return Fail(FVS_ERR_INVALID, "NULL argument");
   *stream = static_cast<void*>(s->stream);
+  return FVS_OK;
+}
+
+int fvs_solver_step_host(fvs_solver* s, double* cons_host, double cfl, double t_end,
+                         fvs_run_stats* stats) {
+  if (!s || !cons_host) return Fail(FVS_ERR_INVALID, "NULL argument");
+  if (!(cfl > 0.0)) return Fail(FVS_ERR_INVALID, "cfl must be positive");
+  if (s->cc)
+    return Fail(FVS_ERR_UNSUPPORTED,
+                "host-resident steps of cut-cell grids: use fvs_solver_upload, _run, _download");
+  if (!s->copy) {
+    FVS_CUDA(cudaStreamCreateWithFlags(&s->copy, cudaStreamNonBlocking));
+    FVS_CUDA(cudaStreamCreateWithFlags(&s->slab, cudaStreamNonBlocking));
+    FVS_CUDA(cudaEventCreateWithFlags(&s->slab_fork, cudaEventDisableTiming));
+    for (cudaEvent_t& e : s->slab_ev)
+      FVS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  const size_t bytes = size_t(s->cells) * s->ncons * sizeof(double);
+  fvs::Control c{};
+  c.t = s->t;
+  c.t_end = t_end;
+  c.cfl = cfl;
+  FVS_CUDA(cudaMemcpyAsync(s->ctrl, &c, sizeof c, cudaMemcpyHostToDevice, s->stream));
+  // The upload, in slabs of z-planes on the copy stream, overlaps the
+  // stable-dt pass, which takes each slab's faces once it has landed (the
+  // first slab last: its z faces read the last plane on a periodic grid).
+  // Methods whose stable-dt pass has no plane ranges upload in one piece.
+  const bool reflective = s->g.bc[0] == FVS_BC_REFLECTIVE || s->g.bc[1] == FVS_BC_REFLECTIVE ||
+                          s->g.bc[2] == FVS_BC_REFLECTIVE;
+  const bool piped = s->g.rank == 3 && s->m.flux_method <= FVS_HLLE && !reflective &&
+                     s->t < t_end && s->g.n[2] >= fvs::kHostSlabs;
+  double* dev = s->buf[s->cur];
+  if (piped) {
+    const int nz = s->g.n[2], ns = fvs::kHostSlabs;
+    const size_t plane = size_t(s->g.n[0]) * s->g.n[1], cs = size_t(s->cells);
+    FVS_CUDA(cudaMemsetAsync(s->ctrl->smax_stable, 0, sizeof(s->ctrl->smax_stable), s->stream));
+    FVS_CUDA(cudaEventRecord(s->slab_ev[fvs::kHostSlabs], s->stream));
+    FVS_CUDA(cudaStreamWaitEvent(s->copy, s->slab_ev[fvs::kHostSlabs], 0));
+    for (int k = 0; k < ns; ++k) {
+      const int z0 = nz * k / ns, z1 = nz * (k + 1) / ns;
+      for (int comp = 0; comp < s->ncons; ++comp)
+        FVS_CUDA(cudaMemcpyAsync(dev + comp * cs + z0 * plane, cons_host + comp * cs + z0 * plane,
+                                 size_t(z1 - z0) * plane * sizeof(double),
+                                 cudaMemcpyHostToDevice, s->copy));
+      FVS_CUDA(cudaEventRecord(s->slab_ev[k], s->copy));
+      if (k == 0) continue;
+      FVS_CUDA(cudaStreamWaitEvent(s->stream, s->slab_ev[k], 0));
+      FVS_CUDA(LaunchStable(s, dev, s->ctrl->smax_stable, s->ctrl, z0, z1));
+    }
+    FVS_CUDA(cudaStreamWaitEvent(s->stream, s->slab_ev[0], 0));
+    FVS_CUDA(LaunchStable(s, dev, s->ctrl->smax_stable, s->ctrl, 0, nz / ns));
+  } else {
+    FVS_CUDA(cudaMemcpyAsync(dev, cons_host, bytes, cudaMemcpyHostToDevice, s->stream));
+  }
+  const int nsweeps = s->g.rank == 1 ? 1 : 2 * s->g.rank;
+  int restarts = 0, committed = 0;
+  bool stable_enqueued = piped;
+  while (s->t < t_end) {
+    FVS_CUDA(EnqueueStep(s, s->cur, s->cycle, 0, cons_host, stable_enqueued));
+    stable_enqueued = false;  // a restart runs the whole step again
+    FVS_CUDA(cudaMemcpyAsync(s->ctrl_host, s->ctrl, sizeof(fvs::Control),
+                             cudaMemcpyDeviceToHost, s->stream));
+    FVS_CUDA(cudaStreamSynchronize(s->stream));
+    const fvs::Control& h = *s->ctrl_host;
+    if (h.steps_done > 0) {
+      s->cur = NextBuffer(s->cur, nsweeps);
+      s->cycle += 1;
+      s->t = h.t;
+      committed = 1;
+      break;
+    }
+    if (!h.abort) break;
+    // a failed per-sweep check: the step is redone from its start buffer with
+    // the failing sweep's dt (its downloads are overwritten by the redo)
+    if (++restarts > 64) return Fail(FVS_ERR_STATE, "step restarted 64 times");
+    const int zero = 0;
+    FVS_CUDA(cudaMemcpyAsync(&s->ctrl->abort, &zero, sizeof zero, cudaMemcpyHostToDevice,
+                             s->stream));
+  }
+  FVS_CUDA(cudaStreamSynchronize(s->stream));
+  const fvs::Control& h = *s->ctrl_host;
+  if (stats) {
+    stats->time = s->t;
+    stats->steps = committed;
+    stats->restarts = restarts;
+    stats->status = committed ? h.status : 0;
+    stats->last_dt = committed ? h.dt : 0.0;
+  }
+  if (committed && (h.status & fvs::kStatusCopyTimeout))
+    return Fail(FVS_ERR_CUDA, "a staged copy of a sweep did not land in time");
+  if (committed && h.status) return Fail(FVS_ERR_STATE, "non-positive density encountered");
   return FVS_OK;
 }
 

@@ -48,6 +48,10 @@ enum StatusBits : int {
   kStatusCopyTimeout = 8,  // a staged (TMA) copy did not land in time
 };
 
+// Slabs of a host-resident step's last sweep (fvs_solver_step_host): each
+// slab's download starts when the slab's cells are final.
+constexpr int kHostSlabs = 8;
+
 // The TMA-staged y/z sweep (mixed flavour): each warp stages its 32 lines
 // in a ring of kTmaStages buffers of kTmaRows cells; blocks of kTmaWarps.
 constexpr int kTmaRows = 2;
@@ -91,6 +95,9 @@ struct SweepArgs {
                         // mixed x sweeps: + 10 for the marching kernel in x;
                         // mixed y/z sweeps: + 20 for the TMA-staged kernel
   const void* tmap;     // host: CUtensorMap of `in` for the TMA-staged kernel, or NULL
+  // grid lines [t_lo, t_hi) only (t: the line index of the marching and
+  // lanes-along-x kernels); t_hi == 0: every line
+  int64_t t_lo, t_hi;
 };
 
 // Stable-dt pass over all directions (max face speed per direction).
@@ -104,6 +111,9 @@ struct StableDtArgs {
   double gamma;
   unsigned long long* smax_out;  // [rank]
   Control* ctrl;
+  // 3-D: the faces of the planes [k_lo, k_hi) only (their z faces read plane
+  // k_lo - 1); k_hi == 0: every plane
+  int k_lo, k_hi;
 };
 
 // Sets the message returned by fvs_last_error() (fvs_capi.cu).

@@ -138,8 +138,9 @@ __global__ void __launch_bounds__(32 * kDtRows) StableDtMarch3Kernel(StableDtArg
   const int jblocks = (ny + kDtRows - 1) / kDtRows;
   const int wx = static_cast<int>(blockIdx.x % xw);
   const int jb = static_cast<int>((blockIdx.x / xw) % jblocks);
-  const int k0 = static_cast<int>(blockIdx.x / (int64_t(xw) * jblocks)) * seg;
-  const int k1 = min(nz, k0 + seg);
+  // planes [k_lo, k_hi) only when k_hi > 0 (an uploaded slab)
+  const int k0 = a.k_lo + static_cast<int>(blockIdx.x / (int64_t(xw) * jblocks)) * seg;
+  const int k1 = min(a.k_hi > 0 ? a.k_hi : nz, k0 + seg);
   const int j = jb * kDtRows + warp;
   const bool jvalid = j < ny;
   const int jc = jvalid ? j : ny - 1;
@@ -233,8 +234,9 @@ __global__ void __launch_bounds__(32 * kDtRows) StableDtScreen3Kernel(StableDtAr
   const int jblocks = (ny + kDtRows - 1) / kDtRows;
   const int wx = static_cast<int>(blockIdx.x % xw);
   const int jb = static_cast<int>((blockIdx.x / xw) % jblocks);
-  const int k0 = static_cast<int>(blockIdx.x / (int64_t(xw) * jblocks)) * seg;
-  const int k1 = min(nz, k0 + seg);
+  // planes [k_lo, k_hi) only when k_hi > 0 (an uploaded slab)
+  const int k0 = a.k_lo + static_cast<int>(blockIdx.x / (int64_t(xw) * jblocks)) * seg;
+  const int k1 = min(a.k_hi > 0 ? a.k_hi : nz, k0 + seg);
   const int j = jb * kDtRows + warp;
   const bool jvalid = j < ny;
   const int jc = jvalid ? j : ny - 1;
@@ -359,12 +361,13 @@ cudaError_t LaunchStableDtT(const StableDtArgs& a, cudaStream_t s) {
   if (a.rank == 3 && !reflective) {
     // blocks of kDtRows x rows; enough blocks for about two waves of the GPU,
     // the planes split accordingly; every block full (see the kernel)
+    const int planes = a.k_hi > 0 ? a.k_hi - a.k_lo : a.n[2];
     const int64_t tiles = int64_t((a.n[0] + 30) / 31) * ((a.n[1] + kDtRows - 1) / kDtRows);
     const int64_t want = int64_t(GridStrideBlocks(int64_t(1) << 40, 32 * kDtRows, 8)) * 2;
     const int64_t zseg =
-        std::max<int64_t>(1, std::min<int64_t>(a.n[2], (want + tiles - 1) / tiles));
-    const int seg = static_cast<int>((a.n[2] + zseg - 1) / zseg);
-    const unsigned grid = static_cast<unsigned>(tiles * ((a.n[2] + seg - 1) / seg));
+        std::max<int64_t>(1, std::min<int64_t>(planes, (want + tiles - 1) / tiles));
+    const int seg = static_cast<int>((planes + zseg - 1) / zseg);
+    const unsigned grid = static_cast<unsigned>(tiles * ((planes + seg - 1) / seg));
     if constexpr (EinfeldtCfl<PT<3>>::value) {
       if (a.gamma > 1.0 && a.gamma <= 2.0 && a.smax_out) {
         StableDtScreen3Kernel<PT><<<grid, 32 * kDtRows, 0, s>>>(a, seg);
@@ -375,7 +378,8 @@ cudaError_t LaunchStableDtT(const StableDtArgs& a, cudaStream_t s) {
     return cudaGetLastError();
   }
   // ranks 1 and 2, and 3-D grids with a reflective direction (the cell-wise
-  // kernel reflects the ghost states of the boundary faces)
+  // kernel reflects the ghost states of the boundary faces); no plane ranges
+  if (a.k_hi > 0) return cudaErrorNotSupported;
   const unsigned grid = GridStrideBlocks(cells, block, 8);
   if (a.rank == 1)
     StableDtKernelT<1, PT><<<grid, block, 0, s>>>(a);

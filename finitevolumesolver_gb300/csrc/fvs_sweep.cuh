@@ -522,13 +522,14 @@ __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepMarchKernel(Sweep
   if (DIR == 0) ntrans = int64_t(ny) * nz;
   else if (DIR == 1) ntrans = int64_t(nx) * nz;
   else ntrans = int64_t(nx) * ny;
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t t_end = a.t_hi > 0 ? a.t_hi : ntrans;
+  const int64_t t = a.t_lo + int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int j0 = blockIdx.y * a.seg_len;
   const int j1 = min(a.n[DIR], j0 + a.seg_len);
 
   const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
   if (!BlockAll(SweepGate(a, split_dt))) return;
-  const bool active = t < ntrans;
+  const bool active = t < t_end;
   const unsigned amask = __ballot_sync(0xffffffffu, active);
 
   GlobalLine<K, DIR> line;
@@ -940,15 +941,16 @@ template <int D, template <int> class PT>
 __global__ void __launch_bounds__(128, PT<D>::kMinBlocks) SweepXWarpKernel(SweepArgs a) {
   using P = PT<D>;
   using R = typename P::Real;
-  const int64_t rows = int64_t(a.n[1]) * a.n[2];
+  const int64_t rows = a.t_hi > 0 ? a.t_hi - a.t_lo : int64_t(a.n[1]) * a.n[2];
   const double split_dt = a.dt_ptr ? a.dt_scale * (*a.dt_ptr) : a.dt_value;
   if (!BlockAll(SweepGate(a, split_dt))) return;
   R smax = R(0);
   int status = 0;
   typename P::Stats stats;
-  const int64_t row = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t rel = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t row = a.t_lo + rel;
   const bool full_block = int64_t(blockIdx.x + 1) * (blockDim.x >> 5) <= rows;  // block-uniform
-  if (row >= rows) return;  // only in a block that is not full
+  if (rel >= rows) return;  // only in a block that is not full
   XWarpRow<D, PT>(a, row, split_dt, smax, status, stats);
   stats.Flush(a.stats_out);
   const double smax_d = static_cast<double>(smax);
@@ -994,6 +996,7 @@ cudaError_t LaunchSweepT(const SweepArgs& a, cudaStream_t s) {
   int64_t ntrans = 1;
   for (int d = 0; d < 3; ++d)
     if (d != a.dir) ntrans *= a.n[d];
+  if (a.t_hi > 0) ntrans = a.t_hi - a.t_lo;  // a range of the lines
   const int block = 128;
   const int seg = a.seg_len > 0 ? a.seg_len : nd;
   SweepArgs b = a;
@@ -1005,7 +1008,7 @@ cudaError_t LaunchSweepT(const SweepArgs& a, cudaStream_t s) {
     if constexpr (P<D>::kWarpX) {
       // (x sweeps of reflective rows take the marching kernel: the caller
       // routes them to a policy without kWarpX)
-      const int64_t rows = int64_t(a.n[1]) * a.n[2];
+      const int64_t rows = ntrans;
       const unsigned xgrid = static_cast<unsigned>((rows * 32 + block - 1) / block);
       SweepXWarpKernel<D, P><<<xgrid, block, 0, s>>>(b);
     } else {
@@ -1015,14 +1018,14 @@ cudaError_t LaunchSweepT(const SweepArgs& a, cudaStream_t s) {
   case 1:
     if constexpr (D >= 2) {
       if constexpr (kTmaStaged<P<D>>)
-        if (a.occupancy >= 20 && a.tmap) return LaunchSweepTma<D, 1, P>(b, s);
+        if (a.occupancy >= 20 && a.tmap && a.t_hi == 0) return LaunchSweepTma<D, 1, P>(b, s);
       SweepMarchKernel<D, 1, P><<<grid, block, 0, s>>>(b);
     }
     break;
   default:
     if constexpr (D >= 3) {
       if constexpr (kTmaStaged<P<D>>)
-        if (a.occupancy >= 20 && a.tmap) return LaunchSweepTma<D, 2, P>(b, s);
+        if (a.occupancy >= 20 && a.tmap && a.t_hi == 0) return LaunchSweepTma<D, 2, P>(b, s);
       SweepMarchKernel<D, 2, P><<<grid, block, 0, s>>>(b);
     }
     break;

@@ -298,6 +298,20 @@ int fvs_solver_create(const fvs_grid_desc* grid, const fvs_method* m,
 int fvs_solver_destroy(fvs_solver* s);
 /* Conservative state, rank+2 components, [c][nz][ny][nx], host memory. */
 int fvs_solver_upload(fvs_solver* s, const double* cons_host);
+/* One split step of a state that lives in host memory, in place: uploads
+ * cons_host (rank+2 components, [c][nz][ny][nx]), advances it by one step as
+ * fvs_solver_run does (stable dt, dt = min(cfl * stable dt, t_end - t), the
+ * sweeps and their checks, a restart on a failed check) and writes the new
+ * state back to cons_host.  The write-back overlaps the step's last sweep:
+ * that sweep runs in slabs of its slowest transverse direction and each
+ * slab is copied to the host as soon as it is final (one cudaMemcpyAsync or
+ * cudaMemcpy2DAsync per component and slab), so only the last slab's copy
+ * adds to the step.  Page-locked cons_host (cudaHostAlloc, cudaHostRegister)
+ * lets the copies run asynchronously.  With t >= t_end nothing is advanced
+ * (stats->steps 0).  Afterwards the solver's device state equals cons_host.
+ * Uniform grids (no embedded boundary). */
+int fvs_solver_step_host(fvs_solver* s, double* cons_host, double cfl, double t_end,
+                         fvs_run_stats* stats);
 int fvs_solver_download(fvs_solver* s, double* cons_host);
 /* Device pointer of the current state (valid until the next call). */
 int fvs_solver_state_device(fvs_solver* s, double** cons_dev);
