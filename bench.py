@@ -542,9 +542,11 @@ def report_cutcell(args, torch, fvs, workloads, peaks=None):
             alpha = geo["alpha"][G:-G, G:-G]
             out["cut_cells"] = int(geo["cut"][G:-G, G:-G].sum())
         rate = 4 * n * n * st.steps / (ms / 1e3)
+        seg, occ = s.tuning()
         out["flavours"][prec] = {
             "steps": st.steps, "restarts": st.restarts, "ms_per_step": ms / max(st.steps, 1),
-            "cell_updates_per_s": rate}
+            "cell_updates_per_s": rate,
+            "autotuned": {"segment_cells": seg, "variant": occ}}
         if peaks:
             # 64 B state + 64 B geometry (alpha, beta, shielded weights, x_B, normal)
             out["flavours"][prec]["hbm_frac_algorithmic"] = rate * 128 / 1e9 / peaks["hbm_gbs"]

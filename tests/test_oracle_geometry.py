@@ -142,3 +142,22 @@ def test_union_of_shapes(orc):
     both_fluid = (a.alpha == 1) & (b.alpha == 1)
     assert np.all(u.alpha[both_fluid] == 1)
     np.testing.assert_array_less(u.betax - 1e-15, np.minimum(a.betax, b.betax) + 1e-15)
+
+
+def test_polygon_known_answer_of_the_reference(orc):
+    """The reference's polygon test (tests/test.Geometry.Polygon.cpp): the
+    triangle (0.1, 0.1), (0.2, 0.1), (0.15, 0.2) has (0.11, 0.105) inside
+    (distance > 0) and (0.09, 0.1) outside.  The reference hands that distance
+    to AMReX's EB generator as the implicit function
+    (include/fub/AMReX/Geometry.hpp:37-45), positive in the body, so here the
+    first point's cell is covered (alpha 0) and the second one's fluid."""
+    n = 1000
+    xy = [(0.1, 0.1), (0.2, 0.1), (0.15, 0.2), (0.1, 0.1)]
+    g = orc.CutCellGeometry(n, n, shapes=[{"kind": "polygon", "xy": xy}])
+    G = g.G
+
+    def cell(x, y):
+        return int(y * n) + G, int(x * n) + G
+
+    assert g.alpha[cell(0.11, 0.105)] == 0.0
+    assert g.alpha[cell(0.09, 0.1)] == 1.0
