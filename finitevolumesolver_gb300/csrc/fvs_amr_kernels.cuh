@@ -64,7 +64,10 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
     int cap = w.cap_begin;
     int next_face = cap < w.cap_end ? a.caps[cap].face : INT_MAX;
     const int j0 = w.j0, j1 = w.j1;
-    auto load = [&](double* u, int j) {
+    // returns whether the cell is a reflective boundary's image, whose
+    // momentum along the row the caller negates after the conversion (so the
+    // prefetched load is not waited for early)
+    auto load = [&](double* u, int j) -> bool {
       const double* src = in;
       int64_t off, cs = N;
       bool flip = false;
@@ -84,17 +87,19 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
       }
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(src + c * cs + off);
-      if (flip) u[1 + DIR] = -u[1 + DIR];  // a reflective boundary's image
+      return flip;
     };
     // the update re-reads the FP64 state of cell j-1 (an L1 hit) instead of
     // carrying a window of FP64 states in registers
     double dn[K];
     R cm[K], cc[K], cp[K];
-    load(dn, j0 - 2);
+    const bool flip_cm = load(dn, j0 - 2);
     P::ToCell(cm, dn);
-    load(dn, j0 - 1);
+    if (flip_cm) cm[1 + DIR] = -cm[1 + DIR];
+    const bool flip_cc = load(dn, j0 - 1);
     P::ToCell(cc, dn);
-    load(dn, j0);
+    if (flip_cc) cc[1 + DIR] = -cc[1 + DIR];
+    bool flip_dn = load(dn, j0);
     using FluxT = typename FluxOf<P>::type;
     typename P::Rec recR_prev;
     typename P::Wave w_prev;
@@ -128,7 +133,8 @@ __global__ void __launch_bounds__(128, PT<2>::kMinBlocks) PatchSweepKernel(Patch
         v_prev = v;
       }
       P::ToCell(cp, dn);
-      if (j + 2 <= j1 + 1) load(dn, j + 2);
+      if (flip_dn) cp[1 + DIR] = -cp[1 + DIR];  // a reflective boundary's image
+      if (j + 2 <= j1 + 1) flip_dn = load(dn, j + 2);
       typename P::Rec recL, recR;
       P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
       typename P::Wave wv{};

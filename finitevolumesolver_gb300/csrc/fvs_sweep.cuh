@@ -355,19 +355,22 @@ struct NewtonStats {
 
 // The cells of one grid line of a marching sweep, read from global memory:
 // Load gives cell j's conservative state (FP64; a ghost cell is the
-// boundary condition's image), CellRef an interior cell's components for
-// the update, Advance is called at the start of every iteration (nothing to
-// do here).
+// boundary condition's image) and returns whether the image's momentum
+// along the line is to be negated (a reflective wall); the caller negates it
+// after the conversion to the compute precision, so that the prefetched load
+// is not waited for one iteration early.  CellRef gives an interior cell's
+// components for the update; Advance is called at the start of every
+// iteration (nothing to do here).
 template <int K, int DIR> struct GlobalLine {
   const double* __restrict__ in;
   int64_t base, stride, cs;  // stride: cells between neighbours (1 in x)
   int nd, bc;
   __device__ __forceinline__ int64_t Stride() const { return DIR == 0 ? 1 : stride; }
-  __device__ __forceinline__ void Load(double* u, int j) const {
+  __device__ __forceinline__ bool Load(double* u, int j) const {
     const int64_t off = base + int64_t(BcIndex(j, nd, bc)) * Stride();
 #pragma unroll
     for (int c = 0; c < K; ++c) u[c] = __ldg(in + c * cs + off);
-    if (BcFlip(j, nd, bc)) u[1 + DIR] = -u[1 + DIR];
+    return BcFlip(j, nd, bc);
   }
   // interior cell j's components for the update (an L1 hit: loaded two
   // iterations earlier)
@@ -414,11 +417,13 @@ __device__ __forceinline__ void MarchSegment(const SweepArgs& a, Line& line, int
   // FP64 states in registers.
   double dn[K];
   R cm[K], cc[K], cp[K];
-  line.Load(dn, j0 - 2);
+  const bool flip_cm = line.Load(dn, j0 - 2);
   P::ToCell(cm, dn);
-  line.Load(dn, j0 - 1);
+  if (flip_cm) cm[1 + DIR] = -cm[1 + DIR];
+  const bool flip_cc = line.Load(dn, j0 - 1);
   P::ToCell(cc, dn);
-  line.Load(dn, j0);
+  if (flip_cc) cc[1 + DIR] = -cc[1 + DIR];
+  bool flip_dn = line.Load(dn, j0);
   using FluxT = typename FluxOf<P>::type;
   typename P::Rec recR_prev;
   typename P::Wave w_prev;
@@ -468,7 +473,8 @@ __device__ __forceinline__ void MarchSegment(const SweepArgs& a, Line& line, int
       }
     }
     P::ToCell(cp, dn);
-    if (j + 2 <= j1 + 1) line.Load(dn, j + 2);
+    if (flip_dn) cp[1 + DIR] = -cp[1 + DIR];  // a reflective wall's image
+    if (j + 2 <= j1 + 1) flip_dn = line.Load(dn, j + 2);
     typename P::Rec recL, recR;
     P::Predict(eq, recL, recR, cm, cc, cp, a.limiter, lambda_half, DIR);
     typename P::Wave w{};
@@ -621,14 +627,12 @@ template <int K, int DIR, int kRows, int kStages> struct TmaLine : GlobalLine<K,
     WaitUpTo(q);
     return ring + (q % kStages) * kBox + (rel % kRows) * 32 + lane;
   }
-  __device__ __forceinline__ void Load(double* u, int j) {
-    if (j < 0 || j >= this->nd) {
-      GlobalLine<K, DIR>::Load(u, j);
-      return;
-    }
+  __device__ __forceinline__ bool Load(double* u, int j) {
+    if (j < 0 || j >= this->nd) return GlobalLine<K, DIR>::Load(u, j);
     const double* p = At(j);
 #pragma unroll
     for (int c = 0; c < K; ++c) u[c] = p[c * kRows * 32];
+    return false;
   }
   struct Ref {
     const double* p;
