@@ -5,8 +5,9 @@ workloads the bench times, where the index paths differ (multi-block row
 tables, segment splits, tens of thousands of patch rows per level, thousands
 of cut cells):
 
-* 3-D octants, 256^3 periodic: one Strang step in exact FP64 (bit for bit)
-  and in fast FP64 (1e-12 relative per cell, tests/tolerance.py);
+* 3-D octants, 256^3 periodic: one Strang step in exact FP64 (bit for bit,
+  also through the host-resident step fvs_solver_step_host) and in fast FP64
+  (1e-12 relative per cell, tests/tolerance.py);
 * 2-D AMR blast, 4096 patches on 3 levels (level 0 1024^2): one subcycled
   coarse step in exact FP64, launch shapes from the autotuner, bit for bit;
 * 2-D Mach-2 shock over 8 circles, 1024^2 with 4171 cut cells: geometry,
@@ -47,6 +48,15 @@ def test_octants_256_exact_strang_step_bit_exact(fvs, orc, octants256):
     np.testing.assert_array_equal(dts, ref_dts)
     np.testing.assert_array_equal(s.download(), ref)
     s.close()
+    # the host-resident step of the e2e benchmark (slabbed upload and stable
+    # dt, slabbed last sweep with overlapped write-back): the same bits
+    import torch
+    h = fvs.Solver([n] * 3, dx, "periodic")
+    host = torch.from_numpy(cons.copy()).pin_memory()
+    sh = h.step_host(host, cfl=0.8, t_end=1e9)
+    assert sh.steps == 1 and sh.last_dt == ref_dts[0]
+    np.testing.assert_array_equal(host.numpy(), ref)
+    h.close()
 
 
 def test_octants_256_fast_strang_step_within_1e12(fvs, orc, octants256):

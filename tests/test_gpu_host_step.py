@@ -88,3 +88,25 @@ def test_step_host_refuses_cut_cells(fvs):
     with pytest.raises(fvs.FvsError):
         s.step_host(np.zeros((4, 1, 32, 32)))
     s.close()
+
+
+@pytest.mark.parametrize("flux_method", ["godunov", "muscl_godunov", "hllem", "muscl_char"])
+def test_step_host_other_flux_methods(fvs, torch_cuda, flux_method):
+    """The slabbed last sweep and the unpiped upload of methods other than
+    MUSCL-HLLE / HLLE (whose stable-dt pass has no plane ranges) give the same
+    steps as upload, run and download."""
+    torch = torch_cuda
+    shape = [24, 20, 18]
+    cons = _state(3, shape, 7)
+    m = fvs.make_method(flux_method=flux_method)
+    a = fvs.Solver(shape, [1.0 / 32] * 3, "transmissive", method=m)
+    b = fvs.Solver(shape, [1.0 / 32] * 3, "transmissive", method=m)
+    host = torch.from_numpy(cons.copy()).pin_memory()
+    b.upload(cons)
+    for _ in range(2):
+        st = a.step_host(host, cfl=0.8)
+        sb, _ = b.run(cfl=0.8, t_end=1e300, max_steps=1)
+        assert st.steps == 1 and st.last_dt == sb.last_dt
+        np.testing.assert_array_equal(host.numpy(), b.download())
+    a.close()
+    b.close()
