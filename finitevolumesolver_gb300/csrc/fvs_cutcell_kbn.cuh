@@ -659,26 +659,45 @@ __device__ __forceinline__ int CellClassAt(const CcGeom& g, int dir, int t, int 
 // The regular and covered cells of a mixed-precision KBN sweep, staged in
 // shared memory.  A block takes 32 grid lines (one tile group) x 64 cells (8
 // tiles) along the sweep direction: it loads the masked FP32 states of the
-// cells and their 2-cell halos once (coalesced, one conversion per value;
-// the x sweep's lanes run along x) into shared memory, then each warp marches
-// one tile that holds a regular cell -- its lanes the 32 lines, each thread
-// 8 cells -- from shared memory: masked MUSCL-Hancock + HLL with every mask
-// true, f + 0 and U + dt/dx (fs_L - fs_R), the FP64 state re-read for the
-// update.  On a regular cell the KBN arithmetic is exactly this (the
-// stabilised flux us_rel f + sL_rel fsL + sR_rel fsR = 1 f + 0 fsL + 0 fsR is
-// f + 0 for every finite f; the + 0 turns a -0 into +0 as the zero terms
-// do), and its stencil (cells j-2 .. j+2) holds only regular-valued data, so
-// computing every cell of the tile this way and writing the regular ones is
-// exact.  Covered cells are written as 0; band cells are the band kernel's.
-// A face's CFL speed is counted here when one of its cells is regular.
+// cells and their 2-cell halos, and their classes, once (coalesced, one
+// conversion per value; the x sweep's lanes run along x) into shared memory,
+// then each warp marches one tile that holds a regular cell -- its lanes the
+// 32 lines, each thread 8 cells -- from shared memory: masked MUSCL-Hancock
+// + HLL with every mask true, f + 0 and U + dt/dx (fs_L - fs_R).  On a
+// regular cell the KBN arithmetic is exactly this (the stabilised flux
+// us_rel f + sL_rel fsL + sR_rel fsR = 1 f + 0 fsL + 0 fsR is f + 0 for
+// every finite f; the + 0 turns a -0 into +0 as the zero terms do), and its
+// stencil (cells j-2 .. j+2) holds only regular-valued data, so computing
+// every cell of the tile this way and writing the regular ones is exact.
+// Covered cells are written as 0; band cells are the band kernel's.  A
+// face's CFL speed is counted here when one of its cells is regular.
+//
+// y sweeps update in the march (a warp's lanes hold 32 x-neighbouring
+// cells: coalesced).  In x sweeps the lanes hold 32 rows, so the march
+// stores its face fluxes in shared memory and, after a barrier, the block
+// updates the tile with its threads along x: the re-read of the FP64 state,
+// the stores and the class reads are coalesced.
+constexpr int kTileLines = 32;
+constexpr int kTileSegs = 8;                          // tiles per block
+constexpr int kTileCells = kCcTile * kTileSegs;      // cells per block along dir
+constexpr int kTileHalo = kTileCells + 4;            // with the 2-cell halos
+constexpr int kTilePitch = kTileLines + 1;           // padded line stride
+template <class T> constexpr size_t KbnTileSmemBytes(int dir) {
+  return sizeof(T) * 4 * kTileHalo * kTilePitch + size_t(kTileHalo) * kTilePitch +
+         (dir == 0 ? sizeof(T) * 4 * (kTileCells + 1) * kTilePitch : 0);
+}
+
 template <class T, class M>
 __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
-  constexpr int kL = 32;                 // lines of a tile group
-  constexpr int kNSeg = 8;               // tiles per block
-  constexpr int kC = kCcTile * kNSeg;    // cells per block along dir
-  constexpr int kH = kC + 4;             // with the 2-cell halos
-  constexpr int kP = kL + 1;             // padded line stride (no bank conflicts)
-  __shared__ T su[4][kH][kP];
+  constexpr int kL = kTileLines, kNSeg = kTileSegs, kC = kTileCells, kH = kTileHalo,
+                kP = kTilePitch;
+  extern __shared__ __align__(16) unsigned char tile_smem[];
+  T (*su)[kH][kP] = reinterpret_cast<T (*)[kH][kP]>(tile_smem);  // [4][kH][kP]
+  signed char (*scls)[kP] =
+      reinterpret_cast<signed char (*)[kP]>(tile_smem + sizeof(T) * 4 * kH * kP);
+  // x sweeps: the face fluxes of the block's cells, faces C0 .. C0 + kC
+  T (*sf)[kC + 1][kP] = reinterpret_cast<T (*)[kC + 1][kP]>(
+      tile_smem + ((sizeof(T) * 4 * kH * kP + size_t(kH) * kP + 15) / 16) * 16);
   const CcGeom& g = a.s.g;
   const int dir = a.dir;
   const int nd = dir == 0 ? g.nx : g.ny;
@@ -697,36 +716,34 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
   const KbnConst<T, M>& kc = KbnBlockConst<T, M>(a);
   if (!kc.run) return;  // block-uniform
   const GasT<T, M> eq = kc.eq;
-  if (any_regular) {
-    for (int idx = threadIdx.x; idx < kH * kL; idx += blockDim.x) {
-      int line, cell;
-      if (dir == 0) {
-        cell = idx % kH;
-        line = idx / kH;
-      } else {
-        line = idx % kL;
-        cell = idx / kL;
-      }
-      const int t = group * kL + line, c = C0 - 2 + cell;
-      T v[4] = {T(0), T(0), T(0), T(0)};
-      if (t < nt && c <= nd + 1) {
-        double vd[4];
-        if (dir == 0)
-          LoadCons(a.s, c, t, vd);
-        else
-          LoadCons(a.s, t, c, vd);
-        T w[4];
-        Narrow(w, vd);
-        C2T<T> q;
-        CompleteMasked(eq, q, w, true);
-        v[0] = q.rho;
-        v[1] = q.m[0];
-        v[2] = q.m[1];
-        v[3] = q.E;
-      }
-#pragma unroll
-      for (int k = 0; k < 4; ++k) su[k][cell][line] = v[k];
+  for (int idx = threadIdx.x; idx < kH * kL; idx += blockDim.x) {
+    int line, cell;
+    if (dir == 0) {
+      cell = idx % kH;
+      line = idx / kH;
+    } else {
+      line = idx % kL;
+      cell = idx / kL;
     }
+    const int t = group * kL + line, c = C0 - 2 + cell;
+    scls[cell][line] = static_cast<signed char>(t < nt ? CellClassAt(g, dir, t, c) : kCcBand);
+    if (!any_regular) continue;
+    T v[4] = {T(0), T(0), T(0), T(0)};
+    if (t < nt && c <= nd + 1) {
+      double vd[4];
+      if (dir == 0)
+        LoadCons(a.s, c, t, vd);
+      else
+        LoadCons(a.s, t, c, vd);
+      T w[4];
+      Narrow(w, vd);
+      // the masked state (CompleteMasked with mask true): zero unless rho > 0
+      const bool pos = w[0] > T(0);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v[k] = pos ? w[k] : T(0);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) su[k][cell][line] = v[k];
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -734,22 +751,24 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
   const int t = group * kL + lane;
   const int c0 = tile * kCcTile, c1 = min(nd, c0 + kCcTile);
   const int64_t cs = int64_t(g.nx) * g.ny;
-  auto offset = [&](int c) {
-    return dir == 0 ? int64_t(t) * g.nx + c : int64_t(c) * g.nx + t;
+  const double dt_dx = kc.dt_dx;
+  auto offset = [&](int tt, int c) {
+    return dir == 0 ? int64_t(tt) * g.nx + c : int64_t(c) * g.nx + tt;
   };
+  auto cls_at = [&](int c) { return static_cast<int>(scls[c - C0 + 2][lane]); };
   T smax = T(0);
   int status = 0;
   if (tile < ntl && t < nt) {
     if (treg[tile] == 0) {
-      for (int c = c0; c < c1; ++c)
-        if (CellClassAt(g, dir, t, c) == kCcCovered) {
-          const int64_t o = offset(c);
+      if (dir != 0)
+        for (int c = c0; c < c1; ++c)
+          if (cls_at(c) == kCcCovered) {
+            const int64_t o = offset(t, c);
 #pragma unroll
-          for (int k = 0; k < 4; ++k) a.out[k * cs + o] = 0.0;
-        }
+            for (int k = 0; k < 4; ++k) a.out[k * cs + o] = 0.0;
+          }
     } else {
       const T lambda_half = kc.lambda_half;
-      const double dt_dx = kc.dt_dx;
       auto fetch = [&](int c, T* u) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) u[k] = su[k][c - C0 + 2][lane];
@@ -762,7 +781,9 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
       // difference is formed by DiffToDouble, one FP64 operation per
       // component in the update)
       T f_prev[4];
-      int cls_prev = CellClassAt(g, dir, t, c0 - 1);
+      int cls_prev = cls_at(c0 - 1);
+      const bool next_marches =
+          warp + 1 < kNSeg && tile + 1 < ntl && treg[tile + 1] != 0 && c1 < nd;
       for (int j = c0 - 1; j <= c1; ++j) {
         fetch(j + 1, up);
         C2T<T> recL, recR;
@@ -770,7 +791,7 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
         C2T<T> q;
         CompleteMasked(eq, q, uc, true);
         if (j >= c0) {
-          const int cls = CellClassAt(g, dir, t, j);
+          const int cls = cls_at(j);
           T f[4];
           HllMasked(eq, f, recR_prev, recL, dir);
           if (cls == kCcRegular || cls_prev == kCcRegular) {
@@ -779,9 +800,16 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
             const T mx = PMaxT(PMaxT(T(0), fabs(s0w)), fabs(s1w));
             smax = mx > smax ? mx : smax;
           }
-          if (j > c0 && cls_prev != kCcBand) {
+          if (dir == 0) {
+            // face j for the block's update: faces c0 .. c1 - 1 of this
+            // tile, and face c1 unless the block's next warp marches (it
+            // computes that face as its first, from the same data)
+            if (j < c1 || !next_marches)
+#pragma unroll
+              for (int k = 0; k < 4; ++k) sf[k][j - C0][lane] = f[k];
+          } else if (j > c0 && cls_prev != kCcBand) {
             // cell j-1: regular, or covered (0)
-            const int64_t o = offset(j - 1);
+            const int64_t o = offset(t, j - 1);
             if (cls_prev == kCcRegular) {
 #pragma unroll
               for (int k = 0; k < 4; ++k) {
@@ -811,6 +839,35 @@ __global__ void __launch_bounds__(256, 3) KbnRegularTileKernel(CcSweepArgs a) {
           uc[k] = up[k];
         }
       }
+    }
+  }
+  if (dir == 0) {
+    // the block's update, threads along x: regular cells from the two face
+    // fluxes, covered cells 0 (band cells are the band kernel's)
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kC * kL; idx += blockDim.x) {
+      const int cell = idx % kC, line = idx / kC;
+      const int c = C0 + cell, tt = group * kL + line;
+      if (c >= nd || tt >= nt) continue;
+      const int cls = scls[cell + 2][line];
+      if (cls == kCcBand) continue;
+      const int64_t o = offset(tt, c);
+      if (cls == kCcCovered) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) a.out[k * cs + o] = 0.0;
+        continue;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const double prev = __ldg(a.s.in + k * cs + o);
+        double d;
+        if constexpr (sizeof(T) == 4)
+          d = DiffToDouble(sf[k][cell][line], sf[k][cell + 1][line]);
+        else
+          d = Widen(sf[k][cell][line] + T(0)) - Widen(sf[k][cell + 1][line] + T(0));
+        a.out[k * cs + o] = prev + dt_dx * d;
+      }
+      if (__double_as_longlong(a.out[o]) <= 0) status |= kStatusNonPositiveDensity;
     }
   }
   const double smax_d = static_cast<double>(smax);
@@ -1067,7 +1124,18 @@ cudaError_t LaunchKbnSweep(const CcSweepArgs& a, bool band, cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
     // mixed: tiles staged in shared memory, 32 lines x 64 cells per block
     const int64_t blocks = int64_t(a.s.g.NGroups(a.dir)) * ((a.s.g.NTiles(a.dir) + 7) / 8);
-    if (blocks > 0) KbnRegularTileKernel<T, M><<<unsigned(blocks), 256, 0, s>>>(a);
+    static bool attr_set = false;
+    if (!attr_set) {
+      const cudaError_t e =
+          cudaFuncSetAttribute(KbnRegularTileKernel<T, M>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(KbnTileSmemBytes<T>(0) + 16));
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+    if (blocks > 0)
+      KbnRegularTileKernel<T, M>
+          <<<unsigned(blocks), 256, KbnTileSmemBytes<T>(a.dir) + 16, s>>>(a);
   } else {
     // FP64 flavours (bound by the FP64 pipe): threads march runs of tiles,
     // one predictor per cell
