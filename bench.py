@@ -57,7 +57,7 @@ def parse():
                     help="skip the secondary workloads (learned start value, 2-D Godunov, "
                          "2-D cut cells)")
     ap.add_argument("--report", choices=["sod", "learned", "godunov", "amr", "cutcell",
-                                         "hllem", "sweep_variants"],
+                                         "hllem", "sweep_variants", "cutcell_sweeps"],
                     help="run only this secondary workload and print its JSON report")
     ap.add_argument("--mlp-samples", type=int, default=10_000_000)
     ap.add_argument("--mlp-epochs", type=int, default=24)
@@ -434,6 +434,52 @@ def report_sweep_variants(args, torch, fvs, workloads, peaks):
     return out
 
 
+def report_cutcell_sweeps(args, torch, fvs, workloads):
+    """Single x and y sweeps of the --cutcell-n^2 shock-over-circles state in
+    --precision, timed with CUDA events on the solver's stream (the cut-cell
+    sweep's band kernel runs on its side stream inside the timed region),
+    with the autotuned launch shapes, and one Strang step averaged over 50;
+    the same grid without a body for comparison."""
+    n = args.cutcell_n
+    circles, cons = workloads.shock_circles_2d(n, seed=5)
+    out = {"workload": f"2D {n}^2 Mach 2 shock, {args.precision}", "grids": {}}
+    for body in (False, True):
+        s = fvs.Solver([n, n], [1.0 / n] * 2, "transmissive",
+                       method=fvs.make_method(precision=args.precision))
+        if body:
+            s.set_embedded_circles(circles)
+        s.upload(cons)
+        s.autotune()
+        stream = torch.cuda.ExternalStream(s.stream_handle())
+        dt = 0.2 * s.ComputeStableDt(-1)
+        us = []
+        for d in (0, 1):
+            ts = []
+            for rep in range(8):
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                s.sweep(d, dt)
+                b.record(stream)
+                torch.cuda.synchronize()
+                if rep >= 2:
+                    ts.append(a.elapsed_time(b))
+            us.append(float(np.mean(ts)) * 1e3)
+        s.upload(cons)
+        s.run(cfl=0.5, t_end=1e9, max_steps=3)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        s.run(cfl=0.5, t_end=1e9, max_steps=50)
+        b.record(stream)
+        torch.cuda.synchronize()
+        out["grids"]["cut_cells" if body else "no_body"] = {
+            "sweep_us": {"x": us[0], "y": us[1]}, "step_us": a.elapsed_time(b) * 1e3 / 50,
+            "autotuned": s.tuning()}
+        s.close()
+    return out
+
+
 def report_amr(args, torch, fvs, workloads, peaks):
     """Batched AMR patch set: 2-D blast (p 10 inside r < 0.1 about a seeded
     centre), 3 levels, ratio 2, 4096 patches with extents from {8, 16, 32,
@@ -721,6 +767,8 @@ def run_ours(args):
             rep = report_amr(args, torch, fvs, workloads, peaks)
         elif args.report == "sweep_variants":
             rep = report_sweep_variants(args, torch, fvs, workloads, peaks)
+        elif args.report == "cutcell_sweeps":
+            rep = report_cutcell_sweeps(args, torch, fvs, workloads)
         elif args.report == "hllem":
             rep = report_hllem(args, torch, fvs, workloads, peaks)
         else:
