@@ -1030,7 +1030,8 @@ int fvs_solver_set_launch(fvs_solver* s, int dir, int seg_len, int variant) {
          (dir == 0 && (variant == 10 || variant == 14 || variant == 15)) ||
          (dir >= 1 && (variant == 20 || variant == 24 || variant == 25) && TmaMapsReady(s));
   if (s->m.precision == FVS_FP64_DF && plain_hlle) ok = variant == 0 || variant == 3;
-  if (s->cc) ok = variant == 0;
+  // cut cells: the mixed flavour's y sweeps march (10) instead of tiling (0)
+  if (s->cc) ok = variant == 0 || (variant == 10 && dir == 1 && s->m.precision == FVS_MIXED);
   if (!ok) return Fail(FVS_ERR_INVALID, "no such launch variant for this method");
   s->seg_tuned[dir] = seg_len;
   s->occ_tuned[dir] = variant;
@@ -1059,6 +1060,7 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   // cut cells: segment lengths of the FP64 flavours' regular-cell sweep (the
   // mixed flavour's cut-cell kernels have no launch parameter to tune)
   const bool cc_cell = s->cc && s->m.precision == FVS_MIXED;
+  const int occs_cc_mixed_y[] = {0, 10};
   const int saved = s->seg_len;
   cudaEvent_t e0, e1;
   FVS_CUDA(cudaEventCreate(&e0));
@@ -1074,8 +1076,11 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   if (s->cc) FVS_CUDA(CcReferenceStates(s, s->buf[s->cur]));
   for (int d = 0; d < s->g.rank; ++d) {
     const int nd = s->g.n[d];
-    const int* occs = mixed ? (d == 0 ? occs_mixed_x : occs_mixed) : (df ? occs_df : occs_plain);
-    const int nocc = mixed ? (d == 0 || tma ? 6 : 3) : (df ? 2 : 1);
+    const int* occs = mixed                ? (d == 0 ? occs_mixed_x : occs_mixed)
+                      : (cc_cell && d == 1) ? occs_cc_mixed_y
+                      : df                  ? occs_df
+                                            : occs_plain;
+    const int nocc = mixed ? (d == 0 || tma ? 6 : 3) : ((cc_cell && d == 1) || df ? 2 : 1);
     float best = 1e30f;
     int best_seg = 0, best_occ = 0;
     for (int oi = 0; oi < nocc; ++oi) {
@@ -1084,7 +1089,8 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
       const bool warp_x = mixed && d == 0 && occs[oi] < 10;
       for (int c : cands) {
         if (c > 2 * nd && c != cands[0]) break;
-        if ((warp_x || cc_cell) && c != cands[0]) break;
+        // the tile kernels (mixed cut cells, variant 0) have no segment length
+        if ((warp_x || (cc_cell && occs[oi] == 0)) && c != cands[0]) break;
         s->seg_len = c;
         float ms_sum = 0.f;
         for (int rep = 0; rep < 3; ++rep) {

@@ -351,6 +351,32 @@ __device__ __forceinline__ double Clamp01(double x) {
 // (cutcell::ReflectiveBoundary, include/fub/AMReX/cutcell/boundary_condition/
 // ReflectiveBoundary.hpp:72-122; where the ghost cell itself has no volume
 // the masked loads zero it).
+// LoadCons without touching the loaded values: returns what the caller applies
+// once they are needed (bit 0: negate m_x, bit 1: negate m_y, bit 2: zero
+// the state -- a reflective image of a cell without volume), so that a
+// prefetched load is not waited for at the load.
+__device__ __forceinline__ int LoadConsDeferred(const CcStateArgs& a, int i, int j, double* u) {
+  const int si = BcIndex(i, a.g.nx, a.bc[0]);
+  const int sj = BcIndex(j, a.g.ny, a.bc[1]);
+  const int64_t cs = int64_t(a.g.nx) * a.g.ny;
+  const int64_t off = int64_t(sj) * a.g.nx + si;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) u[k] = __ldg(a.in + k * cs + off);
+  const bool fx = BcFlip(i, a.g.nx, a.bc[0]), fy = BcFlip(j, a.g.ny, a.bc[1]);
+  int flags = (fx ? 1 : 0) | (fy ? 2 : 0);
+  if ((fx || fy) && !(a.g.alpha[a.g.CellIndex(si, sj)] > 0.0)) flags |= 4;
+  return flags;
+}
+
+template <class T> __device__ __forceinline__ void ApplyLoadFlags(T* u, int flags) {
+  if (flags & 1) u[1] = -u[1];
+  if (flags & 2) u[2] = -u[2];
+  if (flags & 4) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) u[k] = T(0);
+  }
+}
+
 __device__ __forceinline__ void LoadCons(const CcStateArgs& a, int i, int j, double* u) {
   const int si = BcIndex(i, a.g.nx, a.bc[0]);
   const int sj = BcIndex(j, a.g.ny, a.bc[1]);
@@ -913,15 +939,15 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
       return dir == 0 ? int64_t(t) * g.nx + c : int64_t(c) * g.nx + t;
     };
     // state of cell c masked as on a regular cell (alpha 1: zeroed only where
-    // rho <= 0)
-    auto load_cell = [&](int c, T* u) {
-      double vd[4];
-      if (dir == 0)
-        LoadCons(a.s, c, t, vd);
-      else
-        LoadCons(a.s, t, c, vd);
+    // rho <= 0): the FP64 load (fetch, one cell ahead of its use) and its
+    // conversion (finish)
+    auto fetch = [&](int c, double* vd) {
+      return dir == 0 ? LoadConsDeferred(a.s, c, t, vd) : LoadConsDeferred(a.s, t, c, vd);
+    };
+    auto finish = [&](const double* vd, int flags, T* u) {
       T v[4];
       Narrow(v, vd);
+      ApplyLoadFlags(v, flags);
       C2T<T> q;
       CompleteMasked(eq, q, v, true);
       u[0] = q.rho;
@@ -956,16 +982,21 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
       tile = r1;
       // march the run [j0, j1): faces j0 .. j1, cells j0 .. j1-1
       T um[4], uc[4], up[4];
-      load_cell(j0 - 2, um);
-      load_cell(j0 - 1, uc);
+      double dn[4];
+      int fl = fetch(j0 - 2, dn);
+      finish(dn, fl, um);
+      fl = fetch(j0 - 1, dn);
+      finish(dn, fl, uc);
+      int fl_dn = fetch(j0, dn);
       C2T<T> recR_prev, q_prev;
-      double fs_prev[4];
+      T f_prev[4];
       fast::Wave<float> v_prev{};
       bool ok_prev = false;
       bool have_prev = false;
       int cls_prev = CellClassAt(g, dir, t, j0 - 1);
       for (int j = j0 - 1; j <= j1; ++j) {
-        load_cell(j + 1, up);
+        finish(dn, fl_dn, up);
+        if (j + 2 <= j1 + 1) fl_dn = fetch(j + 2, dn);
         C2T<T> recL, recR;
         PredictMasked(eq, recL, recR, um, uc, up, true, a.limiter, lambda_half, dir);
         C2T<T> q;
@@ -1018,9 +1049,6 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
           }
           T f[4];
           HllMasked(eq, f, recR_prev, recL, dir);
-          double fs[4];
-#pragma unroll
-          for (int c = 0; c < 4; ++c) fs[c] = Widen(f[c] + T(0));
           if constexpr (!kScreen) {
             if (count) {
               T s0w, s1w;
@@ -1035,7 +1063,14 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
 #pragma unroll
               for (int c = 0; c < 4; ++c) {
                 const double prev = __ldg(a.s.in + c * cs + o);
-                a.out[c * cs + o] = prev + dt_dx * (fs_prev[c] - fs[c]);
+                // the FP64 flux difference (mixed: formed exactly by
+                // DiffToDouble, as the tile kernel does)
+                double d;
+                if constexpr (sizeof(T) == 4)
+                  d = DiffToDouble(f_prev[c], f[c]);
+                else
+                  d = Widen(f_prev[c] + T(0)) - Widen(f[c] + T(0));
+                a.out[c * cs + o] = prev + dt_dx * d;
               }
               if (__double_as_longlong(a.out[o]) <= 0) status |= kStatusNonPositiveDensity;
             } else {
@@ -1044,7 +1079,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
             }
           }
 #pragma unroll
-          for (int c = 0; c < 4; ++c) fs_prev[c] = fs[c];
+          for (int c = 0; c < 4; ++c) f_prev[c] = f[c];
           cls_prev = cls;
         }
         recR_prev = recR;
@@ -1121,7 +1156,7 @@ cudaError_t LaunchKbnSweep(const CcSweepArgs& a, bool band, cudaStream_t s) {
     if (n > 0) KbnBandKernel<T, M><<<unsigned((n + 63) / 64), 64, 0, s>>>(a);
     return cudaGetLastError();
   }
-  if constexpr (sizeof(T) == 4) {
+  if (sizeof(T) == 4 && !(a.dir == 1 && a.occupancy == 10)) {
     // mixed: tiles staged in shared memory, 32 lines x 64 cells per block
     const int64_t blocks = int64_t(a.s.g.NGroups(a.dir)) * ((a.s.g.NTiles(a.dir) + 7) / 8);
     static bool attr_set = false;
@@ -1137,15 +1172,19 @@ cudaError_t LaunchKbnSweep(const CcSweepArgs& a, bool band, cudaStream_t s) {
       KbnRegularTileKernel<T, M>
           <<<unsigned(blocks), 256, KbnTileSmemBytes<T>(a.dir) + 16, s>>>(a);
   } else {
-    // FP64 flavours (bound by the FP64 pipe): threads march runs of tiles,
-    // one predictor per cell
+    // FP64 flavours (bound by the FP64 pipe), and the mixed flavour's y
+    // sweeps as launch variant 10: threads march runs of tiles, one
+    // predictor per cell
     const int block = 128;
     int seg = a.seg_len > 0 ? a.seg_len : nd;
     seg = (seg + kCcTile - 1) / kCcTile * kCcTile;
     CcSweepArgs b = a;
     b.seg_len = seg;
     dim3 grid(unsigned((nt + block - 1) / block), unsigned((nd + seg - 1) / seg));
-    KbnRegularSweepKernel<T, M, 3><<<grid, block, 0, s>>>(b);
+    if constexpr (sizeof(T) == 4)
+      KbnRegularSweepKernel<T, M, 5><<<grid, block, 0, s>>>(b);
+    else
+      KbnRegularSweepKernel<T, M, 3><<<grid, block, 0, s>>>(b);
   }
   return cudaGetLastError();
 }

@@ -129,6 +129,33 @@ def test_flavours_track_exact_and_conserve(fvs, orc, prec, variant):
     assert drift[0] < 1e-11 and drift[3] < 1e-11, drift
 
 
+def test_mixed_regular_cells_tile_and_march_agree(fvs):
+    """The mixed flavour's regular cells of a y sweep, tiled in shared memory
+    (variant 0) or marched along the column (variant 10, several segment
+    lengths), and after the autotuner: the same results bit for bit."""
+    n = 256
+    circles, cons = workloads.shock_circles_2d(n, seed=5)
+    outs = []
+    for v, seg in ((0, 0), (10, 16), (10, 40), ("tuned", 0)):
+        s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive",
+                       method=fvs.make_method(precision="mixed"))
+        s.set_embedded_circles(circles)
+        s.upload(cons)
+        if v == "tuned":
+            s.autotune()
+        else:
+            s.set_launch(1, seg, v)
+        st, _ = s.run(cfl=0.5, t_end=10.0, max_steps=6)
+        assert st.steps == 6
+        outs.append(s.download())
+        if v == 10:
+            with pytest.raises(fvs.FvsError):
+                s.set_launch(0, seg, 10)  # x sweeps always tile
+        s.close()
+    for o in outs[1:]:
+        np.testing.assert_array_equal(outs[0], o)
+
+
 def _star_polygon(cx, cy, r0, r1, n=5, phase=0.3):
     import math
     pts = []
