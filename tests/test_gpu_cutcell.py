@@ -208,3 +208,34 @@ def test_shock_over_general_geometry_run_bit_exact(fvs, orc, case):
     np.testing.assert_array_equal(dts, ref_dts)
     np.testing.assert_array_equal(s.download(), out)
     s.close()
+
+
+# The wedge of the reference's tests/test.AMReX.EB.plane_nan.cpp:32-53 (the
+# cone y < 0.1 - 0.9 |x| on [-0.5, 0.5] x [0, 1], 64 x 64 cells, its apex on
+# the grid line x = 0), as a polygon cut off below the domain.
+WEDGE = [{"kind": "polygon", "xy": [(0.0, 0.1), (1.0, -0.8), (-1.0, -0.8), (0.0, 0.1)]}]
+
+
+def test_wedge_geometry_and_run_bit_exact(fvs, orc):
+    n = 64
+    ref = orc.CutCellGeometry(n, n, x0=-0.5, y0=0.0, shapes=WEDGE)
+    s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive")
+    s.set_embedded_geometry(WEDGE, x0=-0.5, y0=0.0)
+    g = s.cutcell_geometry()
+    for key in ("alpha", "betax", "betay", "normal", "center"):
+        assert np.isfinite(g[key]).all(), key
+        np.testing.assert_array_equal(g[key], getattr(ref, key), err_msg=key)
+    G = ref.G
+    np.testing.assert_array_equal(g["cut"][G:-G, G:-G].astype(np.int32), ref.cut_cells())
+    for d in (0, 1):
+        for a, b in zip(s.cutcell_shielded(d), ref.shielded(d)):
+            np.testing.assert_array_equal(a, b)
+    _, cons = workloads.shock_circles_2d(n, seed=5, x_shock=0.38)  # reaches the wedge
+    s.upload(cons)
+    st, dts = s.run(cfl=0.5, t_end=10.0, max_steps=8, log_len=8)
+    out, ref_dts, rs = ref.run(cons, 0.5, 10.0, max_steps=8)
+    assert st.steps == 8 and st.restarts == rs
+    np.testing.assert_array_equal(dts, ref_dts)
+    np.testing.assert_array_equal(s.download(), out)
+    assert np.isfinite(out).all()
+    s.close()

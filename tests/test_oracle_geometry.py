@@ -161,3 +161,65 @@ def test_polygon_known_answer_of_the_reference(orc):
 
     assert g.alpha[cell(0.11, 0.105)] == 0.0
     assert g.alpha[cell(0.09, 0.1)] == 1.0
+
+
+def _clip_convex(poly, f):
+    """The part of a convex polygon where the affine f <= 0."""
+    out = []
+    for k in range(len(poly)):
+        p, q = poly[k], poly[(k + 1) % len(poly)]
+        fp, fq = f(*p), f(*q)
+        if fp <= 0:
+            out.append(p)
+        if (fp <= 0) != (fq <= 0):
+            t = fp / (fp - fq)
+            out.append((p[0] + t * (q[0] - p[0]), p[1] + t * (q[1] - p[1])))
+    return out
+
+
+def _area(poly):
+    if len(poly) < 3:
+        return 0.0
+    return 0.5 * abs(sum(poly[k][0] * poly[(k + 1) % len(poly)][1]
+                         - poly[(k + 1) % len(poly)][0] * poly[k][1] for k in range(len(poly))))
+
+
+# The wedge of the reference's tests/test.AMReX.EB.plane_nan.cpp:32-53 on its
+# 64 x 64 grid over [-0.5, 0.5] x [0, 1]: the complement of the intersection
+# of the two planes through p0 = (0, 0.1) along p1 - p0 = (-1, 0.9) and
+# p2 - p0 = (1, 0.9) leaves as body the cone y < 0.1 - 0.9 |x| (a wedge on
+# the lower wall, its apex on the grid line x = 0).  Here it is the polygon
+# of the cone cut off below the domain.
+WEDGE_X0, WEDGE_N = -0.5, 64
+WEDGE = [{"kind": "polygon", "xy": [(0.0, 0.1), (1.0, -0.8), (-1.0, -0.8), (0.0, 0.1)]}]
+
+
+def test_wedge_of_the_reference_plane_nan_case(orc):
+    """That test builds the wedge with floating-point exceptions enabled: no
+    NaN may appear.  Here every array is finite, the fractions lie in [0, 1],
+    no cut cell has a zero volume (the property tests/test.AMReX.EB.Cylinder.cpp
+    prints violations of), and since the apex lies on a cell edge every cell is
+    crossed by at most one straight edge: alpha equals the exact fluid area."""
+    n, h = WEDGE_N, 1.0 / WEDGE_N
+    g = orc.CutCellGeometry(n, n, x0=WEDGE_X0, y0=0.0, shapes=WEDGE)
+    G = g.G
+    for key in ("alpha", "betax", "betay", "normal", "center"):
+        assert np.isfinite(getattr(g, key)).all(), key
+    for key in ("alpha", "betax", "betay"):
+        a = getattr(g, key)
+        assert a.min() >= 0.0 and a.max() <= 1.0, key
+    alpha = g.alpha[G:-G, G:-G]
+    cut = g.cut_cells().astype(bool)
+    assert cut.sum() > 0 and (alpha[cut] > 0.0).all()
+    lines = [lambda x, y: y - (0.1 + 0.9 * x), lambda x, y: y - (0.1 - 0.9 * x)]  # body <= 0
+    for j in range(n):
+        for i in range(n):
+            x0, y0 = WEDGE_X0 + i * h, j * h
+            body = [(x0, y0), (x0 + h, y0), (x0 + h, y0 + h), (x0, y0 + h)]
+            for f in lines:
+                body = _clip_convex(body, f)
+            exact = 1.0 - _area(body) / (h * h)
+            assert abs(alpha[j, i] - exact) < 1e-12, (i, j, alpha[j, i], exact)
+    # the two apex cells either side of x = 0
+    ja, ia = int(0.1 / h), n // 2
+    assert 0.0 < alpha[ja, ia - 1] < 1.0 and abs(alpha[ja, ia - 1] - alpha[ja, ia]) < 1e-12
