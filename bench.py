@@ -406,7 +406,7 @@ def report_sweep_variants(args, torch, fvs, workloads, peaks):
             variants = [0]
         for v in variants:
             best = None
-            segs = [16] if (mixed and d == 0 and v < 10) else [16, 32, 64, 128, 256]
+            segs = [16] if (mixed and d == 0 and v < 10) else [8, 16, 32, 64, 128, 256]
             for seg in segs:
                 try:
                     s.set_launch(d, seg, v)
@@ -741,12 +741,16 @@ def run_ours(args):
     torch.cuda.set_device(local)
     build.build()
     if args.report == "cutcell" and args.profile_steps > 0:
-        # profiling aid: the cut-cell workload in --precision, default launch shapes
+        # profiling aid: the cut-cell workload in --precision, launch shapes from
+        # --launch, default shapes elsewhere
         n = args.cutcell_n
         circles, cons = workloads.shock_circles_2d(n, seed=5)
         solver = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive",
                             method=fvs.make_method(precision=args.precision))
         solver.set_embedded_circles(circles)
+        for spec in args.launch:
+            d, seg, var = (int(v) for v in spec.split(":"))
+            solver.set_launch(d, seg, var)
         solver.upload(cons)
         st, _ = solver.run(cfl=0.5, t_end=1e9, max_steps=args.profile_steps)
         solver.close()

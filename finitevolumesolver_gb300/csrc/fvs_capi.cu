@@ -1046,7 +1046,7 @@ int fvs_solver_autotune(fvs_solver* s, int* seg_out) {
   // register/occupancy variants of the same kernel), timed on the current
   // state with a small dt (output goes to a spare buffer; the state is not
   // changed).
-  const int cands[] = {16, 32, 64, 128, 256, 512};
+  const int cands[] = {8, 16, 32, 64, 128, 256, 512};
   const bool plain_hlle = s->m.flux_method <= FVS_HLLE && !s->cc;
   const bool mixed = s->m.precision == FVS_MIXED && plain_hlle;
   const bool df = s->m.precision == FVS_FP64_DF && plain_hlle;

@@ -23,6 +23,8 @@
 //   MakeRotation, Reflect      include/fub/ext/Eigen.hpp:104-115, src/equations/PerfectGas.cpp:240-252
 #pragma once
 
+#include <algorithm>
+
 #include "fvs_convert.cuh"
 #include "fvs_cutcell.h"
 #include "fvs_internal.h"
@@ -1100,40 +1102,79 @@ __global__ void __launch_bounds__(128, kMinBlocks) KbnRegularSweepKernel(CcSweep
 }
 
 // Masked stable dt over both directions: faces 0..n with beta > 0
-// (KbnStabilisation.hpp:275-345).
+// (KbnStabilisation.hpp:275-345).  A warp owns 32 neighbouring columns,
+// ic = 31 w - 1 + lane (the next warp's lane 0 repeats this warp's lane 31),
+// and a segment of `rows` rows; each lane loads and completes its cells once,
+// marching up the column, and pairs each cell with the one below it (kept
+// from the previous row: the y face) and with the one to its left (lane - 1,
+// a shuffle: the x face).  Every face is evaluated once, by the lane of its
+// right / upper cell, with the arithmetic of the per-face form (masked
+// completion of both cells, masked Einfeldt speeds, max(0, |sL|, |sR|)), so
+// the maximum is the same bit for bit; the per-face form loaded and completed
+// every cell four times.
 template <class T, class M>
-__global__ void KbnStableDtKernel(CcStateArgs a, unsigned long long* smax_out, Control* ctrl) {
+__global__ void __launch_bounds__(128)
+    KbnStableDtKernel(CcStateArgs a, int rows, unsigned long long* smax_out, Control* ctrl) {
   if (!BlockAll(!(ctrl && (ctrl->abort || ctrl->done)))) return;
   const CcGeom& g = a.g;
-  const int w = g.nx + 1, h = g.ny + 1;
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int ncw = (g.nx + 1 + 30) / 31;     // x faces 0..nx on lanes 1..31
+  const int nseg = (g.ny + 1 + rows - 1) / rows;  // face rows 0..ny
   T sm[2] = {T(0), T(0)};
-  const GasT<T, M> eq = MakeGasT<T, M>(a.gamma);
-  // grid-stride over faces; one atomic per block and direction at the end
-  for (int64_t id = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; id < int64_t(w) * h;
-       id += int64_t(gridDim.x) * blockDim.x) {
-    const int i = static_cast<int>(id % w), j = static_cast<int>(id / w);
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      const int f = d == 0 ? i : j;
-      const int t = d == 0 ? j : i;
-      const int nt = d == 0 ? g.ny : g.nx;
-      if (t >= nt) continue;
-      if (!(g.beta[d][g.FaceIndex(d, f, t)] > 0.0)) continue;
-      const int il = d == 0 ? f - 1 : t, jl = d == 0 ? t : f - 1;
-      const int ir = d == 0 ? f : t, jr = d == 0 ? t : f;
-      double uld[4], urd[4];
-      LoadCons(a, il, jl, uld);
-      LoadCons(a, ir, jr, urd);
-      T ul[4], ur[4];
-      Narrow(ul, uld);
-      Narrow(ur, urd);
-      C2T<T> L, R;
-      CompleteMasked(eq, L, ul, g.alpha[g.CellIndex(il, jl)] > 0.0);
-      CompleteMasked(eq, R, ur, g.alpha[g.CellIndex(ir, jr)] > 0.0);
-      T s0, s1;
-      EinfeldtMasked(eq, L, R, d, s0, s1);
-      const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
-      sm[d] = mx > sm[d] ? mx : sm[d];
+  if (gw < int64_t(ncw) * nseg) {  // warp-uniform
+    const int ic = 31 * static_cast<int>(gw % ncw) - 1 + lane;
+    const bool in_grid = ic <= g.nx;  // lanes past column nx load column nx, unused
+    const int icl = in_grid ? ic : g.nx;
+    const int j0 = static_cast<int>(gw / ncw) * rows;
+    const int j1 = min(j0 + rows, g.ny + 1);
+    const GasT<T, M> eq = MakeGasT<T, M>(a.gamma);
+    // a row's cell with its volume fraction and the fractions of its x face
+    // (left) and y face (below), loaded one row before its use
+    struct Row {
+      double u[4];
+      int flags;
+      double alpha, bx, by;
+    };
+    const bool x_face = lane >= 1 && in_grid, y_face = lane >= 1 && ic < g.nx;
+    auto fetch = [&](int j, Row& r) {
+      r.flags = LoadConsDeferred(a, icl, j, r.u);
+      r.alpha = g.alpha[g.CellIndex(icl, j)];
+      r.bx = (x_face && j >= 0 && j < g.ny) ? g.beta[0][g.FaceIndex(0, ic, j)] : 0.0;
+      r.by = (y_face && j >= 0) ? g.beta[1][g.FaceIndex(1, j, ic)] : 0.0;
+    };
+    auto complete = [&](const Row& r, C2T<T>& q) {
+      T u[4];
+      Narrow(u, r.u);
+      ApplyLoadFlags(u, r.flags);
+      CompleteMasked(eq, q, u, r.alpha > 0.0);
+    };
+    Row next;
+    fetch(j0 - 1, next);
+    C2T<T> below;
+    complete(next, below);
+    fetch(j0, next);
+    for (int j = j0; j < j1; ++j) {
+      const Row row = next;
+      if (j + 1 < j1) fetch(j + 1, next);  // the next row, early
+      C2T<T> cur;
+      complete(row, cur);
+      const C2T<T> left = ShflUp(cur, 1);
+      // x face ic of row j (cells ic - 1 and ic)
+      if (row.bx > 0.0) {
+        T s0, s1;
+        EinfeldtMasked(eq, left, cur, 0, s0, s1);
+        const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
+        sm[0] = mx > sm[0] ? mx : sm[0];
+      }
+      // y face j of column ic (cells j - 1 and j)
+      if (row.by > 0.0) {
+        T s0, s1;
+        EinfeldtMasked(eq, below, cur, 1, s0, s1);
+        const T mx = PMaxT(PMaxT(T(0), fabs(s0)), fabs(s1));
+        sm[1] = mx > sm[1] ? mx : sm[1];
+      }
+      below = cur;
     }
   }
   const double smd[2] = {static_cast<double>(sm[0]), static_cast<double>(sm[1])};
@@ -1192,9 +1233,15 @@ cudaError_t LaunchKbnSweep(const CcSweepArgs& a, bool band, cudaStream_t s) {
 template <class T, class M>
 cudaError_t LaunchKbnStableDt(const CcStateArgs& a, unsigned long long* smax_out, Control* ctrl,
                               cudaStream_t s) {
-  const int64_t n = int64_t(a.g.nx + 1) * (a.g.ny + 1);
+  // segments of 4..32 rows, short enough for about 32 warps per SM of 152
+  const int64_t ncw = (a.g.nx + 1 + 30) / 31;
+  const int64_t target = int64_t(152) * 32;
+  const int rows = static_cast<int>(
+      std::min<int64_t>(32, std::max<int64_t>(4, (int64_t(a.g.ny + 1) * ncw + target - 1) / target)));
+  const int64_t warps = ncw * ((a.g.ny + 1 + rows - 1) / rows);
   const int block = 128;
-  KbnStableDtKernel<T, M><<<GridStrideBlocks(n, block, 16), block, 0, s>>>(a, smax_out, ctrl);
+  KbnStableDtKernel<T, M><<<unsigned((warps * 32 + block - 1) / block), block, 0, s>>>(
+      a, rows, smax_out, ctrl);
   return cudaGetLastError();
 }
 
