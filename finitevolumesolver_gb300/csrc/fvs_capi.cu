@@ -240,7 +240,7 @@ struct fvs_solver {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   // tensor maps of the three state buffers for the TMA-staged y and z
   // sweeps of the mixed flavour ([buffer][dir - 1]); built on first use
-  alignas(64) CUtensorMap tmap[3][2];
+  CUtensorMap tmap[3][2];  // aligned as the type requires (new of an over-aligned type, C++17)
   int tmap_state = 0;  // 0 not tried, 1 built, -1 not available
   // host-resident steps (fvs_solver_step_host): the copies of the last
   // sweep's slabs run on `copy`, each after its slab's event
