@@ -148,11 +148,14 @@ __global__ void __launch_bounds__(32 * kDtRows) StableDtMarch3Kernel(StableDtArg
   const bool own = jvalid && lane >= 1 && i < nx;
   const int ic = BcIndex(i, nx, a.bc[0]);  // lane 0: the left neighbour
   const int jbelow = BcIndex(jb * kDtRows - 1, ny, a.bc[1]);
-  auto load = [&](int jj, int kk, R* u) {
+  auto fetch = [&](int jj, int kk, double* ud) {
     const int64_t off = (int64_t(kk) * ny + jj) * nx + ic;
-    double ud[K];
 #pragma unroll
     for (int c = 0; c < K; ++c) ud[c] = __ldg(a.in + c * cs + off);
+  };
+  auto load = [&](int jj, int kk, R* u) {
+    double ud[K];
+    fetch(jj, kk, ud);
     P::ToCell(u, ud);
   };
   auto take = [&](R& m, R v) { m = v > m ? v : m; };
@@ -165,16 +168,31 @@ __global__ void __launch_bounds__(32 * kDtRows) StableDtMarch3Kernel(StableDtArg
     load(jc, BcIndex(k0 - 1, nz, a.bc[2]), u);
     wz_prev = P::MakeWave(eq, u, 2);
   }
+  // the next plane's cell, and for warp 0 the cell of the row below the
+  // block, are loaded one plane before their use
+  double un[K], vn[K] = {};
+  fetch(jc, k0, un);
+  if (warp == 0) fetch(jbelow, k0, vn);
   for (int k = k0; k < k1; ++k) {
+    double ud[K], vd[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+      ud[c] = un[c];
+      vd[c] = vn[c];
+    }
+    if (k + 1 < k1) {
+      fetch(jc, k + 1, un);
+      if (warp == 0) fetch(jbelow, k + 1, vn);
+    }
     R u[K];
-    load(jc, k, u);
+    P::ToCell(u, ud);
     W w[3];
     WavesOf<P>::Get(eq, u, w);
     ywave[k & 1][warp][lane] = w[1];
     W wy_below;
     if (warp == 0) {  // the row below the block
       R v[K];
-      load(jbelow, k, v);
+      P::ToCell(v, vd);
       wy_below = P::MakeWave(eq, v, 1);
     }
     const W wl = ShflUp(w[0], 1);
@@ -245,11 +263,14 @@ __global__ void __launch_bounds__(32 * kDtRows) StableDtScreen3Kernel(StableDtAr
   const int ic = BcIndex(i, nx, a.bc[0]);  // lane 0: the left neighbour
   const int jbelow = BcIndex(jb * kDtRows - 1, ny, a.bc[1]);
   const int jn = warp > 0 ? j - 1 : jbelow;  // the row below this warp's (own lanes)
-  auto load = [&](int jj, int kk, R* u) {
+  auto fetch = [&](int jj, int kk, double* ud) {
     const int64_t off = (int64_t(kk) * ny + jj) * nx + ic;
-    double ud[K];
 #pragma unroll
     for (int c = 0; c < K; ++c) ud[c] = __ldg(a.in + c * cs + off);
+  };
+  auto load = [&](int jj, int kk, R* u) {
+    double ud[K];
+    fetch(jj, kk, ud);
     P::ToCell(u, ud);
   };
   // FP32 waves of a cell in the three directions; h = inf outside the range
@@ -282,16 +303,31 @@ __global__ void __launch_bounds__(32 * kDtRows) StableDtScreen3Kernel(StableDtAr
     screen_waves(u, v);
     vz_prev = v[2];
   }
+  // the next plane's cell, and for warp 0 the cell of the row below the
+  // block, are loaded one plane before their use
+  double un[K], vn[K] = {};
+  fetch(jc, k0, un);
+  if (warp == 0) fetch(jbelow, k0, vn);
   for (int k = k0; k < k1; ++k) {
+    double ud[K], vd[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+      ud[c] = un[c];
+      vd[c] = vn[c];
+    }
+    if (k + 1 < k1) {
+      fetch(jc, k + 1, un);
+      if (warp == 0) fetch(jbelow, k + 1, vn);
+    }
     R u[K];
-    load(jc, k, u);
+    P::ToCell(u, ud);
     V v[3];
     screen_waves(u, v);
     ycell[k & 1][warp][lane] = v[1];
     V vy_below;
     if (warp == 0) {  // the row below the block
       R ub[K];
-      load(jbelow, k, ub);
+      P::ToCell(ub, vd);
       V vb[3];
       screen_waves(ub, vb);
       vy_below = vb[1];
