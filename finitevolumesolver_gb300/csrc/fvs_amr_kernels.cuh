@@ -346,7 +346,10 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.nsegs;
        r += gridDim.x * blockDim.x) {
     const Seg w = a.segs[r];
-    auto cell = [&](int j, R* v) {
+    // loads cell j of the segment's row; returns whether it is a reflective
+    // boundary's image, whose normal momentum `finish` negates after the
+    // conversion (a select on the loaded value would wait for the load)
+    auto fetch = [&](int j, double* u) {
       const double* src = a.in;
       int64_t off, cs = N;
       bool flip = false;
@@ -364,11 +367,25 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
         }
         flip = (w.flip >> h) & 1;
       }
-      double u[K];
 #pragma unroll
       for (int c = 0; c < K; ++c) u[c] = __ldg(src + c * cs + off);
-      if (flip) u[1 + DIR] = -u[1 + DIR];  // a reflective boundary's image
+      return flip;
+    };
+    auto finish = [&](const double* u, bool flip, R* v) {
       P::ToCell(v, u);
+      if (flip) v[1 + DIR] = -v[1 + DIR];
+    };
+    // the cells j0 - 1 .. j1 of faces j0 .. j1, each loaded one face before
+    // its use: shift(f, v) hands out cell f - 1 and fetches cell f
+    double un[K];
+    bool fn = fetch(w.j0 - 1, un);
+    auto shift = [&](int f, R* v) {
+      double uc[K];
+#pragma unroll
+      for (int c = 0; c < K; ++c) uc[c] = un[c];
+      const bool fc = fn;
+      if (f <= w.j1) fn = fetch(f, un);
+      finish(uc, fc, v);
     };
     if constexpr (kFilter) {
       known = *reinterpret_cast<volatile unsigned long long*>(a.smax_out);
@@ -384,14 +401,14 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
         return v;
       };
       R ul[K];
-      cell(w.j0 - 1, ul);
+      shift(w.j0, ul);
       bool ok_l;
       fast::Wave<float> vl = screen_wave(ul, ok_l);
       typename P::Wave wl;
       bool have_l = false;
       for (int f = w.j0; f <= w.j1; ++f) {
         R ur[K];
-        cell(f, ur);
+        shift(f + 1, ur);
         bool ok_r;
         const fast::Wave<float> vr = screen_wave(ur, ok_r);
         const float s32 = fast::FaceMaxSpeed<float>(g32, vl, vr);
@@ -417,14 +434,14 @@ __global__ void __launch_bounds__(128) PatchMaxSpeedKernel(MaxSpeedArgs a) {
           static_cast<unsigned long long>(__double_as_longlong(static_cast<double>(smax)));
       if (b > known) atomicMax(a.smax_out, b);
     } else {
-      auto wave = [&](int j) {
+      auto wave = [&](int f) {
         R v[K];
-        cell(j, v);
+        shift(f, v);
         return P::MakeWave(eq, v, DIR);
       };
-      typename P::Wave wl = wave(w.j0 - 1);
+      typename P::Wave wl = wave(w.j0);
       for (int f = w.j0; f <= w.j1; ++f) {
-        const typename P::Wave wr = wave(f);
+        const typename P::Wave wr = wave(f + 1);
         const R s = P::FaceMaxSpeed(eq, wl, wr);
         smax = s > smax ? s : smax;
         wl = wr;
