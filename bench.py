@@ -858,10 +858,13 @@ def run_ours(args):
     # same pinned buffer, the next step's input (fvs_solver_step_host: the
     # write-back overlaps the step's last sweep, slab by slab).  A second
     # figure keeps the state on the device between one upload and one
-    # download.
+    # download.  Both legs get the same W untimed warm-up steps as the device
+    # leg (the first host-resident step creates the copy streams and events).
     L = fvs.lib()
     state_bytes = cons.nbytes
     pinned = torch.from_numpy(cons).pin_memory()
+    for _ in range(args.warmup):
+        solver.step_host(pinned, cfl=0.8, t_end=1e9)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
