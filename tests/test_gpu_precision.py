@@ -110,7 +110,7 @@ def test_mixed_sod_1d(fvs, orc):
 
 
 @pytest.mark.parametrize("bc", ["periodic", "transmissive"])
-@pytest.mark.parametrize("nx", [256, 100])
+@pytest.mark.parametrize("nx", [256, 100, 33, 32, 31])  # full and partial last chunks of 32
 def test_mixed_x_sweep_matches_marching_kernel(fvs, bc, nx):
     """The mixed x sweep (lanes along x, shuffles) and the marching y sweep
     evaluate the same per-face and per-cell arithmetic.  A state that varies
