@@ -866,10 +866,12 @@ def run_ours(args):
     for _ in range(args.warmup):
         solver.step_host(pinned, cfl=0.8, t_end=1e9)
     torch.cuda.synchronize()
+    e2e_restarts = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         st_h = solver.step_host(pinned, cfl=0.8, t_end=1e9)
         assert st_h.steps == 1
+        e2e_restarts += st_h.restarts
     e2e_s = time.perf_counter() - t0
     e2e_value = 6 * cells * args.steps * world / e2e_s
     pinned.copy_(torch.from_numpy(cons))
@@ -969,6 +971,7 @@ def run_ours(args):
                             "host memory, advances it one Strang step and writes it back "
                             "(fvs_solver_step_host: the last sweep runs in 8 slabs and each "
                             "slab's copy overlaps the rest of the sweep)",
+                    "restarts": e2e_restarts,
                     "amortised": {"value": e2e_amortised, "unit": UNIT,
                                   "h2d_bytes_per_step": (state_bytes + CONTROL_BYTES) /
                                   args.steps,
