@@ -24,6 +24,7 @@ __device__ __forceinline__ GodunovGas MakeGodunovGas(double gamma, int guess, in
   g.opt.max_iterations = max_it;
   g.opt.tol = tol;
   g.opt.mlp = mlp;
+  g.opt.root_n = riemann::RootOrder(gamma);
   return g;
 }
 

@@ -10,8 +10,9 @@
 //   Godunov::ComputeNumericFlux / ComputeStableDt
 //       include/fub/flux_method/GodunovMethod.hpp:129-183
 // with the reference's operation order (the including translation unit is
-// compiled with -fmad=false).  pow() is CUDA's, so results agree with the
-// CPU oracle to a few ulps rather than bit for bit.
+// compiled with -fmad=false).  The powers of pressure ratios are n-th roots
+// (Powers) or CUDA's pow(), so results agree with the CPU oracle to a few
+// ulps rather than bit for bit.
 //
 // Differences by design:
 //  - Newton is bounded by `max_iterations` and never throws: a face that has
@@ -26,6 +27,7 @@
 
 #include "fvs_mlp.cuh"
 #include "fvs_physics_exact.cuh"
+#include "fvs_roots.cuh"
 
 namespace fvs {
 namespace riemann {
@@ -37,14 +39,7 @@ struct Options {
   int max_iterations;
   double tol;
   const float* mlp;  // learned-guess parameters (kGuessMlp)
-};
-
-struct Star {
-  double p;
-  double u;
-  int iterations;
-  int converged;
-  int fallback;  // the learned start value was rejected
+  int root_n;        // RootOrder(gamma): 0, or n with n-th roots in place of pow()
 };
 
 // Scalar-path |m|^2 of the reference's exact solver: (m0^2 + m1^2) + m2^2.
@@ -61,9 +56,9 @@ template <int D> __device__ __forceinline__ double SquaredNormScalar(const doubl
 // PVRS estimate, replaced by the two-rarefaction estimate below min(pL, pR)
 // (Toro, Riemann Solvers and Numerical Methods for Fluid Dynamics, 3rd ed.,
 // section 9.5); floored at 1e-8 min(pL, pR).
-__device__ __forceinline__ double PvrsTrGuess(double g, double rhoL, double uL, double pL,
-                                              double aL, double rhoR, double uR, double pR,
-                                              double aR) {
+__device__ __forceinline__ double PvrsTrGuess(const Powers& pw, double g, double rhoL, double uL,
+                                              double pL, double aL, double rhoR, double uR,
+                                              double pR, double aR) {
   const double pmin = pL < pR ? pL : pR;
   const double ppv = 0.5 * (pL + pR) - 0.125 * (uR - uL) * (rhoL + rhoR) * (aL + aR);
   double p0;
@@ -72,8 +67,8 @@ __device__ __forceinline__ double PvrsTrGuess(double g, double rhoL, double uL, 
   } else {
     const double z = (g - 1.0) / (2.0 * g);
     const double num = aL + aR - 0.5 * (g - 1.0) * (uR - uL);
-    const double den = aL / pow(pL, z) + aR / pow(pR, z);
-    p0 = (num > 0.0) ? pow(num / den, 1.0 / z) : 0.0;
+    const double den = aL / pw.Z(pL, z) + aR / pw.Z(pR, z);
+    p0 = (num > 0.0) ? pw.N(num / den, 1.0 / z) : 0.0;
   }
   const double floor = 1e-8 * pmin;
   return p0 > floor ? p0 : floor;
@@ -84,53 +79,58 @@ struct SideFn {
 };
 
 __device__ __forceinline__ double FSide(const SideFn& s, double gm1, double exponent,
-                                        double q) {
+                                        const Powers& pw, double q) {
   if (q > s.p) {
     return (q - s.p) * sqrt(s.A / (q + s.B));
   }
-  return 2.0 * s.a / gm1 * (pow(q / s.p, exponent) - 1.0);
+  return 2.0 * s.a / gm1 * (pw.Z(q / s.p, exponent) - 1.0);
 }
 
-__device__ __forceinline__ double DfSide(const SideFn& s, double d_exponent, double q) {
+__device__ __forceinline__ double DfSide(const SideFn& s, double d_exponent, const Powers& pw,
+                                         double q) {
   if (q > s.p) {
     return sqrt(s.A / (s.B + q)) * (1.0 - 0.5 * (q - s.p) / (s.B + q));
   }
-  return pow(q / s.p, d_exponent) / (s.rho * s.a);
+  return pw.ZMinus1(q / s.p, d_exponent) / (s.rho * s.a);
 }
 
-// NewtonIteration from x0 with f(x0) = fx0 already evaluated
-// (NewtonIteration.hpp:28-52), bounded.
-__device__ __forceinline__ void NewtonFrom(const SideFn& L, const SideFn& R, double du,
-                                           double gm1, double exponent, double d_exponent,
-                                           double x0, double fx0, double tol, int max_iterations,
-                                           double& x_out, int& iterations, int& converged) {
-  double x = x0;
-  double fx = fx0;
+// The pressure function's two sides at one pressure: f = fR + fL + du
+// (ExactRiemannSolver.hpp:89); the solver's middle velocity reuses fR and fL
+// of its final pressure.
+struct FEval {
+  double x, fR, fL;
+};
+
+__device__ __forceinline__ FEval EvalF(const SideFn& L, const SideFn& R, double gm1,
+                                       double exponent, const Powers& pw, double x) {
+  return FEval{x, FSide(R, gm1, exponent, pw, x), FSide(L, gm1, exponent, pw, x)};
+}
+
+// NewtonIteration from the evaluated start e0 (NewtonIteration.hpp:28-52),
+// bounded; returns the last evaluation.
+__device__ __forceinline__ FEval NewtonFrom(const SideFn& L, const SideFn& R, double du,
+                                            double gm1, double exponent, double d_exponent,
+                                            const Powers& pw, FEval e0, double tol,
+                                            int max_iterations, int& iterations,
+                                            int& converged) {
+  FEval e = e0;
+  double fx = e.fR + e.fL + du;
   int counter = 0;
   double err = fabs(fx);
   while (err > tol && counter < max_iterations) {
-    const double dfx = DfSide(R, d_exponent, x) + DfSide(L, d_exponent, x);
+    const double x = e.x;
+    const double dfx = DfSide(R, d_exponent, pw, x) + DfSide(L, d_exponent, pw, x);
     const double offset = fx / dfx;
     const double next = x - offset;
-    x = ((next - next) != (next - next) || next < 0.0) ? 0.5 * x : next;
-    fx = FSide(R, gm1, exponent, x) + FSide(L, gm1, exponent, x) + du;
+    e = EvalF(L, R, gm1, exponent, pw,
+              ((next - next) != (next - next) || next < 0.0) ? 0.5 * x : next);
+    fx = e.fR + e.fL + du;
     err = fabs(fx);
     counter += 1;
   }
-  x_out = x;
   iterations = counter;
   converged = !(err > tol);
-}
-
-// NewtonIteration from x0 (NewtonIteration.hpp:28-52), bounded.
-__device__ __forceinline__ void Newton(const SideFn& L, const SideFn& R, double du, double gm1,
-                                       double exponent, double d_exponent, double x0,
-                                       double tol, int max_iterations, double& x_out,
-                                       int& iterations, int& converged) {
-  // f(h) = f_right(h) + f_left(h) + du (ExactRiemannSolver.hpp:89)
-  const double fx0 = FSide(R, gm1, exponent, x0) + FSide(L, gm1, exponent, x0) + du;
-  NewtonFrom(L, R, du, gm1, exponent, d_exponent, x0, fx0, tol, max_iterations, x_out,
-             iterations, converged);
+  return e;
 }
 
 template <int D>
@@ -154,6 +154,7 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
   R.B = gm1 / gp1 * R.p;
   const double exponent = 0.5 * gm1 / g;
   const double d_exponent = -0.5 * gp1 / g;
+  const Powers pw(opt.root_n);
   const double uL = left.m[dir] / left.rho;
   const double uR = right.m[dir] / right.rho;
   const double du = uR - uL;
@@ -163,11 +164,11 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
   if (opt.guess == kGuessMean) {
     x0 = 0.5 * (L.p + R.p);
   } else {
-    const double pv = PvrsTrGuess(g, L.rho, uL, L.p, L.a, R.rho, uR, R.p, R.a);
+    const double pv = PvrsTrGuess(pw, g, L.rho, uL, L.p, L.a, R.rho, uR, R.p, R.a);
     x0 = pv;
-    // Cost-aware use of the learned start: the network costs less than one
-    // Newton step (its 5-64-64-1 FP32 multiply-adds against two FP64 pow
-    // evaluations per step), so it is used only where it is expected to
+    // Cost-aware use of the learned start: the network costs about one
+    // Newton step (its 5-64-64-1 FP32 multiply-adds against two FP64 roots
+    // or pow evaluations per step), so it is used only where it is expected to
     // save at least one step.  Newton converges quadratically, so from a
     // start whose relative residual is r = |f(p0)| / (aL + aR) it needs
     // about k(r) = ceil(log2(log(tol') / log(r))) steps to reach
@@ -178,9 +179,11 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
     // strength, keep their start and never pay for the network.
     constexpr float kLearnedRelErr = 0.01f;
     double f_pv = 0.0;
+    FEval e_pv{pv, 0.0, 0.0};
     bool screened = false;
     if (opt.guess == kGuessMlp) {
-      f_pv = FSide(R, gm1, exponent, pv) + FSide(L, gm1, exponent, pv) + du;
+      e_pv = EvalF(L, R, gm1, exponent, pw, pv);
+      f_pv = e_pv.fR + e_pv.fL + du;
       const float scale = static_cast<float>(L.a + R.a);
       const float lt = __log2f(static_cast<float>(opt.tol) / scale);  // < 0 for tol < scale
       auto steps = [&](float r) -> float {
@@ -192,11 +195,10 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
       screened = !(steps(r_pv) >= steps(kLearnedRelErr) + 1.0f);
       if (screened || !opt.mlp) {
         // PVRS/TR start, reusing the residual just evaluated
-        NewtonFrom(L, R, du, gm1, exponent, d_exponent, pv, f_pv, opt.tol, opt.max_iterations,
-                   st.p, st.iterations, st.converged);
-        const double fL = FSide(L, gm1, exponent, st.p);
-        const double fR = FSide(R, gm1, exponent, st.p);
-        st.u = 0.5 * (uL + uR) + 0.5 * (fR - fL);
+        const FEval e = NewtonFrom(L, R, du, gm1, exponent, d_exponent, pw, e_pv, opt.tol,
+                                   opt.max_iterations, st.iterations, st.converged);
+        st.p = e.x;
+        st.u = 0.5 * (uL + uR) + 0.5 * (e.fR - e.fL);
         return st;
       }
     }
@@ -210,36 +212,32 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
       }
     }
     if (opt.guess == kGuessMlp && !st.fallback) {
-      double x;
       int it, ok;
       // a learned start gets at most 64 steps before the PVRS/TR restart
       const int learned_max = opt.max_iterations < 64 ? opt.max_iterations : 64;
-      Newton(L, R, du, gm1, exponent, d_exponent, x0, opt.tol, learned_max, x, it, ok);
+      FEval e = NewtonFrom(L, R, du, gm1, exponent, d_exponent, pw,
+                           EvalF(L, R, gm1, exponent, pw, x0), opt.tol, learned_max, it, ok);
       if (!ok) {
         // the learned start did not converge within the bound: fall back
         st.fallback = 1;
-        double x2;
         int it2, ok2;
-        NewtonFrom(L, R, du, gm1, exponent, d_exponent, pv, f_pv, opt.tol, opt.max_iterations,
-                   x2, it2, ok2);
-        x = x2;
+        e = NewtonFrom(L, R, du, gm1, exponent, d_exponent, pw, e_pv, opt.tol,
+                       opt.max_iterations, it2, ok2);
         it += it2;
         ok = ok2;
       }
-      st.p = x;
+      st.p = e.x;
       st.iterations = it;
       st.converged = ok;
-      const double fL = FSide(L, gm1, exponent, st.p);
-      const double fR = FSide(R, gm1, exponent, st.p);
-      st.u = 0.5 * (uL + uR) + 0.5 * (fR - fL);
+      st.u = 0.5 * (uL + uR) + 0.5 * (e.fR - e.fL);
       return st;
     }
   }
-  Newton(L, R, du, gm1, exponent, d_exponent, x0, opt.tol, opt.max_iterations, st.p,
-         st.iterations, st.converged);
-  const double fL = FSide(L, gm1, exponent, st.p);
-  const double fR = FSide(R, gm1, exponent, st.p);
-  st.u = 0.5 * (uL + uR) + 0.5 * (fR - fL);
+  const FEval e = NewtonFrom(L, R, du, gm1, exponent, d_exponent, pw,
+                             EvalF(L, R, gm1, exponent, pw, x0), opt.tol, opt.max_iterations,
+                             st.iterations, st.converged);
+  st.p = e.x;
+  st.u = 0.5 * (uL + uR) + 0.5 * (e.fR - e.fL);
   return st;
 }
 
@@ -284,7 +282,8 @@ template <int D>
 __device__ __forceinline__ void Sample(const exact::Gas& eq, exact::Complete<D>& state,
                                        const exact::Complete<D>& left,
                                        const exact::Complete<D>& right, int dir, double pM,
-                                       double uM) {
+                                       double uM, const Options& opt) {
+  const Powers pw(opt.root_n);
   const double g = eq.gamma;
   const double gp1 = g + 1.0;
   const double gm1 = g - 1.0;
@@ -321,21 +320,21 @@ __device__ __forceinline__ void Sample(const exact::Gas& eq, exact::Complete<D>&
         state = left;
       }
     } else {
-      const double aM = aL * pow(p_ratio, gm1 / (2.0 * g));
+      const double aM = aL * pw.Z(p_ratio, gm1 / (2.0 * g));
       const double shock_speed_TL = uM - aM;
       const double shock_speed_HL = uL - aL;
       if (0.0 < shock_speed_HL) {
         state = left;
       } else if (shock_speed_TL < 0.0) {
-        state.rho = left.rho * pow(p_ratio, 1 / g);
+        state.rho = left.rho * pw.InvGamma(p_ratio, 1 / g);
         set_momentum(state, state.rho * uM, left);
         state.p = pM;
         from_prim(state);
       } else {
-        state.rho = left.rho * pow(2.0 / gp1 + g_ratio * uL / aL, 2.0 / gm1);
+        state.rho = left.rho * pw.N2(2.0 / gp1 + g_ratio * uL / aL, 2.0 / gm1);
         const double u = 2.0 / gp1 * (aL + 0.5 * gm1 * uL);
         set_momentum(state, state.rho * u, left);
-        state.p = pL * pow(2.0 / gp1 + g_ratio * uL / aL, 2.0 * g / gm1);
+        state.p = pL * pw.N(2.0 / gp1 + g_ratio * uL / aL, 2.0 * g / gm1);
         from_prim(state);
       }
     }
@@ -356,21 +355,21 @@ __device__ __forceinline__ void Sample(const exact::Gas& eq, exact::Complete<D>&
         state = right;
       }
     } else {
-      const double aM = aR * pow(p_ratio, gm1 / (2.0 * g));
+      const double aM = aR * pw.Z(p_ratio, gm1 / (2.0 * g));
       const double shock_speed_TR = uM + aM;
       const double shock_speed_HR = uR + aR;
       if (shock_speed_HR <= 0.0) {
         state = right;
       } else if (shock_speed_TR >= 0.0) {
-        state.rho = right.rho * pow(p_ratio, 1 / g);
+        state.rho = right.rho * pw.InvGamma(p_ratio, 1 / g);
         set_momentum(state, state.rho * uM, right);
         state.p = pM;
         from_prim(state);
       } else {
-        state.rho = right.rho * pow(2.0 / gp1 - g_ratio * uR / aR, 2.0 / gm1);
+        state.rho = right.rho * pw.N2(2.0 / gp1 - g_ratio * uR / aR, 2.0 / gm1);
         const double u = 2.0 / gp1 * (-aR + 0.5 * gm1 * uR);
         set_momentum(state, state.rho * u, right);
-        state.p = pR * pow(2.0 / gp1 - g_ratio * uR / aR, 2.0 * g / gm1);
+        state.p = pR * pw.N(2.0 / gp1 - g_ratio * uR / aR, 2.0 * g / gm1);
         from_prim(state);
       }
     }
@@ -389,7 +388,7 @@ __device__ __forceinline__ Star GodunovFlux(const exact::Gas& eq, double* nf,
   Star st{0.0, 0.0, 0, 1, 0};
   if (0.0 < L.rho && 0.0 < R.rho) {
     st = ComputeMiddleState<D>(eq, L, R, dir, opt);
-    Sample<D>(eq, sol, L, R, dir, st.p, st.u);
+    Sample<D>(eq, sol, L, R, dir, st.p, st.u, opt);
   }
   exact::Flux<D>(nf, sol, dir);
   return st;
