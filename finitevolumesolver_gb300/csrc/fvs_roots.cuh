@@ -4,6 +4,8 @@
 
 #include <cmath>
 
+#include "fvs_convert.cuh"
+
 namespace fvs {
 namespace riemann {
 
@@ -52,13 +54,14 @@ struct Powers {
   __host__ __device__ bool Fast(double x) const { return n > 0 && x > 1e-30 && x < 1e30; }
   // x^(-1/n) for Fast(x)
   __host__ __device__ double RecipRoot(double x) const {
-    const float xf = static_cast<float>(x);
 #ifdef __CUDA_ARCH__
-    const float lg = __log2f(xf);
+    // the estimate's conversions on the integer pipe (the FP64 pipe is the
+    // solver's bottleneck)
+    const float xf = DoubleToFloatBits(x);
+    double r = FloatToDoubleBits(exp2f(-__log2f(xf) * static_cast<float>(inv_n)));
 #else
-    const float lg = log2f(xf);
+    double r = static_cast<double>(exp2f(-log2f(static_cast<float>(x)) * static_cast<float>(inv_n)));
 #endif
-    double r = static_cast<double>(exp2f(-lg * static_cast<float>(inv_n)));
 #pragma unroll
     for (int it = 0; it < 2; ++it) {
       const double e = fma(-x, IPow(r, n), 1.0);
