@@ -331,8 +331,8 @@ def report_mlp(args, torch, fvs, workloads):
 def report_godunov(args, torch, fvs, workloads, net, peaks=None):
     """2-D first-order Godunov with the exact Riemann solver on an n^2
     four-quadrant problem drawn from the sampled distribution, Strang
-    splitting, for the three Newton start values at each Newton tolerance
-    (the reference's 1e-7 and a tight 1e-12)."""
+    splitting, autotuned launch shapes, for the three Newton start values at
+    each Newton tolerance (the reference's 1e-7 and a tight 1e-12)."""
     n = args.godunov_n
     cons = workloads.quadrants_2d(n, seed=3)
     by_tol = {}
@@ -347,6 +347,7 @@ def report_godunov(args, torch, fvs, workloads, net, peaks=None):
             s = fvs.Solver([n, n], [1.0 / n, 1.0 / n], "transmissive", method=m)
             stream = torch.cuda.ExternalStream(s.stream_handle())
             s.upload(cons)
+            s.autotune()
             s.run(cfl=0.8, t_end=1e9, max_steps=3)
             s.upload(cons)
             s.set_cycle(0)
@@ -364,7 +365,7 @@ def report_godunov(args, torch, fvs, workloads, net, peaks=None):
             faces = st.steps * 4 * (n + 1) * n
             rate = 4 * n * n * st.steps / (ms / 1e3)
             out[guess] = {"steps": st.steps, "ms_per_step": ms / max(st.steps, 1),
-                          "cell_updates_per_s": rate,
+                          "cell_updates_per_s": rate, "autotuned": s.tuning(),
                           "hbm_frac_algorithmic": (rate * 64 / 1e9 / peaks["hbm_gbs"]
                                                    if peaks else None),
                           "newton_iterations_per_interface": it / faces,
