@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 from finitevolumesolver_gb300 import workloads
+from tolerance import assert_close_fp64
 
 pytestmark = pytest.mark.gpu
 
@@ -96,8 +97,10 @@ def test_sod_octants_3d_bit_exact(fvs, orc):
 def test_tiled_dt_rule_uses_stencil_width(fvs, orc, kind):
     """dt_rule 1 takes the faces of the reference's MFIter tiles, whose
     windows span 2 w cells for a stencil width w.  Bit for bit, except for
-    the exact Riemann solver, whose pow() differs from the host's in the last
-    bits: 1e-12 relative there."""
+    the exact Riemann solver, whose powers of pressure ratios (n-th roots on
+    the GPU, glibc's pow() in the oracle) differ in the last bits: dt within
+    1e-12 relative and the state within 1e-12 per cell there (momenta
+    relative to the component's largest magnitude, as they cross zero)."""
     n = (20, 21)
     cons = workloads.random_state((n[1], n[0]), 2, seed=5, rho=(0.5, 1.5), p=(0.5, 1.5),
                                   v=0.4).reshape(4, 1, n[1], n[0])
@@ -110,7 +113,7 @@ def test_tiled_dt_rule_uses_stencil_width(fvs, orc, kind):
     st, dts = s.run(cfl=0.6, t_end=10.0, max_steps=3, log_len=4)
     if "godunov" in kind:
         np.testing.assert_allclose(dts, ref_dts, rtol=1e-12)
-        np.testing.assert_allclose(s.download(), ref, rtol=1e-12)
+        assert_close_fp64(s.download(), ref, 2, 1e-12, kind)
     else:
         np.testing.assert_array_equal(dts, ref_dts)
         np.testing.assert_array_equal(s.download(), ref)
