@@ -11,8 +11,9 @@
 //       include/fub/flux_method/GodunovMethod.hpp:129-183
 // with the reference's operation order (the including translation unit is
 // compiled with -fmad=false).  The powers of pressure ratios are n-th roots
-// (Powers) or CUDA's pow(), so results agree with the CPU oracle to a few
-// ulps rather than bit for bit.
+// (Powers) or CUDA's pow(), and the quotients and square roots of variable
+// operands refined reciprocal seeds (Div, Sqrt), so results agree with the
+// CPU oracle to ~1e-15 relative rather than bit for bit.
 //
 // Differences by design:
 //  - Newton is bounded by `max_iterations` and never throws: a face that has
@@ -27,6 +28,7 @@
 
 #include "fvs_mlp.cuh"
 #include "fvs_physics_exact.cuh"
+#include "fvs_physics_fast.cuh"
 #include "fvs_roots.cuh"
 
 namespace fvs {
@@ -41,6 +43,24 @@ struct Options {
   const float* mlp;  // learned-guess parameters (kGuessMlp)
   int root_n;        // RootOrder(gamma): 0, or n with n-th roots in place of pow()
 };
+
+// Quotients and square roots of the solver's variable operands: a reciprocal
+// (reciprocal square root) seed refined by one third-order step, the fast
+// flavour's fast::Math<double> (within ~2 ulp of IEEE), in place of IEEE
+// division and sqrt, which cost the FP64 pipe several times as much.
+// Operands that are zero, negative, not finite or within 2^2 of the FP64
+// range's ends take IEEE division and sqrt, so vacuum and failed states keep
+// IEEE semantics (inf, NaN).
+__device__ __forceinline__ bool InRange(double b) {
+  const unsigned e = static_cast<unsigned>(__double2hiint(b)) & 0x7FFFFFFFu;
+  return e >= 0x00200000u && e < 0x7FD00000u;
+}
+__device__ __forceinline__ double Div(double a, double b) {
+  return InRange(b) ? a * fast::Math<double>::Rcp(b) : a / b;
+}
+__device__ __forceinline__ double Sqrt(double a) {
+  return (a > 0.0 && InRange(a)) ? a * fast::Math<double>::Rsqrt(a) : sqrt(a);
+}
 
 // Scalar-path |m|^2 of the reference's exact solver: (m0^2 + m1^2) + m2^2.
 template <int D> __device__ __forceinline__ double SquaredNormScalar(const double* m) {
@@ -67,8 +87,8 @@ __device__ __forceinline__ double PvrsTrGuess(const Powers& pw, double g, double
   } else {
     const double z = (g - 1.0) / (2.0 * g);
     const double num = aL + aR - 0.5 * (g - 1.0) * (uR - uL);
-    const double den = aL / pw.Z(pL, z) + aR / pw.Z(pR, z);
-    p0 = (num > 0.0) ? pw.N(num / den, 1.0 / z) : 0.0;
+    const double den = Div(aL, pw.Z(pL, z)) + Div(aR, pw.Z(pR, z));
+    p0 = (num > 0.0) ? pw.N(Div(num, den), 1.0 / z) : 0.0;
   }
   const double floor = 1e-8 * pmin;
   return p0 > floor ? p0 : floor;
@@ -81,17 +101,17 @@ struct SideFn {
 __device__ __forceinline__ double FSide(const SideFn& s, double gm1, double exponent,
                                         const Powers& pw, double q) {
   if (q > s.p) {
-    return (q - s.p) * sqrt(s.A / (q + s.B));
+    return (q - s.p) * Sqrt(Div(s.A, q + s.B));
   }
-  return 2.0 * s.a / gm1 * (pw.Z(q / s.p, exponent) - 1.0);
+  return Div(2.0 * s.a, gm1) * (pw.Z(Div(q, s.p), exponent) - 1.0);
 }
 
 __device__ __forceinline__ double DfSide(const SideFn& s, double d_exponent, const Powers& pw,
                                          double q) {
   if (q > s.p) {
-    return sqrt(s.A / (s.B + q)) * (1.0 - 0.5 * (q - s.p) / (s.B + q));
+    return Sqrt(Div(s.A, s.B + q)) * (1.0 - Div(0.5 * (q - s.p), s.B + q));
   }
-  return pw.ZMinus1(q / s.p, d_exponent) / (s.rho * s.a);
+  return Div(pw.ZMinus1(Div(q, s.p), d_exponent), s.rho * s.a);
 }
 
 // The pressure function's two sides at one pressure: f = fR + fL + du
@@ -120,7 +140,7 @@ __device__ __forceinline__ FEval NewtonFrom(const SideFn& L, const SideFn& R, do
   while (err > tol && counter < max_iterations) {
     const double x = e.x;
     const double dfx = DfSide(R, d_exponent, pw, x) + DfSide(L, d_exponent, pw, x);
-    const double offset = fx / dfx;
+    const double offset = Div(fx, dfx);
     const double next = x - offset;
     e = EvalF(L, R, gm1, exponent, pw,
               ((next - next) != (next - next) || next < 0.0) ? 0.5 * x : next);
@@ -145,18 +165,18 @@ __device__ __forceinline__ Star ComputeMiddleState(const exact::Gas& eq,
   L.rho = left.rho;
   L.p = left.p;
   L.a = left.c;
-  L.A = 2.0 / (gp1 * L.rho);
+  L.A = Div(2.0, gp1 * L.rho);
   L.B = gm1 / gp1 * L.p;
   R.rho = right.rho;
   R.p = right.p;
   R.a = right.c;
-  R.A = 2.0 / (gp1 * R.rho);
+  R.A = Div(2.0, gp1 * R.rho);
   R.B = gm1 / gp1 * R.p;
   const double exponent = 0.5 * gm1 / g;
   const double d_exponent = -0.5 * gp1 / g;
   const Powers pw(opt.root_n);
-  const double uL = left.m[dir] / left.rho;
-  const double uR = right.m[dir] / right.rho;
+  const double uL = Div(left.m[dir], left.rho);
+  const double uR = Div(right.m[dir], right.rho);
   const double du = uR - uL;
   Star st;
   st.fallback = 0;
@@ -251,22 +271,22 @@ __device__ __forceinline__ double SignalMaxSpeed(const exact::Gas& eq,
   const double g = eq.gamma;
   const double gp1 = g + 1.0;
   const double gm1 = g - 1.0;
-  const double uL = left.m[dir] / left.rho;
+  const double uL = Div(left.m[dir], left.rho);
   const double aL = left.c;
   const double pL = left.p;
-  const double pL_ratio = pM / pL;
+  const double pL_ratio = Div(pM, pL);
   double s0, s1;
   if (pM > pL) {
-    s0 = uL - aL * sqrt((gp1 * pL_ratio + gm1) / (2.0 * g));
+    s0 = uL - aL * Sqrt(Div(gp1 * pL_ratio + gm1, 2.0 * g));
   } else {
     s0 = uL - aL;
   }
-  const double uR = right.m[dir] / right.rho;
+  const double uR = Div(right.m[dir], right.rho);
   const double aR = right.c;
   const double pR = right.p;
-  const double pR_ratio = pM / pR;
+  const double pR_ratio = Div(pM, pR);
   if (pM > pR) {
-    s1 = uR + aR * sqrt((gp1 * pR_ratio + gm1) / (2.0 * g));
+    s1 = uR + aR * Sqrt(Div(gp1 * pR_ratio + gm1, 2.0 * g));
   } else {
     s1 = uR + aR;
   }
@@ -293,26 +313,26 @@ __device__ __forceinline__ void Sample(const exact::Gas& eq, exact::Complete<D>&
       s.m[0] = momentum;
     } else {
 #pragma unroll
-      for (int d = 0; d < D; ++d) s.m[d] = s.rho * (side.m[d] / side.rho);
+      for (int d = 0; d < D; ++d) s.m[d] = s.rho * Div(side.m[d], side.rho);
       s.m[dir] = momentum;
     }
   };
   auto from_prim = [&eq](exact::Complete<D>& s) {
-    const double rhoE_kin = 0.5 * SquaredNormScalar<D>(s.m) / s.rho;
+    const double rhoE_kin = Div(0.5 * SquaredNormScalar<D>(s.m), s.rho);
     const double rhoE_internal = s.p * eq.gamma_minus_1_inv;
     s.E = rhoE_internal + rhoE_kin;
-    s.c = sqrt(eq.gamma * s.p / s.rho);
+    s.c = Sqrt(Div(eq.gamma * s.p, s.rho));
   };
   if (0.0 <= uM) {
-    const double uL = left.m[dir] / left.rho;
+    const double uL = Div(left.m[dir], left.rho);
     const double aL = left.c;
     const double pL = left.p;
-    const double p_ratio = pM / pL;
+    const double p_ratio = Div(pM, pL);
     const double g_ratio = gm1 / gp1;
     if (pM > pL) {
-      const double shock_speed = uL - aL * sqrt((gp1 * p_ratio + gm1) / (2.0 * g));
+      const double shock_speed = uL - aL * Sqrt(Div(gp1 * p_ratio + gm1, 2.0 * g));
       if (shock_speed < 0.0) {
-        state.rho = left.rho * (p_ratio + g_ratio) / (g_ratio * p_ratio + 1.0);
+        state.rho = Div(left.rho * (p_ratio + g_ratio), g_ratio * p_ratio + 1.0);
         set_momentum(state, state.rho * uM, left);
         state.p = pM;
         from_prim(state);
@@ -331,23 +351,23 @@ __device__ __forceinline__ void Sample(const exact::Gas& eq, exact::Complete<D>&
         state.p = pM;
         from_prim(state);
       } else {
-        state.rho = left.rho * pw.N2(2.0 / gp1 + g_ratio * uL / aL, 2.0 / gm1);
+        state.rho = left.rho * pw.N2(2.0 / gp1 + Div(g_ratio * uL, aL), 2.0 / gm1);
         const double u = 2.0 / gp1 * (aL + 0.5 * gm1 * uL);
         set_momentum(state, state.rho * u, left);
-        state.p = pL * pw.N(2.0 / gp1 + g_ratio * uL / aL, 2.0 * g / gm1);
+        state.p = pL * pw.N(2.0 / gp1 + Div(g_ratio * uL, aL), 2.0 * g / gm1);
         from_prim(state);
       }
     }
   } else {
-    const double uR = right.m[dir] / right.rho;
+    const double uR = Div(right.m[dir], right.rho);
     const double aR = right.c;
     const double pR = right.p;
-    const double p_ratio = pM / pR;
+    const double p_ratio = Div(pM, pR);
     const double g_ratio = gm1 / gp1;
     if (pM > pR) {
-      const double shock_speed = uR + aR * sqrt((gp1 * p_ratio + gm1) / (2.0 * g));
+      const double shock_speed = uR + aR * Sqrt(Div(gp1 * p_ratio + gm1, 2.0 * g));
       if (0.0 < shock_speed) {
-        state.rho = right.rho * (p_ratio + g_ratio) / (g_ratio * p_ratio + 1.0);
+        state.rho = Div(right.rho * (p_ratio + g_ratio), g_ratio * p_ratio + 1.0);
         set_momentum(state, state.rho * uM, right);
         state.p = pM;
         from_prim(state);
@@ -366,10 +386,10 @@ __device__ __forceinline__ void Sample(const exact::Gas& eq, exact::Complete<D>&
         state.p = pM;
         from_prim(state);
       } else {
-        state.rho = right.rho * pw.N2(2.0 / gp1 - g_ratio * uR / aR, 2.0 / gm1);
+        state.rho = right.rho * pw.N2(2.0 / gp1 - Div(g_ratio * uR, aR), 2.0 / gm1);
         const double u = 2.0 / gp1 * (-aR + 0.5 * gm1 * uR);
         set_momentum(state, state.rho * u, right);
-        state.p = pR * pw.N(2.0 / gp1 - g_ratio * uR / aR, 2.0 * g / gm1);
+        state.p = pR * pw.N(2.0 / gp1 - Div(g_ratio * uR, aR), 2.0 * g / gm1);
         from_prim(state);
       }
     }
