@@ -57,13 +57,13 @@ template <int D, bool kMuscl> struct GodunovPolicyT {
     if constexpr (kMuscl) {
       exact::MusclPredictBoth<D>(g.eq, recL, recR, q0, q1, q2, limiter, lambda_half, dir);
     } else {
-      exact::CompleteFromCons<D>(g.eq, recL, q1);
+      riemann::CompleteFromConsFast<D>(g.eq, recL, q1);
       recR = recL;
     }
   }
   static __device__ __forceinline__ Wave MakeWave(const Gas& g, const double* u, int) {
     Wave w;
-    exact::CompleteFromCons<D>(g.eq, w, u);
+    riemann::CompleteFromConsFast<D>(g.eq, w, u);
     return w;
   }
   static __device__ __forceinline__ double Face(const Gas& g, double* F, const Rec& L,

@@ -62,6 +62,32 @@ __device__ __forceinline__ double Sqrt(double a) {
   return (a > 0.0 && InRange(a)) ? a * fast::Math<double>::Rsqrt(a) : sqrt(a);
 }
 
+// PerfectGas::CompleteFromCons and Flux (src/equations/PerfectGas.cpp:52-124)
+// with the quotients and square root above: the Godunov sweeps' cell states
+// and face flux.
+template <int D>
+__device__ __forceinline__ void CompleteFromConsFast(const exact::Gas& eq, exact::Complete<D>& q,
+                                                     const double* u) {
+  q.rho = u[0];
+#pragma unroll
+  for (int d = 0; d < D; ++d) q.m[d] = u[1 + d];
+  q.E = u[1 + D];
+  const double e_kin = Div(0.5 * exact::SquaredNorm<D>(q.m), q.rho);
+  const double e_int = q.E - e_kin;
+  q.p = Div(e_int, eq.gamma_minus_1_inv);
+  q.c = Sqrt(Div(eq.gamma * q.p, q.rho));
+}
+
+template <int D>
+__device__ __forceinline__ void FluxFast(double* f, const exact::Complete<D>& q, int dir) {
+  const double velocity = Div(q.m[dir], q.rho);
+  f[0] = q.m[dir];
+#pragma unroll
+  for (int d = 0; d < D; ++d) f[1 + d] = velocity * q.m[d];
+  f[1 + dir] += q.p;
+  f[1 + D] = velocity * (q.E + q.p);
+}
+
 // Scalar-path |m|^2 of the reference's exact solver: (m0^2 + m1^2) + m2^2.
 template <int D> __device__ __forceinline__ double SquaredNormScalar(const double* m) {
   if constexpr (D == 1) {
@@ -410,7 +436,7 @@ __device__ __forceinline__ Star GodunovFlux(const exact::Gas& eq, double* nf,
     st = ComputeMiddleState<D>(eq, L, R, dir, opt);
     Sample<D>(eq, sol, L, R, dir, st.p, st.u, opt);
   }
-  exact::Flux<D>(nf, sol, dir);
+  FluxFast<D>(nf, sol, dir);
   return st;
 }
 
